@@ -1,0 +1,338 @@
+#!/usr/bin/env python3
+"""Benchmark of the pair-counting hot path: binned pairs/s.
+
+Default workload: the 200,000-galaxy Neyman-Scott periodic box with shapes
+(wg+ and wgg, 64 jackknife cubes, 20 log r_p x 40 Pi bins) -- the workload the
+headline metric "binned pairs/s (wgg+wg+ w/ jackknife)" is quoted on.  Other
+workloads: --workload box_uniform_wgg_20k | box_ns_wpp_20M | box_batch_wpp_64.
+
+One step = one corels2 call (the SD pair type these runs use) over the whole
+catalogue.  `value` times the device work with the catalogues resident in HBM
+(CUDA events on the library's stream around the zeroing, the pair kernel and
+the FP64 edge recheck); L2 is flushed (256 MB write) between timed steps.
+`e2e` times the same through the C ABI from host buffers: both uploads (copy +
+on-device cell list) + count + histogram readback, wall clock.
+
+`--impl reference` times the CPU implementation of the path on this host's
+cores (the oracle restatement of corels2; the reference binary itself is
+built from its sources only where they exist and cannot travel to this host)
+on a bounded row sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "binned pairs/s (wgg+wg+ w/ jackknife) vs plain FP64 GPU & host CPU; % roofline"
+UNIT = "pairs/s"
+
+
+def _workload(name: str):
+    from corr_pc_gb300 import synth
+    if name == "box_ns_wgp_200k":
+        return [synth.box_ns_wgp()]
+    if name == "box_uniform_wgg_20k":
+        return [synth.box_uniform_wgg()]
+    if name == "box_ns_wpp_20M":
+        return [synth.box_ns_large_wpp()]
+    if name == "box_batch_wpp_64":
+        return synth.box_batch_wpp()
+    raise SystemExit(f"unknown workload {name}")
+
+
+def _describe(wls) -> dict:
+    p = wls[0].params
+    d = {"workload": wls[0].name if len(wls) == 1 else "box_batch_wpp_64",
+         "which_corr": p.which_corr, "n_jk": p.n_jk_regions, "rp_bins": p.n_bins,
+         "pi_bins": p.n_p_bin, "rp_range": [p.bin_r_min, p.bin_r_max],
+         "pi_range": [p.p_min, p.p_max], "box": p.periodic_box_size,
+         "n_points": int(sum(w.shape.n for w in wls)), "n_catalogs": len(wls),
+         "pair_type": "SD (shape x density, S and D the same points)",
+         "l2": "flushed between timed steps (256 MB write)"}
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi clocks during the timed region (read-only query)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int = 0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks() -> dict:
+    """Live FP32 FFMA and shared-memory 32-bit atomic peaks (this GPU)."""
+    from corr_pc_gb300 import build as b
+    lib = ctypes.CDLL(b.PEAKS)
+    lib.cpc_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                             ctypes.POINTER(ctypes.c_double)]
+    out = {}
+    for k, nm in ((0, "ffma_flops"), (5, "smem_atomic_u32_ops")):
+        v = ctypes.c_double()
+        rc = lib.cpc_peak(k, ctypes.byref(v), None)
+        out[nm] = v.value if rc == 0 else None
+    return out
+
+
+def _cpu_sample(p, cats, budget_s: float, n_binned_full: int, threads: int, offset: int = 0):
+    """Time the oracle restatement of corels2 on every k-th outer row."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the CPU baseline (test infrastructure)
+    ocats = {r: oracle.OracleCatalog(c.x, c.y, c.z, w=c.w, e1=c.e1, e2=c.e2, phi=c.phi,
+                                      jk=c.jk, jk_prob=c.jk_prob, include_prob=c.include_prob)
+             for r, c in cats.items()}
+    rate_guess = 4e6 * threads  # binned pairs/s on one ARM/x86 core, rough
+    stride = max(1, int(n_binned_full / (rate_guess * budget_s)))
+    t = time.perf_counter()
+    _, _, ntot, nin = oracle.port_corels2(p, "SD", ocats["D"], ocats["S"], n_threads=threads,
+                                          row_stride=stride, row_offset=offset % stride)
+    dt = time.perf_counter() - t
+    return {"value": nin / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"every {stride}-th outer row (offset {offset % stride}): "
+                      f"{nin} binned pairs in {dt:.2f} s"}, stride, nin, dt
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from corr_pc_gb300 import host
+    wls = _workload(args.workload)
+    wl = wls[0]
+    p = wl.params
+    cats = host.prepare(p, [("S", wl.shape), ("D", wl.density)])
+    threads = os.cpu_count() or 1
+    # estimate the full binned count cheaply from a tiny sample
+    probe, stride0, nin0, _ = _cpu_sample(p, cats, 0.5, 10 ** 10, threads)
+    n_full = nin0 * stride0
+    tot_pairs, tot_t, last = 0, 0.0, None
+    for s in range(args.warmup + args.steps):
+        res, stride, nin, dt = _cpu_sample(p, cats, args.ref_budget, n_full, threads, offset=s)
+        if s >= args.warmup:
+            tot_pairs += nin
+            tot_t += dt
+            last = res
+    v = tot_pairs / tot_t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded, in memory)", "config": _describe(wls),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": last["sample"] if last else ""},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="box_ns_wgp_200k")
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline")
+    ap.add_argument("--ref-budget", type=float, default=8.0, help="seconds per reference step")
+    ap.add_argument("--fp64-budget", type=float, default=3.0, help="seconds of FP64 kernel")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from corr_pc_gb300 import build as b
+    b.build()
+    from corr_pc_gb300 import _lib, host, metrics
+
+    wls = _workload(args.workload)
+    preps = [host.prepare(w.params, [("S", w.shape), ("D", w.density)]) for w in wls]
+    ctxs = [_lib.Context(w.params) for w in wls]
+    for c, cat in zip(ctxs, preps):
+        c.upload(0, cat["D"])
+        c.upload(1, cat["S"])
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def step():
+        if len(ctxs) == 1:
+            r = ctxs[0].count("SD", 0, 1)
+            return r["n_binned"], r["kernel_ms"], r["pair_kernel_ms"], r["n_window"]
+        rs = _lib.count_batch([(c, "SD", 0, 1) for c in ctxs])
+        return (sum(r["n_binned"] for r in rs), rs[0]["kernel_ms"], rs[0]["pair_kernel_ms"],
+                sum(r["n_window"] for r in rs))
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step()
+    l0 = sum(c.launches() for c in ctxs)
+    tot_ms = tot_pair_ms = 0.0
+    n_bin = n_win = 0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            nb, ms, pms, nw = step()
+            n_bin += nb
+            n_win += nw
+            tot_ms += ms
+            tot_pair_ms += pms
+    torch.cuda.synchronize()
+    launches = sum(c.launches() for c in ctxs) - l0
+    t_step = tot_ms / args.steps
+    if dist:
+        tt = torch.tensor([t_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+        nn = torch.tensor([float(n_bin)], device="cuda")
+        dist.all_reduce(nn)
+        n_bin_all = float(nn.item())
+    else:
+        n_bin_all = float(n_bin)
+    value = n_bin_all / args.steps / (t_step * 1e-3)
+
+    # ---- end to end through the C ABI from host buffers ----
+    h2d = 0
+    for cat in preps:
+        for g in (cat["D"], cat["S"]):
+            h2d += 8 * 7 * g.n + 4 * g.n  # x y z w e1 e2 phi (f64), jk (i32); keep 1 B
+            h2d += g.n
+    d2h_hist = sum(c.shape[0] * c.shape[1] * c.shape[2] * (8 + 8 * _lib.NF) for c in ctxs)
+    d2h = d2h_hist + sum(20 * (cat["D"].n + cat["S"].n) for cat in preps)
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for c, cat in zip(ctxs, preps):
+            c.upload(0, cat["D"])
+            c.upload(1, cat["S"])
+        step()
+    e2e_t = (time.perf_counter() - t0) / e2e_steps
+    e2e_value = n_bin / args.steps / e2e_t
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    p = wls[0].params
+    peaks = _peaks()
+    F = metrics.FLOPS_PER_PAIR[p.which_corr]
+    A = metrics.smem_updates_per_pair(p.which_corr, bool(p.do_jk))
+    pair_s = tot_pair_ms / args.steps * 1e-3
+    n_per_step = n_bin / args.steps
+    achieved_flops = F * n_per_step / pair_s
+    achieved_atom = A * n_per_step / pair_s
+    roofline = {"bound": "fp32", "achieved": achieved_flops / 1e12,
+                "peak": (peaks["ffma_flops"] or float("nan")) / 1e12, "unit": "TFLOP/s",
+                "frac": achieved_flops / peaks["ffma_flops"] if peaks["ffma_flops"] else None,
+                "traffic": None,
+                "kernel": "fast_pairs_kernel", "kernel_ms_per_launch": tot_pair_ms / args.steps,
+                "work_per_pair": {"fp32_flops": F, "smem_atomic_updates": A},
+                "peak_source": "measured live in this run (FFMA microbenchmark); "
+                               "MEASURED_PEAKS.json has HBM and bf16 peaks only",
+                "smem_atomics": {"achieved": achieved_atom / 1e12,
+                                 "peak": (peaks["smem_atomic_u32_ops"] or float("nan")) / 1e12,
+                                 "unit": "Tops/s",
+                                 "frac": achieved_atom / peaks["smem_atomic_u32_ops"]
+                                 if peaks["smem_atomic_u32_ops"] else None}}
+    # plain FP64 GPU kernel on a bounded row sample of the same workload
+    fp64 = None
+    if len(ctxs) == 1:
+        est_rate = 1.5e8
+        stride = max(1, int(n_per_step / (est_rate * args.fp64_budget)))
+        r64 = ctxs[0].count("SD", 0, 1, engine="fp64", row_stride=stride)
+        fp64 = {"value": r64["n_binned"] / (r64["kernel_ms"] * 1e-3), "unit": UNIT,
+                "sample": f"every {stride}-th outer row: {r64['n_binned']} binned pairs in "
+                          f"{r64['kernel_ms']:.1f} ms"}
+        fp64["speedup_of_fast"] = value / fp64["value"]
+    cpu = None
+    if not args.no_cpu and len(wls) == 1:
+        cpu, _, _, _ = _cpu_sample(p, preps[0], args.cpu_budget, n_per_step,
+                                   os.cpu_count() or 1)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic (seeded generator, in memory)",
+            "config": _describe(wls), "n_binned_per_step": n_per_step,
+            "n_window_per_step": n_win / args.steps,
+            "roofline": roofline, "cpu_baseline": cpu, "fp64_gpu": fp64,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_t},
+            "gpu_launches": launches, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,992 @@
+// capi.cu -- the C ABI (include/corrpc.h): contexts, catalogue upload with the
+// on-device cell list, per-job set-up (the reference's corels2 rules, exact
+// thresholds and FP32 guard bands), work-unit construction and launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/corrpc.h"
+#include "cpc_device.cuh"
+#include "host_helpers.h"
+#include "kernels.h"
+
+using namespace cpc;
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_err;
+
+template <class T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    reset();
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * count);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    n = count;
+    return cudaSuccess;
+  }
+};
+
+struct Slot {
+  bool valid = false;
+  int64_t n = 0;
+  bool has_e = false, exact_f32 = true;
+  double wmax = 1.0, wmin = 1.0, emax = 0.0, cmax = 0.0, phimax = 0.0;
+  uint64_t version = 0;
+  // grid this cell list was built with
+  int ncx = 0, ncy = 0, n_reg = 1;
+  double cw_x = 0, cw_y = 0;
+  // device, cell order
+  DevBuf<float4> pos, shp;
+  DevBuf<float2> lo;
+  DevBuf<float> zf;
+  DevBuf<double> x, y, z, w, e1, e2, phi;
+  DevBuf<int32_t> jk;
+  DevBuf<uint8_t> keep;
+  DevBuf<int64_t> orig;
+  DevBuf<int> bk_start, bk_end, bk_region, col_begin, col_end;
+  DevBuf<float> bk_zmin, bk_zmax;
+  // host copies used to build work units
+  std::vector<float4> h_pos;
+  std::vector<int> h_bk_start, h_bk_end, h_bk_region;
+  // z-ordered FP64 copy for the plain kernel (built on first use)
+  bool zbuilt = false;
+  DevBuf<double> zx, zy, zz, zw, ze1, ze2, zphi;
+  DevBuf<int32_t> zjk;
+  DevBuf<uint8_t> zkeep;
+  DevBuf<int64_t> zorig;
+};
+
+struct UnitCache {
+  uint64_t v1 = 0, v2 = 0;
+  int s1 = -1, s2 = -1, wpi = 0, tile = 0;
+  std::vector<UnitDesc> units;  // job field filled at launch
+};
+
+}  // namespace
+
+struct cpc_ctx {
+  cpc_params p{};
+  std::vector<double> H, dA;
+  std::string err;
+  Slot slots[kMaxSlots];
+  uint64_t version_ctr = 0;
+  double ps = 0, rsize = 0;
+  double thr_rp[kMaxRp + 1];
+  double thr_pi[kMaxPi + 1];
+  int tune_k = 0, tune_wpi = 0, tune_tile = 0;
+  int device = 0, sm_count = 152;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  // scratch
+  DevBuf<JobDev> d_jobs;
+  DevBuf<UnitDesc> d_units;
+  DevBuf<unsigned int> d_unit_ctr;
+  DevBuf<QEntry> d_queue;
+  DevBuf<unsigned long long> d_qcount;
+  unsigned long long qcap = 0;
+  DevBuf<unsigned long long> d_num;
+  DevBuf<double> d_sums;
+  DevBuf<unsigned long long> d_counters;
+  // sort scratch
+  DevBuf<uint64_t> d_keys, d_ktmp;
+  DevBuf<uint32_t> d_vals, d_vtmp, d_hist, d_bucket;
+  DevBuf<unsigned long long> d_census;
+  std::vector<UnitCache> unit_cache;
+  int64_t launches = 0;  // kernels launched by this context (all entry points)
+};
+
+namespace {
+
+cpc_status fail(cpc_ctx *c, cpc_status s, const std::string &msg) {
+  if (c) c->err = msg;
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_err = msg;
+  return s;
+}
+
+cpc_status cuda_fail(cpc_ctx *c, cudaError_t e, const char *where) {
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return fail(c, CPC_ERR_NOMEM, m);
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return fail(c, CPC_ERR_NODEVICE, m);
+  return fail(c, CPC_ERR_CUDA, m);
+}
+
+#define CK(expr, where)                              \
+  do {                                               \
+    cudaError_t _e = (expr);                         \
+    if (_e != cudaSuccess) return cuda_fail(c, _e, where); \
+  } while (0)
+
+// float ULP at magnitude v (v > 0)
+double ulpf(double v) {
+  if (!(v > 0)) return std::ldexp(1.0, -149);
+  int ex;
+  std::frexp(v, &ex);  // v = m * 2^ex, m in [0.5, 1)
+  return std::ldexp(1.0, ex - 1 - 23);
+}
+float f_up(double v) {
+  float f = (float)v;
+  if ((double)f < v) f = std::nextafter(f, INFINITY);
+  return f;
+}
+float f_down(double v) {
+  float f = (float)v;
+  if ((double)f > v) f = std::nextafter(f, -INFINITY);
+  return f;
+}
+
+cpc_status validate_params(cpc_ctx *c, const cpc_params &p) {
+  if (p.coordinates != 6)
+    return fail(c, CPC_ERR_INVALID, "coordinates: only 6 (x,y,z with r_p, Pi) is supported by this build");
+  if (p.which_corr < 0 || p.which_corr > 2) return fail(c, CPC_ERR_INVALID, "which_corr must be 0, 1 or 2");
+  if (p.sig_crit != 0) return fail(c, CPC_ERR_INVALID, "sig_crit weights are not supported");
+  if (p.rand_subsample != 0) return fail(c, CPC_ERR_INVALID, "rand_subsample is not supported");
+  if (p.do_jk != 0 && p.do_jk != 1) return fail(c, CPC_ERR_INVALID, "do_jk must be 0 or 1");
+  if (p.do_jk && (p.n_jk <= 0 || p.n_jk > 100000)) return fail(c, CPC_ERR_INVALID, "n_jk out of range");
+  if (p.n_bins <= 0 || p.n_bins > kMaxRp) return fail(c, CPC_ERR_INVALID, "n_bins must be in 1..64");
+  if (p.n_p_bin <= 0 || p.n_p_bin > kMaxPi) return fail(c, CPC_ERR_INVALID, "n_p_bin must be in 1..128");
+  if (!(p.bin_r_max > p.bin_r_min) || !(p.bin_r_min >= 0) || (!p.lin_bin && !(p.bin_r_min > 0)))
+    return fail(c, CPC_ERR_INVALID, "bad r_p bin limits");
+  if (!(p.p_max > p.p_min)) return fail(c, CPC_ERR_INVALID, "bad Pi bin limits");
+  if (!(p.periodic_box_size > 0)) return fail(c, CPC_ERR_INVALID, "box size must be > 0");
+  if (p.periodic_box) {
+    const double L = p.periodic_box_size;
+    if (p.bin_r_max > L || p.p_max > L || -p.p_min > L)
+      return fail(c, CPC_ERR_INVALID, "bin limits larger than the periodic box");
+  }
+  return CPC_OK;
+}
+
+// corels2's pair-type rules (corr.cpp:226-296) and corel choice
+// (initialization.cpp:699-752).
+struct JobRule {
+  int corel, gws, swapped;
+};
+int job_rule(const cpc_params &p, cpc_pair_kind kind, int64_t n1, int64_t n2, JobRule &r) {
+  int gws = 0;
+  switch (kind) {
+    case CPC_PAIR_DRS: case CPC_PAIR_RSRD: case CPC_PAIR_RSRS: gws = 0; break;
+    case CPC_PAIR_SRD: case CPC_PAIR_SD: case CPC_PAIR_SRS: gws = 2; break;
+    default: return -1;
+  }
+  int corel;
+  if (kind == CPC_PAIR_RSRS || kind == CPC_PAIR_RSRD || p.which_corr == 0) corel = COREL_DD;
+  else if (p.which_corr == 1) corel = COREL_SD;
+  else corel = (kind == CPC_PAIR_SD) ? COREL_SS : COREL_SD;
+  if (corel == COREL_SS && p.estimator != 0) corel = COREL_SSA;
+  r.swapped = 0;
+  if (n2 > n1) {
+    r.swapped = 1;
+    if (gws == 2) gws = 1; else if (gws == 1) gws = 2;
+  }
+  r.corel = corel;
+  r.gws = gws;
+  return 0;
+}
+
+void fill_views(Slot &s, FCat &f, DCat &d) {
+  f.n = s.n;
+  f.pos = s.pos.p;
+  f.shp = s.shp.p;
+  f.lo = s.lo.p;
+  f.zf = s.zf.p;
+  f.keep = s.keep.p;
+  f.bk_start = s.bk_start.p;
+  f.bk_end = s.bk_end.p;
+  f.bk_region = s.bk_region.p;
+  f.bk_zmin = s.bk_zmin.p;
+  f.bk_zmax = s.bk_zmax.p;
+  f.col_begin = s.col_begin.p;
+  f.col_end = s.col_end.p;
+  d.n = s.n;
+  d.x = s.x.p; d.y = s.y.p; d.z = s.z.p; d.w = s.w.p;
+  d.e1 = s.e1.p; d.e2 = s.e2.p; d.phi = s.phi.p;
+  d.jk = s.jk.p; d.keep = s.keep.p; d.orig = s.orig.p;
+}
+
+// error bound (absolute, per coordinate difference) of the FP32 separations
+double eps_abs(const cpc_ctx *c, const Slot &a, const Slot &b) {
+  const cpc_params &p = c->p;
+  const double L = p.periodic_box_size;
+  const double cmax = std::max({a.cmax, b.cmax, L});
+  double e = 0;
+  if (!(a.exact_f32 && b.exact_f32)) e += ulpf(cmax);
+  const double wmax = std::max({p.bin_r_max, p.p_max, -p.p_min});
+  if (p.periodic_box && !(wmax <= 0.45 * L)) e += ulpf(2 * cmax);
+  return e;
+}
+
+struct JobPlan {
+  cpc_ctx *c;
+  cpc_pair_kind kind;
+  int s1, s2;  // after the swap
+  JobRule rule;
+  int wpi, tile;
+  int64_t row_stride, row_offset;
+  cpc_accum *out;
+  JobDev jd;
+  bool empty;
+};
+
+cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, int64_t rs,
+                    int64_t ro, cpc_accum *out, JobPlan &jp) {
+  if (slot_g1 < 0 || slot_g1 >= kMaxSlots || slot_g2 < 0 || slot_g2 >= kMaxSlots)
+    return fail(c, CPC_ERR_INVALID, "slot out of range");
+  Slot &A = c->slots[slot_g1], &B = c->slots[slot_g2];
+  if (!A.valid || !B.valid) return fail(c, CPC_ERR_STATE, "count before upload");
+  if (!out || !out->num || !out->sums) return fail(c, CPC_ERR_INVALID, "null output arrays");
+  const cpc_params &p = c->p;
+  jp.c = c;
+  jp.kind = kind;
+  jp.out = out;
+  jp.row_stride = rs > 1 ? rs : 1;
+  jp.row_offset = ro;
+  if (job_rule(p, kind, A.n, B.n, jp.rule) != 0) return fail(c, CPC_ERR_INVALID, "bad pair kind");
+  jp.s1 = jp.rule.swapped ? slot_g2 : slot_g1;
+  jp.s2 = jp.rule.swapped ? slot_g1 : slot_g2;
+  Slot &g1 = c->slots[jp.s1], &g2 = c->slots[jp.s2];
+  if (g1.ncx != g2.ncx || g1.ncy != g2.ncy || g1.n_reg != g2.n_reg)
+    return fail(c, CPC_ERR_STATE, "catalogues were uploaded with different cell grids");
+  jp.empty = (A.n == 0 || B.n == 0);
+  const int nrp = p.n_bins, npi = p.n_p_bin;
+  const int jk = p.do_jk ? 1 : 0;
+  // block-local Pi window: as many Pi bins as fit two blocks per SM
+  const size_t static_b = fast_static_smem_bytes();
+  const size_t budget = (size_t)(227 * 1024) / 2 - static_b - 1024;
+  int wpi = npi;
+  if (c->tune_wpi > 0) wpi = std::min(npi, c->tune_wpi);
+  else
+    while (wpi > 8 && fast_smem_bytes(jp.rule.corel, jk, nrp * wpi) > budget) wpi--;
+  if (wpi < npi && wpi < 8) wpi = std::min(npi, 8);
+  jp.wpi = wpi;
+  jp.tile = kTileThreads;
+
+  JobDev &J = jp.jd;
+  std::memset(&J, 0, sizeof J);
+  fill_views(g1, J.f1, J.d1);
+  fill_views(g2, J.f2, J.d2);
+  J.corel = jp.rule.corel;
+  J.gws = jp.rule.gws;
+  J.which_corr = p.which_corr;
+  J.estimator = p.estimator;
+  J.do_jk = jk;
+  J.n_jk = p.n_jk;
+  J.periodic = p.periodic_box ? 1 : 0;
+  J.coordinates = p.coordinates;
+  J.nrp = nrp;
+  J.npi = npi;
+  J.wpi = wpi;
+  J.lin_bin = p.lin_bin ? 1 : 0;
+  J.box_same_keep = 1;  // jk_check_PB (jk.cpp:64-71) for coordinates 6
+  J.has_lo = (g1.exact_f32 && g2.exact_f32) ? 0 : 1;
+  J.ncx = g1.ncx;
+  J.ncy = g1.ncy;
+  J.row_stride = jp.row_stride;
+  J.row_offset = jp.row_offset;
+  const double L = p.periodic_box_size;
+  J.L = L;
+  J.Lf = (float)L;
+  J.rmin = p.bin_r_min;
+  J.rmax = p.bin_r_max;
+  J.pmin = p.p_min;
+  J.pmax = p.p_max;
+  J.ps = c->ps;
+  J.rsize = c->rsize;
+  for (int k = 0; k <= nrp; k++) J.thr[k] = c->thr_rp[k];
+  // ---- guard bands (see pair_fast.cu): relative 2^-21 per coordinate
+  // difference, 2^-20 on r^2, plus the absolute representation/wrap error.
+  const double ea = eps_abs(c, g1, g2);
+  const double crel = std::ldexp(1.0, -21);
+  const double dtiny = 1e-12 * (L + std::max({p.bin_r_max, p.p_max, -p.p_min}));
+  const double gxy = crel * p.bin_r_max + 2 * ea + dtiny;
+  J.xy_in = f_down(p.bin_r_max - gxy);
+  J.xy_out = f_up(p.bin_r_max + gxy);
+  auto gp = [&](double v) { return crel * std::fabs(v) + 2 * ea + dtiny + 1e-30; };
+  J.pi_in_lo = f_up(p.p_min + gp(p.p_min));
+  J.pi_out_lo = f_down(p.p_min - gp(p.p_min));
+  J.pi_in_hi = f_down(p.p_max - gp(p.p_max));
+  J.pi_out_hi = f_up(p.p_max + gp(p.p_max));
+  for (int k = 0; k < npi; k++) {
+    const double lo = c->thr_pi[k], hi = c->thr_pi[k + 1];
+    J.PA[k] = f_up(lo + gp(lo));
+    J.PB[k] = f_down(hi - gp(hi));
+  }
+  J.inv_ps_f = (float)(1.0 / c->ps);
+  J.tp0 = (float)(-p.p_min / c->ps);
+  auto gr = [&](double T) {
+    return std::ldexp(1.0, -20) * T * T + 2.0 * std::sqrt(2.0) * T * ea + 2 * ea * ea + 1e-12 * T * T;
+  };
+  for (int k = 0; k < nrp; k++) {
+    const double lo = c->thr_rp[k], hi = c->thr_rp[k + 1];
+    J.A[k] = f_up(lo * lo + gr(lo));
+    J.B[k] = f_down(hi * hi - gr(hi));
+  }
+  J.rej_lo = f_down(c->thr_rp[0] * c->thr_rp[0] - gr(c->thr_rp[0]));
+  J.rej_hi = f_up(c->thr_rp[nrp] * c->thr_rp[nrp] + gr(c->thr_rp[nrp]));
+  J.rmin_f = (float)p.bin_r_min;
+  J.inv_rsize_f = (float)(1.0 / c->rsize);
+  if (p.lin_bin) {  // linear bins: estimate index from r, bands still decide
+    J.l2rmin2 = 0.f;
+    J.inv_lw = 0.f;
+  } else {
+    J.l2rmin2 = (float)(2.0 * std::log2(p.bin_r_min));
+    J.inv_lw = (float)(1.0 / (2.0 * std::log2(p.bin_r_max / p.bin_r_min) / nrp));
+  }
+  // fixed-point scales: field f's terms are rint(v 2^S_f) + B with
+  // B = 2^26 >= max|v_f| 2^S_f (see pair_fast.cu); S_f from a bound on |v_f|
+  {
+    const double wm = std::max(g1.wmax, 1e-30) * std::max(g2.wmax, 1e-30);
+    const double em = std::max({g1.emax, g2.emax, 1e-30});
+    // |phi - theta| folded (calcs.cpp:97-105): phi = -10 for galaxies read
+    // without shapes gives values outside [0, pi/2]
+    const double tm = std::max(M_PI / 2, std::max(g1.phimax, g2.phimax) + M_PI);
+    const double tm2 = (jp.rule.corel == COREL_SSA) ? 2 * tm : tm;
+    double vb[kNF];
+    vb[0] = wm;
+    vb[1] = vb[3] = wm * em;
+    vb[2] = vb[4] = wm * wm * em * em;
+    vb[5] = vb[7] = vb[9] = wm * em * em;
+    vb[6] = vb[8] = vb[10] = wm * wm * em * em * em * em;
+    vb[11] = tm2;
+    vb[12] = 2 * tm * tm;
+    for (int f = 0; f < kNF; f++) {
+      const double v = std::max(vb[f] * 1.0001, 1e-30);
+      int S = 26 - (int)std::ceil(std::log2(v));
+      S = std::min(60, std::max(-60, S));
+      J.qscale[f] = (float)std::ldexp(1.0, S);
+      J.inv_qscale[f] = std::ldexp(1.0, -S);
+    }
+  }
+  J.qbias = 1 << 26;
+  J.unit_w = (g1.wmax == 1.0 && g1.wmin == 1.0 && g2.wmax == 1.0 && g2.wmin == 1.0) ? 1 : 0;
+  return CPC_OK;
+}
+
+// tiles of g1 rows and their units (cached per slot versions and window)
+const std::vector<UnitDesc> &build_units(JobPlan &jp) {
+  cpc_ctx *c = jp.c;
+  for (auto &uc : c->unit_cache)
+    if (uc.s1 == jp.s1 && uc.s2 == jp.s2 && uc.v1 == c->slots[jp.s1].version &&
+        uc.v2 == c->slots[jp.s2].version && uc.wpi == jp.wpi && uc.tile == jp.tile)
+      return uc.units;
+  if (c->unit_cache.size() >= 8) c->unit_cache.erase(c->unit_cache.begin());
+  c->unit_cache.emplace_back();
+  UnitCache &uc = c->unit_cache.back();
+  uc.s1 = jp.s1;
+  uc.s2 = jp.s2;
+  uc.v1 = c->slots[jp.s1].version;
+  uc.v2 = c->slots[jp.s2].version;
+  uc.wpi = jp.wpi;
+  uc.tile = jp.tile;
+  const cpc_params &p = c->p;
+  const Slot &g1 = c->slots[jp.s1];
+  const double L = p.periodic_box_size;
+  const double ps = c->ps;
+  const int npi = p.n_p_bin, wpi = jp.wpi;
+  const double cmax = std::max(g1.cmax, L);
+  const double ea = eps_abs(c, g1, c->slots[jp.s2]);
+  const double guard = 4 * ulpf(2 * cmax) + 2 * ea + std::ldexp(1.0, -20) * (std::fabs(p.p_min) + std::fabs(p.p_max) + p.bin_r_max);
+  // tile z-extent: wide enough that the 32 lanes of a warp (spread over the
+  // tile) see different Pi bins, small enough to fit the block-local window
+  double Emax = 0.25 * (p.p_max - p.p_min);
+  if (wpi < npi) Emax = std::min(Emax, (wpi - 6) * ps / 2.0);
+  Emax = std::max(Emax, std::min(2.0 * ps, 0.25 * (p.p_max - p.p_min)));
+  const int ncx = g1.ncx, ncy = g1.ncy;
+  const double inv_cwx = 1.0 / g1.cw_x, inv_cwy = 1.0 / g1.cw_y;
+  std::vector<UnitDesc> &units = uc.units;
+  units.clear();
+  const int nb = (int)g1.h_bk_start.size();
+  for (int b = 0; b < nb; b++) {
+    const int s = g1.h_bk_start[b], e = g1.h_bk_end[b];
+    int i = s;
+    while (i < e) {
+      // z-chunk of extent <= Emax, dealt round-robin into tiles of <= tile rows
+      const float z0 = g1.h_pos[i].z;
+      int j = i;
+      float bx0 = INFINITY, bx1 = -INFINITY, by0 = INFINITY, by1 = -INFINITY;
+      while (j < e && (double)g1.h_pos[j].z - z0 <= Emax) {
+        bx0 = std::min(bx0, g1.h_pos[j].x);
+        bx1 = std::max(bx1, g1.h_pos[j].x);
+        by0 = std::min(by0, g1.h_pos[j].y);
+        by1 = std::max(by1, g1.h_pos[j].y);
+        j++;
+      }
+      const int m = j - i;
+      const int nt = (m + jp.tile - 1) / jp.tile;
+      const double zt0 = g1.h_pos[i].z, zt1 = g1.h_pos[j - 1].z;
+      const double rg = p.bin_r_max + guard;
+      int cx0 = (int)std::floor((bx0 - rg) * inv_cwx), cx1 = (int)std::floor((bx1 + rg) * inv_cwx);
+      int cy0 = (int)std::floor((by0 - rg) * inv_cwy), cy1 = (int)std::floor((by1 + rg) * inv_cwy);
+      if (p.periodic_box) {
+        cx0 = std::max(cx0, -ncx); cx1 = std::min(cx1, 2 * ncx - 1);
+        cy0 = std::max(cy0, -ncy); cy1 = std::min(cy1, 2 * ncy - 1);
+      } else {
+        cx0 = std::max(cx0, 0); cx1 = std::min(cx1, ncx - 1);
+        cy0 = std::max(cy0, 0); cy1 = std::min(cy1, ncy - 1);
+      }
+      const double Zlo = zt0 + p.p_min - guard, Zhi = zt1 + p.p_max + guard;
+      for (int k = 0; k < nt; k++) {
+        UnitDesc u;
+        std::memset(&u, 0, sizeof u);
+        u.g1_start = i + k;
+        u.g1_stride = nt;
+        u.g1_count = (m - k + nt - 1) / nt;
+        u.region = g1.h_bk_region[b];
+        u.cx_lo = cx0; u.cx_hi = cx1; u.cy_lo = cy0; u.cy_hi = cy1;
+        if (wpi >= npi) {
+          u.n2_base = 0;
+          u.zlo = Zlo;
+          u.zhi = Zhi;
+          units.push_back(u);
+        } else {
+          const double span = std::max(ps, (wpi - 4) * ps - (zt1 - zt0));
+          const int U = std::max(1, (int)std::ceil((Zhi - Zlo) / span));
+          for (int q = 0; q < U; q++) {
+            const double a = (q == 0) ? Zlo : Zlo + (Zhi - Zlo) * q / U;
+            const double bnd = (q == U - 1) ? Zhi : Zlo + (Zhi - Zlo) * (q + 1) / U;
+            int base = (int)std::floor((a - zt1 - p.p_min) / ps) - 1;
+            base = std::max(0, std::min(base, npi - wpi));
+            u.n2_base = base;
+            u.zlo = a;
+            u.zhi = bnd;
+            units.push_back(u);
+          }
+        }
+      }
+      i = j;
+    }
+  }
+  return units;
+}
+
+cpc_status ensure_scratch(cpc_ctx *c, size_t n_units, size_t n_jobs) {
+  CK(c->d_units.alloc(n_units), "alloc units");
+  CK(c->d_jobs.alloc(n_jobs), "alloc jobs");
+  CK(c->d_unit_ctr.alloc(1), "alloc counter");
+  CK(c->d_qcount.alloc(1), "alloc queue counter");
+  if (!c->d_queue.p) {
+    c->qcap = 1ull << 24;
+    cudaError_t e = c->d_queue.alloc(c->qcap);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      c->qcap = 1ull << 20;
+      CK(c->d_queue.alloc(c->qcap), "alloc edge queue");
+    }
+  }
+  return CPC_OK;
+}
+
+cpc_status alloc_accum(cpc_ctx *c) {
+  const cpc_params &p = c->p;
+  const size_t n_hist = 1 + (p.do_jk ? p.n_jk : 0);
+  const size_t cells = n_hist * p.n_bins * p.n_p_bin;
+  CK(c->d_num.alloc(cells), "alloc accum");
+  CK(c->d_sums.alloc(cells * kNF), "alloc accum");
+  CK(c->d_counters.alloc(4), "alloc counters");
+  return CPC_OK;
+}
+
+cpc_status zero_accum(cpc_ctx *c, cudaStream_t st) {
+  const cpc_params &p = c->p;
+  const size_t n_hist = 1 + (p.do_jk ? p.n_jk : 0);
+  const size_t cells = n_hist * p.n_bins * p.n_p_bin;
+  CK(cudaMemsetAsync(c->d_num.p, 0, sizeof(unsigned long long) * cells, st), "memset");
+  CK(cudaMemsetAsync(c->d_sums.p, 0, sizeof(double) * cells * kNF, st), "memset");
+  CK(cudaMemsetAsync(c->d_counters.p, 0, sizeof(unsigned long long) * 4, st), "memset");
+  return CPC_OK;
+}
+
+cpc_status fetch_accum(cpc_ctx *c, cpc_accum *out, cudaStream_t st, int unit_w) {
+  const cpc_params &p = c->p;
+  const size_t n_hist = 1 + (p.do_jk ? p.n_jk : 0);
+  const size_t cells = n_hist * p.n_bins * p.n_p_bin;
+  unsigned long long cnt[4];
+  CK(cudaMemcpyAsync(out->num, c->d_num.p, sizeof(int64_t) * cells, cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaMemcpyAsync(out->sums, c->d_sums.p, sizeof(double) * cells * kNF, cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaMemcpyAsync(cnt, c->d_counters.p, sizeof cnt, cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "sync");
+  if (unit_w)
+    for (size_t k = 0; k < cells; k++) out->sums[k * kNF] = (double)out->num[k];
+  out->n_window = (int64_t)(cnt[0] + cnt[1]);
+  out->n_rechecked = (int64_t)cnt[2];
+  int64_t nb = 0;
+  const size_t c0 = (size_t)p.n_bins * p.n_p_bin;
+  for (size_t k = 0; k < c0; k++) nb += out->num[k];
+  out->n_binned = nb;
+  return CPC_OK;
+}
+
+cpc_status build_zorder(cpc_ctx *c, Slot &s) {
+  if (s.zbuilt) return CPC_OK;
+  const int64_t n = s.n;
+  cudaStream_t st = c->st;
+  CK(c->d_keys.alloc(n), "alloc");
+  CK(c->d_ktmp.alloc(n), "alloc");
+  CK(c->d_vals.alloc(n), "alloc");
+  CK(c->d_vtmp.alloc(n), "alloc");
+  CK(c->d_hist.alloc(radix_hist_words(n)), "alloc");
+  CK(c->d_census.alloc(8 * 256), "alloc");
+  CK(launch_z_keys(n, s.z.p, c->d_keys.p, c->d_vals.p, st), "z keys");
+  CK(radix_sort_pairs(n, c->d_keys.p, c->d_vals.p, c->d_ktmp.p, c->d_vtmp.p, c->d_hist.p,
+                      c->d_census.p, st, &c->launches), "z sort");
+  c->launches += 2;  // z keys + gather
+  CK(s.zx.alloc(n), "alloc"); CK(s.zy.alloc(n), "alloc"); CK(s.zz.alloc(n), "alloc");
+  CK(s.zw.alloc(n), "alloc"); CK(s.ze1.alloc(n), "alloc"); CK(s.ze2.alloc(n), "alloc");
+  CK(s.zphi.alloc(n), "alloc"); CK(s.zjk.alloc(n), "alloc"); CK(s.zkeep.alloc(n), "alloc");
+  CK(s.zorig.alloc(n), "alloc");
+  GatherIn in{s.x.p, s.y.p, s.z.p, s.w.p, s.e1.p, s.e2.p, s.phi.p, s.jk.p, s.keep.p};
+  GatherOut out{};
+  out.x = s.zx.p; out.y = s.zy.p; out.z = s.zz.p; out.w = s.zw.p;
+  out.e1 = s.ze1.p; out.e2 = s.ze2.p; out.phi = s.zphi.p; out.jk = s.zjk.p;
+  out.keep = s.zkeep.p; out.orig = s.zorig.p; out.orig_in = s.orig.p;
+  CK(launch_gather(n, c->d_keys.p, c->d_vals.p, in, out, st), "z gather");
+  CK(cudaStreamSynchronize(st), "sync");
+  s.zbuilt = true;
+  return CPC_OK;
+}
+
+DCat zview(Slot &s) {
+  DCat d;
+  d.n = s.n;
+  d.x = s.zx.p; d.y = s.zy.p; d.z = s.zz.p; d.w = s.zw.p;
+  d.e1 = s.ze1.p; d.e2 = s.ze2.p; d.phi = s.zphi.p;
+  d.jk = s.zjk.p; d.keep = s.zkeep.p; d.orig = s.zorig.p;
+  return d;
+}
+
+cpc_status run_plain(JobPlan &jp) {
+  cpc_ctx *c = jp.c;
+  cpc_status s;
+  if ((s = alloc_accum(c)) != CPC_OK) return s;
+  if ((s = zero_accum(c, c->st)) != CPC_OK) return s;
+  if (jp.empty) return fetch_accum(c, jp.out, c->st, 0);
+  Slot &g1 = c->slots[jp.s1], &g2 = c->slots[jp.s2];
+  if ((s = build_zorder(c, g1)) != CPC_OK) return s;
+  if ((s = build_zorder(c, g2)) != CPC_OK) return s;
+  if ((s = ensure_scratch(c, 1, 1)) != CPC_OK) return s;
+  jp.jd.acc_num = c->d_num.p;
+  jp.jd.acc_sums = c->d_sums.p;
+  jp.jd.counters = c->d_counters.p;
+  DCat a = zview(g1), b = zview(g2);
+  jp.jd.d1 = a;
+  jp.jd.d2 = b;
+  CK(cudaMemcpyAsync(c->d_jobs.p, &jp.jd, sizeof(JobDev), cudaMemcpyHostToDevice, c->st), "H2D job");
+  CK(cudaEventRecord(c->e0, c->st), "event");
+  CK(launch_plain_fp64(c->d_jobs.p, a, b, c->st), "plain fp64 kernel");
+  c->launches += 1;
+  CK(cudaEventRecord(c->e1, c->st), "event");
+  if ((s = fetch_accum(c, jp.out, c->st, 0)) != CPC_OK) return s;
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->e0, c->e1), "event time");
+  jp.out->kernel_ms = ms;
+  jp.out->pair_kernel_ms = ms;
+  return CPC_OK;
+}
+
+// fast engine over one or more jobs (one persistent launch per corel group)
+cpc_status run_fast(std::vector<JobPlan> &jobs) {
+  cpc_ctx *c0 = jobs[0].c;
+  cpc_ctx *c = c0;
+  cudaStream_t st = c0->st;
+  std::vector<UnitDesc> all;
+  for (size_t k = 0; k < jobs.size(); k++) {
+    cpc_status s;
+    if ((s = alloc_accum(jobs[k].c)) != CPC_OK) return s;
+    if ((s = zero_accum(jobs[k].c, st)) != CPC_OK) return s;
+    jobs[k].jd.acc_num = jobs[k].c->d_num.p;
+    jobs[k].jd.acc_sums = jobs[k].c->d_sums.p;
+    jobs[k].jd.counters = jobs[k].c->d_counters.p;
+  }
+  // group by kernel template
+  std::map<std::pair<int, int>, std::vector<int>> groups;
+  for (size_t k = 0; k < jobs.size(); k++)
+    if (!jobs[k].empty) groups[{jobs[k].jd.corel, jobs[k].jd.do_jk}].push_back((int)k);
+  size_t total_units = 0;
+  std::vector<std::pair<size_t, size_t>> ranges;
+  std::vector<std::pair<int, int>> gkeys;
+  for (auto &g : groups) {
+    const size_t b = all.size();
+    for (int k : g.second) {
+      const std::vector<UnitDesc> &u = build_units(jobs[k]);
+      for (UnitDesc d : u) {
+        d.job = k;
+        const int64_t ncol = (int64_t)(d.cx_hi - d.cx_lo + 1) * (d.cy_hi - d.cy_lo + 1);
+        if (ncol < 1 || ncol > 1024 || d.g1_count < 1 || d.g1_count > kTileThreads)
+          return fail(c, CPC_ERR_INVALID, "work unit outside kernel limits (too many neighbour columns)");
+        all.push_back(d);
+      }
+    }
+    ranges.push_back({b, all.size()});
+    gkeys.push_back(g.first);
+  }
+  total_units = all.size();
+  cpc_status s;
+  if ((s = ensure_scratch(c0, std::max<size_t>(1, total_units), jobs.size())) != CPC_OK) return s;
+  std::vector<JobDev> jds(jobs.size());
+  for (size_t k = 0; k < jobs.size(); k++) jds[k] = jobs[k].jd;
+  CK(cudaMemcpyAsync(c0->d_jobs.p, jds.data(), sizeof(JobDev) * jds.size(), cudaMemcpyHostToDevice, st), "H2D jobs");
+  if (total_units)
+    CK(cudaMemcpyAsync(c0->d_units.p, all.data(), sizeof(UnitDesc) * total_units, cudaMemcpyHostToDevice, st), "H2D units");
+  CK(cudaMemsetAsync(c0->d_qcount.p, 0, sizeof(unsigned long long), st), "memset");
+  CK(cudaEventRecord(c0->e0, st), "event");
+  for (size_t g = 0; g < ranges.size(); g++) {
+    const int corel = gkeys[g].first, jk = gkeys[g].second;
+    int wmax = 0;
+    for (size_t k = ranges[g].first; k < ranges[g].second; k++) {
+      const JobPlan &jp = jobs[all[k].job];
+      wmax = std::max(wmax, jp.wpi * jp.jd.nrp);
+    }
+    const size_t smem = fast_smem_bytes(corel, jk, wmax);
+    int bps = fast_blocks_per_sm(corel, jk, smem);
+    if (bps <= 0) return fail(c, CPC_ERR_INVALID, "fast kernel does not fit on an SM with these bins");
+    const int n_units = (int)(ranges[g].second - ranges[g].first);
+    const int grid = (int)std::min<int64_t>((int64_t)c0->sm_count * bps, n_units);
+    CK(cudaMemsetAsync(c0->d_unit_ctr.p, 0, sizeof(unsigned int), st), "memset");
+    CK(launch_fast(corel, jk, c0->d_jobs.p, c0->d_units.p + ranges[g].first, n_units,
+                   c0->d_unit_ctr.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, smem, grid, st),
+       "fast kernel");
+    c0->launches += 1;
+  }
+  CK(cudaEventRecord(c0->e2, st), "event");
+  CK(launch_recheck(c0->d_jobs.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, c0->sm_count * 8, st),
+     "recheck kernel");
+  c0->launches += 1;
+  CK(cudaEventRecord(c0->e1, st), "event");
+  CK(cudaStreamSynchronize(st), "fast kernels");
+  float ms = 0, pms = 0;
+  CK(cudaEventElapsedTime(&ms, c0->e0, c0->e1), "event time");
+  CK(cudaEventElapsedTime(&pms, c0->e0, c0->e2), "event time");
+  unsigned long long qn = 0;
+  CK(cudaMemcpy(&qn, c0->d_qcount.p, sizeof qn, cudaMemcpyDeviceToHost), "D2H");
+  for (size_t k = 0; k < jobs.size(); k++) {
+    if ((s = fetch_accum(jobs[k].c, jobs[k].out, st, jobs[k].jd.unit_w)) != CPC_OK) return s;
+    jobs[k].out->kernel_ms = ms;
+    jobs[k].out->pair_kernel_ms = pms;
+    if (qn > c0->qcap) jobs[k].out->n_rechecked += (int64_t)(qn - c0->qcap);
+  }
+  return CPC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cpc_version(void) { return "corr_pc_gb300 0.1 (sm_103a)"; }
+
+const char *cpc_last_error(const cpc_ctx *ctx) {
+  if (ctx) return ctx->err.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_err.c_str();
+}
+
+cpc_status cpc_create(cpc_ctx **out, const cpc_params *params) {
+  if (!out || !params) return fail(nullptr, CPC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  cpc_status s = validate_params(nullptr, *params);
+  if (s != CPC_OK) return s;
+  std::unique_ptr<cpc_ctx> c(new (std::nothrow) cpc_ctx());
+  if (!c) return fail(nullptr, CPC_ERR_NOMEM, "host allocation failed");
+  c->p = *params;
+  if (params->H_z && params->n_table > 0) {
+    c->H.assign(params->H_z, params->H_z + params->n_table);
+    c->p.H_z = c->H.data();
+  }
+  if (params->dA_z && params->n_table > 0) {
+    c->dA.assign(params->dA_z, params->dA_z + params->n_table);
+    c->p.dA_z = c->dA.data();
+  }
+  const cpc_params &p = c->p;
+  c->ps = (p.p_max - p.p_min) / (p.n_p_bin);
+  if (p.lin_bin) c->rsize = (p.bin_r_max - p.bin_r_min) / p.n_bins;
+  else c->rsize = (std::log10(p.bin_r_max) - std::log10(p.bin_r_min)) / p.n_bins;
+  int rc = rp_thresholds(p.lin_bin, p.n_bins, p.bin_r_min, p.bin_r_max, c->thr_rp);
+  if (rc != 0) return fail(nullptr, CPC_ERR_INVALID, "r_p bin thresholds could not be derived (non-monotone bin function)");
+  rc = pi_thresholds(p.n_p_bin, p.p_min, p.p_max, c->thr_pi);
+  if (rc != 0) return fail(nullptr, CPC_ERR_INVALID, "Pi bin thresholds could not be derived");
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDevice");
+  e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "device attribute");
+  e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "stream");
+  e = cudaEventCreate(&c->e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->e1);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->e2);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "event");
+  *out = c.release();
+  return CPC_OK;
+}
+
+cpc_status cpc_destroy(cpc_ctx *c) {
+  if (!c) return CPC_OK;
+  cudaStreamSynchronize(c->st);
+  if (c->e0) cudaEventDestroy(c->e0);
+  if (c->e1) cudaEventDestroy(c->e1);
+  if (c->e2) cudaEventDestroy(c->e2);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return CPC_OK;
+}
+
+cpc_status cpc_accum_shape(const cpc_ctx *c, int *n_hist, int *n_bins, int *n_p_bin) {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (n_hist) *n_hist = 1 + (c->p.do_jk ? c->p.n_jk : 0);
+  if (n_bins) *n_bins = c->p.n_bins;
+  if (n_p_bin) *n_p_bin = c->p.n_p_bin;
+  return CPC_OK;
+}
+
+cpc_status cpc_set_tuning(cpc_ctx *c, int cells_per_rmax, int pi_window, int tile) {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (cells_per_rmax < 0 || cells_per_rmax > 16 || pi_window < 0 || (tile != 0 && tile != kTileThreads))
+    return fail(c, CPC_ERR_INVALID, "tuning values out of range");
+  c->tune_k = cells_per_rmax;
+  c->tune_wpi = pi_window;
+  c->tune_tile = tile;
+  return CPC_OK;
+}
+
+cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
+  if (!c || !cat) return fail(c, CPC_ERR_INVALID, "null argument");
+  if (slot < 0 || slot >= kMaxSlots) return fail(c, CPC_ERR_INVALID, "slot out of range");
+  const cpc_params &p = c->p;
+  const int64_t n = cat->n;
+  if (n < 0 || n >= 2147483647LL) return fail(c, CPC_ERR_INVALID, "catalogue size out of range");
+  if (n > 0 && (!cat->x || !cat->y || !cat->z)) return fail(c, CPC_ERR_INVALID, "null positions");
+  if (p.do_jk && n > 0 && !cat->jk) return fail(c, CPC_ERR_INVALID, "jackknife labels required (do_jk=1)");
+  Slot &s = c->slots[slot];
+  s.valid = false;
+  s.zbuilt = false;
+  s.n = n;
+  s.version = ++c->version_ctr;
+  const double L = p.periodic_box_size;
+  // host-side validation and derived per-galaxy arrays
+  std::vector<double> w(n, 1.0), e1(n, 0.0), e2(n, 0.0), phi(n, -10.0);
+  std::vector<int32_t> jk(n, 0);
+  std::vector<uint8_t> keep(n, 0);
+  s.has_e = cat->e1 && cat->e2;
+  s.exact_f32 = true;
+  s.wmax = 0;
+  s.phimax = 0.0;
+  s.wmin = n > 0 ? 1e300 : 1.0;
+  s.emax = 0;
+  s.cmax = 0;
+  for (int64_t i = 0; i < n; i++) {
+    const double x = cat->x[i], y = cat->y[i], z = cat->z[i];
+    if (!std::isfinite(x) || !std::isfinite(y) || !std::isfinite(z))
+      return fail(c, CPC_ERR_RANGE, "non-finite position at row " + std::to_string(i));
+    if (x < 0 || y < 0 || z < 0 || x > L || y > L || z > L)
+      return fail(c, CPC_ERR_RANGE, "position outside [0, box_size] at row " + std::to_string(i));
+    if ((double)(float)x != x || (double)(float)y != y || (double)(float)z != z) s.exact_f32 = false;
+    s.cmax = std::max(s.cmax, std::max(x, std::max(y, z)));
+    if (cat->w) {
+      if (!std::isfinite(cat->w[i])) return fail(c, CPC_ERR_RANGE, "non-finite weight");
+      w[i] = cat->w[i];
+    }
+    s.wmax = std::max(s.wmax, std::fabs(w[i]));
+    s.wmin = std::min(s.wmin, w[i]);
+    if (s.has_e) {
+      if (!std::isfinite(cat->e1[i]) || !std::isfinite(cat->e2[i])) return fail(c, CPC_ERR_RANGE, "non-finite ellipticity");
+      e1[i] = cat->e1[i];
+      e2[i] = cat->e2[i];
+      s.emax = std::max(s.emax, std::max(std::fabs(e1[i]), std::fabs(e2[i])));
+    }
+    if (cat->phi) {
+      if (!std::isfinite(cat->phi[i])) return fail(c, CPC_ERR_RANGE, "non-finite phi");
+      phi[i] = cat->phi[i];
+    }
+    s.phimax = std::max(s.phimax, std::fabs(phi[i]));
+    if (p.do_jk) {
+      const int r = cat->jk[i];
+      if (r < 0 || r >= p.n_jk)
+        return fail(c, CPC_ERR_RANGE, "jackknife label out of range at row " + std::to_string(i));
+      jk[i] = r;
+    }
+    if (cat->jk_prob) keep[i] = cat->jk_prob[i] >= 0.5 ? 1 : 0;
+  }
+  // grid: columns of width >= r_max / k over [0, box)
+  const int k = c->tune_k > 0 ? c->tune_k : 2;
+  int nc = (int)std::floor(L / (p.bin_r_max / k));
+  nc = std::max(1, std::min(nc, 2048));
+  s.ncx = s.ncy = nc;
+  s.cw_x = s.cw_y = L / nc;
+  s.n_reg = p.do_jk ? p.n_jk : 1;
+  if ((double)nc * nc * s.n_reg >= 4294967295.0) return fail(c, CPC_ERR_INVALID, "too many cell buckets");
+  cudaStream_t st = c->st;
+  // device originals (temporary) + sort scratch
+  DevBuf<double> ox, oy, oz, ow, oe1, oe2, ophi;
+  DevBuf<int32_t> ojk;
+  DevBuf<uint8_t> okeep;
+  const size_t nn = std::max<int64_t>(n, 1);
+  CK(ox.alloc(nn), "alloc"); CK(oy.alloc(nn), "alloc"); CK(oz.alloc(nn), "alloc");
+  CK(ow.alloc(nn), "alloc"); CK(oe1.alloc(nn), "alloc"); CK(oe2.alloc(nn), "alloc");
+  CK(ophi.alloc(nn), "alloc"); CK(ojk.alloc(nn), "alloc"); CK(okeep.alloc(nn), "alloc");
+  if (n > 0) {
+    CK(cudaMemcpyAsync(ox.p, cat->x, 8 * n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(oy.p, cat->y, 8 * n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(oz.p, cat->z, 8 * n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(ow.p, w.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(oe1.p, e1.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(oe2.p, e2.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(ophi.p, phi.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(ojk.p, jk.data(), 4 * n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(okeep.p, keep.data(), n, cudaMemcpyHostToDevice, st), "H2D");
+  }
+  CK(c->d_keys.alloc(nn), "alloc"); CK(c->d_ktmp.alloc(nn), "alloc");
+  CK(c->d_vals.alloc(nn), "alloc"); CK(c->d_vtmp.alloc(nn), "alloc");
+  CK(c->d_hist.alloc(radix_hist_words(nn)), "alloc");
+  CK(c->d_census.alloc(8 * 256), "alloc");
+  CK(c->d_bucket.alloc(nn), "alloc");
+  CK(s.pos.alloc(nn), "alloc"); CK(s.shp.alloc(nn), "alloc"); CK(s.zf.alloc(nn), "alloc");
+  CK(s.lo.alloc(nn), "alloc");
+  CK(s.x.alloc(nn), "alloc"); CK(s.y.alloc(nn), "alloc"); CK(s.z.alloc(nn), "alloc");
+  CK(s.w.alloc(nn), "alloc"); CK(s.e1.alloc(nn), "alloc"); CK(s.e2.alloc(nn), "alloc");
+  CK(s.phi.alloc(nn), "alloc"); CK(s.jk.alloc(nn), "alloc"); CK(s.keep.alloc(nn), "alloc");
+  CK(s.orig.alloc(nn), "alloc");
+  CK(launch_cell_keys(n, ox.p, oy.p, oz.p, ojk.p, 1.0 / s.cw_x, 1.0 / s.cw_y, s.ncx, s.ncy, s.n_reg,
+                      c->d_keys.p, c->d_vals.p, st), "cell keys");
+  CK(radix_sort_pairs(n, c->d_keys.p, c->d_vals.p, c->d_ktmp.p, c->d_vtmp.p, c->d_hist.p,
+                      c->d_census.p, st, &c->launches), "radix sort");
+  if (n > 0) c->launches += 2;  // cell keys + gather
+  GatherIn in{ox.p, oy.p, oz.p, ow.p, oe1.p, oe2.p, ophi.p, ojk.p, okeep.p};
+  GatherOut go{};
+  go.pos = s.pos.p; go.shp = s.shp.p; go.lo = s.lo.p; go.zf = s.zf.p; go.bucket = c->d_bucket.p;
+  go.x = s.x.p; go.y = s.y.p; go.z = s.z.p; go.w = s.w.p; go.e1 = s.e1.p; go.e2 = s.e2.p;
+  go.phi = s.phi.p; go.jk = s.jk.p; go.keep = s.keep.p; go.orig = s.orig.p; go.orig_in = nullptr;
+  CK(launch_gather(n, c->d_keys.p, c->d_vals.p, in, go, st), "gather");
+  // buckets on the host
+  std::vector<uint32_t> hb(n);
+  s.h_pos.resize(n);
+  if (n > 0) {
+    CK(cudaMemcpyAsync(hb.data(), c->d_bucket.p, 4 * n, cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(s.h_pos.data(), s.pos.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, st), "D2H");
+  }
+  CK(cudaStreamSynchronize(st), "upload");
+  s.h_bk_start.clear(); s.h_bk_end.clear(); s.h_bk_region.clear();
+  std::vector<float> bz0, bz1;
+  const int ncol = s.ncx * s.ncy;
+  std::vector<int> cb(ncol, 0), ce(ncol, 0);
+  for (int64_t i = 0; i < n;) {
+    int64_t j = i + 1;
+    while (j < n && hb[j] == hb[i]) j++;
+    const int b = (int)s.h_bk_start.size();
+    const int col = (int)(hb[i] / s.n_reg), reg = (int)(hb[i] % s.n_reg);
+    if (ce[col] == 0 && cb[col] == 0) cb[col] = b;
+    ce[col] = b + 1;
+    s.h_bk_start.push_back((int)i);
+    s.h_bk_end.push_back((int)j);
+    s.h_bk_region.push_back(reg);
+    bz0.push_back(s.h_pos[i].z);
+    bz1.push_back(s.h_pos[j - 1].z);
+    i = j;
+  }
+  // columns with no bucket: empty range
+  for (int q = 0; q < ncol; q++)
+    if (ce[q] == 0) cb[q] = 0;
+  const size_t nbk = std::max<size_t>(1, s.h_bk_start.size());
+  CK(s.bk_start.alloc(nbk), "alloc"); CK(s.bk_end.alloc(nbk), "alloc");
+  CK(s.bk_region.alloc(nbk), "alloc"); CK(s.bk_zmin.alloc(nbk), "alloc");
+  CK(s.bk_zmax.alloc(nbk), "alloc"); CK(s.col_begin.alloc(ncol), "alloc");
+  CK(s.col_end.alloc(ncol), "alloc");
+  const size_t nb = s.h_bk_start.size();
+  if (nb) {
+    CK(cudaMemcpyAsync(s.bk_start.p, s.h_bk_start.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.bk_end.p, s.h_bk_end.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.bk_region.p, s.h_bk_region.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.bk_zmin.p, bz0.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.bk_zmax.p, bz1.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
+  }
+  CK(cudaMemcpyAsync(s.col_begin.p, cb.data(), 4 * ncol, cudaMemcpyHostToDevice, st), "H2D");
+  CK(cudaMemcpyAsync(s.col_end.p, ce.data(), 4 * ncol, cudaMemcpyHostToDevice, st), "H2D");
+  CK(cudaStreamSynchronize(st), "upload");
+  s.valid = true;
+  return CPC_OK;
+}
+
+cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, cpc_engine engine,
+                     int64_t row_stride, int64_t row_offset, cpc_accum *out) {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  std::vector<JobPlan> jobs(1);
+  cpc_status s = plan_job(c, kind, slot_g1, slot_g2, row_stride, row_offset, out, jobs[0]);
+  if (s != CPC_OK) return s;
+  if (engine == CPC_ENGINE_FP64) return run_plain(jobs[0]);
+  if (engine != CPC_ENGINE_FAST) return fail(c, CPC_ERR_INVALID, "unknown engine");
+  return run_fast(jobs);
+}
+
+cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind *kinds,
+                           const int *slots_g1, const int *slots_g2, cpc_accum *outs) {
+  if (n_jobs <= 0 || !ctxs || !kinds || !slots_g1 || !slots_g2 || !outs)
+    return fail(nullptr, CPC_ERR_INVALID, "bad batch arguments");
+  std::vector<JobPlan> jobs(n_jobs);
+  for (int k = 0; k < n_jobs; k++) {
+    if (!ctxs[k]) return fail(nullptr, CPC_ERR_INVALID, "null context in batch");
+    if (ctxs[k]->device != ctxs[0]->device) return fail(ctxs[k], CPC_ERR_INVALID, "batch spans devices");
+    cpc_status s = plan_job(ctxs[k], kinds[k], slots_g1[k], slots_g2[k], 1, 0, &outs[k], jobs[k]);
+    if (s != CPC_OK) return s;
+  }
+  return run_fast(jobs);
+}
+
+cpc_status cpc_host_rand_uniform(uint32_t seed, int64_t skip, int64_t n, double *out) {
+  if (n < 0 || skip < 0 || (n > 0 && !out)) return fail(nullptr, CPC_ERR_INVALID, "bad arguments");
+  std::vector<int32_t> r(n);
+  glibc_rand_stream(seed, skip, n, r.data());
+  for (int64_t i = 0; i < n; i++) out[i] = r[i] / (2147483647 + 1.);
+  return CPC_OK;
+}
+
+cpc_status cpc_host_elip_angle(int64_t n, const double *e1, const double *e2, double *phi) {
+  if (n < 0 || (n > 0 && (!e1 || !e2 || !phi))) return fail(nullptr, CPC_ERR_INVALID, "bad arguments");
+  for (int64_t i = 0; i < n; i++) phi[i] = elip_angle(e1[i], e2[i]);
+  return CPC_OK;
+}
+
+cpc_status cpc_host_rp_thresholds(const cpc_params *p, double *thr) {
+  if (!p || !thr) return fail(nullptr, CPC_ERR_INVALID, "null argument");
+  if (p->n_bins <= 0 || p->n_bins > kMaxRp) return fail(nullptr, CPC_ERR_INVALID, "n_bins out of range");
+  const int rc = rp_thresholds(p->lin_bin, p->n_bins, p->bin_r_min, p->bin_r_max, thr);
+  return rc == 0 ? CPC_OK : fail(nullptr, CPC_ERR_INVALID, "threshold derivation failed");
+}
+
+cpc_status cpc_launch_count(const cpc_ctx *c, int64_t *launches) {
+  if (!c || !launches) return fail(nullptr, CPC_ERR_INVALID, "null argument");
+  *launches = c->launches;
+  return CPC_OK;
+}
+
+cpc_status cpc_host_pi_thresholds(const cpc_params *p, double *thr) {
+  if (!p || !thr) return fail(nullptr, CPC_ERR_INVALID, "null argument");
+  if (p->n_p_bin <= 0 || p->n_p_bin > kMaxPi) return fail(nullptr, CPC_ERR_INVALID, "n_p_bin out of range");
+  const int rc = pi_thresholds(p->n_p_bin, p->p_min, p->p_max, thr);
+  return rc == 0 ? CPC_OK : fail(nullptr, CPC_ERR_INVALID, "threshold derivation failed");
+}
+
+}  // extern "C"

@@ -1,0 +1,256 @@
+// cpc_device.cuh -- device-side data layout and the exact FP64 pair evaluation.
+//
+// Data layout in HBM (per uploaded catalogue, "slot"), all in cell-list order
+// (sorted by column, jackknife region, then z):
+//   pos  float4 (x, y, z, w)          16 B  -- the fast kernel's only hot stream
+//   shp  float4 (e1, e2, phi, 0)      16 B  -- read for binned pairs with shapes
+//   keep uint8  jk_prob >= 0.5         1 B
+//   xd,yd,zd,wd,e1d,e2d,phid double   56 B  -- FP64 edge recheck only
+//   jk   int32 region label            4 B
+//   orig int64 original row index      8 B  -- row subsampling only
+// plus the compact list of non-empty (column, region) buckets.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cpc {
+
+constexpr int kNF = 13;        // wt, d1v, d1e, ..., d6v, d6e
+constexpr int kMaxRp = 64;     // r_p bins supported
+constexpr int kMaxPi = 128;    // Pi bins supported
+constexpr int kMaxSlots = 8;
+
+enum Corel { COREL_DD = 0, COREL_SD = 1, COREL_SS = 2, COREL_SSA = 3 };
+
+// double-precision catalogue view (recheck and plain FP64 kernel)
+struct DCat {
+  int64_t n;
+  const double *x, *y, *z, *w, *e1, *e2, *phi;
+  const int32_t *jk;
+  const uint8_t *keep;
+  const int64_t *orig;
+};
+
+// single-precision cell-list view (fast kernel)
+struct FCat {
+  int64_t n;
+  const float4 *pos;
+  const float4 *shp;
+  const float2 *lo;   // x - (float)x, y - (float)y (non-float32 inputs)
+  const float *zf;
+  const uint8_t *keep;
+  // non-empty buckets (column-major, region-minor)
+  const int *bk_start, *bk_end, *bk_region;
+  const float *bk_zmin, *bk_zmax;
+  const int *col_begin, *col_end;  // per column: range into the bucket list
+};
+
+struct JobDev {
+  FCat f1, f2;  // g1 (outer rows) and g2 after the swap rule
+  DCat d1, d2;  // same catalogues, FP64, cell order
+  int corel, gws, which_corr, estimator, do_jk, n_jk;
+  int periodic, coordinates, nrp, npi, wpi, lin_bin;
+  int box_same_keep;        // 1 for the box (jk_check_PB), 0 for the sky
+  int has_lo;               // positions are not float32-exact: use hi+lo for theta
+  int ncx, ncy;
+  int64_t row_stride, row_offset;
+  // ---- fast-path single precision constants ----
+  float Lf;
+  float xy_in, xy_out;                 // definite window bounds on max(|dx|,|dy|)
+  float pi_in_lo, pi_in_hi, pi_out_lo, pi_out_hi;
+  float inv_ps_f, tp0;                 // approximate Pi bin: floor(dz*inv_ps + tp0)
+  float l2rmin2, inv_lw;               // log2(r_min^2), 1/(log2 width in r^2)
+  float rmin_f, inv_rsize_f;           // linear-bin estimate
+  float rej_lo, rej_hi;                // definite r^2 rejection bounds
+  float qscale[kNF];                   // per-field fixed-point scale 2^S_f
+  int qbias;                           // fixed-point bias B (> max |v_f| 2^S_f)
+  int unit_w;                          // every weight is 1: wt_num = count
+  float A[kMaxRp], B[kMaxRp];          // definite r^2 band of r_p bin k
+  float PA[kMaxPi], PB[kMaxPi];        // definite Pi band of Pi bin k
+  // ---- FP64 exact constants ----
+  double L, rmin, rmax, pmin, pmax, ps, rsize;
+  double inv_qscale[kNF];
+  double thr[kMaxRp + 1];              // exact r_p thresholds (host libm)
+  // ---- outputs ----
+  unsigned long long *acc_num;         // [n_hist][nrp][npi]
+  double *acc_sums;                    // [n_hist][nrp][npi][kNF]
+  unsigned long long *counters;        // [0] window (fast), [1] window (recheck), [2] rechecked
+};
+
+struct UnitDesc {
+  int job;
+  int g1_start, g1_count, g1_stride;  // tile rows g1_start + q*g1_stride, q < g1_count
+  int region;      // jackknife region of every g1 row in the tile (0 without jk)
+  int n2_base;     // first Pi bin of the block-local window
+  int cx_lo, cx_hi, cy_lo, cy_hi;  // neighbour columns (may run past the grid: periodic wrap)
+  double zlo, zhi; // candidate range of the shifted z2 + L*sz
+};
+
+struct QEntry {
+  int job, i1, j2, shift;  // shift code: (sx+1) + 3*(sy+1) + 9*(sz+1)
+};
+
+__host__ __device__ inline int shift_code(int sx, int sy, int sz) {
+  return (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
+}
+__host__ __device__ inline void shift_decode(int c, int &sx, int &sy, int &sz) {
+  sx = c % 3 - 1;
+  sy = (c / 3) % 3 - 1;
+  sz = c / 9 - 1;
+}
+
+// ---------------------------------------------------------------------------
+// Exact evaluation of one (g1, g2, image) triple with the reference's double
+// arithmetic: no contraction into FMA (explicit _rn intrinsics), same operation
+// order.  Window predicates: PB_calcs.cpp:12-61 and corr.cpp:67-86; binning:
+// corels.cpp:21-46 with PB_calcs.cpp:87-98; r_p bin from the host-computed
+// exact thresholds of floor(log10(r/r_min)/r_size).
+// Returns: 0 not a window pair, 1 window pair outside the bins, 2 binned.
+// ---------------------------------------------------------------------------
+__device__ inline int exact_classify(const JobDev &J, const DCat &g1, int64_t i,
+                                     const DCat &g2, int64_t j, int sx, int sy, int sz,
+                                     int &n1, int &n2) {
+  const double x1 = g1.x[i], y1 = g1.y[i], z1 = g1.z[i];
+  const double x2 = g2.x[j], y2 = g2.y[j], z2 = g2.z[j];
+  // lim_calc_xyz / lim_calc_PB
+  const double z_max = __dadd_rn(z1, J.pmax), z_min = __dadd_rn(z1, J.pmin);
+  const double ra_max = __dadd_rn(x1, J.rmax), ra_min = __dsub_rn(x1, J.rmax);
+  const double dec_max = __dadd_rn(y1, J.rmax), dec_min = __dsub_rn(y1, J.rmax);
+  if (J.periodic) {
+    if (sz == 1 && !(z_max > J.L)) return 0;
+    if (sz == -1 && !(z_min < 0)) return 0;
+    if (sx == 1 && !(ra_max > J.L)) return 0;
+    if (sx == -1 && !(ra_min < 0)) return 0;
+    if (sy == 1 && !(dec_max > J.L)) return 0;
+    if (sy == -1 && !(dec_min < 0)) return 0;
+  } else if (sx | sy | sz) {
+    return 0;
+  }
+  const double Lsx = J.L * sx, Lsy = J.L * sy, Lsz = J.L * sz;  // exact (s in -1..1)
+  const double z2s = __dadd_rn(z2, Lsz);
+  if (z2s > z_max || z2s < z_min) return 0;
+  const double y2s = __dadd_rn(y2, Lsy);
+  if (y2s > dec_max || y2s < dec_min) return 0;
+  const double x2s = __dadd_rn(x2, Lsx);
+  if (x2s < ra_min || x2s > ra_max) return 0;
+  // corel_bin
+  const double dP = __dsub_rn(z2s, z1);
+  const double v2 = floor(__ddiv_rn(__dsub_rn(dP, J.pmin), J.ps));
+  if (!(v2 >= 0.0) || v2 >= (double)J.npi) return 1;
+  const double t0 = __dsub_rn(x1, x2s), t1 = __dsub_rn(y1, y2s);
+  const double rp = __dsqrt_rn(__dadd_rn(__dmul_rn(t0, t0), __dmul_rn(t1, t1)));
+  int k1;
+  if (J.lin_bin) {
+    const double v1 = floor(__ddiv_rn(__dsub_rn(rp, J.rmin), J.rsize));
+    if (!(v1 >= 0.0) || v1 >= (double)J.nrp) return 1;
+    k1 = (int)v1;
+  } else {
+    if (!(rp >= J.thr[0]) || rp >= J.thr[J.nrp]) return 1;
+    int lo = 0, hi = J.nrp;  // thr[lo] <= rp < thr[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (rp >= J.thr[mid]) lo = mid; else hi = mid;
+    }
+    k1 = lo;
+  }
+  n1 = k1;
+  n2 = (int)v2;
+  return 2;
+}
+
+// Per-pair accumulator values in double (corels.cpp:48-77, 122-244; calcs.cpp
+// 54-64, 97-105) for a binned pair.  f[0..12] as in the output layout.
+__device__ inline void exact_values(const JobDev &J, const DCat &g1, int64_t i, const DCat &g2,
+                                    int64_t j, double f[kNF]) {
+  for (int q = 0; q < kNF; q++) f[q] = 0.0;
+  const double wt = __dmul_rn(g1.w[i], g2.w[j]);
+  f[0] = wt;
+  if (J.corel == COREL_DD) return;
+  const double theta = atan((g2.y[j] - g1.y[i]) / (g2.x[j] - g1.x[i]));
+  const double c2 = cos(2.0 * theta), s2 = sin(2.0 * theta);
+  const double kpi = 3.141592653589793;
+  auto ephi = [&](double phi) {
+    double t = fabs(phi - theta);
+    if (t > kpi / 2.0) t = kpi - t;
+    return t;
+  };
+  if (J.corel == COREL_SD) {
+    const DCat &gs = (J.gws == 2) ? g2 : g1;
+    const int64_t is = (J.gws == 2) ? j : i;
+    const double e0 = gs.e1[is], e1 = gs.e2[is];
+    const double ep = c2 * e0 - s2 * e1, ex = s2 * e0 + c2 * e1;
+    f[1] = wt * ep;
+    f[2] = f[1] * f[1];
+    f[3] = wt * ex;
+    f[4] = f[3] * f[3];
+    const double et = ephi(g1.phi[i]);
+    f[11] = et;
+    f[12] = et * et;
+    return;
+  }
+  const double ei0 = c2 * g1.e1[i] - s2 * g1.e2[i], ei1 = s2 * g1.e1[i] + c2 * g1.e2[i];
+  const double ej0 = c2 * g2.e1[j] - s2 * g2.e2[j], ej1 = s2 * g2.e1[j] + c2 * g2.e2[j];
+  if (J.corel == COREL_SS) {
+    if (J.gws == 2) {
+      f[1] = wt * ej0;
+      const double et = ephi(g2.phi[j]);
+      f[11] = et;
+      f[12] = et * et;
+    } else if (J.gws == 1) {
+      f[1] = wt * ei0;
+      const double et = ephi(g1.phi[i]);
+      f[11] = et;
+      f[12] = et * et;
+    }
+    f[2] = f[1] * f[1];
+  } else {
+    f[1] = wt * (ei0 + ej0) / 2.0;
+    f[2] = (wt * ei0 / 2.0) * (wt * ei0 / 2.0) + (wt * ej0 / 2.0) * (wt * ej0 / 2.0);
+    f[3] = wt * (ei1 + ej1) / 2.0;
+    f[4] = (wt * ei1 / 2.0) * (wt * ei1 / 2.0) + (wt * ej1 / 2.0) * (wt * ej1 / 2.0);
+    const double a = ephi(g1.phi[i]), b = ephi(g2.phi[j]);
+    f[11] = a + b;
+    f[12] = a * a + b * b;
+  }
+  f[5] = wt * (ei0 * ej0);
+  f[6] = f[5] * f[5];
+  f[7] = wt * (ei1 * ej1);
+  f[8] = f[7] * f[7];
+  f[9] = wt * (ei1 * ej0 + ei0 * ej1) / 2.0;
+  const double pa = wt * (ei1 * ej0) / 2.0, pb = wt * ei0 * ej1 / 2.0;
+  f[10] = pa * pa + pb * pb;
+}
+
+// Add one binned pair (FP64 values) to the global accumulators, including the
+// jackknife attribution of corel_jk (jk.cpp:201-223 with jk_check_PB / _sky).
+__device__ inline void exact_accumulate(const JobDev &J, const DCat &g1, int64_t i,
+                                        const DCat &g2, int64_t j, int n1, int n2,
+                                        const double f[kNF]) {
+  const int64_t cell = (int64_t)n1 * J.npi + n2;
+  const int64_t hstride = (int64_t)J.nrp * J.npi;
+  atomicAdd(&J.acc_num[cell], 1ull);
+  double *s = J.acc_sums + cell * kNF;
+  for (int q = 0; q < kNF; q++)
+    if (f[q] != 0.0) atomicAdd(&s[q], f[q]);
+  if (!J.do_jk) return;
+  const int r1 = g1.jk[i], r2 = g2.jk[j];
+  int k1 = g1.keep[i], k2 = g2.keep[j];
+  if (r1 == r2) {
+    if (J.box_same_keep) k1 = 1;
+    k2 = 0;
+  }
+  const int rs[2] = {r1, r2};
+  const int ks[2] = {k1, k2};
+  for (int t = 0; t < 2; t++) {
+    if (!ks[t]) continue;
+    const int64_t hc = (int64_t)(1 + rs[t]) * hstride + cell;
+    atomicAdd(&J.acc_num[hc], 1ull);
+    double *sj = J.acc_sums + hc * kNF;
+    if (f[0] != 0.0) atomicAdd(&sj[0], f[0]);
+    if (J.which_corr == 0) continue;
+    for (int q = 1; q < kNF; q += 2)
+      if (f[q] != 0.0) atomicAdd(&sj[q], f[q]);
+  }
+}
+
+}  // namespace cpc

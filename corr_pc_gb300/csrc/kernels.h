@@ -1,0 +1,54 @@
+// kernels.h -- host-callable launchers of the device code.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cpc_device.cuh"
+
+namespace cpc {
+
+struct GatherIn {
+  const double *x, *y, *z, *w, *e1, *e2, *phi;
+  const int32_t *jk;
+  const uint8_t *keep;
+};
+struct GatherOut {
+  float4 *pos, *shp;  // null for the z-ordered (FP64) copy
+  float2 *lo;
+  float *zf;
+  uint32_t *bucket;   // null for the z-ordered copy
+  double *x, *y, *z, *w, *e1, *e2, *phi;
+  int32_t *jk;
+  uint8_t *keep;
+  int64_t *orig;
+  const int64_t *orig_in;  // when set, orig[k] = orig_in[perm[k]]
+};
+
+// cell_list.cu
+cudaError_t radix_sort_pairs(int64_t n, uint64_t *keys, uint32_t *vals, uint64_t *ktmp,
+                             uint32_t *vtmp, uint32_t *hist, unsigned long long *census_d,
+                             cudaStream_t st, int64_t *launches);
+int64_t radix_hist_words(int64_t n);
+cudaError_t launch_cell_keys(int64_t n, const double *x, const double *y, const double *z,
+                             const int32_t *jk, double inv_cw_x, double inv_cw_y, int ncx, int ncy,
+                             int n_reg, uint64_t *keys, uint32_t *vals, cudaStream_t st);
+cudaError_t launch_z_keys(int64_t n, const double *z, uint64_t *keys, uint32_t *vals,
+                          cudaStream_t st);
+cudaError_t launch_gather(int64_t n, const uint64_t *keys, const uint32_t *perm, const GatherIn &in,
+                          const GatherOut &out, cudaStream_t st);
+
+// pair_fast.cu
+constexpr int kTileThreads = 128;
+size_t fast_smem_bytes(int corel, int do_jk, int NB);
+size_t fast_static_smem_bytes();
+int fast_blocks_per_sm(int corel, int jk, size_t smem);
+cudaError_t launch_fast(int corel, int jk, const JobDev *jobs, const UnitDesc *units, int n_units,
+                        unsigned int *unit_ctr, QEntry *q, unsigned long long *qcount,
+                        unsigned long long qcap, size_t smem, int grid, cudaStream_t st);
+cudaError_t launch_recheck(const JobDev *jobs, const QEntry *q, const unsigned long long *qcount,
+                           unsigned long long qcap, int grid, cudaStream_t st);
+
+// pair_fp64.cu
+cudaError_t launch_plain_fp64(const JobDev *job, const DCat &a, const DCat &b, cudaStream_t st);
+
+}  // namespace cpc

@@ -1,0 +1,694 @@
+// pair_fast.cu -- the mixed-precision pair-counting kernel (sm_103a).
+//
+// One persistent launch drains a device work queue of "units".  A unit is a
+// tile of up to kTile g1 rows (one row per thread, held in registers) from a
+// single (column, jackknife region) bucket, paired with every g2 candidate of
+// the neighbouring columns inside the unit's shifted-z range.  Candidates are
+// staged through shared memory in batches of kTile and every thread tests its
+// row against every staged candidate (broadcast reads, no bank conflicts).
+//
+// Precision: separations, r_p^2 and Pi are computed in FP32.  A pair is
+// resolved on this path only when it is farther than a rigorous error bound
+// from every decision boundary (the r_p / Pi window, every r_p and Pi bin
+// edge); otherwise it is appended to an edge queue and re-evaluated with the
+// reference's exact double-precision arithmetic (recheck_kernel), so integer
+// counts are bit-identical with the reference.
+//
+// Accumulation: block-private histograms over (r_p bin, block-local Pi window)
+// in shared memory -- the full sample ("main"), the tile's own jackknife region
+// ("X") and one other region ("Y", the partner's region for cross-region
+// pairs) -- with 32-bit counts and 64-bit fixed-point sums (exact integer
+// addition, order independent), flushed to the FP64 global histogram block
+// with one atomic per non-empty (bin, field) at the end of the unit.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <climits>
+
+#include "cpc_device.cuh"
+#include "kernels.h"
+
+namespace cpc {
+
+constexpr int kTile = kTileThreads;
+constexpr int kMaxSeg = 512;
+constexpr int kMaxCols = 1024;
+
+template <int C> struct FieldMap;
+template <> struct FieldMap<COREL_DD> {
+  static constexpr int FM = 1, FJ = 1;
+  __device__ static constexpr int m(int) { return 0; }
+  __device__ static constexpr int j(int) { return 0; }
+};
+template <> struct FieldMap<COREL_SD> {
+  static constexpr int FM = 7, FJ = 4;
+  __device__ static constexpr int m(int k) {
+    return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 2 : k == 3 ? 3 : k == 4 ? 4 : k == 5 ? 11 : 12;
+  }
+  __device__ static constexpr int j(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 3 : 11; }
+};
+template <> struct FieldMap<COREL_SS> {
+  static constexpr int FM = 11, FJ = 6;
+  __device__ static constexpr int m(int k) { return k < 2 ? k : k == 2 ? 2 : k + 2; }
+  __device__ static constexpr int j(int k) { return k == 0 ? 0 : 2 * k - 1 + (k >= 2 ? 2 : 0); }
+};
+template <> struct FieldMap<COREL_SSA> {
+  static constexpr int FM = 13, FJ = 7;
+  __device__ static constexpr int m(int k) { return k; }
+  __device__ static constexpr int j(int k) { return k == 0 ? 0 : 2 * k - 1; }
+};
+
+// Shared-memory bytes a block needs for a job with NB = nrp * wpi local bins.
+size_t fast_smem_bytes(int corel, int do_jk, int NB) {
+  int FM = 1, FJ = 1;
+  if (corel == COREL_SD) { FM = 7; FJ = 4; }
+  if (corel == COREL_SS) { FM = 11; FJ = 6; }
+  if (corel == COREL_SSA) { FM = 13; FJ = 7; }
+  size_t b = sizeof(float4) * 2 * kTile;                 // staging
+  b += 8ull * FM * NB + 4ull * NB;
+  if (do_jk) b += 2 * (8ull * FJ * NB + 4ull * NB);
+  return b;
+}
+
+// 64-bit fixed-point sums held as two 32-bit words (low word + carry word):
+// each term is q = rint(v * 2^S) + B with B > |v| * 2^S, so 0 <= q < 2B <= 2^27;
+// the low word wraps at most once per add, detected from the returned old
+// value, and the carry goes to the high word (rare).  The bias B * count is
+// removed at the flush.  32-bit shared atomics are several times faster than
+// 64-bit ones on this part, and same-address 32-bit adds are combined in hardware.
+__device__ __forceinline__ unsigned to_fixed(float v, float scale, int bias) {
+  return (unsigned)(__float2int_rn(v * scale) + bias);
+}
+__device__ __forceinline__ void acc_add(unsigned *lw, unsigned *hw, unsigned u) {
+  const unsigned old = atomicAdd(lw, u);
+  if (old + u < old) atomicAdd(hw, 1u);
+}
+__device__ __forceinline__ double fixed_total(unsigned lw, unsigned hw, unsigned cnt, int bias,
+                                              double inv_scale) {
+  const long long tot = (long long)(((unsigned long long)hw << 32) | lw) -
+                        (long long)cnt * (long long)bias;
+  return (double)tot * inv_scale;
+}
+
+__device__ __forceinline__ int floordiv(int a, int b) {
+  int q = a / b;
+  if ((a % b != 0) && ((a < 0) != (b < 0))) --q;
+  return q;
+}
+
+// first index in [lo, hi) with zf[idx] >= v
+__device__ __forceinline__ int lower_bound_f(const float *zf, int lo, int hi, float v) {
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(zf + mid) < v) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __noinline__ void fallback_exact(const JobDev &J, int64_t i1, int64_t j2, int code) {
+  int sx, sy, sz, n1, n2;
+  shift_decode(code, sx, sy, sz);
+  const int r = exact_classify(J, J.d1, i1, J.d2, j2, sx, sy, sz, n1, n2);
+  if (r == 0) return;
+  atomicAdd(&J.counters[1], 1ull);
+  if (r == 2) {
+    double f[kNF];
+    exact_values(J, J.d1, i1, J.d2, j2, f);
+    exact_accumulate(J, J.d1, i1, J.d2, j2, n1, n2, f);
+  }
+}
+
+__device__ __forceinline__ void enqueue(const JobDev &J, int job, int64_t i1, int64_t j2, int code,
+                                        QEntry *q, unsigned long long *qcount,
+                                        unsigned long long qcap) {
+  const unsigned long long pos = atomicAdd(qcount, 1ull);
+  if (pos < qcap) {
+    QEntry e;
+    e.job = job;
+    e.i1 = (int)i1;
+    e.j2 = (int)j2;
+    e.shift = code;
+    q[pos] = e;
+  } else {
+    fallback_exact(J, i1, j2, code);
+  }
+}
+
+// ephi_calc (calcs.cpp:97-105) in FP32
+__device__ __forceinline__ float ephi_f(float phi, float theta) {
+  float t = fabsf(phi - theta);
+  return t > 1.5707963267948966f ? 3.14159265358979f - t : t;
+}
+
+template <int C, bool JK>
+__global__ void __launch_bounds__(kTile)
+fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ units,
+                  int n_units, unsigned int *__restrict__ unit_ctr, QEntry *__restrict__ queue,
+                  unsigned long long *__restrict__ qcount, unsigned long long qcap,
+                  int zero_words) {
+  using F = FieldMap<C>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4 *s_pos = reinterpret_cast<float4 *>(smem);
+  float4 *s_shp = s_pos + kTile;
+  unsigned char *hist_base = smem + sizeof(float4) * 2 * kTile;
+
+  __shared__ int s_unit;
+  __shared__ int s_cnt[kMaxCols + 1];
+  __shared__ int s_slot_b[kMaxSeg];
+  __shared__ int s_slot_info[kMaxSeg];  // shift code | (sz+1) << 8 ... (code only)
+  __shared__ int s_seg_a[kMaxSeg], s_seg_len[kMaxSeg], s_seg_key[kMaxSeg];
+  __shared__ int s_order[kMaxSeg], s_pre[kMaxSeg + 1];
+  __shared__ int s_jidx[kTile];
+  __shared__ unsigned char s_keep[kTile];
+  __shared__ float2 s_lo[kTile];
+  __shared__ unsigned long long s_red[kTile / 32];
+  __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
+  __shared__ float s_qs[kNF];
+  __shared__ double s_iqs[kNF];
+
+  const int t = threadIdx.x;
+  // histograms start zeroed; every flush re-zeroes what it used
+  {
+    unsigned int *z = reinterpret_cast<unsigned int *>(hist_base);
+    for (int k = t; k < zero_words; k += kTile) z[k] = 0u;
+  }
+  __syncthreads();
+
+  for (;;) {
+    if (t == 0) s_unit = (int)atomicAdd(unit_ctr, 1u);
+    __syncthreads();
+    const int u = s_unit;
+    if (u >= n_units) break;
+    const UnitDesc U = units[u];
+    const JobDev &J = jobs[U.job];
+    const int nrp = J.nrp, wpi = J.wpi, npi = J.npi, NB = nrp * wpi;
+    // per histogram: count[NB], low words [F][NB], carry words [F][NB]
+    unsigned *s_mnum = reinterpret_cast<unsigned *>(hist_base);
+    unsigned *s_mlo = s_mnum + NB;
+    unsigned *s_mhi = s_mlo + (size_t)F::FM * NB;
+    unsigned *s_xnum = s_mhi + (size_t)F::FM * NB;
+    unsigned *s_xlo = s_xnum + NB;
+    unsigned *s_xhi = s_xlo + (size_t)F::FJ * NB;
+    unsigned *s_ynum = s_xhi + (size_t)F::FJ * NB;
+    unsigned *s_ylo = s_ynum + NB;
+    unsigned *s_yhi = s_ylo + (size_t)F::FJ * NB;
+    const int qbias = J.qbias;
+    const int f0 = J.unit_w ? 1 : 0;  // unit weights: wt_num = count, not accumulated
+
+    // ---- this thread's g1 row: the lanes of a warp are spread over the whole
+    // tile (tile row q = lane * W + warp), so simultaneous pairs of a warp fall
+    // in different Pi bins and the shared-memory atomics rarely collide ----
+    const int W = (U.g1_count + 31) >> 5;
+    const int q = (t & 31) * W + (t >> 5);
+    const bool has1 = (t >> 5) < W && q < U.g1_count;
+    const int64_t i1 = (int64_t)U.g1_start + (int64_t)q * U.g1_stride;
+    float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), e1v = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 lo1 = make_float2(0.f, 0.f);
+    bool keep1 = false, valid = false;
+    const bool has_lo = C != COREL_DD && J.has_lo;
+    const int gws = J.gws, lin_bin = J.lin_bin, box_same_keep = J.box_same_keep;
+    const float rmin_f = J.rmin_f, inv_rsize_f = J.inv_rsize_f;
+    if (has1) {
+      p1 = J.f1.pos[i1];
+      if (has_lo) lo1 = J.f1.lo[i1];
+      if (C != COREL_DD) e1v = J.f1.shp[i1];
+      if (JK) keep1 = J.f1.keep[i1] != 0;
+      valid = true;
+      if (J.row_stride > 1) {
+        int64_t o = J.d1.orig[i1] - J.row_offset;
+        valid = (o % J.row_stride) == 0;
+      }
+    }
+    const float Lf = J.Lf;
+    const float xy_in = J.xy_in, xy_out = J.xy_out;
+    const float pi_in_lo = J.pi_in_lo, pi_in_hi = J.pi_in_hi;
+    const float pi_out_lo = J.pi_out_lo, pi_out_hi = J.pi_out_hi;
+    const float inv_ps = J.inv_ps_f, tp0 = J.tp0;
+    for (int k = t; k < nrp; k += kTile) { s_A[k] = J.A[k]; s_B[k] = J.B[k]; }
+    for (int k = t; k < npi; k += kTile) { s_PA[k] = J.PA[k]; s_PB[k] = J.PB[k]; }
+    if (t < kNF) { s_qs[t] = J.qscale[t]; s_iqs[t] = J.inv_qscale[t]; }
+    const float l2rmin2 = J.l2rmin2, inv_lw = J.inv_lw, rej_lo = J.rej_lo, rej_hi = J.rej_hi;
+    const int n2_base = U.n2_base;
+    unsigned long long nwin = 0;
+
+    // ---- enumerate candidate slots: (column, bucket, sz) overlapping the unit's z range ----
+    const int ncxu = U.cx_hi - U.cx_lo + 1;
+    const int ncol = ncxu * (U.cy_hi - U.cy_lo + 1);
+    const int nsz_lo = J.periodic ? -1 : 0, nsz_hi = J.periodic ? 1 : 0;
+    for (int c = t; c < ncol; c += kTile) {
+      const int cx = U.cx_lo + c % ncxu, cy = U.cy_lo + c / ncxu;
+      const int sx = J.periodic ? floordiv(cx, J.ncx) : 0, sy = J.periodic ? floordiv(cy, J.ncy) : 0;
+      int cnt = 0;
+      if (sx >= -1 && sx <= 1 && sy >= -1 && sy <= 1) {
+        const int col = (cy - sy * J.ncy) * J.ncx + (cx - sx * J.ncx);
+        const int b0 = J.f2.col_begin[col], b1 = J.f2.col_end[col];
+        for (int b = b0; b < b1; b++) {
+          const float bz0 = J.f2.bk_zmin[b], bz1 = J.f2.bk_zmax[b];
+          for (int sz = nsz_lo; sz <= nsz_hi; sz++) {
+            const float lo = (float)(U.zlo - J.L * sz), hi = (float)(U.zhi - J.L * sz);
+            if (bz1 >= lo && bz0 < hi) cnt++;
+          }
+        }
+      }
+      s_cnt[c] = cnt;
+    }
+    __syncthreads();
+    if (t == 0) {
+      int run = 0;
+      for (int c = 0; c < ncol; c++) {
+        const int v = s_cnt[c];
+        s_cnt[c] = run;
+        run += v;
+      }
+      s_cnt[ncol] = run;
+    }
+    __syncthreads();
+    const int total_slots = s_cnt[ncol];
+    int cur_y = -1;  // region currently held in the Y histogram
+
+    for (int chunk0 = 0; chunk0 < total_slots; chunk0 += kMaxSeg) {
+      const int nslot = min(kMaxSeg, total_slots - chunk0);
+      for (int c = t; c < ncol; c += kTile) {
+        int pos = s_cnt[c];
+        if (pos >= chunk0 + kMaxSeg || s_cnt[c + 1] <= chunk0) continue;
+        const int cx = U.cx_lo + c % ncxu, cy = U.cy_lo + c / ncxu;
+        const int sx = J.periodic ? floordiv(cx, J.ncx) : 0, sy = J.periodic ? floordiv(cy, J.ncy) : 0;
+        const int col = (cy - sy * J.ncy) * J.ncx + (cx - sx * J.ncx);
+        const int b0 = J.f2.col_begin[col], b1 = J.f2.col_end[col];
+        for (int b = b0; b < b1; b++) {
+          const float bz0 = J.f2.bk_zmin[b], bz1 = J.f2.bk_zmax[b];
+          for (int sz = nsz_lo; sz <= nsz_hi; sz++) {
+            const float lo = (float)(U.zlo - J.L * sz), hi = (float)(U.zhi - J.L * sz);
+            if (!(bz1 >= lo && bz0 < hi)) continue;
+            const int k = pos - chunk0;
+            if (k >= 0 && k < kMaxSeg) {
+              s_slot_b[k] = b;
+              s_slot_info[k] = shift_code(sx, sy, sz);
+            }
+            pos++;
+          }
+        }
+      }
+      __syncthreads();
+      for (int k = t; k < nslot; k += kTile) {
+        const int b = s_slot_b[k], code = s_slot_info[k];
+        const int sz = code / 9 - 1;
+        const float lo = (float)(U.zlo - J.L * sz), hi = (float)(U.zhi - J.L * sz);
+        const int bs = J.f2.bk_start[b], be = J.f2.bk_end[b];
+        const int a = lower_bound_f(J.f2.zf, bs, be, lo);
+        const int e = lower_bound_f(J.f2.zf, a, be, hi);
+        s_seg_a[k] = a;
+        s_seg_len[k] = e - a;
+        s_seg_key[k] = (e > a) ? J.f2.bk_region[b] * 27 + code : INT_MAX;
+      }
+      __syncthreads();
+      for (int k = t; k < nslot; k += kTile) {  // stable rank sort by key
+        const int key = s_seg_key[k];
+        int r = 0;
+        for (int m = 0; m < nslot; m++) {
+          const int km = s_seg_key[m];
+          r += (km < key) || (km == key && m < k);
+        }
+        s_order[r] = k;
+      }
+      __syncthreads();
+      if (t == 0) {
+        int run = 0;
+        for (int k = 0; k < nslot; k++) {
+          s_pre[k] = run;
+          run += s_seg_len[s_order[k]];
+        }
+        s_pre[nslot] = run;
+      }
+      __syncthreads();
+
+      int k = 0;
+      while (k < nslot) {
+        const int key = s_seg_key[s_order[k]];
+        if (key == INT_MAX) break;
+        int g = k + 1;
+        while (g < nslot && s_seg_key[s_order[g]] == key) g++;
+        const int region2 = key / 27, code = key % 27;
+        int sx, sy, sz;
+        shift_decode(code, sx, sy, sz);
+        const bool same_region = region2 == U.region;
+        if (JK && !same_region && cur_y != region2) {
+          if (cur_y >= 0) {  // flush Y for the previous region
+            __syncthreads();
+            const int64_t hb = (int64_t)(1 + cur_y) * nrp * npi;
+            for (int lb = t; lb < NB; lb += kTile) {
+              const unsigned n = s_ynum[lb];
+              if (!n) continue;
+              const int n2 = n2_base + lb % wpi;
+              const int64_t cell = hb + (int64_t)(lb / wpi) * npi + n2;
+              atomicAdd(&J.acc_num[cell], (unsigned long long)n);
+              s_ynum[lb] = 0u;
+#pragma unroll
+              for (int f = 0; f < F::FJ; f++) {
+                const size_t o = (size_t)f * NB + lb;
+                if (f >= f0) {
+                  const double v = fixed_total(s_ylo[o], s_yhi[o], n, qbias, s_iqs[F::j(f)]);
+                  if (v != 0.0) atomicAdd(&J.acc_sums[cell * kNF + F::j(f)], v);
+                }
+                s_ylo[o] = 0u;
+                s_yhi[o] = 0u;
+              }
+            }
+            __syncthreads();
+          }
+          cur_y = region2;
+        }
+        // g1-side shift for +1 images (x1 - L exact for x1 >= L/2), g2-side for -1
+        const float x1s = sx == 1 ? p1.x - Lf : p1.x;
+        const float y1s = sy == 1 ? p1.y - Lf : p1.y;
+        const float z1s = sz == 1 ? p1.z - Lf : p1.z;
+        const float g2sx = sx == -1 ? Lf : 0.f, g2sy = sy == -1 ? Lf : 0.f, g2sz = sz == -1 ? Lf : 0.f;
+        const bool xsame = JK && same_region && (box_same_keep || keep1);
+        const bool xdiff = JK && !same_region && keep1;
+
+        for (int base = s_pre[k]; base < s_pre[g]; base += kTile) {
+          const int nb = min(kTile, s_pre[g] - base);
+          if (t < nb) {
+            const int p = base + t;
+            int lo = k, hi = g;  // segment s_order[lo] with s_pre[lo] <= p < s_pre[lo+1]
+            while (hi - lo > 1) {
+              const int mid = (lo + hi) >> 1;
+              if (s_pre[mid] <= p) lo = mid; else hi = mid;
+            }
+            const int sg = s_order[lo];
+            const int j2 = s_seg_a[sg] + (p - s_pre[lo]);
+            float4 q2 = J.f2.pos[j2];
+            q2.x -= g2sx;
+            q2.y -= g2sy;
+            q2.z -= g2sz;
+            s_pos[t] = q2;
+            if (C != COREL_DD) s_shp[t] = J.f2.shp[j2];
+            if (has_lo) s_lo[t] = J.f2.lo[j2];
+            s_jidx[t] = j2;
+            if (JK) s_keep[t] = J.f2.keep[j2];
+          }
+          __syncthreads();
+          if (valid) {
+            for (int c = 0; c < nb; ++c) {
+              const float4 p2 = s_pos[c];
+              const float dz = p2.z - z1s;
+              const float dx = x1s - p2.x;
+              const float dy = y1s - p2.y;
+              const float m = fmaxf(fabsf(dx), fabsf(dy));
+              if (!(dz >= pi_out_lo && dz <= pi_out_hi && m <= xy_out)) continue;
+              bool amb = !(dz >= pi_in_lo && dz <= pi_in_hi && m <= xy_in);
+              const float r2 = fmaf(dx, dx, dy * dy);
+              // Pi bin: approximate index, confirmed against the definite band
+              int n2 = (int)floorf(fmaf(dz, inv_ps, tp0));
+              n2 = min(max(n2, 0), npi - 1);
+              if (!(dz >= s_PA[n2] && dz < s_PB[n2])) {
+                if (n2 > 0 && dz >= s_PA[n2 - 1] && dz < s_PB[n2 - 1]) n2--;
+                else if (n2 + 1 < npi && dz >= s_PA[n2 + 1] && dz < s_PB[n2 + 1]) n2++;
+                else amb = true;
+              }
+              // r_p bin: log2 estimate, confirmed against the definite band
+              bool rout = false;
+              int n1 = 0;
+              if (r2 < rej_lo || r2 >= rej_hi) {
+                rout = true;
+              } else {
+                n1 = lin_bin ? (int)floorf((sqrtf(r2) - rmin_f) * inv_rsize_f)
+                               : (int)floorf((__log2f(r2) - l2rmin2) * inv_lw);
+                n1 = min(max(n1, 0), nrp - 1);
+                if (!(r2 >= s_A[n1] && r2 < s_B[n1])) {
+                  if (n1 > 0 && r2 >= s_A[n1 - 1] && r2 < s_B[n1 - 1]) n1--;
+                  else if (n1 + 1 < nrp && r2 >= s_A[n1 + 1] && r2 < s_B[n1 + 1]) n1++;
+                  else amb = true;
+                }
+              }
+              if (amb) {
+                enqueue(J, U.job, i1, s_jidx[c], code, queue, qcount, qcap);
+                continue;
+              }
+              if (rout) {
+                nwin++;
+                continue;
+              }
+              const int lk = n2 - n2_base;
+              if ((unsigned)lk >= (unsigned)wpi) {  // outside the block-local Pi window
+                enqueue(J, U.job, i1, s_jidx[c], code, queue, qcount, qcap);
+                continue;
+              }
+              nwin++;
+              const int lb = n1 * wpi + lk;
+              float v[kNF];
+              const float w = p1.w * p2.w;
+              v[0] = w;
+              if (C != COREL_DD) {
+                const float4 s2 = s_shp[c];
+                float dxr = (p2.x + g2sx) - p1.x;
+                float dyr = (p2.y + g2sy) - p1.y;
+                if (has_lo) {
+                  const float2 lo2 = s_lo[c];
+                  dxr += lo2.x - lo1.x;
+                  dyr += lo2.y - lo1.y;
+                }
+                const float a = dxr * dxr, b = dyr * dyr;
+                const float inv = 1.0f / (a + b);
+                const float c2 = (a - b) * inv, s2v = 2.0f * dxr * dyr * inv;
+                const float theta = atanf(dyr / dxr);
+                if (C == COREL_SD) {
+                  const float es0 = gws == 2 ? s2.x : e1v.x, es1 = gws == 2 ? s2.y : e1v.y;
+                  const float ep = c2 * es0 - s2v * es1, ex = s2v * es0 + c2 * es1;
+                  v[1] = w * ep;
+                  v[2] = v[1] * v[1];
+                  v[3] = w * ex;
+                  v[4] = v[3] * v[3];
+                  v[11] = ephi_f(e1v.z, theta);
+                  v[12] = v[11] * v[11];
+                } else {
+                  const float ei0 = c2 * e1v.x - s2v * e1v.y, ei1 = s2v * e1v.x + c2 * e1v.y;
+                  const float ej0 = c2 * s2.x - s2v * s2.y, ej1 = s2v * s2.x + c2 * s2.y;
+                  if (C == COREL_SS) {
+                    const bool g2s = gws == 2;
+                    v[1] = w * (g2s ? ej0 : ei0);
+                    v[2] = v[1] * v[1];
+                    v[11] = ephi_f(g2s ? s2.z : e1v.z, theta);
+                    v[12] = v[11] * v[11];
+                  } else {
+                    v[1] = w * (ei0 + ej0) * 0.5f;
+                    const float pa = w * ei0 * 0.5f, pb = w * ej0 * 0.5f;
+                    v[2] = pa * pa + pb * pb;
+                    v[3] = w * (ei1 + ej1) * 0.5f;
+                    const float qa = w * ei1 * 0.5f, qb = w * ej1 * 0.5f;
+                    v[4] = qa * qa + qb * qb;
+                    const float ta = ephi_f(e1v.z, theta), tb = ephi_f(s2.z, theta);
+                    v[11] = ta + tb;
+                    v[12] = ta * ta + tb * tb;
+                  }
+                  v[5] = w * (ei0 * ej0);
+                  v[6] = v[5] * v[5];
+                  v[7] = w * (ei1 * ej1);
+                  v[8] = v[7] * v[7];
+                  v[9] = w * (ei1 * ej0 + ei0 * ej1) * 0.5f;
+                  const float xa = w * (ei1 * ej0) * 0.5f, xb = w * ei0 * ej1 * 0.5f;
+                  v[10] = xa * xa + xb * xb;
+                }
+              }
+              atomicAdd(&s_mnum[lb], 1u);
+#pragma unroll
+              for (int f = 0; f < F::FM; f++) {
+                if (f < f0) continue;
+                const size_t o = (size_t)f * NB + lb;
+                acc_add(&s_mlo[o], &s_mhi[o], to_fixed(v[F::m(f)], s_qs[F::m(f)], qbias));
+              }
+              if (JK) {
+                const bool xc = same_region ? xsame : xdiff;
+                const bool yc = !same_region && s_keep[c];
+                if (xc) {
+                  atomicAdd(&s_xnum[lb], 1u);
+#pragma unroll
+                  for (int f = 0; f < F::FJ; f++) {
+                    if (f < f0) continue;
+                    const size_t o = (size_t)f * NB + lb;
+                    acc_add(&s_xlo[o], &s_xhi[o], to_fixed(v[F::j(f)], s_qs[F::j(f)], qbias));
+                  }
+                }
+                if (yc) {
+                  atomicAdd(&s_ynum[lb], 1u);
+#pragma unroll
+                  for (int f = 0; f < F::FJ; f++) {
+                    if (f < f0) continue;
+                    const size_t o = (size_t)f * NB + lb;
+                    acc_add(&s_ylo[o], &s_yhi[o], to_fixed(v[F::j(f)], s_qs[F::j(f)], qbias));
+                  }
+                }
+              }
+            }
+          }
+          __syncthreads();
+        }
+        k = g;
+      }
+      __syncthreads();
+    }
+
+    // ---- flush main, X and the last Y ----
+    __syncthreads();
+    {
+      const int64_t hstride = (int64_t)nrp * npi;
+      for (int lb = t; lb < NB; lb += kTile) {
+        const int n2 = n2_base + lb % wpi;
+        const int64_t cell = (int64_t)(lb / wpi) * npi + n2;
+        unsigned n = s_mnum[lb];
+        if (n) {
+          atomicAdd(&J.acc_num[cell], (unsigned long long)n);
+          s_mnum[lb] = 0u;
+#pragma unroll
+          for (int f = 0; f < F::FM; f++) {
+            const size_t o = (size_t)f * NB + lb;
+            if (f >= f0) {
+              const double v = fixed_total(s_mlo[o], s_mhi[o], n, qbias, s_iqs[F::m(f)]);
+              if (v != 0.0) atomicAdd(&J.acc_sums[cell * kNF + F::m(f)], v);
+            }
+            s_mlo[o] = 0u;
+            s_mhi[o] = 0u;
+          }
+        }
+        if (JK) {
+          n = s_xnum[lb];
+          if (n) {
+            const int64_t hc = (int64_t)(1 + U.region) * hstride + cell;
+            atomicAdd(&J.acc_num[hc], (unsigned long long)n);
+            s_xnum[lb] = 0u;
+#pragma unroll
+            for (int f = 0; f < F::FJ; f++) {
+              const size_t o = (size_t)f * NB + lb;
+              if (f >= f0) {
+                const double v = fixed_total(s_xlo[o], s_xhi[o], n, qbias, s_iqs[F::j(f)]);
+                if (v != 0.0) atomicAdd(&J.acc_sums[hc * kNF + F::j(f)], v);
+              }
+              s_xlo[o] = 0u;
+              s_xhi[o] = 0u;
+            }
+          }
+          n = s_ynum[lb];
+          if (n) {
+            const int64_t hc = (int64_t)(1 + cur_y) * hstride + cell;
+            atomicAdd(&J.acc_num[hc], (unsigned long long)n);
+            s_ynum[lb] = 0u;
+#pragma unroll
+            for (int f = 0; f < F::FJ; f++) {
+              const size_t o = (size_t)f * NB + lb;
+              if (f >= f0) {
+                const double v = fixed_total(s_ylo[o], s_yhi[o], n, qbias, s_iqs[F::j(f)]);
+                if (v != 0.0) atomicAdd(&J.acc_sums[hc * kNF + F::j(f)], v);
+              }
+              s_ylo[o] = 0u;
+              s_yhi[o] = 0u;
+            }
+          }
+        }
+      }
+    }
+    // window-pair counter
+    {
+      unsigned long long v = nwin;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if ((t & 31) == 0) s_red[t >> 5] = v;
+      __syncthreads();
+      if (t == 0) {
+        unsigned long long s = 0;
+        for (int w = 0; w < kTile / 32; w++) s += s_red[w];
+        if (s) atomicAdd(&J.counters[0], s);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Exact FP64 re-evaluation of the edge queue.
+__global__ void recheck_kernel(const JobDev *__restrict__ jobs, const QEntry *__restrict__ queue,
+                               const unsigned long long *__restrict__ qcount,
+                               unsigned long long qcap) {
+  const unsigned long long n = min(*qcount, qcap);
+  for (unsigned long long idx = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+       idx += (unsigned long long)gridDim.x * blockDim.x) {
+    const QEntry e = queue[idx];
+    const JobDev &J = jobs[e.job];
+    int sx, sy, sz, n1, n2;
+    shift_decode(e.shift, sx, sy, sz);
+    const int r = exact_classify(J, J.d1, e.i1, J.d2, e.j2, sx, sy, sz, n1, n2);
+    atomicAdd(&J.counters[2], 1ull);
+    if (r == 0) continue;
+    atomicAdd(&J.counters[1], 1ull);
+    if (r == 2) {
+      double f[kNF];
+      exact_values(J, J.d1, e.i1, J.d2, e.j2, f);
+      exact_accumulate(J, J.d1, e.i1, J.d2, e.j2, n1, n2, f);
+    }
+  }
+}
+
+// ---- host-side launchers (called from capi.cu) ----
+template <int C, bool JK>
+static cudaError_t launch_fast_t(const JobDev *jobs, const UnitDesc *units, int n_units,
+                                 unsigned int *unit_ctr, QEntry *q, unsigned long long *qcount,
+                                 unsigned long long qcap, size_t smem, int grid,
+                                 cudaStream_t st) {
+  auto kern = fast_pairs_kernel<C, JK>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  const int zero_words = (int)((smem - sizeof(float4) * 2 * kTile) / 4);
+  kern<<<grid, kTile, smem, st>>>(jobs, units, n_units, unit_ctr, q, qcount, qcap, zero_words);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fast(int corel, int jk, const JobDev *jobs, const UnitDesc *units, int n_units,
+                        unsigned int *unit_ctr, QEntry *q, unsigned long long *qcount,
+                        unsigned long long qcap, size_t smem, int grid, cudaStream_t st) {
+#define CPC_CASE(CC)                                                                         \
+  if (corel == CC) {                                                                         \
+    return jk ? launch_fast_t<CC, true>(jobs, units, n_units, unit_ctr, q, qcount, qcap, smem, \
+                                        grid, st)                                            \
+              : launch_fast_t<CC, false>(jobs, units, n_units, unit_ctr, q, qcount, qcap,    \
+                                         smem, grid, st);                                    \
+  }
+  CPC_CASE(COREL_DD)
+  CPC_CASE(COREL_SD)
+  CPC_CASE(COREL_SS)
+  CPC_CASE(COREL_SSA)
+#undef CPC_CASE
+  return cudaErrorInvalidValue;
+}
+
+int fast_blocks_per_sm(int corel, int jk, size_t smem) {
+  int nb = 0;
+  cudaError_t e = cudaErrorInvalidValue;
+#define CPC_OCC(CC)                                                                             \
+  if (corel == CC) {                                                                            \
+    if (jk) {                                                                                   \
+      cudaFuncSetAttribute(fast_pairs_kernel<CC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fast_pairs_kernel<CC, true>, kTile, smem); \
+    } else {                                                                                    \
+      cudaFuncSetAttribute(fast_pairs_kernel<CC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fast_pairs_kernel<CC, false>, kTile, smem); \
+    }                                                                                           \
+  }
+  CPC_OCC(COREL_DD)
+  CPC_OCC(COREL_SD)
+  CPC_OCC(COREL_SS)
+  CPC_OCC(COREL_SSA)
+#undef CPC_OCC
+  return e == cudaSuccess ? nb : 0;
+}
+
+cudaError_t launch_recheck(const JobDev *jobs, const QEntry *q, const unsigned long long *qcount,
+                           unsigned long long qcap, int grid, cudaStream_t st) {
+  recheck_kernel<<<grid, 256, 0, st>>>(jobs, q, qcount, qcap);
+  return cudaGetLastError();
+}
+
+}  // namespace cpc
+
+namespace cpc {
+size_t fast_static_smem_bytes() {
+  cudaFuncAttributes a;
+  if (cudaFuncGetAttributes(&a, fast_pairs_kernel<COREL_SS, true>) != cudaSuccess) return 24 * 1024;
+  return a.sharedSizeBytes;
+}
+}  // namespace cpc

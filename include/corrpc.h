@@ -1,0 +1,193 @@
+/*
+ * corrpc.h -- C ABI of the GB300 pair-counting library (libcorrpc_gb300.so).
+ *
+ * Drop-in boundary for corr_pc's pair loop.  The reference runs one pair type
+ * per call of
+ *     long corels2(gal g1[], gal g2[], bin_jk &bjk, data_info &data_inf)
+ *     (corr.cpp:219-459, called from do_corr.cpp:70,78,110,115,125,131)
+ * selecting the pair type through data_inf.do_SD/do_SRd/do_DRs/do_RsRd/do_RsRs/
+ * do_SRs.  This ABI replaces that body: the caller flattens the two gal[]
+ * arrays into plain arrays (cpc_catalog), uploads them once, and calls
+ * cpc_count with the same pair-type code; the library applies corels2's own
+ * rules (shape-holder choice and g1/g2 swap, corr.cpp:226-296; corel choice,
+ * initialization.cpp:699-752), counts on the GPU and returns the histogram
+ * block, which the caller scatters into its bin_jk tree followed by the
+ * delete-one conversion final_jk_bins (jk.cpp:74-81), exactly as corels2 ends.
+ *
+ * Conventions: plain pointers and sizes only; every entry point returns a
+ * cpc_status and never aborts; cpc_last_error() gives a message.  One context
+ * per host thread; a context owns all its device memory.  Host arrays are
+ * copied (never aliased after the call returns).
+ */
+#ifndef CORRPC_H
+#define CORRPC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  CPC_OK = 0,
+  CPC_ERR_INVALID = 1,     /* bad argument or unsupported configuration */
+  CPC_ERR_CUDA = 2,        /* CUDA runtime error (message in cpc_last_error) */
+  CPC_ERR_NOMEM = 3,       /* device or host allocation failed */
+  CPC_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
+  CPC_ERR_STATE = 5,       /* call order (e.g. count before upload) */
+  CPC_ERR_RANGE = 6,       /* data out of range (jackknife label, NaN position) */
+  CPC_ERR_NODEVICE = 7     /* no CUDA device */
+} cpc_status;
+
+/* pair type: the data_info.do_* flag set around each corels2 call
+ * (do_corr.cpp:61-131) */
+typedef enum {
+  CPC_PAIR_SD = 0,   /* do_SD   : corels2(gdensity, gshape, ...)        */
+  CPC_PAIR_SRD = 1,  /* do_SRd  : corels2(grand_density, gshape, ...)   */
+  CPC_PAIR_DRS = 2,  /* do_DRs  : corels2(grand_shape, gdensity, ...)   */
+  CPC_PAIR_RSRD = 3, /* do_RsRd : corels2(grand_density, grand_shape)   */
+  CPC_PAIR_RSRS = 4, /* do_RsRs : corels2(grand_shape, grand_shape)     */
+  CPC_PAIR_SRS = 5   /* do_SRs  : corels2(grand_shape, gshape, ...)     */
+} cpc_pair_kind;
+
+/* which kernel counts the pairs */
+typedef enum {
+  CPC_ENGINE_FAST = 0, /* FP32 cell-list kernel with FP64 recheck near edges */
+  CPC_ENGINE_FP64 = 1  /* plain all-FP64 kernel: one thread per g1 row      */
+} cpc_engine;
+
+/* Parameters: the data_info fields the pair loop reads (data_def.h:46-96),
+ * with the values data_ini computes (initialization.cpp:62-352). */
+typedef struct {
+  int which_corr;    /* 0 wgg, 1 wg+, 2 w++ */
+  int coordinates;   /* 6: x,y,z (r_p, Pi); 0: sky ra,dec,z (r_p, Pi) */
+  int estimator;     /* 0..3 (affects the shape-shape accumulators only) */
+  int periodic_box;  /* 1: periodic images (coordinates 6 only) */
+  int data_sorted;   /* 0/1: as in the .inp (results follow set semantics) */
+  int do_jk;         /* 0 or 1 (1 = delete-one jackknife) */
+  int n_jk;          /* number of jackknife regions (labels 0..n_jk-1) */
+  int sig_crit;      /* must be 0 (lensing weights are not supported) */
+  int rand_subsample;/* must be 0 */
+  int n_bins;        /* r_p bins */
+  int lin_bin;       /* 1 linear, 0 log10 */
+  int n_p_bin;       /* Pi bins */
+  double bin_r_min, bin_r_max;
+  double p_min, p_max;
+  double periodic_box_size;
+  /* sky only (coordinates 0): */
+  double z_max, dz, z_sep_max;
+  const double *H_z;   /* distance table columns as read by da_Z */
+  const double *dA_z;  /* (initialization.cpp:23-60), n_table entries */
+  int64_t n_table;
+} cpc_params;
+
+/* One catalogue: the gal[] fields the pair loop reads (data_def.h:23-44),
+ * flattened.  Box: x,y,z = ra.val_deg, dec.val_deg, redshift.  Sky: x = RA
+ * degrees, y = Dec degrees, z = redshift, plus dc/da.  Optional arrays may be
+ * NULL: w (weights 1), e1/e2 (no shapes: treated as 0), phi (-10, the
+ * reference's value for galaxies read without e), jk (required when do_jk),
+ * jk_prob (0), dc/da (sky only). */
+typedef struct {
+  int64_t n;
+  const double *x, *y, *z;
+  const double *w;
+  const double *e1, *e2;
+  const double *phi;
+  const int32_t *jk;
+  const double *jk_prob;
+  const double *dc, *da;
+} cpc_catalog;
+
+#define CPC_NF 13 /* wt_num, data[1..6].val, data[1..6].err interleaved */
+
+/* Histogram block written by cpc_count (caller-owned host memory):
+ *   num [n_hist][n_bins][n_p_bin]            p_bin.num      (int64)
+ *   sums[n_hist][n_bins][n_p_bin][CPC_NF]    p_bin.wt_num, data[j].val/.err
+ * field f: 0 wt_num; 1+2(j-1) data[j].val; 2+2(j-1) data[j].err (j = 1..6).
+ * h = 0 is the full sample; h = 1+r is the RAW sum over pairs attributed to
+ * jackknife region r (jk.cpp:138-171), before the delete-one conversion.
+ * n_hist = 1 + (do_jk ? n_jk : 0).  The 1-D r_p count b[i].num is the sum of
+ * num over the Pi bins. */
+typedef struct {
+  int64_t *num;
+  double *sums;
+  int64_t n_window;   /* corels2 "total pair"  (window pairs) */
+  int64_t n_binned;   /* corels2 "pairs in"    (its return value) */
+  int64_t n_rechecked;/* pairs resolved on the FP64 edge path (diagnostic) */
+  double kernel_ms;   /* device time of the whole count (zeroing, pair kernel, recheck) */
+  double pair_kernel_ms; /* device time of the pair-kernel launch(es) alone */
+} cpc_accum;
+
+typedef struct cpc_ctx cpc_ctx;
+
+/* Library version string. */
+const char *cpc_version(void);
+
+/* Create a context on the current CUDA device.  Validates params. */
+cpc_status cpc_create(cpc_ctx **ctx, const cpc_params *params);
+
+/* Destroy a context and free its device memory (NULL is a no-op). */
+cpc_status cpc_destroy(cpc_ctx *ctx);
+
+/* Message for the last failing call on ctx (or a global message if ctx is
+ * NULL).  The pointer stays valid until the next call on ctx. */
+const char *cpc_last_error(const cpc_ctx *ctx);
+
+/* Copy a catalogue into slot `slot` (0..7) and build its on-device cell list
+ * (radix sort by (column, region, z)).  Replaces any previous catalogue in the
+ * slot.  Validates labels (0 <= jk < n_jk when do_jk) and finite positions. */
+cpc_status cpc_upload(cpc_ctx *ctx, int slot, const cpc_catalog *cat);
+
+/* Count one pair type between the catalogues in slots slot_g1, slot_g2 --
+ * the two arrays corels2 receives, in its argument order -- and write the
+ * histogram block into *out (arrays sized by the caller, see cpc_accum).
+ * row_stride/row_offset > 1 restrict the outer loop to rows whose original
+ * index i (after the swap rule) has (i - row_offset) % row_stride == 0
+ * (1, 0 = all rows).  Synchronous. */
+cpc_status cpc_count(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_g2,
+                     cpc_engine engine, int64_t row_stride, int64_t row_offset,
+                     cpc_accum *out);
+
+/* Histogram shape for this context: n_hist, n_bins, n_p_bin. */
+cpc_status cpc_accum_shape(const cpc_ctx *ctx, int *n_hist, int *n_bins, int *n_p_bin);
+
+/* Batched counting: run n_jobs pair types, possibly on different contexts
+ * (e.g. many periodic sub-boxes), in ONE persistent launch of the fast
+ * kernel that drains a single device work queue.  ctxs[k], kinds[k],
+ * slots_g1[k], slots_g2[k] and outs[k] describe job k.  All contexts must
+ * live on the current device.  Synchronous. */
+cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind *kinds,
+                           const int *slots_g1, const int *slots_g2, cpc_accum *outs);
+
+/* Tuning knobs of the fast kernel (0 = automatic).  cells_per_rmax: column
+ * width = r_max / k; pi_window: Pi bins held per block; tile: g1 rows per
+ * block (64 or 128). */
+cpc_status cpc_set_tuning(cpc_ctx *ctx, int cells_per_rmax, int pi_window, int tile);
+
+/* Number of GPU kernels this context has launched so far (all entry points;
+ * for a batch, counted on the first job's context). */
+cpc_status cpc_launch_count(const cpc_ctx *ctx, int64_t *launches);
+
+/* ---- host helpers of the reference's read path (no GPU needed) ---- */
+
+/* glibc rand() stream after srand(seed): out[i] = rand_{skip+i}() /
+ * (RAND_MAX + 1.) (read_dat.cpp:243, 320; seed 124693517 per jk.cpp:40-43). */
+cpc_status cpc_host_rand_uniform(uint32_t seed, int64_t skip, int64_t n, double *out);
+
+/* phi = 0.5 * arctan(e1, -e2) with the reference's quadrant rule, NaN -> 0
+ * (elip_angle, calcs.cpp:73-83). */
+cpc_status cpc_host_elip_angle(int64_t n, const double *e1, const double *e2, double *phi);
+
+/* The exact r_p bin thresholds the library uses: thr[k] = smallest double r
+ * with floor(log10(r/r_min)/r_size) >= k (log bins) or the linear analogue,
+ * k = 0..n_bins (corels.cpp:41-44).  thr has n_bins+1 entries. */
+cpc_status cpc_host_rp_thresholds(const cpc_params *params, double *thr);
+
+/* The exact Pi bin thresholds: thr[k] = smallest double Pi with
+ * floor((Pi - p_min)/p_size) >= k, k = 0..n_p_bin (corels.cpp:26). */
+cpc_status cpc_host_pi_thresholds(const cpc_params *params, double *thr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CORRPC_H */
