@@ -26,7 +26,7 @@ NF = 13
 EXPORTED = ["cpc_version", "cpc_create", "cpc_destroy", "cpc_last_error", "cpc_upload",
             "cpc_count", "cpc_accum_shape", "cpc_count_batch", "cpc_set_tuning",
             "cpc_host_rand_uniform", "cpc_host_elip_angle", "cpc_host_rp_thresholds",
-            "cpc_host_pi_thresholds", "cpc_launch_count"]
+            "cpc_host_pi_thresholds", "cpc_launch_count", "cpc_host_finalize_cross"]
 
 
 class CpcError(RuntimeError):
@@ -85,10 +85,11 @@ def load() -> ctypes.CDLL:
     lib.cpc_host_rp_thresholds.argtypes = [P(cpc_params), V]
     lib.cpc_host_pi_thresholds.argtypes = [P(cpc_params), V]
     lib.cpc_launch_count.argtypes = [V, P(I64)]
+    lib.cpc_host_finalize_cross.argtypes = [ctypes.c_char_p] + [V] * 9
     for fn in ("cpc_create", "cpc_destroy", "cpc_upload", "cpc_count", "cpc_accum_shape",
                "cpc_count_batch", "cpc_set_tuning", "cpc_host_rand_uniform",
                "cpc_host_elip_angle", "cpc_host_rp_thresholds", "cpc_host_pi_thresholds",
-               "cpc_launch_count"):
+               "cpc_launch_count", "cpc_host_finalize_cross"):
         getattr(lib, fn).restype = I
     _lib = lib
     return lib
@@ -242,3 +243,20 @@ def pi_thresholds(inp_params) -> np.ndarray:
     out = np.empty(inp_params.n_p_bin + 1, dtype=np.float64)
     check(load().cpc_host_pi_thresholds(ctypes.byref(cp), out.ctypes.data))
     return out
+
+
+def finalize_cross(inp_path: str, terms: dict, weights) -> None:
+    """Finalisation + output files from RAW histogram blocks.  terms: dict with
+    keys among SD, SRd, DRs, RsRd -> (num, sums); weights: 8 totals."""
+    args = []
+    for k in ("SD", "SRd", "DRs", "RsRd"):
+        if k in terms:
+            n, s = terms[k]
+            n = np.ascontiguousarray(n, dtype=np.int64)
+            s = np.ascontiguousarray(s, dtype=np.float64)
+            terms[k] = (n, s)
+            args += [n.ctypes.data, s.ctypes.data]
+        else:
+            args += [None, None]
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    check(load().cpc_host_finalize_cross(inp_path.encode(), *args, w.ctypes.data))

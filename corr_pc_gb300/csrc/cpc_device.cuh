@@ -87,8 +87,10 @@ struct UnitDesc {
 };
 
 struct QEntry {
-  int job, i1, j2, shift;  // shift code: (sx+1) + 3*(sy+1) + 9*(sz+1)
+  int job, i1, j2, shift;  // shift code: (sx+1) + 3*(sy+1) + 9*(sz+1), | kWindowCounted
 };
+constexpr int kShiftMask = 31;
+constexpr int kWindowCounted = 32;  // the fast path already counted this window pair
 
 __host__ __device__ inline int shift_code(int sx, int sy, int sz) {
   return (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);

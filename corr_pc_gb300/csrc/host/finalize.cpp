@@ -1,0 +1,306 @@
+// finalize.cpp -- bin trees and the estimator finalisation of a cross run
+// (do_corr.cpp:326-431 with bins_calcs.cpp:30-52, 94-256, 331-462 and the
+// analytic periodic-box RR of PB_calcs.cpp:63-85).  Bin edges are formed in
+// single precision exactly as the reference's initialisers do
+// (initialization.cpp:357-444), because they are printed in the outputs.
+#include <cmath>
+#include <cstdio>
+#include <sstream>
+
+#include "host.h"
+
+namespace cpch {
+
+int outp_bins(const Bins &b, int h, const std::string &path);
+int outp_2Dbins(const Bins &b, int h, const std::string &path);
+
+void Bins::init(const Info &d, int n_hist) {
+  nb = d.n_bins;
+  np = d.n_p_bin;
+  nh = n_hist;
+  b_min.assign(nb, 0); b_max.assign(nb, 0); p_min.assign(np, 0); p_max.assign(np, 0);
+  if (d.lin_bin) {  // bin_lin
+    const float b_size = (d.bin_r_max - d.bin_r_min) / (float)d.n_bins;
+    float temp = d.bin_r_min;
+    for (int i = 0; i < nb; i++) {
+      b_min[i] = temp;
+      temp += b_size;
+      b_max[i] = temp;
+    }
+  } else {  // bin_log
+    float lo = std::log10(d.bin_r_min);
+    const float hi = std::log10(d.bin_r_max);
+    const float b_size = (hi - lo) / (float)d.n_bins;
+    for (int i = 0; i < nb; i++) {
+      b_min[i] = std::pow(10.0, lo);
+      lo += b_size;
+      b_max[i] = std::pow(10.0, lo);
+    }
+  }
+  {  // P_bin_ini
+    const float ps = d.p_size;
+    float temp = d.p_min;
+    for (int k = 0; k < np; k++) {
+      p_min[k] = temp;
+      temp += ps;
+      p_max[k] = temp;
+    }
+  }
+  const size_t nbh = (size_t)nh * nb, nph = nbh * np;
+  bnum.assign(nbh, 0); bwt.assign(nbh, 0); bdat.assign(nbh * 14, 0); bls.assign(nbh, 0);
+  bsig.assign(nbh, 0);
+  pnum.assign(nph, 0); pwt.assign(nph, 0); pdat.assign(nph * 14, 0); pls.assign(nph, 0);
+}
+
+void add_count(Bins &b, const Info &d, const int64_t *num, const double *sums) {
+  for (int h = 0; h < b.nh; h++)
+    for (int i = 0; i < b.nb; i++)
+      for (int k = 0; k < b.np; k++) {
+        const size_t c = b.pi(h, i, k);
+        const int64_t n = num[c];
+        b.pnum[c] += n;
+        b.bnum[b.bi(h, i)] += n;  // b[n1].num++ for every binned pair
+        const double *s = sums + c * CPC_NF;
+        b.pwt[c] += s[0];
+        for (int j = 1; j <= 6; j++) {
+          b.pd(h, i, k, j, 0) += s[1 + 2 * (j - 1)];
+          b.pd(h, i, k, j, 1) += s[2 + 2 * (j - 1)];
+        }
+      }
+  if (!d.do_jk) return;
+  // final_jk_bins: every field of sample r := full - region r
+  for (int h = 1; h < b.nh; h++)
+    for (int i = 0; i < b.nb; i++) {
+      const size_t f = b.bi(0, i), r = b.bi(h, i);
+      b.bnum[r] = b.bnum[f] - b.bnum[r];
+      b.bwt[r] = b.bwt[f] - b.bwt[r];
+      b.bls[r] = b.bls[f] - b.bls[r];
+      b.bsig[r] = b.bsig[f] - b.bsig[r];
+      for (int j = 0; j < 7; j++)
+        for (int e = 0; e < 2; e++) b.bd(h, i, j, e) = b.bd(0, i, j, e) - b.bd(h, i, j, e);
+      for (int k = 0; k < b.np; k++) {
+        const size_t pf = b.pi(0, i, k), pr = b.pi(h, i, k);
+        b.pnum[pr] = b.pnum[pf] - b.pnum[pr];
+        b.pwt[pr] = b.pwt[pf] - b.pwt[pr];
+        b.pls[pr] = b.pls[pf] - b.pls[pr];
+        for (int j = 0; j < 7; j++)
+          for (int e = 0; e < 2; e++) b.pd(h, i, k, j, e) = b.pd(0, i, k, j, e) - b.pd(h, i, k, j, e);
+      }
+    }
+}
+
+namespace {
+
+// RR_PB_calc: expected pair fraction per (r_p, Pi) bin in a periodic box
+void rr_periodic(Bins &rr, int h, const Info &d) {
+  const double total_volume = std::pow(d.periodic_box_size, 3);
+  for (int i = 0; i < rr.nb; i++) {
+    double area = 0;
+    if (d.coordinates == 6) area = M_PI * (rr.b_max[i] * rr.b_max[i] - rr.b_min[i] * rr.b_min[i]);
+    rr.bnum[rr.bi(h, i)] = 1;
+    for (int k = 0; k < rr.np; k++) {
+      double volume = 0;
+      if (d.coordinates == 6) volume = area * (rr.p_max[k] - rr.p_min[k]);
+      rr.pwt[rr.pi(h, i, k)] = volume / total_volume;
+      rr.pnum[rr.pi(h, i, k)] = 1;
+    }
+  }
+}
+
+// final_calc_bins (bins_calcs.cpp:94-256) for sample h of each term
+void final_bins(Bins &sd, Bins &sr, Bins &dr, Bins &rr, Bins &fin, int h, const Info &d) {
+  const double SD_wt = d.SD_wt[0], SR_wt = d.SRd_wt[0], DR_wt = d.DRs_wt[0], RR_wt = d.RsRd_wt[0];
+  for (int i = 0; i < sd.nb; i++) {
+    for (int k = 0; k < sd.np; k++) {
+      const size_t c = sd.pi(h, i, k);
+      fin.bnum[fin.bi(h, i)] += sd.pnum[c];
+      const double sd_num = (double)sd.pnum[c], sr_num = (double)sr.pnum[c];
+      const double rr_num = (double)rr.pnum[c];
+      const double sd_w = sd.pwt[c], sr_w = sr.pwt[c], dr_w = dr.pwt[c], rr_w = rr.pwt[c];
+      if (rr_num == 0) continue;
+      const double sd_rel = (sd_w / rr_w) * (RR_wt / SD_wt);
+      const double sr_rel = (sr_w / rr_w) * (RR_wt / SR_wt);
+      const double dr_rel = (dr_w / rr_w) * (RR_wt / DR_wt);
+      double w = sd_rel - sr_rel - dr_rel + 1.0;  // Landy-Szalay
+      if (d.periodic_box) w = sd_rel - 1.0;
+      fin.pd(h, i, k, 0, 0) = w;
+      sd.pd(h, i, k, 0, 0) = sd_rel;
+      sr.pd(h, i, k, 0, 0) = sr_rel;
+      dr.pd(h, i, k, 0, 0) = dr_rel;
+      rr.pd(h, i, k, 0, 0) = 1.0;
+      if (d.which_corr == 0) continue;
+      for (int j = 1; j < 7; j++) {
+        const double sd_val = sd.pd(h, i, k, j, 0), sr_val = sr.pd(h, i, k, j, 0);
+        const double sd_norm = (sd_val / rr_w) * (RR_wt / SD_wt);
+        const double sr_norm = (sr_val / rr_w) * (RR_wt / SR_wt);
+        double val = sd_norm - sr_norm;
+        if (sd_num == 0 || sr_num == 0 || rr_num == 0) {
+          val = 0;
+          if (d.periodic_box) val = sd_norm;
+        }
+        fin.pd(h, i, k, j, 0) = val;
+        sr.pd(h, i, k, j, 0) = sr_norm;  // sd keeps its raw sum
+        if (j == 6) {
+          sd.pd(h, i, k, j, 0) = sd_num == 0 ? 0.0 : sd_val;
+          sr.pd(h, i, k, j, 0) = sr_num == 0 ? 0.0 : sr_val;
+        }
+      }
+    }
+  }
+}
+
+// int_calc (bins_calcs.cpp:331-357): integrate over Pi
+void integrate(Bins &b, int h, const Info &d) {
+  const double dC = d.p_size;
+  for (int i = 0; i < b.nb; i++) {
+    const size_t bi = b.bi(h, i);
+    for (int k = 0; k < b.np; k++) {
+      const size_t c = b.pi(h, i, k);
+      b.bwt[bi] += b.pwt[c];
+      for (int j = 0; j < 7; j++) {
+        b.bd(h, i, j, 0) += b.pd(h, i, k, j, 0) * dC;
+        b.bd(h, i, j, 1) += std::pow(b.pd(h, i, k, j, 1) * dC, 2);
+      }
+      b.bls[bi] += std::pow(b.pls[c] * dC, 2);
+    }
+    for (int j = 0; j < 7; j++) b.bd(h, i, j, 1) = std::sqrt(b.bd(h, i, j, 1));
+    b.bls[bi] = std::sqrt(b.bls[bi]);
+  }
+}
+
+// final_calc (6-argument form, bins_calcs.cpp:30-52)
+void final_calc(Info &d, Bins &sd, Bins &sr, Bins &dr, Bins &rr, Bins &fin, int h) {
+  auto rel = [](const double *w) { return w[1] / std::pow(w[0], 2); };
+  d.SD_wt[0] = d.S_wt[0] * d.D_wt[0];
+  d.SD_wt[1] = d.SD_wt[0] * std::sqrt(rel(d.S_wt) + rel(d.D_wt));
+  d.DRs_wt[0] = d.Rs_wt[0] * d.D_wt[0];
+  d.DRs_wt[1] = d.DRs_wt[0] * std::sqrt(rel(d.Rs_wt) + rel(d.D_wt));
+  d.SRd_wt[0] = d.S_wt[0] * d.Rd_wt[0];
+  d.SRd_wt[1] = d.SRd_wt[0] * std::sqrt(rel(d.S_wt) + rel(d.Rd_wt));
+  d.RsRd_wt[0] = d.Rs_wt[0] * d.Rd_wt[0] * d.include_prob_RR * d.include_prob_RR;
+  d.RsRd_wt[1] = d.RsRd_wt[0] * std::sqrt(rel(d.Rs_wt) + rel(d.Rd_wt));
+  if (d.periodic_box) {
+    d.RsRd_wt[0] = 1;
+    d.RsRd_wt[1] = 0;
+    rr_periodic(rr, h, d);
+  }
+  final_bins(sd, sr, dr, rr, fin, h, d);
+  integrate(sd, h, d);
+  integrate(sr, h, d);
+  integrate(dr, h, d);
+  integrate(rr, h, d);
+  integrate(fin, h, d);
+}
+
+// jk_final / jk_final2D (bins_calcs.cpp:393-462): value of the full sample,
+// error from the spread of the delete-one samples
+void jk_final(Bins &out, Bins &fin, const Info &d) {
+  const int nj = d.n_jk;
+  const double f = (nj - 1.0) / nj;
+  for (int i = 0; i < fin.nb; i++) {
+    for (int j = 0; j < 7; j++) {
+      double mean = 0, var = 0;
+      for (int r = 1; r <= nj; r++) mean += fin.bd(r, i, j, 0);
+      mean /= nj;
+      for (int r = 1; r <= nj; r++) var += std::pow(fin.bd(r, i, j, 0) - mean, 2.0);
+      var *= f;
+      out.bd(0, i, j, 0) = fin.bd(0, i, j, 0);
+      out.bd(0, i, j, 1) = std::sqrt(var);
+    }
+    for (int k = 0; k < fin.np; k++)
+      for (int j = 0; j < 7; j++) {
+        double mean = 0, var = 0;
+        for (int r = 1; r <= nj; r++) mean += fin.pd(r, i, k, j, 0);
+        mean /= nj;
+        for (int r = 1; r <= nj; r++) var += std::pow(fin.pd(r, i, k, j, 0) - mean, 2.0);
+        var *= f;
+        out.pd(0, i, k, j, 0) = fin.pd(0, i, k, j, 0);
+        out.pd(0, i, k, j, 1) = std::sqrt(var);
+      }
+  }
+}
+
+}  // namespace
+
+int do_bining_cross(Info &d, Bins &SD, Bins &SRd, Bins &DRs, Bins &RsRd, std::string &err) {
+  const std::string &o = d.out_file;
+  Bins SRs;  // the auto-term histogram, never filled in a cross run
+  SRs.init(d, 1);
+  int bad = 0;
+  bad |= outp_2Dbins(SRs, 0, o + "bins_auto_SR.temp");
+  bad |= outp_2Dbins(SRd, 0, o + "bins_cross_SR.temp");
+  Bins fin;
+  fin.init(d, SD.nh);
+  final_calc(d, SD, SRd, DRs, RsRd, fin, 0);
+  bad |= outp_bins(fin, 0, o + "bins_cross_final.dat");
+  bad |= outp_2Dbins(fin, 0, o + "bins2D_cross_final.dat");
+  bad |= outp_bins(SD, 0, o + "bins_cross_SD.dat");
+  bad |= outp_2Dbins(SD, 0, o + "bins2D_cross_SD.dat");
+  bad |= outp_bins(SRd, 0, o + "bins_cross_SR.dat");
+  bad |= outp_2Dbins(SRd, 0, o + "bins2D_cross_SR.dat");
+  bad |= outp_bins(DRs, 0, o + "bins_cross_DR.dat");
+  bad |= outp_2Dbins(DRs, 0, o + "bins2D_cross_DR.dat");
+  bad |= outp_bins(RsRd, 0, o + "bins_cross_RR.dat");
+  bad |= outp_2Dbins(RsRd, 0, o + "bins2D_cross_RR.dat");
+  if (d.do_jk) {
+    for (int r = 0; r < d.n_jk; r++) {
+      const int h = r + 1;
+      final_calc(d, SD, SRd, DRs, RsRd, fin, h);
+      const std::string s = o + "bins_cross_jk" + std::to_string(r);
+      const std::string s2 = o + "bins2D_cross_jk" + std::to_string(r);
+      bad |= outp_bins(SD, h, s + "_SD.dat");
+      bad |= outp_bins(RsRd, h, s + "_RR.dat");
+      bad |= outp_bins(DRs, h, s + "_DR.dat");
+      bad |= outp_bins(SRd, h, s + "_SR.dat");
+      bad |= outp_bins(fin, h, s + "_final.dat");
+      bad |= outp_2Dbins(fin, h, s2 + "_final.dat");
+      bad |= outp_2Dbins(SD, h, s2 + "_SD.dat");
+      bad |= outp_2Dbins(RsRd, h, s2 + "_RR.dat");
+      bad |= outp_2Dbins(DRs, h, s2 + "_DR.dat");
+      bad |= outp_2Dbins(SRd, h, s2 + "_SR.dat");
+    }
+    Bins jk;
+    jk.init(d, 1);
+    jk_final(jk, fin, d);
+    bad |= outp_bins(jk, 0, o + "bins_cross_jk_final.dat");
+    bad |= outp_2Dbins(jk, 0, o + "bins2D_cross_jk_final.dat");
+  }
+  if (bad) {
+    err = "could not write output files with prefix " + o;
+    return 1;
+  }
+  return 0;
+}
+
+}  // namespace cpch
+
+// C ABI: finalisation and output files of a cross run from raw histogram
+// blocks (the cpc_count layout), e.g. blocks counted elsewhere or summed over
+// several processes.  NULL term arrays are empty terms.
+extern "C" cpc_status cpc_host_finalize_cross(const char *inp_path, const int64_t *sd_num,
+                                              const double *sd_sums, const int64_t *srd_num,
+                                              const double *srd_sums, const int64_t *drs_num,
+                                              const double *drs_sums, const int64_t *rsrd_num,
+                                              const double *rsrd_sums, const double *weights) {
+  using namespace cpch;
+  if (!inp_path || !weights) return CPC_ERR_INVALID;
+  Info d;
+  std::string err;
+  if (read_inp(inp_path, d, err) || derive_info(d, err)) return CPC_ERR_INVALID;
+  d.S_wt[0] = weights[0]; d.S_wt[1] = weights[1];
+  d.D_wt[0] = weights[2]; d.D_wt[1] = weights[3];
+  d.Rs_wt[0] = weights[4]; d.Rs_wt[1] = weights[5];
+  d.Rd_wt[0] = weights[6]; d.Rd_wt[1] = weights[7];
+  const int nh = 1 + (d.do_jk ? d.n_jk : 0);
+  Bins SD, SRd, DRs, RsRd;
+  SD.init(d, nh); SRd.init(d, nh); DRs.init(d, nh); RsRd.init(d, nh);
+  const int64_t *nums[4] = {sd_num, srd_num, drs_num, rsrd_num};
+  const double *sums[4] = {sd_sums, srd_sums, drs_sums, rsrd_sums};
+  Bins *terms[4] = {&SD, &SRd, &DRs, &RsRd};
+  for (int k = 0; k < 4; k++)
+    if (nums[k] && sums[k]) add_count(*terms[k], d, nums[k], sums[k]);
+  outp_data_info(d, d.out_file + "inp.info");
+  if (do_bining_cross(d, SD, SRd, DRs, RsRd, err)) return CPC_ERR_INVALID;
+  outp_data_info(d, d.out_file + "inp2.info");
+  return CPC_OK;
+}

@@ -1,0 +1,150 @@
+// reader.cpp -- the reference's catalogue input format (read_dat.cpp:18-347):
+// <prefix>_pos.dat (two columns), _z.dat, _e.dat (e1 e2), _wt.dat, _jk.dat
+// (integer labels), "0" meaning "absent".  Per galaxy it derives what the pair
+// loop reads: jk_prob (glibc rand()/(RAND_MAX+1.) in a periodic box, one draw
+// per galaxy in read order after srand(124693517); 1 otherwise, 0 without
+// jackknife), phi (elip_angle, or -10 without shapes), include_prob (a second
+// draw for random catalogues), and the weight totals.  Numbers are parsed with
+// std::from_chars, which rounds exactly as the reference's istream >> double.
+#include <charconv>
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <sstream>
+
+#include "../host_helpers.h"
+#include "host.h"
+
+namespace cpch {
+
+namespace {
+
+struct TextCols {
+  std::string buf;
+  size_t pos = 0;
+  bool open(const std::string &path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f.is_open()) return false;
+    std::ostringstream ss;
+    ss << f.rdbuf();
+    buf = ss.str();
+    pos = 0;
+    return true;
+  }
+  void skip_ws() {
+    while (pos < buf.size() && (buf[pos] == ' ' || buf[pos] == '\t' || buf[pos] == '\n' ||
+                                buf[pos] == '\r'))
+      pos++;
+  }
+  bool get(double &v) {
+    skip_ws();
+    if (pos >= buf.size()) return false;
+    const char *b = buf.data() + pos, *e = buf.data() + buf.size();
+    if (*b == '+') b++;
+    auto r = std::from_chars(b, e, v);
+    if (r.ec != std::errc()) return false;
+    pos = r.ptr - buf.data();
+    return true;
+  }
+  bool get(int32_t &v) {
+    skip_ws();
+    if (pos >= buf.size()) return false;
+    const char *b = buf.data() + pos, *e = buf.data() + buf.size();
+    if (*b == '+') b++;
+    auto r = std::from_chars(b, e, v);
+    if (r.ec != std::errc()) return false;
+    pos = r.ptr - buf.data();
+    return true;
+  }
+};
+
+}  // namespace
+
+cpc_catalog Catalog::view() const {
+  cpc_catalog c{};
+  c.n = n;
+  c.x = x.data();
+  c.y = y.data();
+  c.z = z.data();
+  c.w = w.data();
+  c.e1 = has_e ? e1.data() : nullptr;
+  c.e2 = has_e ? e2.data() : nullptr;
+  c.phi = phi.data();
+  c.jk = jk.empty() ? nullptr : jk.data();
+  c.jk_prob = jk_prob.data();
+  return c;
+}
+
+int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &err) {
+  // which samples read ellipticities (read_dat.cpp:27-150)
+  bool read_e = d.which_corr == 1 || d.which_corr == 2;
+  const bool cross_shape_shape = d.which_corr == 2;
+  std::string p_f, z_f, e_f, w_f, jk_f;
+  double *wt = nullptr;
+  int n_gal = 0;
+  if (role == ROLE_S) {
+    p_f = d.shape_pos; z_f = d.shape_z; e_f = d.shape_e; w_f = d.shape_wt; jk_f = d.shape_jk;
+    n_gal = d.n_shape; wt = d.S_wt;
+  } else if (role == ROLE_D) {
+    p_f = d.density_pos; z_f = d.density_z; w_f = d.density_wt; jk_f = d.density_jk;
+    n_gal = d.n_density; wt = d.D_wt;
+    if (cross_shape_shape) e_f = d.density_e; else read_e = false;
+  } else if (role == ROLE_RS) {
+    p_f = d.srand_pos; z_f = d.srand_z; w_f = d.srand_wt; jk_f = d.srand_jk;
+    n_gal = d.n_shape_rand; wt = d.Rs_wt; read_e = false;
+  } else {
+    p_f = d.drand_pos; z_f = d.drand_z; w_f = d.drand_wt; jk_f = d.drand_jk;
+    n_gal = d.n_density_rand; wt = d.Rd_wt; read_e = false;
+  }
+  c = Catalog();
+  if (n_gal == 0) return 0;  // read_dat.cpp:152-156: nothing read, no draws
+  const bool randoms = role == ROLE_RS || role == ROLE_RD;
+  const bool read_jk = jk_f != "0" && d.do_jk;
+  TextCols fp, fz, fe, fw, fj;
+  if (!fp.open(p_f)) { err = "pos file not open: " + p_f; return 1; }
+  if (!fz.open(z_f)) { err = "z file not open: " + z_f; return 1; }
+  if (w_f != "0" && !fw.open(w_f)) { err = "wt file not open: " + w_f; return 1; }
+  if (read_jk && !fj.open(jk_f)) { err = "jk file not open: " + jk_f; return 1; }
+  if (read_e && !fe.open(e_f)) { err = "e file not open: " + e_f; return 1; }
+  const uint32_t seed = d.periodic_box ? 124693517u : 1u;  // srand only in a box
+  cpc::GlibcRand rng(seed);
+  for (int64_t s = 0; s < draws; s++) rng.next();
+  c.n = n_gal;
+  c.x.resize(n_gal); c.y.resize(n_gal); c.z.resize(n_gal); c.w.assign(n_gal, 1.0);
+  c.phi.assign(n_gal, -10.0); c.jk_prob.assign(n_gal, 1.0); c.include_prob.assign(n_gal, 0.0);
+  if (read_jk) c.jk.assign(n_gal, -1);
+  c.has_e = read_e;
+  if (read_e) { c.e1.resize(n_gal); c.e2.resize(n_gal); }
+  for (int i = 0; i < n_gal; i++) {
+    if (!fp.get(c.x[i]) || !fp.get(c.y[i]) || !fz.get(c.z[i])) {
+      err = "gal data reading ended unexpectedly at row " + std::to_string(i) + " of " + p_f;
+      return 1;
+    }
+    if (c.z[i] < 0) c.z[i] = 0;
+    if (c.z[i] > d.z_max) {
+      err = "wrong z at row " + std::to_string(i) + " (above z_max)";
+      return 1;
+    }
+    if (d.periodic_box) {
+      c.jk_prob[i] = rng.next() / (2147483647 + 1.);
+      draws++;
+    }
+    if (d.do_jk == 0 || d.n_jk == 0) c.jk_prob[i] = 0;
+    if (w_f != "0" && !fw.get(c.w[i])) { err = "wt file ended early"; return 1; }
+    if (read_jk && !fj.get(c.jk[i])) { err = "jk file ended early"; return 1; }
+    if (read_e) {
+      if (!fe.get(c.e1[i]) || !fe.get(c.e2[i])) { err = "e file ended early"; return 1; }
+      c.phi[i] = cpc::elip_angle(c.e1[i], c.e2[i]);
+    }
+    if (randoms) {
+      c.include_prob[i] = rng.next() / (2147483647 + 1.);
+      draws++;
+    }
+    wt[0] += c.w[i];
+    wt[1] += c.w[i] * c.w[i];
+  }
+  if (!read_jk && d.do_jk) c.jk.assign(n_gal, -1);
+  return 0;
+}
+
+}  // namespace cpch

@@ -124,3 +124,26 @@ int pi_thresholds(int n_p_bin, double pmin, double pmax, double *thr) {
 }
 
 }  // namespace cpc
+
+namespace cpc {
+GlibcRand::GlibcRand(uint32_t seed) {
+  int32_t r[34];
+  r[0] = (int32_t)(seed == 0 ? 1u : seed);
+  for (int i = 1; i < 31; i++) {
+    const int64_t hi = r[i - 1] / 127773, lo = r[i - 1] % 127773;
+    int64_t word = 16807 * lo - 2836 * hi;
+    if (word < 0) word += 2147483647;
+    r[i] = (int32_t)word;
+  }
+  for (int i = 31; i < 34; i++) r[i] = r[i - 31];
+  for (int i = 0; i < 34; i++) buf_[i] = (uint32_t)r[i];
+  k_ = 34;
+  for (int t = 0; t < 310; t++) next();
+}
+int32_t GlibcRand::next() {
+  const uint32_t v = buf_[(k_ - 31) % 34] + buf_[(k_ - 3) % 34];
+  buf_[k_ % 34] = v;
+  k_++;
+  return (int32_t)(v >> 1);
+}
+}  // namespace cpc

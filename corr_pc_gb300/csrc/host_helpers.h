@@ -12,3 +12,15 @@ int rp_thresholds(int lin_bin, int n_bins, double rmin, double rmax, double *thr
 // exact Pi thresholds (n_p_bin + 1 entries).
 int pi_thresholds(int n_p_bin, double pmin, double pmax, double *thr);
 }  // namespace cpc
+
+namespace cpc {
+// glibc rand() as a running stream (same algorithm as glibc_rand_stream).
+class GlibcRand {
+ public:
+  explicit GlibcRand(uint32_t seed);
+  int32_t next();  // the next rand() value, 0 .. RAND_MAX
+ private:
+  uint32_t buf_[34];
+  int64_t k_;
+};
+}  // namespace cpc

@@ -38,7 +38,7 @@ cudaError_t launch_gather(int64_t n, const uint64_t *keys, const uint32_t *perm,
                           const GatherOut &out, cudaStream_t st);
 
 // pair_fast.cu
-constexpr int kTileThreads = 128;
+constexpr int kTileThreads = 128;  // g1 rows per tile (the block has 2 warp groups over them)
 size_t fast_smem_bytes(int corel, int do_jk, int NB);
 size_t fast_static_smem_bytes();
 int fast_blocks_per_sm(int corel, int jk, size_t smem);

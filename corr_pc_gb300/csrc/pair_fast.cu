@@ -29,7 +29,10 @@
 
 namespace cpc {
 
-constexpr int kTile = kTileThreads;
+constexpr int kTile = kTileThreads;          // g1 rows per tile
+constexpr int kGroups = 2;                    // warp groups sharing the rows
+constexpr int kThreads = kTile * kGroups;     // block size
+constexpr int kBatch = kThreads;              // candidates staged per batch
 constexpr int kMaxSeg = 512;
 constexpr int kMaxCols = 1024;
 
@@ -63,30 +66,41 @@ size_t fast_smem_bytes(int corel, int do_jk, int NB) {
   if (corel == COREL_SD) { FM = 7; FJ = 4; }
   if (corel == COREL_SS) { FM = 11; FJ = 6; }
   if (corel == COREL_SSA) { FM = 13; FJ = 7; }
-  size_t b = sizeof(float4) * 2 * kTile;                 // staging
+  size_t b = sizeof(float4) * 2 * kBatch;                // staging
   b += 8ull * FM * NB + 4ull * NB;
   if (do_jk) b += 2 * (8ull * FJ * NB + 4ull * NB);
   return b;
 }
 
-// 64-bit fixed-point sums held as two 32-bit words (low word + carry word):
-// each term is q = rint(v * 2^S) + B with B > |v| * 2^S, so 0 <= q < 2B <= 2^27;
-// the low word wraps at most once per add, detected from the returned old
-// value, and the carry goes to the high word (rare).  The bias B * count is
-// removed at the flush.  32-bit shared atomics are several times faster than
-// 64-bit ones on this part, and same-address 32-bit adds are combined in hardware.
+// Fixed-point sums in 32-bit shared words.  A term v of field f becomes
+// u = rint(v * 2^S_f) + B with B = 2^26 >= max|v| 2^S_f, so 0 <= u < 2^27; u is
+// split into a 14-bit low part and a 13-bit high part, each added to its own
+// 32-bit word with a plain reduction (no return value: no scoreboard wait, and
+// same-address adds of a warp are combined in hardware).  A block flushes its
+// histograms after every kFlushCands staged candidates, so a bin takes at most
+// kTile * kFlushCands = 2^18 terms between flushes and neither word can wrap.
+constexpr int kFlushCands = 2048;
+static_assert((long long)kTileThreads * kFlushCands <= (1ll << 18), "fixed-point word headroom");
 __device__ __forceinline__ unsigned to_fixed(float v, float scale, int bias) {
   return (unsigned)(__float2int_rn(v * scale) + bias);
 }
-__device__ __forceinline__ void acc_add(unsigned *lw, unsigned *hw, unsigned u) {
-  const unsigned old = atomicAdd(lw, u);
-  if (old + u < old) atomicAdd(hw, 1u);
+__device__ __forceinline__ void red_split(unsigned *lo, unsigned *hi, unsigned u) {
+  atomicAdd(lo, u & 0x3FFFu);
+  atomicAdd(hi, u >> 14);
 }
 __device__ __forceinline__ double fixed_total(unsigned lw, unsigned hw, unsigned cnt, int bias,
                                               double inv_scale) {
-  const long long tot = (long long)(((unsigned long long)hw << 32) | lw) -
-                        (long long)cnt * (long long)bias;
+  const long long tot = ((long long)hw << 14) + (long long)lw - (long long)cnt * (long long)bias;
   return (double)tot * inv_scale;
+}
+
+__device__ __forceinline__ int gcd_int(int a, int b) {
+  while (b) {
+    const int r = a % b;
+    a = b;
+    b = r;
+  }
+  return a;
 }
 
 __device__ __forceinline__ int floordiv(int a, int b) {
@@ -106,10 +120,10 @@ __device__ __forceinline__ int lower_bound_f(const float *zf, int lo, int hi, fl
 
 __device__ __noinline__ void fallback_exact(const JobDev &J, int64_t i1, int64_t j2, int code) {
   int sx, sy, sz, n1, n2;
-  shift_decode(code, sx, sy, sz);
+  shift_decode(code & kShiftMask, sx, sy, sz);
   const int r = exact_classify(J, J.d1, i1, J.d2, j2, sx, sy, sz, n1, n2);
   if (r == 0) return;
-  atomicAdd(&J.counters[1], 1ull);
+  if (!(code & kWindowCounted)) atomicAdd(&J.counters[1], 1ull);
   if (r == 2) {
     double f[kNF];
     exact_values(J, J.d1, i1, J.d2, j2, f);
@@ -139,8 +153,37 @@ __device__ __forceinline__ float ephi_f(float phi, float theta) {
   return t > 1.5707963267948966f ? 3.14159265358979f - t : t;
 }
 
+// Flush one block histogram (count, low and high words of each field) into
+// the global FP64 block at histogram index h, and zero it.
+template <int NF, bool JKMAP, class FM>
+__device__ __forceinline__ void flush_hist(unsigned *cnt, unsigned *lo, unsigned *hi, int NB,
+                                           int wpi, int npi, int nrp, int n2_base, int h, int f0,
+                                           int qbias, const double *s_iqs, const JobDev &J) {
+  const int64_t hb = (int64_t)h * nrp * npi;
+  for (int lb = threadIdx.x; lb < NB; lb += kThreads) {
+    const unsigned n = cnt[lb];
+    if (!n) continue;
+    const int64_t cell = hb + (int64_t)(lb / wpi) * npi + n2_base + lb % wpi;
+    atomicAdd(&J.acc_num[cell], (unsigned long long)n);
+    cnt[lb] = 0u;
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+      const size_t o = (size_t)f * NB + lb;
+      const int fld = JKMAP ? FM::j(f) : FM::m(f);
+      if (f >= f0) {
+        const double v = fixed_total(lo[o], hi[o], n, qbias, s_iqs[fld]);
+        if (v != 0.0) atomicAdd(&J.acc_sums[cell * kNF + fld], v);
+      }
+      lo[o] = 0u;
+      hi[o] = 0u;
+    }
+  }
+}
+
+constexpr int kQCap = 64;  // per-warp ring of binned pairs awaiting the heavy step
+
 template <int C, bool JK>
-__global__ void __launch_bounds__(kTile)
+__global__ void __launch_bounds__(kThreads, 2)
 fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ units,
                   int n_units, unsigned int *__restrict__ unit_ctr, QEntry *__restrict__ queue,
                   unsigned long long *__restrict__ qcount, unsigned long long qcap,
@@ -148,28 +191,33 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   using F = FieldMap<C>;
   extern __shared__ __align__(16) unsigned char smem[];
   float4 *s_pos = reinterpret_cast<float4 *>(smem);
-  float4 *s_shp = s_pos + kTile;
-  unsigned char *hist_base = smem + sizeof(float4) * 2 * kTile;
+  float4 *s_shp = s_pos + kBatch;
+  unsigned char *hist_base = smem + sizeof(float4) * 2 * kBatch;
 
   __shared__ int s_unit;
   __shared__ int s_cnt[kMaxCols + 1];
   __shared__ int s_slot_b[kMaxSeg];
-  __shared__ int s_slot_info[kMaxSeg];  // shift code | (sz+1) << 8 ... (code only)
+  __shared__ int s_slot_info[kMaxSeg];
   __shared__ int s_seg_a[kMaxSeg], s_seg_len[kMaxSeg], s_seg_key[kMaxSeg];
   __shared__ int s_order[kMaxSeg], s_pre[kMaxSeg + 1];
-  __shared__ int s_jidx[kTile];
-  __shared__ unsigned char s_keep[kTile];
-  __shared__ float2 s_lo[kTile];
-  __shared__ unsigned long long s_red[kTile / 32];
+  __shared__ int s_jidx[kBatch];
+  __shared__ unsigned char s_keep[kBatch];
+  __shared__ float2 s_lo[kBatch];
+  __shared__ unsigned long long s_red[kThreads / 32];
   __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
   __shared__ float s_qs[kNF];
   __shared__ double s_iqs[kNF];
+  // the tile's g1 rows, for the heavy step (any lane may process any row)
+  __shared__ float4 s_rpos[kTile], s_rshp[kTile];
+  __shared__ float2 s_rlo[kTile];
+  __shared__ unsigned char s_rkeep[kTile];
+  __shared__ unsigned s_wq[kThreads / 32][kQCap];
 
-  const int t = threadIdx.x;
-  // histograms start zeroed; every flush re-zeroes what it used
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const unsigned lt_mask = (1u << lane) - 1u;
   {
     unsigned int *z = reinterpret_cast<unsigned int *>(hist_base);
-    for (int k = t; k < zero_words; k += kTile) z[k] = 0u;
+    for (int k = t; k < zero_words; k += kThreads) z[k] = 0u;
   }
   __syncthreads();
 
@@ -181,7 +229,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     const UnitDesc U = units[u];
     const JobDev &J = jobs[U.job];
     const int nrp = J.nrp, wpi = J.wpi, npi = J.npi, NB = nrp * wpi;
-    // per histogram: count[NB], low words [F][NB], carry words [F][NB]
+    // per histogram: count[NB], low words [F][NB], high words [F][NB]
     unsigned *s_mnum = reinterpret_cast<unsigned *>(hist_base);
     unsigned *s_mlo = s_mnum + NB;
     unsigned *s_mhi = s_mlo + (size_t)F::FM * NB;
@@ -194,28 +242,32 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     const int qbias = J.qbias;
     const int f0 = J.unit_w ? 1 : 0;  // unit weights: wt_num = count, not accumulated
 
-    // ---- this thread's g1 row: the lanes of a warp are spread over the whole
-    // tile (tile row q = lane * W + warp), so simultaneous pairs of a warp fall
-    // in different Pi bins and the shared-memory atomics rarely collide ----
+    // ---- this thread's g1 row.  The lanes of a warp are spread over the whole
+    // tile (tile row q = lane * W + warp) so that simultaneous pairs of a warp
+    // fall in different Pi bins; both warp groups hold the same rows and split
+    // the candidates. ----
+    const int tr = t & (kTile - 1), grp = t / kTile;
     const int W = (U.g1_count + 31) >> 5;
-    const int q = (t & 31) * W + (t >> 5);
-    const bool has1 = (t >> 5) < W && q < U.g1_count;
+    const int q = (tr & 31) * W + (tr >> 5);
+    const bool has1 = (tr >> 5) < W && q < U.g1_count;
     const int64_t i1 = (int64_t)U.g1_start + (int64_t)q * U.g1_stride;
-    float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), e1v = make_float4(0.f, 0.f, 0.f, 0.f);
-    float2 lo1 = make_float2(0.f, 0.f);
-    bool keep1 = false, valid = false;
+    float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool valid = false;
     const bool has_lo = C != COREL_DD && J.has_lo;
     const int gws = J.gws, lin_bin = J.lin_bin, box_same_keep = J.box_same_keep;
     const float rmin_f = J.rmin_f, inv_rsize_f = J.inv_rsize_f;
     if (has1) {
       p1 = J.f1.pos[i1];
-      if (has_lo) lo1 = J.f1.lo[i1];
-      if (C != COREL_DD) e1v = J.f1.shp[i1];
-      if (JK) keep1 = J.f1.keep[i1] != 0;
       valid = true;
       if (J.row_stride > 1) {
-        int64_t o = J.d1.orig[i1] - J.row_offset;
+        const int64_t o = J.d1.orig[i1] - J.row_offset;
         valid = (o % J.row_stride) == 0;
+      }
+      if (grp == 0) {
+        s_rpos[tr] = p1;
+        if (C != COREL_DD) s_rshp[tr] = J.f1.shp[i1];
+        if (has_lo) s_rlo[tr] = J.f1.lo[i1];
+        if (JK) s_rkeep[tr] = J.f1.keep[i1];
       }
     }
     const float Lf = J.Lf;
@@ -223,8 +275,8 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     const float pi_in_lo = J.pi_in_lo, pi_in_hi = J.pi_in_hi;
     const float pi_out_lo = J.pi_out_lo, pi_out_hi = J.pi_out_hi;
     const float inv_ps = J.inv_ps_f, tp0 = J.tp0;
-    for (int k = t; k < nrp; k += kTile) { s_A[k] = J.A[k]; s_B[k] = J.B[k]; }
-    for (int k = t; k < npi; k += kTile) { s_PA[k] = J.PA[k]; s_PB[k] = J.PB[k]; }
+    for (int k = t; k < nrp; k += kThreads) { s_A[k] = J.A[k]; s_B[k] = J.B[k]; }
+    for (int k = t; k < npi; k += kThreads) { s_PA[k] = J.PA[k]; s_PB[k] = J.PB[k]; }
     if (t < kNF) { s_qs[t] = J.qscale[t]; s_iqs[t] = J.inv_qscale[t]; }
     const float l2rmin2 = J.l2rmin2, inv_lw = J.inv_lw, rej_lo = J.rej_lo, rej_hi = J.rej_hi;
     const int n2_base = U.n2_base;
@@ -234,7 +286,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     const int ncxu = U.cx_hi - U.cx_lo + 1;
     const int ncol = ncxu * (U.cy_hi - U.cy_lo + 1);
     const int nsz_lo = J.periodic ? -1 : 0, nsz_hi = J.periodic ? 1 : 0;
-    for (int c = t; c < ncol; c += kTile) {
+    for (int c = t; c < ncol; c += kThreads) {
       const int cx = U.cx_lo + c % ncxu, cy = U.cy_lo + c / ncxu;
       const int sx = J.periodic ? floordiv(cx, J.ncx) : 0, sy = J.periodic ? floordiv(cy, J.ncy) : 0;
       int cnt = 0;
@@ -263,11 +315,12 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     }
     __syncthreads();
     const int total_slots = s_cnt[ncol];
-    int cur_y = -1;  // region currently held in the Y histogram
+    int cur_y = -1;        // region held in the Y histogram
+    int since_flush = 0;   // candidates staged since the last flush
 
     for (int chunk0 = 0; chunk0 < total_slots; chunk0 += kMaxSeg) {
       const int nslot = min(kMaxSeg, total_slots - chunk0);
-      for (int c = t; c < ncol; c += kTile) {
+      for (int c = t; c < ncol; c += kThreads) {
         int pos = s_cnt[c];
         if (pos >= chunk0 + kMaxSeg || s_cnt[c + 1] <= chunk0) continue;
         const int cx = U.cx_lo + c % ncxu, cy = U.cy_lo + c / ncxu;
@@ -289,7 +342,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         }
       }
       __syncthreads();
-      for (int k = t; k < nslot; k += kTile) {
+      for (int k = t; k < nslot; k += kThreads) {
         const int b = s_slot_b[k], code = s_slot_info[k];
         const int sz = code / 9 - 1;
         const float lo = (float)(U.zlo - J.L * sz), hi = (float)(U.zhi - J.L * sz);
@@ -301,7 +354,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         s_seg_key[k] = (e > a) ? J.f2.bk_region[b] * 27 + code : INT_MAX;
       }
       __syncthreads();
-      for (int k = t; k < nslot; k += kTile) {  // stable rank sort by key
+      for (int k = t; k < nslot; k += kThreads) {  // stable rank sort by key
         const int key = s_seg_key[k];
         int r = 0;
         for (int m = 0; m < nslot; m++) {
@@ -331,28 +384,20 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         int sx, sy, sz;
         shift_decode(code, sx, sy, sz);
         const bool same_region = region2 == U.region;
+        // staging order: position (i * ks) mod N over the group's N candidates,
+        // ks coprime with N and ~0.618 N, so a batch is a spread-out sample of
+        // the group's columns and z range (decorrelated bins, fewer collisions)
+        const int gN = s_pre[g] - s_pre[k];
+        int ks = 1;
+        if (gN > 2) {
+          ks = max(1, (int)(0.6180339887f * gN));
+          while (gcd_int(ks, gN) != 1) ks++;
+        }
         if (JK && !same_region && cur_y != region2) {
-          if (cur_y >= 0) {  // flush Y for the previous region
+          if (cur_y >= 0) {
             __syncthreads();
-            const int64_t hb = (int64_t)(1 + cur_y) * nrp * npi;
-            for (int lb = t; lb < NB; lb += kTile) {
-              const unsigned n = s_ynum[lb];
-              if (!n) continue;
-              const int n2 = n2_base + lb % wpi;
-              const int64_t cell = hb + (int64_t)(lb / wpi) * npi + n2;
-              atomicAdd(&J.acc_num[cell], (unsigned long long)n);
-              s_ynum[lb] = 0u;
-#pragma unroll
-              for (int f = 0; f < F::FJ; f++) {
-                const size_t o = (size_t)f * NB + lb;
-                if (f >= f0) {
-                  const double v = fixed_total(s_ylo[o], s_yhi[o], n, qbias, s_iqs[F::j(f)]);
-                  if (v != 0.0) atomicAdd(&J.acc_sums[cell * kNF + F::j(f)], v);
-                }
-                s_ylo[o] = 0u;
-                s_yhi[o] = 0u;
-              }
-            }
+            flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
+                                       1 + cur_y, f0, qbias, s_iqs, J);
             __syncthreads();
           }
           cur_y = region2;
@@ -362,13 +407,25 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         const float y1s = sy == 1 ? p1.y - Lf : p1.y;
         const float z1s = sz == 1 ? p1.z - Lf : p1.z;
         const float g2sx = sx == -1 ? Lf : 0.f, g2sy = sy == -1 ? Lf : 0.f, g2sz = sz == -1 ? Lf : 0.f;
-        const bool xsame = JK && same_region && (box_same_keep || keep1);
-        const bool xdiff = JK && !same_region && keep1;
 
-        for (int base = s_pre[k]; base < s_pre[g]; base += kTile) {
-          const int nb = min(kTile, s_pre[g] - base);
+        for (int base = 0; base < gN; base += kBatch) {
+          const int nb = min(kBatch, gN - base);
+          if (since_flush + nb > kFlushCands) {  // keep every word below 2^32
+            __syncthreads();
+            flush_hist<F::FM, false, F>(s_mnum, s_mlo, s_mhi, NB, wpi, npi, nrp, n2_base, 0, f0,
+                                        qbias, s_iqs, J);
+            if (JK) {
+              flush_hist<F::FJ, true, F>(s_xnum, s_xlo, s_xhi, NB, wpi, npi, nrp, n2_base,
+                                         1 + U.region, f0, qbias, s_iqs, J);
+              if (cur_y >= 0)
+                flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
+                                           1 + cur_y, f0, qbias, s_iqs, J);
+            }
+            since_flush = 0;
+          }
+          since_flush += nb;
           if (t < nb) {
-            const int p = base + t;
+            const int p = s_pre[k] + (int)(((long long)(base + t) * ks) % gN);
             int lo = k, hi = g;  // segment s_order[lo] with s_pre[lo] <= p < s_pre[lo+1]
             while (hi - lo > 1) {
               const int mid = (lo + hi) >> 1;
@@ -387,68 +444,98 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             if (JK) s_keep[t] = J.f2.keep[j2];
           }
           __syncthreads();
-          if (valid) {
-            for (int c = 0; c < nb; ++c) {
+
+          // ---- light pass over the batch, binned pairs queued per warp; the
+          // heavy step runs whenever 32 are queued (all lanes busy) ----
+          // group g takes batch slots [c0, c0 + nk); lane l at step s takes slot
+          // c0 + (s + l) mod nk, so a warp works on 32 different candidates
+          const int nk0 = (nb + 1) >> 1;
+          const int c0 = grp ? nk0 : 0, nk = grp ? nb - nk0 : nk0;
+          int step = 0;
+          int qhead = 0, qtail = 0;
+          for (;;) {
+            while (step < nk && (qtail - qhead) < 32) {
+              int cr = step + lane;
+              if (cr >= nk) cr -= nk;
+              if (cr >= nk) cr %= nk;
+              const int c = c0 + cr;
               const float4 p2 = s_pos[c];
               const float dz = p2.z - z1s;
               const float dx = x1s - p2.x;
               const float dy = y1s - p2.y;
               const float m = fmaxf(fabsf(dx), fabsf(dy));
-              if (!(dz >= pi_out_lo && dz <= pi_out_hi && m <= xy_out)) continue;
-              bool amb = !(dz >= pi_in_lo && dz <= pi_in_hi && m <= xy_in);
-              const float r2 = fmaf(dx, dx, dy * dy);
-              // Pi bin: approximate index, confirmed against the definite band
-              int n2 = (int)floorf(fmaf(dz, inv_ps, tp0));
-              n2 = min(max(n2, 0), npi - 1);
-              if (!(dz >= s_PA[n2] && dz < s_PB[n2])) {
-                if (n2 > 0 && dz >= s_PA[n2 - 1] && dz < s_PB[n2 - 1]) n2--;
-                else if (n2 + 1 < npi && dz >= s_PA[n2 + 1] && dz < s_PB[n2 + 1]) n2++;
-                else amb = true;
-              }
-              // r_p bin: log2 estimate, confirmed against the definite band
-              bool rout = false;
-              int n1 = 0;
-              if (r2 < rej_lo || r2 >= rej_hi) {
-                rout = true;
-              } else {
-                n1 = lin_bin ? (int)floorf((sqrtf(r2) - rmin_f) * inv_rsize_f)
-                               : (int)floorf((__log2f(r2) - l2rmin2) * inv_lw);
-                n1 = min(max(n1, 0), nrp - 1);
-                if (!(r2 >= s_A[n1] && r2 < s_B[n1])) {
-                  if (n1 > 0 && r2 >= s_A[n1 - 1] && r2 < s_B[n1 - 1]) n1--;
-                  else if (n1 + 1 < nrp && r2 >= s_A[n1 + 1] && r2 < s_B[n1 + 1]) n1++;
-                  else amb = true;
+              bool binned = false;
+              if (valid && dz >= pi_out_lo && dz <= pi_out_hi && m <= xy_out) {
+                if (!(dz >= pi_in_lo && dz <= pi_in_hi && m <= xy_in)) {
+                  // near the window edge: exact FP64 evaluation of the whole pair
+                  enqueue(J, U.job, i1, s_jidx[c], code, queue, qcount, qcap);
+                } else {
+                  nwin++;
+                  const float r2 = fmaf(dx, dx, dy * dy);
+                  binned = r2 >= rej_lo && r2 < rej_hi;
                 }
               }
+              const unsigned bm = __ballot_sync(0xffffffffu, binned);
+              if (binned)
+                s_wq[wid][(qtail + __popc(bm & lt_mask)) & (kQCap - 1)] = (unsigned)tr | ((unsigned)c << 7);
+              qtail += __popc(bm);
+              step++;
+            }
+            const int avail = qtail - qhead;
+            if (avail == 0) break;
+            __syncwarp();
+            const int take = min(avail, 32);
+            if (lane < take) {
+              // ---- heavy step for one queued pair ----
+              const unsigned e = s_wq[wid][(qhead + lane) & (kQCap - 1)];
+              const int er = e & 127, ec = (e >> 7) & 255;
+              const float4 r1 = s_rpos[er];
+              const float4 p2 = s_pos[ec];
+              // exact bins: approximate index confirmed against the definite bands
+              const float hdz = p2.z - (sz == 1 ? r1.z - Lf : r1.z);
+              const float hdx = (sx == 1 ? r1.x - Lf : r1.x) - p2.x;
+              const float hdy = (sy == 1 ? r1.y - Lf : r1.y) - p2.y;
+              const float r2 = fmaf(hdx, hdx, hdy * hdy);
+              bool amb = false;
+              int n2 = (int)floorf(fmaf(hdz, inv_ps, tp0));
+              n2 = min(max(n2, 0), npi - 1);
+              if (!(hdz >= s_PA[n2] && hdz < s_PB[n2])) {
+                if (n2 > 0 && hdz >= s_PA[n2 - 1] && hdz < s_PB[n2 - 1]) n2--;
+                else if (n2 + 1 < npi && hdz >= s_PA[n2 + 1] && hdz < s_PB[n2 + 1]) n2++;
+                else amb = true;
+              }
+              int n1 = lin_bin ? (int)floorf((sqrtf(r2) - rmin_f) * inv_rsize_f)
+                               : (int)floorf((__log2f(r2) - l2rmin2) * inv_lw);
+              n1 = min(max(n1, 0), nrp - 1);
+              if (!(r2 >= s_A[n1] && r2 < s_B[n1])) {
+                if (n1 > 0 && r2 >= s_A[n1 - 1] && r2 < s_B[n1 - 1]) n1--;
+                else if (n1 + 1 < nrp && r2 >= s_A[n1 + 1] && r2 < s_B[n1 + 1]) n1++;
+                else amb = true;
+              }
+              const int elk = n2 - n2_base;
+              if ((unsigned)elk >= (unsigned)wpi) amb = true;
               if (amb) {
-                enqueue(J, U.job, i1, s_jidx[c], code, queue, qcount, qcap);
-                continue;
-              }
-              if (rout) {
-                nwin++;
-                continue;
-              }
-              const int lk = n2 - n2_base;
-              if ((unsigned)lk >= (unsigned)wpi) {  // outside the block-local Pi window
-                enqueue(J, U.job, i1, s_jidx[c], code, queue, qcount, qcap);
-                continue;
-              }
-              nwin++;
-              const int lb = n1 * wpi + lk;
+                // near a bin edge: exact FP64 binning (window already counted)
+                const int64_t gi1 = (int64_t)U.g1_start +
+                                    (int64_t)(((er & 31) * W) + (er >> 5)) * U.g1_stride;
+                enqueue(J, U.job, gi1, s_jidx[ec], code | kWindowCounted, queue, qcount, qcap);
+              } else {
+              const int lb = n1 * wpi + elk;
               float v[kNF];
-              const float w = p1.w * p2.w;
+              const float w = r1.w * p2.w;
               v[0] = w;
               if (C != COREL_DD) {
-                const float4 s2 = s_shp[c];
-                float dxr = (p2.x + g2sx) - p1.x;
-                float dyr = (p2.y + g2sy) - p1.y;
+                const float4 e1v = s_rshp[er];
+                const float4 s2 = s_shp[ec];
+                float dxr = (p2.x + g2sx) - r1.x;
+                float dyr = (p2.y + g2sy) - r1.y;
                 if (has_lo) {
-                  const float2 lo2 = s_lo[c];
+                  const float2 lo1 = s_rlo[er], lo2 = s_lo[ec];
                   dxr += lo2.x - lo1.x;
                   dyr += lo2.y - lo1.y;
                 }
                 const float a = dxr * dxr, b = dyr * dyr;
-                const float inv = 1.0f / (a + b);
+                const float inv = __fdividef(1.0f, a + b);
                 const float c2 = (a - b) * inv, s2v = 2.0f * dxr * dyr * inv;
                 const float theta = atanf(dyr / dxr);
                 if (C == COREL_SD) {
@@ -491,34 +578,36 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               }
               atomicAdd(&s_mnum[lb], 1u);
 #pragma unroll
-              for (int f = 0; f < F::FM; f++) {
-                if (f < f0) continue;
-                const size_t o = (size_t)f * NB + lb;
-                acc_add(&s_mlo[o], &s_mhi[o], to_fixed(v[F::m(f)], s_qs[F::m(f)], qbias));
-              }
+              for (int f = 0; f < F::FM; f++)
+                if (f >= f0)
+                  red_split(&s_mlo[(size_t)f * NB + lb], &s_mhi[(size_t)f * NB + lb],
+                            to_fixed(v[F::m(f)], s_qs[F::m(f)], qbias));
               if (JK) {
-                const bool xc = same_region ? xsame : xdiff;
-                const bool yc = !same_region && s_keep[c];
+                const bool k1 = s_rkeep[er] != 0;
+                const bool xc = same_region ? (box_same_keep || k1) : k1;
+                const bool yc = !same_region && s_keep[ec];
                 if (xc) {
                   atomicAdd(&s_xnum[lb], 1u);
 #pragma unroll
-                  for (int f = 0; f < F::FJ; f++) {
-                    if (f < f0) continue;
-                    const size_t o = (size_t)f * NB + lb;
-                    acc_add(&s_xlo[o], &s_xhi[o], to_fixed(v[F::j(f)], s_qs[F::j(f)], qbias));
-                  }
+                  for (int f = 0; f < F::FJ; f++)
+                    if (f >= f0)
+                      red_split(&s_xlo[(size_t)f * NB + lb], &s_xhi[(size_t)f * NB + lb],
+                                to_fixed(v[F::j(f)], s_qs[F::j(f)], qbias));
                 }
                 if (yc) {
                   atomicAdd(&s_ynum[lb], 1u);
 #pragma unroll
-                  for (int f = 0; f < F::FJ; f++) {
-                    if (f < f0) continue;
-                    const size_t o = (size_t)f * NB + lb;
-                    acc_add(&s_ylo[o], &s_yhi[o], to_fixed(v[F::j(f)], s_qs[F::j(f)], qbias));
-                  }
+                  for (int f = 0; f < F::FJ; f++)
+                    if (f >= f0)
+                      red_split(&s_ylo[(size_t)f * NB + lb], &s_yhi[(size_t)f * NB + lb],
+                                to_fixed(v[F::j(f)], s_qs[F::j(f)], qbias));
                 }
               }
+              }
             }
+            qhead += take;
+            __syncwarp();
+            if (step >= nk && qtail == qhead) break;
           }
           __syncthreads();
         }
@@ -529,72 +618,25 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
 
     // ---- flush main, X and the last Y ----
     __syncthreads();
-    {
-      const int64_t hstride = (int64_t)nrp * npi;
-      for (int lb = t; lb < NB; lb += kTile) {
-        const int n2 = n2_base + lb % wpi;
-        const int64_t cell = (int64_t)(lb / wpi) * npi + n2;
-        unsigned n = s_mnum[lb];
-        if (n) {
-          atomicAdd(&J.acc_num[cell], (unsigned long long)n);
-          s_mnum[lb] = 0u;
-#pragma unroll
-          for (int f = 0; f < F::FM; f++) {
-            const size_t o = (size_t)f * NB + lb;
-            if (f >= f0) {
-              const double v = fixed_total(s_mlo[o], s_mhi[o], n, qbias, s_iqs[F::m(f)]);
-              if (v != 0.0) atomicAdd(&J.acc_sums[cell * kNF + F::m(f)], v);
-            }
-            s_mlo[o] = 0u;
-            s_mhi[o] = 0u;
-          }
-        }
-        if (JK) {
-          n = s_xnum[lb];
-          if (n) {
-            const int64_t hc = (int64_t)(1 + U.region) * hstride + cell;
-            atomicAdd(&J.acc_num[hc], (unsigned long long)n);
-            s_xnum[lb] = 0u;
-#pragma unroll
-            for (int f = 0; f < F::FJ; f++) {
-              const size_t o = (size_t)f * NB + lb;
-              if (f >= f0) {
-                const double v = fixed_total(s_xlo[o], s_xhi[o], n, qbias, s_iqs[F::j(f)]);
-                if (v != 0.0) atomicAdd(&J.acc_sums[hc * kNF + F::j(f)], v);
-              }
-              s_xlo[o] = 0u;
-              s_xhi[o] = 0u;
-            }
-          }
-          n = s_ynum[lb];
-          if (n) {
-            const int64_t hc = (int64_t)(1 + cur_y) * hstride + cell;
-            atomicAdd(&J.acc_num[hc], (unsigned long long)n);
-            s_ynum[lb] = 0u;
-#pragma unroll
-            for (int f = 0; f < F::FJ; f++) {
-              const size_t o = (size_t)f * NB + lb;
-              if (f >= f0) {
-                const double v = fixed_total(s_ylo[o], s_yhi[o], n, qbias, s_iqs[F::j(f)]);
-                if (v != 0.0) atomicAdd(&J.acc_sums[hc * kNF + F::j(f)], v);
-              }
-              s_ylo[o] = 0u;
-              s_yhi[o] = 0u;
-            }
-          }
-        }
-      }
+    flush_hist<F::FM, false, F>(s_mnum, s_mlo, s_mhi, NB, wpi, npi, nrp, n2_base, 0, f0, qbias,
+                                s_iqs, J);
+    if (JK) {
+      flush_hist<F::FJ, true, F>(s_xnum, s_xlo, s_xhi, NB, wpi, npi, nrp, n2_base, 1 + U.region,
+                                 f0, qbias, s_iqs, J);
+      if (cur_y >= 0)
+        flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y,
+                                   f0, qbias, s_iqs, J);
     }
     // window-pair counter
     {
       unsigned long long v = nwin;
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-      if ((t & 31) == 0) s_red[t >> 5] = v;
+      if (lane == 0) s_red[wid] = v;
       __syncthreads();
       if (t == 0) {
-        unsigned long long s = 0;
-        for (int w = 0; w < kTile / 32; w++) s += s_red[w];
-        if (s) atomicAdd(&J.counters[0], s);
+        unsigned long long sm = 0;
+        for (int w = 0; w < kThreads / 32; w++) sm += s_red[w];
+        if (sm) atomicAdd(&J.counters[0], sm);
       }
     }
     __syncthreads();
@@ -611,11 +653,11 @@ __global__ void recheck_kernel(const JobDev *__restrict__ jobs, const QEntry *__
     const QEntry e = queue[idx];
     const JobDev &J = jobs[e.job];
     int sx, sy, sz, n1, n2;
-    shift_decode(e.shift, sx, sy, sz);
+    shift_decode(e.shift & kShiftMask, sx, sy, sz);
     const int r = exact_classify(J, J.d1, e.i1, J.d2, e.j2, sx, sy, sz, n1, n2);
     atomicAdd(&J.counters[2], 1ull);
     if (r == 0) continue;
-    atomicAdd(&J.counters[1], 1ull);
+    if (!(e.shift & kWindowCounted)) atomicAdd(&J.counters[1], 1ull);
     if (r == 2) {
       double f[kNF];
       exact_values(J, J.d1, e.i1, J.d2, e.j2, f);
@@ -633,8 +675,8 @@ static cudaError_t launch_fast_t(const JobDev *jobs, const UnitDesc *units, int 
   auto kern = fast_pairs_kernel<C, JK>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
-  const int zero_words = (int)((smem - sizeof(float4) * 2 * kTile) / 4);
-  kern<<<grid, kTile, smem, st>>>(jobs, units, n_units, unit_ctr, q, qcount, qcap, zero_words);
+  const int zero_words = (int)((smem - sizeof(float4) * 2 * kBatch) / 4);
+  kern<<<grid, kThreads, smem, st>>>(jobs, units, n_units, unit_ctr, q, qcount, qcap, zero_words);
   return cudaGetLastError();
 }
 
@@ -663,10 +705,10 @@ int fast_blocks_per_sm(int corel, int jk, size_t smem) {
   if (corel == CC) {                                                                            \
     if (jk) {                                                                                   \
       cudaFuncSetAttribute(fast_pairs_kernel<CC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fast_pairs_kernel<CC, true>, kTile, smem); \
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fast_pairs_kernel<CC, true>, kThreads, smem); \
     } else {                                                                                    \
       cudaFuncSetAttribute(fast_pairs_kernel<CC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fast_pairs_kernel<CC, false>, kTile, smem); \
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fast_pairs_kernel<CC, false>, kThreads, smem); \
     }                                                                                           \
   }
   CPC_OCC(COREL_DD)

@@ -187,6 +187,18 @@ cpc_status cpc_host_rp_thresholds(const cpc_params *params, double *thr);
  * floor((Pi - p_min)/p_size) >= k, k = 0..n_p_bin (corels.cpp:26). */
 cpc_status cpc_host_pi_thresholds(const cpc_params *params, double *thr);
 
+/* Finalisation of a cross-correlation run (do_corr.cpp:203-433: final_calc,
+ * int_calc, jk_final, analytic periodic RR) and its output files, written
+ * with the .inp's out_file prefix, from the RAW histogram blocks of the four
+ * pair types (cpc_accum layout; NULL = empty term; the delete-one conversion
+ * is applied here).  weights: S_wt, S_wt2, D_wt, D_wt2, Rs_wt, Rs_wt2, Rd_wt,
+ * Rd_wt2 (sums of w and w^2 per sample, as read_data accumulates them). */
+cpc_status cpc_host_finalize_cross(const char *inp_path, const int64_t *sd_num,
+                                   const double *sd_sums, const int64_t *srd_num,
+                                   const double *srd_sums, const int64_t *drs_num,
+                                   const double *drs_sums, const int64_t *rsrd_num,
+                                   const double *rsrd_sums, const double *weights);
+
 #ifdef __cplusplus
 }
 #endif
