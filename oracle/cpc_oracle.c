@@ -457,3 +457,19 @@ void orc_glibc_rand(uint32_t seed, int64_t skip, int64_t n, int32_t *out) {
     if (o >= 0) out[o] = (int32_t)(v >> 1);
   }
 }
+
+/* elip_angle (calcs.cpp:35-46, 73-83) with the C library's atan, as the
+ * reference calls it: phi = 0.5*arctan(e1, -e2), quadrant-corrected, NaN -> 0. */
+void orc_elip_angle(int64_t n, const double *e1, const double *e2, double *phi) {
+  for (int64_t i = 0; i < n; i++) {
+    const double x = e1[i], y = -1 * e2[i];
+    double t = atan(y / x);
+    if (x < 0) {
+      if (y < 0) t -= M_PI;
+      else t += M_PI;
+    }
+    double p = 0.5 * t;
+    if (p != p) p = 0;
+    phi[i] = p;
+  }
+}

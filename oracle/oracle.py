@@ -75,6 +75,9 @@ def lib():
         _lib.orc_corels2.argtypes = [ctypes.POINTER(_Params), ctypes.c_int,
                                      ctypes.POINTER(_Cat), ctypes.POINTER(_Cat),
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        _lib.orc_elip_angle.restype = None
+        _lib.orc_elip_angle.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p]
         _lib.orc_glibc_rand.restype = None
         _lib.orc_glibc_rand.argtypes = [ctypes.c_uint32, ctypes.c_int64, ctypes.c_int64,
                                         ctypes.c_void_p]
@@ -115,14 +118,13 @@ class OracleCatalog:
 
 def elip_angle(e1, e2):
     """phi = 0.5*arctan(e1, -e2) with the reference's quadrant rule
-    (calcs.cpp:35-46, 73-83); NaN -> 0."""
-    e1 = np.asarray(e1, dtype=np.float64)
-    y = -1.0 * np.asarray(e2, dtype=np.float64)
-    with np.errstate(divide="ignore", invalid="ignore"):
-        t = np.arctan(y / e1)
-    t = np.where(e1 < 0, np.where(y < 0, t - np.pi, t + np.pi), t)
-    phi = 0.5 * t
-    return np.where(np.isnan(phi), 0.0, phi)
+    (calcs.cpp:35-46, 73-83); NaN -> 0.  Evaluated in C with the C library's
+    atan, as the reference does."""
+    e1 = np.ascontiguousarray(e1, dtype=np.float64)
+    e2 = np.ascontiguousarray(e2, dtype=np.float64)
+    out = np.empty_like(e1)
+    lib().orc_elip_angle(e1.shape[0], e1.ctypes.data, e2.ctypes.data, out.ctypes.data)
+    return out
 
 
 def read_like_reference(params, cats_in_read_order):

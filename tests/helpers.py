@@ -1,0 +1,98 @@
+"""Test helpers: golden fixtures and tolerance checks."""
+from __future__ import annotations
+
+import glob
+import json
+import os
+
+import numpy as np
+
+from corr_pc_gb300 import synth
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+# fields whose sums do not cancel (weights, squares, theta term): checked per bin
+NONCANCEL = [0, 2, 4, 6, 8, 10, 11, 12]
+
+
+def golden_names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+class Golden:
+    def __init__(self, name):
+        z = np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False)
+        self.meta = json.loads(str(z["meta"]))
+        self.arr = {k: z[k] for k in z.files if k != "meta"}
+        p = synth.InpParams()
+        for k, v in self.meta["params"].items():
+            setattr(p, k, v)
+        self.params = p
+        self.S = self._cat("S")
+        self.D = self._cat("D")
+        self.raw_num = self.arr["raw_num"]
+        self.raw_sums = self.arr["raw_sums"]
+        self.n_in = int(self.arr["n_in"])
+        self.n_total = int(self.arr["n_total"])
+        self.files = self.meta["files"]
+
+    def _cat(self, role):
+        g = lambda a: self.arr.get(f"{role}_{a}")
+        return synth.Catalog(g("x"), g("y"), g("z"), g("w"), g("e1"), g("e2"), g("jk"))
+
+    def weights(self):
+        w = []
+        for c in (self.S, self.D):
+            ww = np.ones(c.n) if c.w is None else c.w
+            w += [float(ww.sum()), float((ww * ww).sum())]
+        return w + [0.0, 0.0, 0.0, 0.0]
+
+
+def check_sums(got, ref, rtol=1e-6, label="", big_frac=1e-2):
+    """Accuracy bar: every bin of every field within rtol relative, with an
+    absolute floor of rtol x the largest |value| of that field for bins whose
+    true value is near zero; non-cancelling fields (weights, squares, theta
+    term) also within rtol per bin wherever the bin holds at least big_frac of
+    the field's largest value (tiny bins are covered by the floor)."""
+    got = np.asarray(got)
+    ref = np.asarray(ref)
+    for f in range(ref.shape[-1]):
+        r = ref[..., f]
+        g = got[..., f]
+        fmax = np.abs(r).max()
+        if fmax == 0:
+            assert np.abs(g).max() == 0, f"{label} field {f}: expected zeros"
+            continue
+        err = np.abs(g - r)
+        assert err.max() <= rtol * fmax, f"{label} field {f}: max err {err.max()} vs floor {rtol * fmax}"
+        if f in NONCANCEL:
+            big = np.abs(r) >= big_frac * fmax
+            rel = err[big] / np.abs(r[big])
+            assert rel.max() <= rtol, f"{label} field {f}: per-bin rel err {rel.max()}"
+
+
+def parse_table(text):
+    """Numeric tokens of an output file (header skipped); nan/-nan -> nan."""
+    rows = []
+    for line in text.splitlines():
+        if not line.strip() or line.startswith("#"):
+            continue
+        rows.append([float(t.replace("-nan", "nan")) for t in line.split()])
+    return rows
+
+
+def compare_files(got_text, ref_text, rtol=2e-5, label=""):
+    """Numbers are printed with 6 significant digits: allow last-digit rounding
+    (rtol) per value, and 1e-6 of the column's largest value for entries that
+    are themselves tiny results of cancellation."""
+    a, b = parse_table(got_text), parse_table(ref_text)
+    assert len(a) == len(b), f"{label}: {len(a)} rows vs {len(b)}"
+    a = np.array(a, dtype=np.float64)
+    b = np.array(b, dtype=np.float64)
+    assert a.shape == b.shape, f"{label}: shape {a.shape} vs {b.shape}"
+    nan_b = np.isnan(b)
+    assert np.array_equal(np.isnan(a), nan_b), f"{label}: nan pattern differs"
+    colmax = np.nanmax(np.where(nan_b, 0, np.abs(b)), axis=0)
+    d = np.abs(np.where(nan_b, 0, a - b))
+    ok = (d <= rtol * np.abs(np.where(nan_b, 0, b))) | (d <= 1e-6 * colmax[None, :])
+    bad = np.argwhere(~ok)
+    assert bad.size == 0, f"{label}: {len(bad)} values differ, first at {bad[0]}: {a[tuple(bad[0])]} vs {b[tuple(bad[0])]}"

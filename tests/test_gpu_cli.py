@@ -1,0 +1,27 @@
+"""The corr_pc_gb300 command line (the reference's argv, .inp and files) on
+the golden cases: every output file equals the reference's."""
+import os
+import subprocess
+
+import pytest
+
+from corr_pc_gb300 import build, synth
+from helpers import Golden, compare_files
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", ["box_wgg_uniform", "box_wgp_clustered", "box_wpp_weighted_distinct",
+                                  "box_wgp_swap", "box_linear_bins_nojk"])
+def test_cli_output_files_match_reference(name, tmp_path):
+    g = Golden(name)
+    wl = synth.Workload(name, g.params, g.S, g.D)
+    inp = synth.write_box_run(str(tmp_path), wl, same_files=g.meta["same_files"])
+    r = subprocess.run([build.CLI, inp], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert f"pairs in={g.n_in}" in r.stdout
+    out = os.path.join(str(tmp_path), "out", "run_")
+    for fname, ref in g.files.items():
+        if fname.endswith(".info"):
+            continue
+        compare_files(open(out + fname).read(), ref, label=f"{name}:{fname}")

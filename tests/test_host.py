@@ -1,0 +1,132 @@
+"""Host side of the library (no GPU): exported ABI, read-path helpers,
+bin thresholds, parameter files, finalisation against the reference's files."""
+import math
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+import oracle
+from corr_pc_gb300 import _lib, host, synth
+from helpers import Golden, compare_files, golden_names
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_declared_symbol():
+    hdr = open(os.path.join(ROOT, "include", "corrpc.h")).read()
+    declared = sorted(set(re.findall(r"\b(cpc_[a-z_0-9]+)\s*\(", hdr)))
+    assert declared, "no declarations found"
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r" T (cpc_[a-z_0-9]+)", out))
+    missing = [d for d in declared if d not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+    lib = _lib.load()
+    for d in declared:
+        assert hasattr(lib, d)
+    assert lib.cpc_version().startswith(b"corr_pc_gb300")
+
+
+def test_rand_stream_matches_oracle_and_glibc():
+    r = _lib.rand_uniform(124693517, 0, 5000)
+    o = oracle.glibc_rand(124693517, 0, 5000) / (2147483647 + 1.0)
+    assert np.array_equal(r, o)
+    assert np.array_equal(_lib.rand_uniform(124693517, 1234, 10), o[1234:1244])
+
+
+def test_elip_angle_matches_reference_formula():
+    rng = np.random.default_rng(3)
+    e1, e2 = rng.normal(0, 0.5, 4000), rng.normal(0, 0.5, 4000)
+    e1[:3] = [0.0, -0.0, 0.0]
+    e2[:3] = [0.0, 0.3, -0.3]
+    assert np.array_equal(_lib.elip_angle(e1, e2), oracle.elip_angle(e1, e2))
+
+
+@pytest.mark.parametrize("lin", [0, 1])
+def test_rp_thresholds_reproduce_reference_binning(lin):
+    p = synth.box_ns_wgp().params
+    p.lin_bin = lin
+    thr = _lib.rp_thresholds(p)
+    if lin:
+        rs = (p.bin_r_max - p.bin_r_min) / p.n_bins
+        f = lambda r: math.floor((r - p.bin_r_min) / rs)
+    else:
+        rs = (math.log10(p.bin_r_max) - math.log10(p.bin_r_min)) / p.n_bins
+        f = lambda r: math.floor(math.log10(r / p.bin_r_min) / rs) if r > 0 else -10 ** 9
+    for k in range(p.n_bins + 1):
+        assert f(thr[k]) >= k
+        assert f(np.nextafter(thr[k], 0.0)) < k
+    rng = np.random.default_rng(0)
+    for r in rng.uniform(0, p.bin_r_max * 1.1, 20000):
+        want = f(r)
+        got = int(np.searchsorted(thr, r, side="right")) - 1
+        if 0 <= want < p.n_bins:
+            assert got == want
+        else:
+            assert got < 0 or got >= p.n_bins
+
+
+def test_pi_thresholds_reproduce_reference_binning():
+    p = synth.box_uniform_wgg().params
+    thr = _lib.pi_thresholds(p)
+    ps = (p.p_max - p.p_min) / p.n_p_bin
+    f = lambda x: math.floor((x - p.p_min) / ps)
+    for k in range(p.n_p_bin + 1):
+        assert f(thr[k]) >= k and f(np.nextafter(thr[k], -np.inf)) < k
+
+
+def test_inp_round_trip(tmp_path):
+    p = synth.box_ns_wgp().params
+    p.out_file = str(tmp_path / "out_")
+    path = str(tmp_path / "x.inp")
+    p.write(path)
+    q = synth.InpParams.read(path)
+    for _k, a, _t in synth.INP_KEYS:
+        assert getattr(p, a) == getattr(q, a), a
+
+
+def test_prepare_matches_reference_read_path():
+    g = Golden("box_wpp_weighted_distinct")
+    a = host.prepare(g.params, [("S", g.S), ("D", g.D)])
+    b = oracle.read_like_reference(g.params, [("S", g.S), ("D", g.D)])
+    for role in ("S", "D"):
+        assert np.array_equal(a[role].jk_prob, b[role].jk_prob)
+        assert np.array_equal(a[role].phi, b[role].phi)
+        assert np.array_equal(a[role].w, b[role].w)
+
+
+def test_create_rejects_bad_parameters():
+    p = synth.box_uniform_wgg().params
+    p.n_bins = 0
+    with pytest.raises(_lib.CpcError) as e:
+        _lib.Context(p)
+    assert e.value.status == 1
+    p = synth.box_uniform_wgg().params
+    p.sig_crit = 1
+    with pytest.raises(_lib.CpcError):
+        _lib.Context(p)
+    p = synth.box_uniform_wgg().params
+    p.coordinates = 3
+    with pytest.raises(_lib.CpcError):
+        _lib.Context(p)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_finalisation_matches_reference_files(name, tmp_path):
+    """Reference raw histograms -> this library's finalisation -> the
+    reference's own output files."""
+    g = Golden(name)
+    p = g.params
+    p.out_file = str(tmp_path) + "/run_"
+    inp = str(tmp_path / "run.inp")
+    p.write(inp)
+    _lib.finalize_cross(inp, {"SD": (g.raw_num, g.raw_sums)}, g.weights())
+    for fname, ref in g.files.items():
+        got = open(p.out_file + fname).read()
+        if fname.endswith(".info"):
+            continue
+        compare_files(got, ref, label=f"{name}:{fname}")

@@ -1,0 +1,53 @@
+"""The oracle (C restatement of corels2) pinned against the reference's own
+outputs: golden fixtures generated by running the reference (tests/golden)."""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import Golden, golden_names
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_port_matches_reference(name):
+    g = Golden(name)
+    p = g.params
+    cats = oracle.read_like_reference(p, [("S", g.S), ("D", g.D)])
+    num, sums, n_total, n_in = oracle.port_corels2(p, "SD", cats["D"], cats["S"], n_threads=2)
+    assert n_in == g.n_in
+    assert n_total == g.n_total
+    assert np.array_equal(num, g.raw_num)
+    scale = np.abs(g.raw_sums).max(axis=(0, 1, 2)) + 1e-300
+    assert (np.abs(sums - g.raw_sums) / scale).max() < 1e-12
+
+
+def test_port_thread_count_independent():
+    g = Golden("box_wgp_clustered")
+    cats = oracle.read_like_reference(g.params, [("S", g.S), ("D", g.D)])
+    a = oracle.port_corels2(g.params, "SD", cats["D"], cats["S"], n_threads=1)
+    b = oracle.port_corels2(g.params, "SD", cats["D"], cats["S"], n_threads=4)
+    assert np.array_equal(a[0], b[0]) and a[2:] == b[2:]
+    assert np.allclose(a[1], b[1], rtol=1e-12, atol=1e-12)
+
+
+def test_port_row_subsample_partitions():
+    """Row subsamples with offsets 0..k-1 add up to the full count."""
+    g = Golden("box_wgg_uniform")
+    cats = oracle.read_like_reference(g.params, [("S", g.S), ("D", g.D)])
+    full = oracle.port_corels2(g.params, "SD", cats["D"], cats["S"])
+    parts = [oracle.port_corels2(g.params, "SD", cats["D"], cats["S"], row_stride=3, row_offset=o)
+             for o in range(3)]
+    assert np.array_equal(sum(q[0] for q in parts), full[0])
+    assert sum(q[3] for q in parts) == full[3]
+
+
+def test_glibc_rand_restatement():
+    """The rand() restatement equals glibc's own stream (where glibc is the libc)."""
+    import ctypes
+    try:
+        libc = ctypes.CDLL("libc.so.6")
+    except OSError:
+        pytest.skip("no glibc")
+    libc.srand(124693517)
+    ref = np.array([libc.rand() for _ in range(2000)], dtype=np.int32)
+    assert np.array_equal(oracle.glibc_rand(124693517, 0, 2000), ref)
+    assert np.array_equal(oracle.glibc_rand(124693517, 777, 100), ref[777:877])
