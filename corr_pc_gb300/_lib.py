@@ -26,7 +26,8 @@ NF = 13
 EXPORTED = ["cpc_version", "cpc_create", "cpc_destroy", "cpc_last_error", "cpc_upload",
             "cpc_count", "cpc_accum_shape", "cpc_count_batch", "cpc_set_tuning",
             "cpc_host_rand_uniform", "cpc_host_elip_angle", "cpc_host_rp_thresholds",
-            "cpc_host_pi_thresholds", "cpc_launch_count", "cpc_host_finalize_cross"]
+            "cpc_host_pi_thresholds", "cpc_launch_count", "cpc_host_finalize_cross",
+            "cpc_count_fp64_noalloc"]
 
 
 class CpcError(RuntimeError):
@@ -48,6 +49,11 @@ class cpc_params(ctypes.Structure):
 class cpc_catalog(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64)] + [(n, ctypes.c_void_p) for n in (
         "x", "y", "z", "w", "e1", "e2", "phi", "jk", "jk_prob", "dc", "da")]
+
+
+class cpc_device_catalog(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64)] + [(n, ctypes.c_void_p) for n in (
+        "x", "y", "z", "w", "e1", "e2", "phi", "jk", "jk_prob")]
 
 
 class cpc_accum(ctypes.Structure):
@@ -86,6 +92,10 @@ def load() -> ctypes.CDLL:
     lib.cpc_host_pi_thresholds.argtypes = [P(cpc_params), V]
     lib.cpc_launch_count.argtypes = [V, P(I64)]
     lib.cpc_host_finalize_cross.argtypes = [ctypes.c_char_p] + [V] * 9
+    lib.cpc_count_fp64_noalloc.argtypes = [P(cpc_params), I, P(cpc_device_catalog),
+                                           P(cpc_device_catalog), V, V, P(I64), P(I64), V,
+                                           ctypes.c_char_p, ctypes.c_size_t]
+    lib.cpc_count_fp64_noalloc.restype = I
     for fn in ("cpc_create", "cpc_destroy", "cpc_upload", "cpc_count", "cpc_accum_shape",
                "cpc_count_batch", "cpc_set_tuning", "cpc_host_rand_uniform",
                "cpc_host_elip_angle", "cpc_host_rp_thresholds", "cpc_host_pi_thresholds",
@@ -260,3 +270,28 @@ def finalize_cross(inp_path: str, terms: dict, weights) -> None:
             args += [None, None]
     w = np.ascontiguousarray(weights, dtype=np.float64)
     check(load().cpc_host_finalize_cross(inp_path.encode(), *args, w.ctypes.data))
+
+
+def count_fp64_noalloc(inp_params, kind: str, g1: dict, g2: dict, d_num: int, d_sums: int,
+                       stream: int = 0) -> dict:
+    """cpc_count_fp64_noalloc: g1/g2 map field name -> (device pointer or None)
+    plus "n"; d_num/d_sums are device pointers to the output blocks."""
+    lib = load()
+    cp = params_from_inp(inp_params)
+
+    def dc(g):
+        c = cpc_device_catalog()
+        c.n = int(g["n"])
+        for f in ("x", "y", "z", "w", "e1", "e2", "phi", "jk", "jk_prob"):
+            setattr(c, f, g.get(f))
+        return c
+
+    c1, c2 = dc(g1), dc(g2)
+    nw, nb = ctypes.c_int64(), ctypes.c_int64()
+    err = ctypes.create_string_buffer(512)
+    st = lib.cpc_count_fp64_noalloc(ctypes.byref(cp), PAIR[kind], ctypes.byref(c1),
+                                    ctypes.byref(c2), d_num, d_sums, ctypes.byref(nw),
+                                    ctypes.byref(nb), stream or None, err, 512)
+    if st != CPC_OK:
+        raise CpcError(st, err.value.decode(errors="replace"))
+    return {"n_window": nw.value, "n_binned": nb.value}

@@ -22,7 +22,7 @@ CLI = os.path.join(OUT, "corr_pc_gb300")
 PEAKS = os.path.join(OUT, "libcpc_peaks.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["cell_list.cu", "pair_fast.cu", "pair_fp64.cu", "capi.cu"]
+CU_SOURCES = ["cell_list.cu", "pair_fast.cu", "pair_fp64.cu", "capi.cu", "pair_noalloc.cu"]
 CPP_SOURCES = ["host_helpers.cpp"]
 HOST_SOURCES = ["host/inp.cpp", "host/reader.cpp", "host/finalize.cpp", "host/outp.cpp",
                 "host/driver.cpp"]

@@ -22,6 +22,7 @@
 #ifndef CORRPC_H
 #define CORRPC_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -198,6 +199,53 @@ cpc_status cpc_host_finalize_cross(const char *inp_path, const int64_t *sd_num,
                                    const double *srd_sums, const int64_t *drs_num,
                                    const double *drs_sums, const int64_t *rsrd_num,
                                    const double *rsrd_sums, const double *weights);
+
+/* ---- counting without any GPU allocation (no counterpart in the reference) ----
+ *
+ * For callers that cannot allocate GPU memory themselves -- code embedded in a
+ * host application or framework that owns every device allocation, runs a
+ * memory pool that forbids cudaMalloc after start-up, or must not grow the
+ * device footprint -- this entry point counts one pair type with the plain
+ * FP64 kernel and allocates nothing: the inputs and outputs are the caller's
+ * device buffers, and the kernel's scratch (job descriptor with the exact bin
+ * thresholds, pair counters, an input-order flag) lives in a fixed 16 KiB
+ * array inside the library, resident on every device that loads it until the
+ * process exits.
+ *
+ *  - g1/g2: device arrays as corels2 receives them (same rules: swap when g2
+ *    is larger, shape holder, corel choice); after the swap the scanned
+ *    catalogue must be sorted by z (checked; CPC_ERR_INVALID otherwise), as
+ *    the reference requires for data_sorted 1.  NULL optional arrays as in
+ *    cpc_catalog; jk_prob replaces the host-side keep flags.
+ *  - d_num / d_sums: device buffers laid out as cpc_accum's num / sums (raw
+ *    region sums); zeroed by the call.  n_window / n_binned: host outputs.
+ *  - limits: coordinates 6, n_bins <= 64, n_p_bin <= 128 (the scratch holds
+ *    the thresholds), catalogue sizes < 2^31; larger values are rejected with
+ *    CPC_ERR_INVALID and a message.
+ *  - the first call on a device looks up the scratch array's device address
+ *    (with that device current); make that first call before any stream
+ *    capture.  The call synchronises `stream` (a cudaStream_t, NULL = legacy
+ *    default stream).
+ *  - every call on a device shares the one scratch array and leaves its
+ *    contents behind; calls are safe one after another, but calls that overlap
+ *    on the GPU race on it and must be serialised by the caller.
+ *  - errors: a message is written to err (err_len bytes) if err is not NULL. */
+typedef struct {
+  int64_t n;
+  const double *x, *y, *z;
+  const double *w;
+  const double *e1, *e2;
+  const double *phi;
+  const int32_t *jk;
+  const double *jk_prob;
+} cpc_device_catalog;
+
+#define CPC_NOALLOC_SCRATCH_BYTES 16384
+
+cpc_status cpc_count_fp64_noalloc(const cpc_params *params, cpc_pair_kind kind,
+                                  const cpc_device_catalog *g1, const cpc_device_catalog *g2,
+                                  int64_t *d_num, double *d_sums, int64_t *n_window,
+                                  int64_t *n_binned, void *stream, char *err, size_t err_len);
 
 #ifdef __cplusplus
 }
