@@ -396,3 +396,147 @@ def write_box_run(dirpath: str, wl: Workload, *, same_files: bool = True,
     inp = os.path.join(dirpath, "run.inp")
     p.write(inp)
     return inp
+
+
+# ---------------------------------------------------------------------------
+# sky catalogues (coordinates 0: RA, Dec in degrees, redshift)
+# ---------------------------------------------------------------------------
+
+C_KMS = 299792.458
+
+
+@dataclass
+class DistanceTable:
+    """Rows of the distances file read by da_Z (initialization.cpp:23-60):
+    z, H(z) [km/s per Mpc/h], D_A, D_C, and a fifth column that da_Z stores as
+    the transverse distance when use_comoving is 1 (Gen_inp_HSC writes the
+    comoving distance there; so does this generator)."""
+
+    z: np.ndarray
+    H: np.ndarray
+    DA: np.ndarray
+    DC: np.ndarray
+
+    @property
+    def transverse(self) -> np.ndarray:
+        return self.DC
+
+    def write(self, path: str) -> None:
+        np.savetxt(path, np.column_stack((self.z, self.H, self.DA, self.DC, self.DC)),
+                   fmt="%.18e")
+
+
+def flat_lcdm_table(z_max: float, dz: float, omega_m: float = 0.3,
+                    h0: float = 100.0) -> DistanceTable:
+    """Flat LCDM distances on the grid z_k = k dz, k = 0 .. ceil((z_max+1)/dz)+20
+    (the length data_ini allocates), D_C by the trapezoid rule."""
+    n = int(np.ceil((z_max + 1.0) / dz)) + 21
+    z = np.arange(n, dtype=np.float64) * dz
+    H = h0 * np.sqrt(omega_m * (1.0 + z) ** 3 + 1.0 - omega_m)
+    inv = C_KMS / H
+    dc = np.concatenate(([0.0], np.cumsum(0.5 * (inv[1:] + inv[:-1]) * dz)))
+    return DistanceTable(z, H, dc / (1.0 + z), dc)
+
+
+def jk_sky_grid(ra, dec, ra_range, dec_range, n_ra: int, n_dec: int) -> np.ndarray:
+    """Jackknife regions on an RA/Dec grid: label = i_ra * n_dec + i_dec."""
+    fa = n_ra / (ra_range[1] - ra_range[0])
+    fd = n_dec / (dec_range[1] - dec_range[0])
+    ia = np.clip(((ra - ra_range[0]) * fa).astype(np.int64), 0, n_ra - 1)
+    idd = np.clip(((dec - dec_range[0]) * fd).astype(np.int64), 0, n_dec - 1)
+    return (ia * n_dec + idd).astype(np.int32)
+
+
+def sky_patch(n: int, seed: int, table: DistanceTable, *, ra_deg: float = 10.0,
+              dec_deg: float = 10.0, chi_range=(500.0, 1500.0), nside_jk: int = 10,
+              with_shapes: bool = False, weights: bool = False) -> Catalog:
+    """Points uniform on the patch RA in [0, ra_deg), sin(Dec) uniform on
+    [0, sin(dec_deg)), comoving distance with p(chi) ~ chi^2 on chi_range,
+    converted to redshift through the table; sorted by redshift."""
+    rng = np.random.default_rng(seed)
+    ra = rng.uniform(0.0, ra_deg, n)
+    dec = np.degrees(np.arcsin(rng.uniform(0.0, np.sin(np.radians(dec_deg)), n)))
+    c0, c1 = chi_range
+    chi = np.cbrt(rng.uniform(c0 ** 3, c1 ** 3, n))
+    z = np.interp(chi, table.DC, table.z)
+    e1 = e2 = None
+    if with_shapes:
+        e1, e2 = shapes(rng, n)
+    w = rng.uniform(0.5, 1.5, n) if weights else None
+    jk = jk_sky_grid(ra, dec, (0.0, ra_deg), (0.0, dec_deg), nside_jk, nside_jk) \
+        if nside_jk else None
+    return Catalog(ra, dec, z, w, e1, e2, jk).sorted_by_z()
+
+
+@dataclass
+class SkyWorkload:
+    name: str
+    params: InpParams
+    table: DistanceTable
+    shape: Catalog       # S
+    density: Catalog     # D
+    shape_rand: Catalog  # Rs
+    density_rand: Catalog  # Rd
+
+
+def _sky_params(*, which_corr, rmin, rmax, nrp, npi, pmax, njk, z_max=1.0) -> InpParams:
+    return InpParams(which_corr=which_corr, coordinates=0, estimator=0, data_sorted=1,
+                     use_comoving=1, do_jk=1 if njk else 0, sig_crit=0,
+                     n_jk_regions=njk, bin_r_min=rmin, bin_r_max=rmax, n_bins=nrp,
+                     lin_bin=0, n_p_bin=npi, p_min=-pmax, p_max=pmax, z_min=0.0,
+                     z_max=z_max, dz=0.0001, z_sep_min=0.0, z_sep_max=0.0,
+                     periodic_box=0, periodic_box_size=0.0)
+
+
+def sky_wgp(n_data: int = 500000, n_rand: int = 5000000, seed: int = 0,
+            which_corr: int = 1) -> SkyWorkload:
+    """Sky survey: data (with shapes and U(0.5,1.5) weights) and randoms on a
+    10x10 degree patch, chi 500-1500 Mpc/h, 15 log r_p bins 0.3-60, 30 Pi bins
+    over +-60, 100 jackknife regions on a 10x10 RA/Dec grid; terms SRd, RsRd, SD,
+    DRs.  S and D are the same points, Rs and Rd the same randoms."""
+    p = _sky_params(which_corr=which_corr, rmin=0.3, rmax=60.0, nrp=15, npi=30, pmax=60.0,
+                    njk=100)
+    t = flat_lcdm_table(p.z_max, p.dz)
+    d = sky_patch(n_data, seed, t, with_shapes=True, weights=True)
+    r = sky_patch(n_rand, seed + 1, t)
+    return SkyWorkload(f"sky_wgp_{n_data}_{n_rand}", p, t, d, d, r, r)
+
+
+def write_sky_run(dirpath: str, wl: SkyWorkload, *, n_threads: int = 0,
+                  same_files: bool = True) -> str:
+    """Write the four catalogues, the distances file and the .inp of a sky cross
+    run (terms SRd, RsRd, SD, DRs); returns the .inp path."""
+    os.makedirs(os.path.join(dirpath, "out"), exist_ok=True)
+    p = wl.params
+    s = write_catalog(os.path.join(dirpath, "S"), wl.shape)
+    d = s if same_files else write_catalog(os.path.join(dirpath, "D"), wl.density)
+    rs = write_catalog(os.path.join(dirpath, "Rs"), wl.shape_rand, write_e=False)
+    rd = rs if same_files else write_catalog(os.path.join(dirpath, "Rd"), wl.density_rand,
+                                             write_e=False)
+    dist = os.path.join(dirpath, "distances.dat")
+    wl.table.write(dist)
+    p.shape_pos_file, p.shape_z_file, p.shape_e_file = s["pos"], s["z"], s["e"]
+    p.shape_wt_file, p.shape_jk_file = s["wt"], s["jk"]
+    p.density_pos_file, p.density_z_file = d["pos"], d["z"]
+    p.density_wt_file, p.density_jk_file, p.density_e_file = d["wt"], d["jk"], d["e"]
+    p.shape_rand_pos_file, p.shape_rand_z_file = rs["pos"], rs["z"]
+    p.shape_rand_wt_file, p.shape_rand_jk_file = rs["wt"], rs["jk"]
+    p.density_rand_pos_file, p.density_rand_z_file = rd["pos"], rd["z"]
+    p.density_rand_wt_file, p.density_rand_jk_file = rd["wt"], rd["jk"]
+    p.distance_file = dist
+    p.out_file = os.path.join(dirpath, "out", "run_")
+    p.n_threads = n_threads
+    p.n_shape, p.n_density = wl.shape.n, wl.density.n
+    p.n_shape_rand, p.n_density_rand = wl.shape_rand.n, wl.density_rand.n
+    inp = os.path.join(dirpath, "run.inp")
+    p.write(inp)
+    return inp
+
+
+def derived_z_sep(p: InpParams, table: DistanceTable) -> tuple:
+    """z_sep_max / z_sep_min as data_ini derives them for coordinates 0
+    (initialization.cpp:223-276): p_max * H(z_idx) / 300000 + 0.001 with
+    z_idx = ceil(z_max / dz)."""
+    k = int(np.ceil(p.z_max / p.dz))
+    return (p.p_max * table.H[k] / 300000.0 + 0.001,
+            p.p_min * table.H[k] / 300000.0 - 0.001)

@@ -127,12 +127,16 @@ def elip_angle(e1, e2):
     return out
 
 
-def read_like_reference(params, cats_in_read_order):
+def read_like_reference(params, cats_in_read_order, table=None):
     """Attach jk_prob / phi / include_prob as read_data does, consuming one glibc
     rand() stream across the catalogues in the reference's read order.
 
     ``cats_in_read_order``: list of (role, Catalog-like with x,y,z,w,e1,e2,jk)
     with role in {"S", "Rs", "D", "Rd"}.  Returns dict role -> OracleCatalog.
+    ``table`` (sky runs): the distances table (z, H, DA, DC rows); each galaxy
+    gets DC = D_C[floor(z/dz)] and DA = the transverse column at the same row,
+    without interpolation (read_dat.cpp:247-251; use_comoving 1 stores the
+    table's fifth column as D_A, initialization.cpp:40-44).
     """
     p = params
     pos = 0
@@ -162,8 +166,13 @@ def read_like_reference(params, cats_in_read_order):
         phi = elip_angle(e1, e2) if read_e else np.full(n, -10.0)
         w = c.w if c.w is not None else np.ones(n)
         jk = c.jk if (p.do_jk and c.jk is not None) else None
+        dc = da = None
+        if not p.periodic_box:
+            it = np.floor(np.asarray(c.z) / p.dz).astype(np.int64)
+            dc = table.DC[it]
+            da = (table.transverse if p.use_comoving else table.DA)[it]
         out[role] = OracleCatalog(c.x, c.y, c.z, w=w, e1=e1, e2=e2, phi=phi, jk=jk,
-                                  jk_prob=jkp, include_prob=inc)
+                                  jk_prob=jkp, include_prob=inc, dc=dc, da=da)
     return out
 
 
@@ -212,8 +221,10 @@ def reference_available() -> bool:
     return os.path.exists(REF_BIN)
 
 
-def run_reference(inp: str, dump: str, *, bining: bool = True, timeout: float = 3600):
-    args = [REF_BIN, inp, dump] + ([] if bining else ["--no-bining"])
+def run_reference(inp: str, dump: str, *, bining: bool = True, timeout: float = 3600,
+                  drs_wgg: bool = False):
+    args = [REF_BIN, inp, dump] + ([] if bining else ["--no-bining"]) + \
+        (["--drs-wgg"] if drs_wgg else [])
     r = subprocess.run(args, capture_output=True, text=True, timeout=timeout)
     if r.returncode != 0:
         raise RuntimeError(f"reference harness failed: {r.stdout[-2000:]} {r.stderr[-2000:]}")

@@ -10,7 +10,7 @@
 // periodic-box jackknife draws -- then the corels2/corels1 calls per estimator,
 // then do_bining which writes the reference's own output files).
 //
-// Usage: ref_harness <file.inp> <dump.txt> [--no-bining]
+// Usage: ref_harness <file.inp> <dump.txt> [--no-bining] [--drs-wgg]
 // Test infrastructure only: the product never links or runs this.
 #include <cstdio>
 #include <cstring>
@@ -53,7 +53,11 @@ int main(int argc, char **argv) {
     std::fprintf(stderr, "usage: %s file.inp dump.txt [--no-bining]\n", argv[0]);
     return 2;
   }
-  bool bining = !(argc > 3 && std::strcmp(argv[3], "--no-bining") == 0);
+  bool bining = true, drs_wgg = false;
+  for (int a = 3; a < argc; a++) {
+    if (std::strcmp(argv[a], "--no-bining") == 0) bining = false;
+    if (std::strcmp(argv[a], "--drs-wgg") == 0) drs_wgg = true;
+  }
   data_info d = data_info();
   if (data_ini(d, argv[1]) != 0) {
     std::printf("Bad initialization!! Bye\n");
@@ -134,9 +138,16 @@ int main(int argc, char **argv) {
     d.do_SD = 0;
     dump_bin_jk(f, "SD", n, B.SD, d);
     if (!d.periodic_box) {
+      // --drs-wgg: run this term as a density-density count.  With which_corr
+      // 1 the reference's DRs term rotates the ellipticities of randoms that
+      // were read without any (an uninitialised pointer, corels.cpp:216-219)
+      // and crashes; its counts and weights do not depend on which_corr.
+      const int wc = d.which_corr;
+      if (drs_wgg) d.which_corr = 0;
       d.do_DRs = 1;
       n = corels2(grand_shape, gdensity, B.DRs, d);
       d.do_DRs = 0;
+      d.which_corr = wc;
       dump_bin_jk(f, "DRs", n, B.DRs, d);
     }
   }

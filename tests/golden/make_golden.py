@@ -127,10 +127,86 @@ def run_case(name, p, S, D, same):
     print(f"{name}: n_in={sd['n_in']} n_total={totals[-1][0]} files={len(files)}")
 
 
+SKY_TERMS = ("SRd", "RsRd", "SD", "DRs")  # do_corr.cpp:98-133 order
+
+
+def sky_cases():
+    """Sky cross runs (coordinates 0): data and randoms on a small RA/Dec patch
+    with a flat LCDM distance table on a coarse dz grid (keeps the fixture
+    small; the table is stored in the fixture)."""
+    out = []
+    p = synth._sky_params(which_corr=1, rmin=0.3, rmax=30.0, nrp=8, npi=12, pmax=40.0,
+                          njk=9, z_max=0.5)
+    p.dz = 0.001
+    t = synth.flat_lcdm_table(p.z_max, p.dz)
+    d = synth.sky_patch(1500, 31, t, ra_deg=6, dec_deg=6, chi_range=(500, 900), nside_jk=3,
+                        with_shapes=True, weights=True)
+    r = synth.sky_patch(4000, 32, t, ra_deg=6, dec_deg=6, chi_range=(500, 900), nside_jk=3)
+    out.append(("sky_wgp_jk", synth.SkyWorkload("sky_wgp_jk", p, t, d, d, r, r), True))
+
+    p = synth._sky_params(which_corr=0, rmin=0.5, rmax=40.0, nrp=10, npi=10, pmax=50.0,
+                          njk=4, z_max=0.6)
+    p.dz = 0.001
+    p.data_sorted = 0
+    t = synth.flat_lcdm_table(p.z_max, p.dz)
+    # RA across 0/360 exercises the reference's RA wrap (sky_calcs.cpp:134-141)
+    s = synth.sky_patch(1200, 33, t, ra_deg=8, dec_deg=30, chi_range=(600, 1200), nside_jk=2,
+                        weights=True)
+    dd = synth.sky_patch(900, 34, t, ra_deg=8, dec_deg=30, chi_range=(600, 1200), nside_jk=2)
+    rs = synth.sky_patch(3000, 35, t, ra_deg=8, dec_deg=30, chi_range=(600, 1200), nside_jk=2)
+    rd = synth.sky_patch(2500, 36, t, ra_deg=8, dec_deg=30, chi_range=(600, 1200), nside_jk=2)
+    for c in (s, dd, rs, rd):
+        c.x = np.where(c.x < 3.0, c.x + 357.0, c.x - 3.0)
+        c.y = c.y - 10.0
+    rng = np.random.default_rng(37)
+    for c in (s, dd, rs, rd):  # unsorted input (data_sorted 0)
+        perm = rng.permutation(c.n)
+        c2 = c.subset(perm)
+        c.x, c.y, c.z, c.w, c.e1, c.e2, c.jk = c2.x, c2.y, c2.z, c2.w, c2.e1, c2.e2, c2.jk
+    out.append(("sky_wgg_distinct_wrap", synth.SkyWorkload("sky_wgg_distinct_wrap", p, t, s, dd,
+                                                           rs, rd), False))
+    return out
+
+
+def run_sky_case(name, wl, same):
+    with tempfile.TemporaryDirectory() as tmp:
+        inp = synth.write_sky_run(tmp, wl, n_threads=1, same_files=same)
+        totals, _ = oracle.run_reference(inp, os.path.join(tmp, "dump.txt"), bining=True,
+                                         drs_wgg=True)
+        dump = oracle.parse_dump(os.path.join(tmp, "dump.txt"))
+        files = {}
+        for f in KEEP_FILES:
+            fp = os.path.join(tmp, "out", "run_" + f)
+            if os.path.exists(fp):
+                files[f] = open(fp).read()
+        params = {a: getattr(wl.params, a) for _k, a, _t in synth.INP_KEYS}
+    arrays = {"table_H": wl.table.H, "table_DC": wl.table.DC, "table_DA": wl.table.DA}
+    for role, c in (("S", wl.shape), ("D", wl.density), ("Rs", wl.shape_rand),
+                    ("Rd", wl.density_rand)):
+        for a in ("x", "y", "z", "w", "e1", "e2", "jk"):
+            v = getattr(c, a)
+            if v is not None:
+                arrays[f"{role}_{a}"] = v
+    for k, term in enumerate(SKY_TERMS):
+        arrays[f"{term}_raw_num"] = dump[term]["raw_num"]
+        arrays[f"{term}_raw_sums"] = dump[term]["raw_sums"]
+        arrays[f"{term}_n_in"] = np.array(dump[term]["n_in"])
+        arrays[f"{term}_n_total"] = np.array(totals[k][0])
+    meta = {"name": name, "params": params, "same_files": same, "files": files,
+            "terms": list(SKY_TERMS), "drs_as_wgg": True}
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **arrays)
+    print(f"{name}: " + " ".join(f"{t}={dump[t]['n_in']}" for t in SKY_TERMS))
+
+
 def main():
     oracle.build_reference()
+    only = sys.argv[1:]
     for name, p, S, D, same in cases():
-        run_case(name, p, S, D, same)
+        if not only or name in only:
+            run_case(name, p, S, D, same)
+    for name, wl, same in sky_cases():
+        if not only or name in only:
+            run_sky_case(name, wl, same)
 
 
 if __name__ == "__main__":

@@ -15,7 +15,50 @@ NONCANCEL = [0, 2, 4, 6, 8, 10, 11, 12]
 
 
 def golden_names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """Periodic-box fixtures (one SD term each)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "box_*.npz")))
+
+
+def sky_golden_names():
+    """Sky fixtures (four terms each: SRd, RsRd, SD, DRs)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "sky_*.npz")))
+
+
+class SkyGolden:
+    """A sky cross run as the reference computed it: four catalogues, the
+    distances table and, per term, the raw histograms and pair counters.  The
+    reference's DRs term was run as a density-density count (its wg+ DRs term
+    crashes), so only its counts and weights are compared."""
+
+    KIND = {"SRd": ("SRd", "Rd", "S"), "RsRd": ("RsRd", "Rd", "Rs"), "SD": ("SD", "D", "S"),
+            "DRs": ("DRs", "Rs", "D")}
+
+    def __init__(self, name):
+        z = np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False)
+        self.meta = json.loads(str(z["meta"]))
+        self.arr = {k: z[k] for k in z.files if k != "meta"}
+        p = synth.InpParams()
+        for k, v in self.meta["params"].items():
+            setattr(p, k, v)
+        self.params = p
+        a = self.arr
+        self.table = synth.DistanceTable(p.dz * np.arange(a["table_H"].shape[0]), a["table_H"],
+                                         a["table_DA"], a["table_DC"])
+        self.cats = {r: self._cat(r) for r in ("S", "D", "Rs", "Rd")}
+        self.terms = self.meta["terms"]
+        self.files = self.meta["files"]
+
+    def _cat(self, role):
+        g = lambda a: self.arr.get(f"{role}_{a}")
+        return synth.Catalog(g("x"), g("y"), g("z"), g("w"), g("e1"), g("e2"), g("jk"))
+
+    def read_order(self):
+        return [(r, self.cats[r]) for r in ("S", "Rs", "D", "Rd")]
+
+    def term(self, t):
+        a = self.arr
+        return (a[f"{t}_raw_num"], a[f"{t}_raw_sums"], int(a[f"{t}_n_in"]),
+                int(a[f"{t}_n_total"]))
 
 
 class Golden:

@@ -4,7 +4,10 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import Golden, golden_names
+import copy
+
+from corr_pc_gb300 import synth
+from helpers import Golden, SkyGolden, golden_names, sky_golden_names
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -51,3 +54,28 @@ def test_glibc_rand_restatement():
     ref = np.array([libc.rand() for _ in range(2000)], dtype=np.int32)
     assert np.array_equal(oracle.glibc_rand(124693517, 0, 2000), ref)
     assert np.array_equal(oracle.glibc_rand(124693517, 777, 100), ref[777:877])
+
+
+@pytest.mark.parametrize("name", sky_golden_names())
+def test_port_matches_reference_sky(name):
+    """Sky terms SRd, RsRd, SD, DRs: windows (sky_calcs.cpp:105-196), great-circle
+    r_p with the C library's trigonometry, comoving Pi, jackknife to both
+    regions, table lookups of DC/DA."""
+    g = SkyGolden(name)
+    p = g.params
+    cats = oracle.read_like_reference(p, g.read_order(), table=g.table)
+    zsep = synth.derived_z_sep(p, g.table)[0]
+    for t in g.terms:
+        kind, a, b = SkyGolden.KIND[t]
+        pp = p
+        if t == "DRs" and g.meta["drs_as_wgg"]:
+            pp = copy.copy(p)
+            pp.which_corr = 0
+        num, sums, n_total, n_in = oracle.port_corels2(pp, kind, cats[a], cats[b], n_threads=2,
+                                                       H_z=g.table.H, dA_z=g.table.transverse,
+                                                       z_sep_max=zsep)
+        rnum, rsums, rin, rtot = g.term(t)
+        assert (n_in, n_total) == (rin, rtot), t
+        assert np.array_equal(num, rnum), t
+        scale = np.abs(rsums).max(axis=(0, 1, 2)) + 1e-300
+        assert (np.abs(sums - rsums) / scale).max() < 1e-12, t
