@@ -120,6 +120,26 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _profile_traffic(workload: str):
+    """DRAM bytes per launch of the fast kernel (dram__bytes_read.sum +
+    dram__bytes_write.sum) from the committed ncu summary of this workload."""
+    path = os.path.join(ROOT, "profiles", f"fast_pairs_kernel_{workload}.md")
+    try:
+        for line in open(path):
+            if line.startswith("| traffic_bytes_per_launch |"):
+                return float(line.split("|")[2])
+    except OSError:
+        pass
+    return None
+
+
+def _hbm_peak():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def _peaks() -> dict:
     """Live FP32 FFMA and shared-memory 32-bit atomic peaks (this GPU)."""
     from corr_pc_gb300 import build as b
@@ -292,10 +312,20 @@ def main() -> None:
     n_per_step = n_bin / args.steps
     achieved_flops = F * n_per_step / pair_s
     achieved_atom = A * n_per_step / pair_s
+    traffic = _profile_traffic(_describe(wls)["workload"])
+    hbm_peak = _hbm_peak()
+    hbm = None
+    if traffic is not None:
+        hbm_gbs = traffic / (tot_pair_ms / args.steps * 1e-3) / 1e9
+        hbm = {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
+               "frac": hbm_gbs / hbm_peak if hbm_peak else None,
+               "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+               "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                 "profiles/fast_pairs_kernel_<workload>.md"}
     roofline = {"bound": "fp32", "achieved": achieved_flops / 1e12,
                 "peak": (peaks["ffma_flops"] or float("nan")) / 1e12, "unit": "TFLOP/s",
                 "frac": achieved_flops / peaks["ffma_flops"] if peaks["ffma_flops"] else None,
-                "traffic": None,
+                "traffic": traffic,
                 "kernel": "fast_pairs_kernel", "kernel_ms_per_launch": tot_pair_ms / args.steps,
                 "work_per_pair": {"fp32_flops": F, "smem_atomic_updates": A},
                 "peak_source": "measured live in this run (FFMA microbenchmark); "
@@ -304,7 +334,8 @@ def main() -> None:
                                  "peak": (peaks["smem_atomic_u32_ops"] or float("nan")) / 1e12,
                                  "unit": "Tops/s",
                                  "frac": achieved_atom / peaks["smem_atomic_u32_ops"]
-                                 if peaks["smem_atomic_u32_ops"] else None}}
+                                 if peaks["smem_atomic_u32_ops"] else None},
+                "hbm": hbm}
     # plain FP64 GPU kernel on a bounded row sample of the same workload
     fp64 = None
     if len(ctxs) == 1:
