@@ -131,12 +131,28 @@ def _f64(a):
 
 
 class Context:
-    """One GPU context (the state corels2 works on for one .inp parameter set)."""
+    """One GPU context (the state corels2 works on for one .inp parameter set).
 
-    def __init__(self, inp_params):
+    Sky runs (coordinates 0) also take the distance table (``table`` with
+    columns z, H, DA, DC as data_ini reads them): the library needs H(z) and
+    the transverse distance for the per-row windows, and z_sep_max is derived
+    from the table as data_ini does."""
+
+    def __init__(self, inp_params, table=None):
         self.lib = load()
         self.params = inp_params
         self._cp = params_from_inp(inp_params)
+        self._table = None
+        if inp_params.coordinates == 0:
+            if table is None:
+                raise ValueError("sky contexts need the distance table")
+            from . import synth
+            H = np.ascontiguousarray(table.H, dtype=np.float64)
+            dA = np.ascontiguousarray(table.transverse if inp_params.use_comoving else table.DA,
+                                      dtype=np.float64)
+            self._table = (H, dA)
+            self._cp.H_z, self._cp.dA_z, self._cp.n_table = H.ctypes.data, dA.ctypes.data, H.shape[0]
+            self._cp.z_sep_max = synth.derived_z_sep(inp_params, table)[0]
         h = ctypes.c_void_p()
         check(self.lib.cpc_create(ctypes.byref(h), ctypes.byref(self._cp)))
         self.h = h
@@ -161,7 +177,8 @@ class Context:
         check(self.lib.cpc_set_tuning(self.h, cells_per_rmax, pi_window, tile), self.h)
 
     def upload(self, slot: int, cat) -> None:
-        """cat: object with x, y, z and optional w, e1, e2, phi, jk, jk_prob."""
+        """cat: object with x, y, z and optional w, e1, e2, phi, jk, jk_prob
+        (and dc, da for sky catalogues)."""
         keep = []
 
         def ptr(a, dt=np.float64):
@@ -179,6 +196,7 @@ class Context:
         c.phi = ptr(getattr(cat, "phi", None))
         c.jk = ptr(getattr(cat, "jk", None), np.int32)
         c.jk_prob = ptr(getattr(cat, "jk_prob", None))
+        c.dc, c.da = ptr(getattr(cat, "dc", None)), ptr(getattr(cat, "da", None))
         check(self.lib.cpc_upload(self.h, slot, ctypes.byref(c)), self.h)
         self.sizes[slot] = c.n
 

@@ -22,11 +22,12 @@ CLI = os.path.join(OUT, "corr_pc_gb300")
 PEAKS = os.path.join(OUT, "libcpc_peaks.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["cell_list.cu", "pair_fast.cu", "pair_fp64.cu", "capi.cu", "pair_noalloc.cu"]
+CU_SOURCES = ["cell_list.cu", "pair_fast.cu", "pair_fp64.cu", "pair_sky.cu", "capi.cu",
+              "pair_noalloc.cu"]
 CPP_SOURCES = ["host_helpers.cpp"]
 HOST_SOURCES = ["host/inp.cpp", "host/reader.cpp", "host/finalize.cpp", "host/outp.cpp",
                 "host/driver.cpp"]
-HEADERS = ["cpc_device.cuh", "kernels.h", "host_helpers.h", "host/host.h"]
+HEADERS = ["cpc_device.cuh", "kernels.h", "host_helpers.h", "pair_values.h", "host/host.h"]
 
 
 def nvcc() -> str:

@@ -81,6 +81,14 @@ struct Slot {
   DevBuf<int32_t> zjk;
   DevBuf<uint8_t> zkeep;
   DevBuf<int64_t> zorig;
+  // sky (coordinates 0): x, y, z, w, e1, e2, phi, jk, keep, orig above hold the
+  // redshift-ordered catalogue; these the sky-only per-galaxy quantities
+  bool sky = false;
+  DevBuf<double> dc, da, sd, cd, rar, decr, win;
+  // host copies in the same order for the host edge tier
+  std::vector<double> hs_ra, hs_dec, hs_dc, hs_da, hs_w, hs_e1, hs_e2, hs_phi;
+  std::vector<int32_t> hs_jk;
+  std::vector<uint8_t> hs_keep;
 };
 
 struct UnitCache {
@@ -118,6 +126,9 @@ struct cpc_ctx {
   DevBuf<uint64_t> d_keys, d_ktmp;
   DevBuf<uint32_t> d_vals, d_vtmp, d_hist, d_bucket;
   DevBuf<unsigned long long> d_census;
+  // sky host edge queue
+  DevBuf<int2> d_hq;
+  DevBuf<unsigned long long> d_hq_n;
   std::vector<UnitCache> unit_cache;
   int64_t launches = 0;  // kernels launched by this context (all entry points)
 };
@@ -163,8 +174,9 @@ float f_down(double v) {
 }
 
 cpc_status validate_params(cpc_ctx *c, const cpc_params &p) {
-  if (p.coordinates != 6)
-    return fail(c, CPC_ERR_INVALID, "coordinates: only 6 (x,y,z with r_p, Pi) is supported by this build");
+  if (p.coordinates != 6 && p.coordinates != 0)
+    return fail(c, CPC_ERR_INVALID,
+                "coordinates: 6 (x,y,z with r_p, Pi) and 0 (sky, r_p and Pi) are supported");
   if (p.which_corr < 0 || p.which_corr > 2) return fail(c, CPC_ERR_INVALID, "which_corr must be 0, 1 or 2");
   if (p.sig_crit != 0) return fail(c, CPC_ERR_INVALID, "sig_crit weights are not supported");
   if (p.rand_subsample != 0) return fail(c, CPC_ERR_INVALID, "rand_subsample is not supported");
@@ -175,6 +187,14 @@ cpc_status validate_params(cpc_ctx *c, const cpc_params &p) {
   if (!(p.bin_r_max > p.bin_r_min) || !(p.bin_r_min >= 0) || (!p.lin_bin && !(p.bin_r_min > 0)))
     return fail(c, CPC_ERR_INVALID, "bad r_p bin limits");
   if (!(p.p_max > p.p_min)) return fail(c, CPC_ERR_INVALID, "bad Pi bin limits");
+  if (p.coordinates == 0) {
+    if (p.periodic_box) return fail(c, CPC_ERR_INVALID, "coordinates 0 (sky) cannot be periodic");
+    if (!p.H_z || !p.dA_z || p.n_table < 2)
+      return fail(c, CPC_ERR_INVALID, "sky runs need the distance table (H_z, dA_z, n_table)");
+    if (!(p.dz > 0) || !(p.z_max > 0) || !std::isfinite(p.z_sep_max))
+      return fail(c, CPC_ERR_INVALID, "sky runs need dz > 0, z_max > 0 and a finite z_sep_max");
+    return CPC_OK;
+  }
   if (!(p.periodic_box_size > 0)) return fail(c, CPC_ERR_INVALID, "box size must be > 0");
   if (p.periodic_box) {
     const double L = p.periodic_box_size;
@@ -694,6 +714,279 @@ cpc_status run_fast(std::vector<JobPlan> &jobs) {
   return CPC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// sky path (coordinates 0)
+// ---------------------------------------------------------------------------
+
+SkyParams sky_params(const cpc_ctx *c) {
+  const cpc_params &p = c->p;
+  SkyParams sp;
+  sp.H = c->H.data();
+  sp.dA = c->dA.data();
+  sp.n_table = (int64_t)std::min(c->H.size(), c->dA.size());
+  sp.dz = p.dz;
+  sp.z_max = p.z_max;
+  sp.z_sep_max = p.z_sep_max;
+  sp.p_min = p.p_min;
+  sp.p_max = p.p_max;
+  sp.p_size = c->ps;
+  sp.r_min = p.bin_r_min;
+  sp.r_max = p.bin_r_max;
+  sp.r_size = c->rsize;
+  sp.lin_bin = p.lin_bin ? 1 : 0;
+  sp.n_bins = p.n_bins;
+  sp.n_p_bin = p.n_p_bin;
+  return sp;
+}
+
+// Upload a sky catalogue: per-galaxy windows and angles on the host (C
+// library, exactly the reference's values), redshift order from the device
+// radix sort, then every array in that order on the device and on the host.
+cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
+  const cpc_params &p = c->p;
+  const int64_t n = cat->n;
+  if (n > 0 && (!cat->dc || !cat->da))
+    return fail(c, CPC_ERR_INVALID, "sky catalogues need dc and da (distance-table lookups)");
+  Slot &s = c->slots[slot];
+  s.valid = false;
+  s.zbuilt = false;
+  s.sky = true;
+  s.n = n;
+  s.version = ++c->version_ctr;
+  const SkyParams sp = sky_params(c);
+  std::vector<double> w(n, 1.0), e1(n, 0.0), e2(n, 0.0), phi(n, -10.0);
+  std::vector<double> rar(n), decr(n), sd(n), cd(n), win(6 * (size_t)n);
+  std::vector<int32_t> jk(n, 0);
+  std::vector<uint8_t> keep(n, 0);
+  s.has_e = cat->e1 && cat->e2;
+  for (int64_t i = 0; i < n; i++) {
+    const double ra = cat->x[i], dec = cat->y[i], z = cat->z[i];
+    if (!std::isfinite(ra) || !std::isfinite(dec) || !std::isfinite(z) ||
+        !std::isfinite(cat->dc[i]) || !std::isfinite(cat->da[i]))
+      return fail(c, CPC_ERR_RANGE, "non-finite position or distance at row " + std::to_string(i));
+    if (z < 0 || z > p.z_max)  // read_dat.cpp:228-234
+      return fail(c, CPC_ERR_RANGE, "redshift outside [0, z_max] at row " + std::to_string(i));
+    if (cat->w) {
+      if (!std::isfinite(cat->w[i])) return fail(c, CPC_ERR_RANGE, "non-finite weight");
+      w[i] = cat->w[i];
+    }
+    if (s.has_e) {
+      if (!std::isfinite(cat->e1[i]) || !std::isfinite(cat->e2[i]))
+        return fail(c, CPC_ERR_RANGE, "non-finite ellipticity");
+      e1[i] = cat->e1[i];
+      e2[i] = cat->e2[i];
+    }
+    if (cat->phi) {
+      if (!std::isfinite(cat->phi[i])) return fail(c, CPC_ERR_RANGE, "non-finite phi");
+      phi[i] = cat->phi[i];
+    }
+    if (p.do_jk) {
+      const int r = cat->jk[i];
+      if (r < 0 || r >= p.n_jk)
+        return fail(c, CPC_ERR_RANGE, "jackknife label out of range at row " + std::to_string(i));
+      jk[i] = r;
+    }
+    if (cat->jk_prob) keep[i] = cat->jk_prob[i] >= 0.5 ? 1 : 0;
+    sky_angles(ra, dec, &rar[i], &decr[i], &sd[i], &cd[i]);
+    double wv[6];
+    const int rc = sky_window(sp, ra, dec, z, wv);
+    if (rc == 1)  // lim_calc_ra_dec exits the program here (sky_calcs.cpp:109-113)
+      return fail(c, CPC_ERR_RANGE, "window z_min above z_max at row " + std::to_string(i));
+    if (rc == 2)
+      return fail(c, CPC_ERR_RANGE, "distance table too short for the window of row " + std::to_string(i));
+    for (int q = 0; q < 6; q++) win[(size_t)q * n + i] = wv[q];
+  }
+  // redshift order (stable: ties keep the input order)
+  cudaStream_t st = c->st;
+  const size_t nn = std::max<int64_t>(n, 1);
+  std::vector<uint32_t> perm(n);
+  {
+    DevBuf<double> oz;
+    CK(oz.alloc(nn), "alloc");
+    CK(c->d_keys.alloc(nn), "alloc"); CK(c->d_ktmp.alloc(nn), "alloc");
+    CK(c->d_vals.alloc(nn), "alloc"); CK(c->d_vtmp.alloc(nn), "alloc");
+    CK(c->d_hist.alloc(radix_hist_words(nn)), "alloc");
+    CK(c->d_census.alloc(8 * 256), "alloc");
+    if (n > 0) {
+      CK(cudaMemcpyAsync(oz.p, cat->z, 8 * n, cudaMemcpyHostToDevice, st), "H2D");
+      CK(launch_z_keys(n, oz.p, c->d_keys.p, c->d_vals.p, st), "z keys");
+      c->launches += 1;
+      CK(radix_sort_pairs(n, c->d_keys.p, c->d_vals.p, c->d_ktmp.p, c->d_vtmp.p, c->d_hist.p,
+                          c->d_census.p, st, &c->launches), "z sort");
+      CK(cudaMemcpyAsync(perm.data(), c->d_vals.p, 4 * n, cudaMemcpyDeviceToHost, st), "D2H");
+    }
+    CK(cudaStreamSynchronize(st), "sort");
+  }
+  auto take = [&](const double *src, std::vector<double> &dst) {
+    dst.resize(n);
+    for (int64_t k = 0; k < n; k++) dst[k] = src[perm[k]];
+  };
+  std::vector<double> zs, sds, cds, rars, decrs;
+  take(cat->x, s.hs_ra);
+  take(cat->y, s.hs_dec);
+  take(cat->z, zs);
+  take(cat->dc, s.hs_dc);
+  take(cat->da, s.hs_da);
+  take(w.data(), s.hs_w);
+  take(e1.data(), s.hs_e1);
+  take(e2.data(), s.hs_e2);
+  take(phi.data(), s.hs_phi);
+  take(sd.data(), sds);
+  take(cd.data(), cds);
+  take(rar.data(), rars);
+  take(decr.data(), decrs);
+  s.hs_jk.resize(n);
+  s.hs_keep.resize(n);
+  std::vector<int64_t> orig(n);
+  std::vector<double> wins(6 * (size_t)n);
+  for (int64_t k = 0; k < n; k++) {
+    const uint32_t o = perm[k];
+    s.hs_jk[k] = jk[o];
+    s.hs_keep[k] = keep[o];
+    orig[k] = o;
+    for (int q = 0; q < 6; q++) wins[(size_t)q * n + k] = win[(size_t)q * n + o];
+  }
+  auto put = [&](DevBuf<double> &d, const std::vector<double> &h, size_t cnt) -> cudaError_t {
+    cudaError_t e = d.alloc(std::max<size_t>(cnt, 1));
+    if (e != cudaSuccess || cnt == 0) return e;
+    return cudaMemcpyAsync(d.p, h.data(), 8 * cnt, cudaMemcpyHostToDevice, st);
+  };
+  CK(put(s.x, s.hs_ra, n), "sky upload"); CK(put(s.y, s.hs_dec, n), "sky upload");
+  CK(put(s.z, zs, n), "sky upload"); CK(put(s.w, s.hs_w, n), "sky upload");
+  CK(put(s.e1, s.hs_e1, n), "sky upload"); CK(put(s.e2, s.hs_e2, n), "sky upload");
+  CK(put(s.phi, s.hs_phi, n), "sky upload"); CK(put(s.dc, s.hs_dc, n), "sky upload");
+  CK(put(s.da, s.hs_da, n), "sky upload"); CK(put(s.sd, sds, n), "sky upload");
+  CK(put(s.cd, cds, n), "sky upload"); CK(put(s.rar, rars, n), "sky upload");
+  CK(put(s.decr, decrs, n), "sky upload"); CK(put(s.win, wins, 6 * (size_t)n), "sky upload");
+  CK(s.jk.alloc(nn), "alloc"); CK(s.keep.alloc(nn), "alloc"); CK(s.orig.alloc(nn), "alloc");
+  if (n > 0) {
+    CK(cudaMemcpyAsync(s.jk.p, s.hs_jk.data(), 4 * n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.keep.p, s.hs_keep.data(), n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.orig.p, orig.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
+  }
+  CK(cudaStreamSynchronize(st), "sky upload");
+  s.valid = true;
+  return CPC_OK;
+}
+
+SkyView sky_view(Slot &s) {
+  SkyView v;
+  v.d.n = s.n;
+  v.d.x = s.x.p; v.d.y = s.y.p; v.d.z = s.z.p; v.d.w = s.w.p;
+  v.d.e1 = s.e1.p; v.d.e2 = s.e2.p; v.d.phi = s.phi.p;
+  v.d.jk = s.jk.p; v.d.keep = s.keep.p; v.d.orig = s.orig.p;
+  v.dc = s.dc.p; v.da = s.da.p; v.sd = s.sd.p; v.cd = s.cd.p;
+  v.rar = s.rar.p; v.decr = s.decr.p; v.win = s.win.p;
+  return v;
+}
+
+// one sky corels2 call: GPU FP64 kernel, then the host edge tier
+cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, int64_t rs,
+                     int64_t ro, cpc_accum *out) {
+  if (slot_g1 < 0 || slot_g1 >= kMaxSlots || slot_g2 < 0 || slot_g2 >= kMaxSlots)
+    return fail(c, CPC_ERR_INVALID, "slot out of range");
+  Slot &A = c->slots[slot_g1], &B = c->slots[slot_g2];
+  if (!A.valid || !B.valid || !A.sky || !B.sky) return fail(c, CPC_ERR_STATE, "count before upload");
+  if (!out || !out->num || !out->sums) return fail(c, CPC_ERR_INVALID, "null output arrays");
+  const cpc_params &p = c->p;
+  JobRule rule;
+  if (job_rule(p, kind, A.n, B.n, rule) != 0) return fail(c, CPC_ERR_INVALID, "bad pair kind");
+  const int s1 = rule.swapped ? slot_g2 : slot_g1, s2 = rule.swapped ? slot_g1 : slot_g2;
+  Slot &g1 = c->slots[s1], &g2 = c->slots[s2];
+  cpc_status st_;
+  if ((st_ = alloc_accum(c)) != CPC_OK) return st_;
+  if ((st_ = zero_accum(c, c->st)) != CPC_OK) return st_;
+  out->kernel_ms = out->pair_kernel_ms = 0;
+  if (A.n == 0 || B.n == 0) return fetch_accum(c, out, c->st, 0);  // corr.cpp:273-277
+  JobDev J;
+  std::memset(&J, 0, sizeof J);
+  J.corel = rule.corel;
+  J.gws = rule.gws;
+  J.which_corr = p.which_corr;
+  J.estimator = p.estimator;
+  J.do_jk = p.do_jk ? 1 : 0;
+  J.n_jk = p.n_jk;
+  J.coordinates = 0;
+  J.nrp = p.n_bins;
+  J.npi = p.n_p_bin;
+  J.lin_bin = p.lin_bin ? 1 : 0;
+  J.box_same_keep = 0;  // jk_check_sky (jk.cpp:53-57)
+  J.row_stride = rs > 1 ? rs : 1;
+  J.row_offset = ro;
+  J.rmin = p.bin_r_min;
+  J.rmax = p.bin_r_max;
+  J.pmin = p.p_min;
+  J.pmax = p.p_max;
+  J.ps = c->ps;
+  J.rsize = c->rsize;
+  for (int k = 0; k <= p.n_bins; k++) J.thr[k] = c->thr_rp[k];
+  J.acc_num = c->d_num.p;
+  J.acc_sums = c->d_sums.p;
+  J.counters = c->d_counters.p;
+  if ((st_ = ensure_scratch(c, 1, 1)) != CPC_OK) return st_;
+  CK(c->d_hq.alloc(kSkyHostQueue), "alloc host queue");
+  CK(c->d_hq_n.alloc(1), "alloc");
+  CK(cudaMemsetAsync(c->d_hq_n.p, 0, sizeof(unsigned long long), c->st), "memset");
+  CK(cudaMemcpyAsync(c->d_jobs.p, &J, sizeof J, cudaMemcpyHostToDevice, c->st), "H2D job");
+  // bound on |sum_gpu - sum_libm|: cos differs by <= 3 ulp (CUDA 2 + C library
+  // 1), one more ulp from each of the product and the sum, doubled
+  const double esum = 8.0 * std::ldexp(1.0, -52);
+  CK(cudaEventRecord(c->e0, c->st), "event");
+  CK(launch_sky_fp64(c->d_jobs.p, sky_view(g1), sky_view(g2), c->d_hq.p, c->d_hq_n.p,
+                     kSkyHostQueue, esum, c->st), "sky kernel");
+  c->launches += 1;
+  CK(cudaEventRecord(c->e1, c->st), "event");
+  if ((st_ = fetch_accum(c, out, c->st, 0)) != CPC_OK) return st_;
+  unsigned long long nq = 0;
+  CK(cudaMemcpy(&nq, c->d_hq_n.p, sizeof nq, cudaMemcpyDeviceToHost), "D2H");
+  if (nq > kSkyHostQueue)
+    return fail(c, CPC_ERR_RANGE, "too many pairs within the trigonometry error bound of a bin edge");
+  std::vector<int2> q(nq);
+  if (nq) CK(cudaMemcpy(q.data(), c->d_hq.p, sizeof(int2) * nq, cudaMemcpyDeviceToHost), "D2H");
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->e0, c->e1), "event time");
+  // host edge tier: the reference's own arithmetic with the C library
+  const SkyParams sp = sky_params(c);
+  const int nb = p.n_bins, npb = p.n_p_bin;
+  const size_t hstride = (size_t)nb * npb;
+  for (const int2 &e : q) {
+    const int i = e.x, j = e.y;
+    int n1, n2;
+    if (sky_bin(sp, g1.hs_ra[i], g1.hs_dec[i], g1.hs_dc[i], g1.hs_da[i], g2.hs_ra[j],
+                g2.hs_dec[j], g2.hs_dc[j], g2.hs_da[j], &n1, &n2) != 2)
+      continue;
+    const double wt = g1.hs_w[i] * g2.hs_w[j];
+    const double theta = rule.corel == COREL_DD
+                             ? 0.0 : sky_orient(g1.hs_ra[i], g1.hs_dec[i], g2.hs_ra[j], g2.hs_dec[j]);
+    double f[kNF];
+    pair_values(rule.corel, rule.gws, wt, theta, PairGal{g1.hs_e1[i], g1.hs_e2[i], g1.hs_phi[i]},
+                PairGal{g2.hs_e1[j], g2.hs_e2[j], g2.hs_phi[j]}, f);
+    const size_t cell = (size_t)n1 * npb + n2;
+    out->num[cell] += 1;
+    for (int k = 0; k < kNF; k++) out->sums[cell * kNF + k] += f[k];
+    if (!p.do_jk) continue;
+    const int r1 = g1.hs_jk[i], r2 = g2.hs_jk[j];
+    int k1 = g1.hs_keep[i], k2 = g2.hs_keep[j];
+    if (r1 == r2) k2 = 0;
+    const int rr[2] = {r1, r2}, kk[2] = {k1, k2};
+    for (int t = 0; t < 2; t++) {
+      if (!kk[t]) continue;
+      const size_t hc = (size_t)(1 + rr[t]) * hstride + cell;
+      out->num[hc] += 1;
+      out->sums[hc * kNF] += f[0];
+      if (p.which_corr == 0) continue;
+      for (int k = 1; k < kNF; k += 2) out->sums[hc * kNF + k] += f[k];
+    }
+  }
+  int64_t nbin = 0;
+  for (size_t k = 0; k < hstride; k++) nbin += out->num[k];
+  out->n_binned = nbin;
+  out->n_rechecked = (int64_t)nq;
+  out->kernel_ms = ms;
+  out->pair_kernel_ms = ms;
+  return CPC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -781,7 +1074,9 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   if (n < 0 || n >= 2147483647LL) return fail(c, CPC_ERR_INVALID, "catalogue size out of range");
   if (n > 0 && (!cat->x || !cat->y || !cat->z)) return fail(c, CPC_ERR_INVALID, "null positions");
   if (p.do_jk && n > 0 && !cat->jk) return fail(c, CPC_ERR_INVALID, "jackknife labels required (do_jk=1)");
+  if (p.coordinates == 0) return sky_upload(c, slot, cat);
   Slot &s = c->slots[slot];
+  s.sky = false;
   s.valid = false;
   s.zbuilt = false;
   s.n = n;
@@ -933,6 +1228,10 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
 cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, cpc_engine engine,
                      int64_t row_stride, int64_t row_offset, cpc_accum *out) {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
+    return fail(c, CPC_ERR_INVALID, "unknown engine");
+  // the sky has one engine: FP64 on the GPU with the host edge tier
+  if (c->p.coordinates == 0) return sky_count(c, kind, slot_g1, slot_g2, row_stride, row_offset, out);
   std::vector<JobPlan> jobs(1);
   cpc_status s = plan_job(c, kind, slot_g1, slot_g2, row_stride, row_offset, out, jobs[0]);
   if (s != CPC_OK) return s;
@@ -945,9 +1244,19 @@ cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind
                            const int *slots_g1, const int *slots_g2, cpc_accum *outs) {
   if (n_jobs <= 0 || !ctxs || !kinds || !slots_g1 || !slots_g2 || !outs)
     return fail(nullptr, CPC_ERR_INVALID, "bad batch arguments");
+  for (int k = 0; k < n_jobs; k++)
+    if (!ctxs[k]) return fail(nullptr, CPC_ERR_INVALID, "null context in batch");
+  for (int k = 0; k < n_jobs; k++)
+    if (ctxs[k]->p.coordinates == 0) {  // sky jobs: one launch each
+      for (int m = 0; m < n_jobs; m++) {
+        const cpc_status s = cpc_count(ctxs[m], kinds[m], slots_g1[m], slots_g2[m],
+                                       CPC_ENGINE_FAST, 1, 0, &outs[m]);
+        if (s != CPC_OK) return s;
+      }
+      return CPC_OK;
+    }
   std::vector<JobPlan> jobs(n_jobs);
   for (int k = 0; k < n_jobs; k++) {
-    if (!ctxs[k]) return fail(nullptr, CPC_ERR_INVALID, "null context in batch");
     if (ctxs[k]->device != ctxs[0]->device) return fail(ctxs[k], CPC_ERR_INVALID, "batch spans devices");
     cpc_status s = plan_job(ctxs[k], kinds[k], slots_g1[k], slots_g2[k], 1, 0, &outs[k], jobs[k]);
     if (s != CPC_OK) return s;

@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "pair_values.h"
+
 namespace cpc {
 
 constexpr int kNF = 13;        // wt, d1v, d1e, ..., d6v, d6e
@@ -21,6 +23,7 @@ constexpr int kMaxPi = 128;    // Pi bins supported
 constexpr int kMaxSlots = 8;
 
 enum Corel { COREL_DD = 0, COREL_SD = 1, COREL_SS = 2, COREL_SSA = 3 };
+static_assert(kNF == kPairFields, "field count");
 
 // double-precision catalogue view (recheck and plain FP64 kernel)
 struct DCat {
@@ -29,6 +32,17 @@ struct DCat {
   const int32_t *jk;
   const uint8_t *keep;
   const int64_t *orig;
+};
+
+// sky catalogue (coordinates 0) in redshift order: d.x = RA and d.y = Dec in
+// degrees, d.z = redshift, plus the per-galaxy quantities the pair loop reads
+struct SkyView {
+  DCat d;
+  const double *dc, *da;     // comoving (Pi) and transverse (r_p) distance
+  const double *sd, *cd;     // sin and cos of Dec in radians (host libm)
+  const double *rar, *decr;  // RA and Dec in radians (degrees / r2d)
+  const double *win;         // per-row windows, 6 blocks of n: z_min, z_max,
+                             // ra_min, ra_max, dec_min, dec_max (host libm)
 };
 
 // single-precision cell-list view (fast kernel)
@@ -161,66 +175,15 @@ __device__ inline int exact_classify(const JobDev &J, const DCat &g1, int64_t i,
 }
 
 // Per-pair accumulator values in double (corels.cpp:48-77, 122-244; calcs.cpp
-// 54-64, 97-105) for a binned pair.  f[0..12] as in the output layout.
+// 54-64, 97-105) for a binned pair of the box: theta from the raw, un-shifted
+// positions (angle_orient_axis_PB).  f[0..12] as in the output layout.
 __device__ inline void exact_values(const JobDev &J, const DCat &g1, int64_t i, const DCat &g2,
                                     int64_t j, double f[kNF]) {
-  for (int q = 0; q < kNF; q++) f[q] = 0.0;
   const double wt = __dmul_rn(g1.w[i], g2.w[j]);
-  f[0] = wt;
-  if (J.corel == COREL_DD) return;
-  const double theta = atan((g2.y[j] - g1.y[i]) / (g2.x[j] - g1.x[i]));
-  const double c2 = cos(2.0 * theta), s2 = sin(2.0 * theta);
-  const double kpi = 3.141592653589793;
-  auto ephi = [&](double phi) {
-    double t = fabs(phi - theta);
-    if (t > kpi / 2.0) t = kpi - t;
-    return t;
-  };
-  if (J.corel == COREL_SD) {
-    const DCat &gs = (J.gws == 2) ? g2 : g1;
-    const int64_t is = (J.gws == 2) ? j : i;
-    const double e0 = gs.e1[is], e1 = gs.e2[is];
-    const double ep = c2 * e0 - s2 * e1, ex = s2 * e0 + c2 * e1;
-    f[1] = wt * ep;
-    f[2] = f[1] * f[1];
-    f[3] = wt * ex;
-    f[4] = f[3] * f[3];
-    const double et = ephi(g1.phi[i]);
-    f[11] = et;
-    f[12] = et * et;
-    return;
-  }
-  const double ei0 = c2 * g1.e1[i] - s2 * g1.e2[i], ei1 = s2 * g1.e1[i] + c2 * g1.e2[i];
-  const double ej0 = c2 * g2.e1[j] - s2 * g2.e2[j], ej1 = s2 * g2.e1[j] + c2 * g2.e2[j];
-  if (J.corel == COREL_SS) {
-    if (J.gws == 2) {
-      f[1] = wt * ej0;
-      const double et = ephi(g2.phi[j]);
-      f[11] = et;
-      f[12] = et * et;
-    } else if (J.gws == 1) {
-      f[1] = wt * ei0;
-      const double et = ephi(g1.phi[i]);
-      f[11] = et;
-      f[12] = et * et;
-    }
-    f[2] = f[1] * f[1];
-  } else {
-    f[1] = wt * (ei0 + ej0) / 2.0;
-    f[2] = (wt * ei0 / 2.0) * (wt * ei0 / 2.0) + (wt * ej0 / 2.0) * (wt * ej0 / 2.0);
-    f[3] = wt * (ei1 + ej1) / 2.0;
-    f[4] = (wt * ei1 / 2.0) * (wt * ei1 / 2.0) + (wt * ej1 / 2.0) * (wt * ej1 / 2.0);
-    const double a = ephi(g1.phi[i]), b = ephi(g2.phi[j]);
-    f[11] = a + b;
-    f[12] = a * a + b * b;
-  }
-  f[5] = wt * (ei0 * ej0);
-  f[6] = f[5] * f[5];
-  f[7] = wt * (ei1 * ej1);
-  f[8] = f[7] * f[7];
-  f[9] = wt * (ei1 * ej0 + ei0 * ej1) / 2.0;
-  const double pa = wt * (ei1 * ej0) / 2.0, pb = wt * ei0 * ej1 / 2.0;
-  f[10] = pa * pa + pb * pb;
+  double theta = 0.0;
+  if (J.corel != COREL_DD) theta = atan((g2.y[j] - g1.y[i]) / (g2.x[j] - g1.x[i]));
+  pair_values(J.corel, J.gws, wt, theta, PairGal{g1.e1[i], g1.e2[i], g1.phi[i]},
+              PairGal{g2.e1[j], g2.e2[j], g2.phi[j]}, f);
 }
 
 // Add one binned pair (FP64 values) to the global accumulators, including the

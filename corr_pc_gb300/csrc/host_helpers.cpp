@@ -11,6 +11,10 @@
 //    found by bisection over the ordered doubles with the host libm -- the
 //    same log10 the reference calls.  Comparing a double r_p against these
 //    thresholds reproduces the reference's bin index exactly.
+//  * sky geometry: per-row windows (lim_calc_sky / lim_calc_ra_dec,
+//    sky_calcs.cpp:105-196), the exact bin of a sky pair (corel_bin with
+//    pi_calc, rp_calc_sky and dA_calc) and the pair's orientation angle, all
+//    with the C library's trigonometry in the reference's operation order.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -146,4 +150,87 @@ int32_t GlibcRand::next() {
   k_++;
   return (int32_t)(v >> 1);
 }
+}  // namespace cpc
+
+namespace cpc {
+
+static const double kR2d = 180.0 / M_PI;  // sky_calcs.cpp:10, calcs.cpp
+
+void sky_angles(double ra_deg, double dec_deg, double *ra_rad, double *dec_rad, double *sin_dec,
+                double *cos_dec) {
+  *ra_rad = ra_deg / kR2d;  // angle_deg_to_rad (calcs.cpp:19-22)
+  *dec_rad = dec_deg / kR2d;
+  *sin_dec = sin(*dec_rad);
+  *cos_dec = cos(*dec_rad);
+}
+
+// table interpolation of sky_calcs.cpp:71-81 (dAR_to_dA, p_to_dz)
+static bool table_row(const SkyParams &p, double z, int *i) {
+  const double f = floor(z / p.dz);
+  if (!(f >= 0) || f + 1 >= (double)p.n_table) return false;
+  *i = (int)f;
+  return true;
+}
+
+int sky_window(const SkyParams &p, double ra_deg, double dec_deg, double z, double win[6]) {
+  const double dec_rad = dec_deg / kR2d;
+  int i;
+  // lim_calc_sky, default case (sky_calcs.cpp:183-186)
+  double z_max = z + p.z_sep_max;
+  if (!table_row(p, z_max, &i)) return 2;
+  z_max = z + p.p_max * (p.H[i] + ((p.H[i + 1] - p.H[i]) * (z_max - p.dz * i) / p.dz)) / 300000.0;
+  if (!table_row(p, z, &i)) return 2;
+  double z_min = z + p.p_min * (p.H[i] + ((p.H[i + 1] - p.H[i]) * (z - p.dz * i) / p.dz)) / 300000.0;
+  // lim_calc_ra_dec (sky_calcs.cpp:105-145)
+  if (z_min < 0.001) z_min = 0.001;
+  if (z_min > p.z_max) return 1;
+  if (!table_row(p, z_min, &i)) return 2;
+  const double da_max =
+      p.r_max / (p.dA[i] + ((p.dA[i + 1] - p.dA[i]) * (z_min - p.dz * i) / p.dz));
+  double ra_lim = acos((pow(cos(da_max), 1) - pow(sin(dec_rad), 2)) / pow(cos(dec_rad), 2)) *
+                  1.02 * kR2d;
+  double ra_max = ra_deg + ra_lim;
+  double ra_min = ra_deg - ra_lim;
+  if (ra_max > 360) {
+    ra_min = 0;
+    ra_lim = 360;
+  }
+  if (ra_min < 0) {
+    ra_max = 360;
+    ra_lim = 360;
+  }
+  (void)ra_lim;
+  win[0] = z_min;
+  win[1] = z_max;
+  win[2] = ra_min;
+  win[3] = ra_max;
+  win[4] = dec_deg - da_max * kR2d * 1.05;
+  win[5] = dec_deg + da_max * kR2d * 1.05;
+  return 0;
+}
+
+int sky_bin(const SkyParams &p, double ra1, double dec1, double dc1, double da1, double ra2,
+            double dec2, double dc2, double da2, int *n1, int *n2) {
+  // pi_calc (calcs.cpp:126-132) then rp_calc_sky (sky_calcs.cpp:91-96)
+  const double d_P = dc2 - dc1;
+  const double d1 = dec1 / kR2d, d2 = dec2 / kR2d, a1 = ra1 / kR2d, a2 = ra2 / kR2d;
+  const double sum = sin(d1) * sin(d2) + cos(d1) * cos(d2) * cos((a1 - a2));
+  const double da = (sum > 0.9999999999) ? acos(1.0) : acos(sum);
+  const double da_R = da * (da1 + da2) / 2.;
+  // corel_bin (corels.cpp:21-46)
+  const double v2 = floor((d_P - p.p_min) / p.p_size);
+  if (!(v2 >= 0) || v2 >= p.n_p_bin) return 1;
+  double v1;
+  if (p.lin_bin) v1 = floor((da_R - p.r_min) / p.r_size);
+  else v1 = floor(log10(da_R / p.r_min) / p.r_size);
+  if (!(v1 >= 0) || v1 >= p.n_bins) return 1;
+  *n1 = (int)v1;
+  *n2 = (int)v2;
+  return 2;
+}
+
+double sky_orient(double ra1, double dec1, double ra2, double dec2) {
+  return atan((dec2 - dec1) / ((ra2 - ra1) * cos((dec1 / kR2d + dec2 / kR2d) / 2.0)));
+}
+
 }  // namespace cpc

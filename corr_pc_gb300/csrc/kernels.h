@@ -51,4 +51,12 @@ cudaError_t launch_recheck(const JobDev *jobs, const QEntry *q, const unsigned l
 // pair_fp64.cu
 cudaError_t launch_plain_fp64(const JobDev *job, const DCat &a, const DCat &b, cudaStream_t st);
 
+// pair_sky.cu
+// Sky pairs (coordinates 0) in FP64; pairs whose r_p may bin differently with
+// the C library's trigonometry are appended to hq (host edge tier).
+constexpr unsigned long long kSkyHostQueue = 1ull << 22;
+cudaError_t launch_sky_fp64(const JobDev *job, const SkyView &a, const SkyView &b, int2 *hq,
+                            unsigned long long *hq_n, unsigned long long hq_cap, double esum,
+                            cudaStream_t st);
+
 }  // namespace cpc

@@ -37,6 +37,8 @@ class Galaxies:
     jk: np.ndarray | None
     jk_prob: np.ndarray
     include_prob: np.ndarray
+    dc: np.ndarray | None = None  # sky: comoving distance (table row of z)
+    da: np.ndarray | None = None  # sky: transverse distance (table row of z)
 
     @property
     def n(self) -> int:
@@ -52,9 +54,11 @@ def reads_e(params, role: str) -> bool:
     return False
 
 
-def prepare(params, cats_in_read_order) -> dict:
+def prepare(params, cats_in_read_order, table=None) -> dict:
     """cats_in_read_order: list of (role, catalogue with x,y,z[,w,e1,e2,jk]) in the
-    order do_corr reads them (S, Rs, D, Rd; do_corr.cpp:40-96)."""
+    order do_corr reads them (S, Rs, D, Rd; do_corr.cpp:40-96).  Sky runs pass
+    the distance table: DC and DA are the table rows at floor(z/dz), without
+    interpolation (read_dat.cpp:247-251)."""
     out = {}
     pos = 0
     for role, c in cats_in_read_order:
@@ -81,11 +85,16 @@ def prepare(params, cats_in_read_order) -> dict:
         w = getattr(c, "w", None)
         w = np.ones(n) if w is None else np.ascontiguousarray(w, dtype=np.float64)
         jk = getattr(c, "jk", None) if params.do_jk else None
+        dc = da = None
+        if not params.periodic_box and table is not None:
+            it = np.floor(np.asarray(c.z, dtype=np.float64) / params.dz).astype(np.int64)
+            dc = np.ascontiguousarray(table.DC[it])
+            da = np.ascontiguousarray((table.transverse if params.use_comoving else table.DA)[it])
         out[role] = Galaxies(np.ascontiguousarray(c.x, dtype=np.float64),
                              np.ascontiguousarray(c.y, dtype=np.float64),
                              np.ascontiguousarray(c.z, dtype=np.float64), w, e1, e2, phi,
                              None if jk is None else np.ascontiguousarray(jk, dtype=np.int32),
-                             jkp, inc)
+                             jkp, inc, dc, da)
     return out
 
 

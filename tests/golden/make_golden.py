@@ -165,6 +165,28 @@ def sky_cases():
         c.x, c.y, c.z, c.w, c.e1, c.e2, c.jk = c2.x, c2.y, c2.z, c2.w, c2.e1, c2.e2, c2.jk
     out.append(("sky_wgg_distinct_wrap", synth.SkyWorkload("sky_wgg_distinct_wrap", p, t, s, dd,
                                                            rs, rd), False))
+
+    # twins at almost exactly the clamp angle of dA_calc (sum = 0.9999999999,
+    # theta ~ 1.41421e-5 rad): the pairs whose count depends on the last bits of
+    # cos and acos, binned by the host edge tier
+    p = synth._sky_params(which_corr=0, rmin=0.005, rmax=30.0, nrp=12, npi=8, pmax=40.0,
+                          njk=4, z_max=0.5)
+    p.dz = 0.001
+    t = synth.flat_lcdm_table(p.z_max, p.dz)
+    base = synth.sky_patch(700, 38, t, ra_deg=4, dec_deg=4, chi_range=(600, 900), nside_jk=2)
+    rng = np.random.default_rng(39)
+    th = np.sqrt(2e-10) * (1.0 + rng.uniform(-3e-5, 3e-5, base.n))
+    ang = rng.uniform(0, 2 * np.pi, base.n)
+    th_deg = np.degrees(th)
+    tw = synth.Catalog(base.x + th_deg * np.cos(ang) / np.cos(np.radians(base.y)),
+                       base.y + th_deg * np.sin(ang), base.z.copy(), None, None, None,
+                       base.jk.copy())
+    both = synth.Catalog(np.concatenate([base.x, tw.x]), np.concatenate([base.y, tw.y]),
+                         np.concatenate([base.z, tw.z]), None, None, None,
+                         np.concatenate([base.jk, tw.jk])).sorted_by_z()
+    r = synth.sky_patch(1500, 40, t, ra_deg=4, dec_deg=4, chi_range=(600, 900), nside_jk=2)
+    out.append(("sky_twins_clamp", synth.SkyWorkload("sky_twins_clamp", p, t, both, both, r, r),
+                True))
     return out
 
 
