@@ -85,6 +85,7 @@ struct Slot {
   // redshift-ordered catalogue; these the sky-only per-galaxy quantities
   bool sky = false;
   DevBuf<double> dc, da, sd, cd, rar, decr, win;
+  DevBuf<float4> sky_su, sky_sw;  // float unit vector + D_A; float RA, Dec, z, D_C
   // host copies in the same order for the host edge tier
   std::vector<double> hs_ra, hs_dec, hs_dc, hs_da, hs_w, hs_e1, hs_e2, hs_phi;
   std::vector<int32_t> hs_jk;
@@ -858,8 +859,18 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   CK(put(s.da, s.hs_da, n), "sky upload"); CK(put(s.sd, sds, n), "sky upload");
   CK(put(s.cd, cds, n), "sky upload"); CK(put(s.rar, rars, n), "sky upload");
   CK(put(s.decr, decrs, n), "sky upload"); CK(put(s.win, wins, 6 * (size_t)n), "sky upload");
+  // float views for the fast kernel's prefilters
+  std::vector<float4> su(n), sw(n);
+  for (int64_t k = 0; k < n; k++) {
+    const double ca = std::cos(rars[k]), sa = std::sin(rars[k]);
+    su[k] = make_float4((float)(cds[k] * ca), (float)(cds[k] * sa), (float)sds[k], (float)s.hs_da[k]);
+    sw[k] = make_float4((float)s.hs_ra[k], (float)s.hs_dec[k], (float)zs[k], (float)s.hs_dc[k]);
+  }
+  CK(s.sky_su.alloc(nn), "alloc"); CK(s.sky_sw.alloc(nn), "alloc");
   CK(s.jk.alloc(nn), "alloc"); CK(s.keep.alloc(nn), "alloc"); CK(s.orig.alloc(nn), "alloc");
   if (n > 0) {
+    CK(cudaMemcpyAsync(s.sky_su.p, su.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.sky_sw.p, sw.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st), "H2D");
     CK(cudaMemcpyAsync(s.jk.p, s.hs_jk.data(), 4 * n, cudaMemcpyHostToDevice, st), "H2D");
     CK(cudaMemcpyAsync(s.keep.p, s.hs_keep.data(), n, cudaMemcpyHostToDevice, st), "H2D");
     CK(cudaMemcpyAsync(s.orig.p, orig.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
@@ -882,7 +893,7 @@ SkyView sky_view(Slot &s) {
 
 // one sky corels2 call: GPU FP64 kernel, then the host edge tier
 cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, int64_t rs,
-                     int64_t ro, cpc_accum *out) {
+                     int64_t ro, cpc_engine engine, cpc_accum *out) {
   if (slot_g1 < 0 || slot_g1 >= kMaxSlots || slot_g2 < 0 || slot_g2 >= kMaxSlots)
     return fail(c, CPC_ERR_INVALID, "slot out of range");
   Slot &A = c->slots[slot_g1], &B = c->slots[slot_g2];
@@ -931,9 +942,19 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
   // bound on |sum_gpu - sum_libm|: cos differs by <= 3 ulp (CUDA 2 + C library
   // 1), one more ulp from each of the product and the sum, doubled
   const double esum = 8.0 * std::ldexp(1.0, -52);
+  CK(cudaMemsetAsync(c->d_unit_ctr.p, 0, sizeof(unsigned int), c->st), "memset");
   CK(cudaEventRecord(c->e0, c->st), "event");
-  CK(launch_sky_fp64(c->d_jobs.p, sky_view(g1), sky_view(g2), c->d_hq.p, c->d_hq_n.p,
-                     kSkyHostQueue, esum, c->st), "sky kernel");
+  if (engine == CPC_ENGINE_FP64) {
+    CK(launch_sky_fp64(c->d_jobs.p, sky_view(g1), sky_view(g2), c->d_hq.p, c->d_hq_n.p,
+                       kSkyHostQueue, esum, c->st), "sky kernel");
+  } else {
+    const SkyFast fa{g1.sky_su.p, g1.sky_sw.p}, fb{g2.sky_su.p, g2.sky_sw.p};
+    const float rp_lo_f = f_down(c->thr_rp[0]), rp_hi_f = f_up(c->thr_rp[p.n_bins]);
+    CK(launch_sky_warp(c->d_jobs.p, sky_view(g1), sky_view(g2), fa, fb, c->d_unit_ctr.p,
+                       c->d_hq.p, c->d_hq_n.p, kSkyHostQueue, esum, rp_lo_f, rp_hi_f,
+                       c->thr_rp[0] <= 0.0 ? 1 : 0, p.n_bins, p.n_p_bin, c->sm_count, c->st),
+       "sky kernel");
+  }
   c->launches += 1;
   CK(cudaEventRecord(c->e1, c->st), "event");
   if ((st_ = fetch_accum(c, out, c->st, 0)) != CPC_OK) return st_;
@@ -1230,8 +1251,10 @@ cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, c
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
   if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
     return fail(c, CPC_ERR_INVALID, "unknown engine");
-  // the sky has one engine: FP64 on the GPU with the host edge tier
-  if (c->p.coordinates == 0) return sky_count(c, kind, slot_g1, slot_g2, row_stride, row_offset, out);
+  // sky: FP32-prefiltered warp kernel (fast) or plain FP64 kernel, both with
+  // the FP64 path and the host edge tier for the pairs that can bin
+  if (c->p.coordinates == 0)
+    return sky_count(c, kind, slot_g1, slot_g2, row_stride, row_offset, engine, out);
   std::vector<JobPlan> jobs(1);
   cpc_status s = plan_job(c, kind, slot_g1, slot_g2, row_stride, row_offset, out, jobs[0]);
   if (s != CPC_OK) return s;

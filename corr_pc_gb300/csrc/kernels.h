@@ -55,6 +55,15 @@ cudaError_t launch_plain_fp64(const JobDev *job, const DCat &a, const DCat &b, c
 // Sky pairs (coordinates 0) in FP64; pairs whose r_p may bin differently with
 // the C library's trigonometry are appended to hq (host edge tier).
 constexpr unsigned long long kSkyHostQueue = 1ull << 22;
+struct SkyFast {
+  const float4 *su;  // unit vector (cos d cos a, cos d sin a, sin d) and transverse distance
+  const float4 *sw;  // RA, Dec, redshift, comoving distance
+};
+cudaError_t launch_sky_warp(const JobDev *job, const SkyView &a, const SkyView &b,
+                            const SkyFast &fa, const SkyFast &fb, unsigned int *row_ctr, int2 *hq,
+                            unsigned long long *hq_n, unsigned long long hq_cap, double esum,
+                            float rp_lo_f, float rp_hi_f, int zero_bin, int nrp, int npi,
+                            int sm_count, cudaStream_t st);
 cudaError_t launch_sky_fp64(const JobDev *job, const SkyView &a, const SkyView &b, int2 *hq,
                             unsigned long long *hq_n, unsigned long long hq_cap, double esum,
                             cudaStream_t st);

@@ -20,8 +20,24 @@
 // queue and binned there with the C library.  All other pairs are binned here
 // against the exact host-derived thresholds, so the integer counts equal the
 // reference's.  Shape sums use CUDA's atan/cos/sin (within 1e-6).
+//
+// Two kernels:
+//  * sky_fp64_kernel -- the plain FP64 kernel: one thread per g1 row, every
+//    window pair through the FP64 path, global atomics (CPC_ENGINE_FP64).
+//  * sky_warp_kernel -- the fast kernel (CPC_ENGINE_FAST): one warp per g1 row
+//    (dynamic row queue), lanes take consecutive candidates of the row's
+//    redshift range (coalesced float4 loads); FP32 definite-in/definite-out
+//    window tests (ambiguous ones re-tested in double); FP32 prefilters that
+//    reject pairs certainly outside the Pi range or certainly outside
+//    [thr_0, thr_nrp) in r_p (the chord |u1 - u2| of float unit vectors with a
+//    rigorous error bound); survivors are compacted into a per-warp queue and
+//    run through the FP64 path 32 at a time with every lane busy; the main
+//    histogram lives in shared memory (FP64 atomics) and is flushed once per
+//    block.
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <algorithm>
 
 #include "cpc_device.cuh"
 #include "kernels.h"
@@ -106,6 +122,259 @@ sky_fp64_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, int2 *hq,
     exact_accumulate(J, a.d, i, b.d, j, k - 1, (int)v2, f);
   }
   if (nwin) atomicAdd(&J.counters[1], nwin);
+}
+
+// ---------------------------------------------------------------------------
+// fast kernel
+// ---------------------------------------------------------------------------
+
+constexpr int kSkyThreads = 256;
+constexpr int kSkyWarps = kSkyThreads / 32;
+constexpr int kSkyQ = 64;
+
+struct SkyRow {
+  int64_t i;
+  double ra, dec, dc, da, sd, cd, rar, decr, w, e1, e2, phi;
+  int jk, keep;
+};
+
+// FP64 path of one window pair whose Pi and r_p may fall in the bins: exact
+// Pi bin, great-circle r_p, ambiguity test, values and accumulation.
+template <bool SMEM>
+__device__ __forceinline__ void sky_pair_fp64(const JobDev &J, const SkyRow &r, const SkyView &b,
+                                              int64_t j, unsigned long long *s_num,
+                                              double *s_sums, int2 *hq,
+                                              unsigned long long *hq_n,
+                                              unsigned long long hq_cap, double esum) {
+  const double dP = __dsub_rn(b.dc[j], r.dc);
+  const double v2 = floor(__ddiv_rn(__dsub_rn(dP, J.pmin), J.ps));
+  if (!(v2 >= 0.0) || v2 >= (double)J.npi) return;
+  const double cdel = cos(__dsub_rn(r.rar, b.rar[j]));
+  const double sum = __dadd_rn(__dmul_rn(r.sd, b.sd[j]), __dmul_rn(__dmul_rn(r.cd, b.cd[j]), cdel));
+  const double kClamp = 0.9999999999;
+  const double kEps = 2.220446049250313e-16;
+  bool amb = fabs(sum - kClamp) <= esum;
+  double daR = 0.0, tol = 0.0;
+  if (!(sum > kClamp)) {
+    const double th = acos(sum);
+    daR = __ddiv_rn(__dmul_rn(th, __dadd_rn(r.da, b.da[j])), 2.0);
+    const double rel = esum / fmax(sin(th) * th, 1e-300) + 8.0 * kEps;
+    tol = 2.0 * daR * rel;
+  }
+  const int k = thr_count(J, daR);
+  if (!amb && tol > 0.0) amb = thr_count(J, daR - tol) != k || thr_count(J, daR + tol) != k;
+  if (amb) {
+    const unsigned long long q = atomicAdd(hq_n, 1ull);
+    if (q < hq_cap) hq[q] = make_int2((int)r.i, (int)j);
+    return;
+  }
+  if (k < 1 || k > J.nrp) return;
+  const double wt = __dmul_rn(r.w, b.d.w[j]);
+  double theta = 0.0;
+  if (J.corel != COREL_DD)
+    theta = atan((b.d.y[j] - r.dec) / ((b.d.x[j] - r.ra) * cos((r.decr + b.decr[j]) / 2.0)));
+  double f[kNF];
+  pair_values(J.corel, J.gws, wt, theta, PairGal{r.e1, r.e2, r.phi},
+              PairGal{b.d.e1[j], b.d.e2[j], b.d.phi[j]}, f);
+  const int64_t cell = (int64_t)(k - 1) * J.npi + (int)v2;
+  const int nf = J.corel == COREL_DD ? 1 : kNF;
+  if (SMEM) {
+    atomicAdd(&s_num[cell], 1ull);
+    for (int q = 0; q < nf; q++)
+      if (f[q] != 0.0) atomicAdd(&s_sums[cell * kNF + q], f[q]);
+  } else {
+    atomicAdd(&J.acc_num[cell], 1ull);
+    for (int q = 0; q < nf; q++)
+      if (f[q] != 0.0) atomicAdd(&J.acc_sums[cell * kNF + q], f[q]);
+  }
+  if (!J.do_jk) return;
+  // jk_check_sky (jk.cpp:53-57) then corel_jk1 (jk.cpp:138-171)
+  const int r2 = b.d.jk[j];
+  const int k1 = r.keep, k2 = (r2 == r.jk) ? 0 : b.d.keep[j];
+  const int64_t hstride = (int64_t)J.nrp * J.npi;
+  const int rs[2] = {r.jk, r2};
+  const int ks[2] = {k1, k2};
+  for (int t = 0; t < 2; t++) {
+    if (!ks[t]) continue;
+    const int64_t hc = (int64_t)(1 + rs[t]) * hstride + cell;
+    atomicAdd(&J.acc_num[hc], 1ull);
+    double *sj = J.acc_sums + hc * kNF;
+    if (f[0] != 0.0) atomicAdd(&sj[0], f[0]);
+    if (J.which_corr == 0) continue;
+    for (int q = 1; q < kNF; q += 2)
+      if (f[q] != 0.0) atomicAdd(&sj[q], f[q]);
+  }
+}
+
+// window membership of x in [lo, hi] from the float value: 1 in, 0 out,
+// -1 undecided (x within a float ulp of a bound, or a NaN bound)
+__device__ __forceinline__ int fwin(float x, float lo_ru, float hi_rd, float lo_rd, float hi_ru) {
+  if (x > lo_ru && x < hi_rd) return 1;
+  if (x < lo_rd || x > hi_ru) return 0;
+  return -1;
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(kSkyThreads, 2)
+sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast fa, SkyFast fb,
+                unsigned int *row_ctr, int2 *hq, unsigned long long *hq_n,
+                unsigned long long hq_cap, double esum, float rp_lo_f, float rp_hi_f,
+                int zero_bin) {
+  extern __shared__ __align__(16) unsigned char sky_smem[];
+  __shared__ int s_q[kSkyWarps][kSkyQ];
+  const JobDev &J = *jobp;
+  const int ncell = J.nrp * J.npi;
+  unsigned long long *s_num = reinterpret_cast<unsigned long long *>(sky_smem);
+  double *s_sums = reinterpret_cast<double *>(s_num + ncell);
+  if (SMEM) {
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) s_num[c] = 0ull;
+    for (int c = threadIdx.x; c < ncell * kNF; c += blockDim.x) s_sums[c] = 0.0;
+    __syncthreads();
+  }
+  const unsigned FULL = 0xffffffffu;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int *q = s_q[warp];
+  const int64_t n1 = a.d.n, n2 = b.d.n;
+  const float pmin_f = (float)J.pmin, pmax_f = (float)J.pmax;
+  unsigned long long nwin = 0;
+  for (;;) {
+    int64_t i = 0;
+    if (lane == 0) i = atomicAdd(row_ctr, 1u);
+    i = __shfl_sync(FULL, i, 0);
+    if (i >= n1) break;
+    if (J.row_stride > 1 && ((a.d.orig[i] - J.row_offset) % J.row_stride) != 0) continue;
+    SkyRow r;
+    r.i = i;
+    r.ra = a.d.x[i]; r.dec = a.d.y[i]; r.dc = a.dc[i]; r.da = a.da[i];
+    r.sd = a.sd[i]; r.cd = a.cd[i]; r.rar = a.rar[i]; r.decr = a.decr[i];
+    r.w = a.d.w[i]; r.e1 = a.d.e1[i]; r.e2 = a.d.e2[i]; r.phi = a.d.phi[i];
+    r.jk = a.d.jk[i]; r.keep = a.d.keep[i];
+    const double z_min = a.win[i], z_max = a.win[n1 + i];
+    const double ra_min = a.win[2 * n1 + i], ra_max = a.win[3 * n1 + i];
+    const double dec_min = a.win[4 * n1 + i], dec_max = a.win[5 * n1 + i];
+    const float ra_lru = __double2float_ru(ra_min), ra_hrd = __double2float_rd(ra_max);
+    const float ra_lrd = __double2float_rd(ra_min), ra_hru = __double2float_ru(ra_max);
+    const float de_lru = __double2float_ru(dec_min), de_hrd = __double2float_rd(dec_max);
+    const float de_lrd = __double2float_rd(dec_min), de_hru = __double2float_ru(dec_max);
+    const float4 u1 = fa.su[i];
+    const float dc1f = fa.sw[i].w;
+    // redshift range [lo, hi): z_min <= z <= z_max
+    int64_t lo = 0, hi = n2;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (b.d.z[mid] < z_min) lo = mid + 1; else hi = mid;
+    }
+    int64_t end = n2, l2 = lo;
+    while (l2 < end) {
+      const int64_t mid = (l2 + end) >> 1;
+      if (b.d.z[mid] > z_max) end = mid; else l2 = mid + 1;
+    }
+    int count = 0;
+    for (int64_t base = lo; base < end; base += 32) {
+      const int64_t j = base + lane;
+      bool need = false;
+      if (j < end) {
+        const float4 w2 = fb.sw[j];
+        int in = fwin(w2.y, de_lru, de_hrd, de_lrd, de_hru);
+        if (in < 0) {
+          const double d2 = b.d.y[j];
+          in = !(d2 > dec_max || d2 < dec_min);
+        }
+        if (in) {
+          int ir = fwin(w2.x, ra_lru, ra_hrd, ra_lrd, ra_hru);
+          if (ir < 0) {
+            const double a2 = b.d.x[j];
+            ir = !(a2 < ra_min || a2 > ra_max);
+          }
+          in = ir;
+        }
+        if (in) {
+          nwin++;
+          // Pi certainly outside [p_min, p_max): float dc carry <= 1 ulp each
+          const float pf = w2.w - dc1f;
+          const float pe = 4.0f * 5.96e-8f * (fabsf(w2.w) + fabsf(dc1f)) + 1e-30f;
+          const bool pi_out = (pf < pmin_f - pe) || (pf > pmax_f + pe);
+          if (!pi_out) {
+            // r_p bounds from the chord of float unit vectors
+            const float4 u2 = fb.su[j];
+            const float dx = u1.x - u2.x, dy = u1.y - u2.y, dz = u1.z - u2.z;
+            const float c2 = dx * dx + dy * dy + dz * dz;
+            const float ch = sqrtf(c2);
+            const float dsum = 0.5f * (u1.w + u2.w);
+            const float ch_lo = fmaxf(ch * (1.0f - 1e-6f) - 4e-7f, 0.0f);
+            const float ch_hi = ch * (1.0f + 1e-6f) + 4e-7f;
+            const float rlo = ch_lo * dsum * (1.0f - 1e-6f);
+            const float rhi = ch_hi * (1.0f + ch_hi * ch_hi * (1.0f / 6.0f)) * dsum * (1.0f + 1e-6f);
+            // a clamped pair (theta < 1.41421e-5, r_p = 0) can bin when
+            // thr_0 <= 0: never reject it as "above the range" then
+            const bool above = rlo >= rp_hi_f && (!zero_bin || ch_lo > 1.5e-5f);
+            need = !(above || rhi < rp_lo_f);
+          }
+        }
+      }
+      const unsigned m = __ballot_sync(FULL, need);
+      if (need) q[count + __popc(m & ((1u << lane) - 1u))] = (int)j;
+      count += __popc(m);
+      __syncwarp();
+      if (count >= 32) {
+        sky_pair_fp64<SMEM>(J, r, b, q[lane], s_num, s_sums, hq, hq_n, hq_cap, esum);
+        __syncwarp();
+        if (lane < count - 32) q[lane] = q[lane + 32];
+        count -= 32;
+        __syncwarp();
+      }
+    }
+    if (lane < count) sky_pair_fp64<SMEM>(J, r, b, q[lane], s_num, s_sums, hq, hq_n, hq_cap, esum);
+    __syncwarp();
+  }
+  if (nwin) atomicAdd(&J.counters[1], nwin);
+  if (SMEM) {
+    __syncthreads();
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+      const unsigned long long v = s_num[c];
+      if (!v) continue;
+      atomicAdd(&J.acc_num[c], v);
+      for (int f = 0; f < kNF; f++) {
+        const double x = s_sums[c * kNF + f];
+        if (x != 0.0) atomicAdd(&J.acc_sums[c * kNF + f], x);
+      }
+    }
+  }
+}
+
+size_t sky_warp_smem_bytes(int nrp, int npi) {
+  return (size_t)nrp * npi * (sizeof(unsigned long long) + kNF * sizeof(double));
+}
+
+cudaError_t launch_sky_warp(const JobDev *job, const SkyView &a, const SkyView &b,
+                            const SkyFast &fa, const SkyFast &fb, unsigned int *row_ctr, int2 *hq,
+                            unsigned long long *hq_n, unsigned long long hq_cap, double esum,
+                            float rp_lo_f, float rp_hi_f, int zero_bin, int nrp, int npi,
+                            int sm_count, cudaStream_t st) {
+  if (a.d.n == 0 || b.d.n == 0) return cudaSuccess;
+  const size_t smem = sky_warp_smem_bytes(nrp, npi);
+  const bool use_smem = smem <= 100 * 1024;
+  int bps = 0;
+  cudaError_t e;
+  if (use_smem) {
+    e = cudaFuncSetAttribute(sky_warp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sky_warp_kernel<true>, kSkyThreads, smem);
+  } else {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sky_warp_kernel<false>, kSkyThreads, 0);
+  }
+  if (e != cudaSuccess) return e;
+  if (bps < 1) bps = 1;
+  const int64_t rows_blocks = (a.d.n + kSkyWarps - 1) / kSkyWarps;
+  const int grid = (int)std::min<int64_t>((int64_t)sm_count * bps, rows_blocks);
+  if (use_smem)
+    sky_warp_kernel<true><<<grid, kSkyThreads, smem, st>>>(job, a, b, fa, fb, row_ctr, hq, hq_n,
+                                                           hq_cap, esum, rp_lo_f, rp_hi_f, zero_bin);
+  else
+    sky_warp_kernel<false><<<grid, kSkyThreads, 0, st>>>(job, a, b, fa, fb, row_ctr, hq, hq_n,
+                                                         hq_cap, esum, rp_lo_f, rp_hi_f, zero_bin);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_sky_fp64(const JobDev *job, const SkyView &a, const SkyView &b, int2 *hq,
