@@ -4,7 +4,8 @@
 Default workload: the 200,000-galaxy Neyman-Scott periodic box with shapes
 (wg+ and wgg, 64 jackknife cubes, 20 log r_p x 40 Pi bins) -- the workload the
 headline metric "binned pairs/s (wgg+wg+ w/ jackknife)" is quoted on.  Other
-workloads: --workload box_uniform_wgg_20k | box_ns_wpp_20M | box_batch_wpp_64.
+workloads: --workload box_uniform_wgg_20k | box_ns_wpp_20M | box_batch_wpp_64 |
+sky_wgp_500k_5M | sky_wgp_50k_500k (sky survey: SRd, RsRd, SD, DRs on a row sample).
 
 One step = one corels2 call (the SD pair type these runs use) over the whole
 catalogue.  `value` times the device work with the catalogues resident in HBM
@@ -203,6 +204,185 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# sky survey workload (coordinates 0): terms SRd, RsRd, SD, DRs
+# ---------------------------------------------------------------------------
+
+SKY_TERMS = (("SRd", "Rd", "S"), ("RsRd", "Rd", "Rs"), ("SD", "D", "S"), ("DRs", "Rs", "D"))
+SKY_SLOTS = {"S": 0, "Rs": 1, "D": 2, "Rd": 3}
+
+
+def _sky_setup(name):
+    from corr_pc_gb300 import host, synth
+    sizes = {"sky_wgp_500k_5M": (500000, 5000000), "sky_wgp_50k_500k": (50000, 500000)}
+    if name not in sizes:
+        raise SystemExit(f"unknown workload {name}")
+    wl = synth.sky_wgp(*sizes[name])
+    wl.name = name
+    order = [("S", wl.shape), ("Rs", wl.shape_rand), ("D", wl.density), ("Rd", wl.density_rand)]
+    cats = host.prepare(wl.params, order, table=wl.table)
+    return wl, order, cats
+
+
+def _sky_describe(wl, rows):
+    p = wl.params
+    return {"workload": wl.name, "which_corr": p.which_corr, "n_jk": p.n_jk_regions,
+            "rp_bins": p.n_bins, "pi_bins": p.n_p_bin, "rp_range": [p.bin_r_min, p.bin_r_max],
+            "pi_range": [p.p_min, p.p_max], "n_data": wl.shape.n, "n_randoms": wl.shape_rand.n,
+            "patch_deg": [10, 10], "chi_range": [500, 1500],
+            "pair_types": [t for t, _, _ in SKY_TERMS],
+            "row_sample": f"about {rows} outer rows per pair type per step (row stride, offset "
+                          "changes every step)",
+            "l2": "inputs larger than L2 (about 1.2 GB per random catalogue); L2 flushed "
+                  "between steps"}
+
+
+def _sky_strides(cats, rows):
+    out = []
+    for t, a, b in SKY_TERMS:
+        n1 = max(cats[a].n, cats[b].n)
+        out.append(max(1, n1 // rows))
+    return out
+
+
+def _sky_oracle_sample(wl, cats, budget_s, rows_hint, threads, offset=0):
+    """The oracle restatement of corels2 on a row sample of every sky term."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the CPU baseline (test infrastructure)
+    from corr_pc_gb300 import synth
+    p = wl.params
+    ocats = oracle.read_like_reference(p, [(r, c) for r, c in
+                                           (("S", wl.shape), ("Rs", wl.shape_rand),
+                                            ("D", wl.density), ("Rd", wl.density_rand))],
+                                       table=wl.table)
+    zsep = synth.derived_z_sep(p, wl.table)[0]
+    strides = _sky_strides(cats, rows_hint)
+    tot, dt = 0, 0.0
+    for (t, a, b), st in zip(SKY_TERMS, strides):
+        t0 = time.perf_counter()
+        _, _, _, nin = oracle.port_corels2(p, t, ocats[a], ocats[b], n_threads=threads,
+                                           row_stride=st, row_offset=offset % st,
+                                           H_z=wl.table.H, dA_z=wl.table.transverse,
+                                           z_sep_max=zsep)
+        dt += time.perf_counter() - t0
+        tot += nin
+        if dt > budget_s:
+            break
+    return tot, dt, strides
+
+
+def run_sky(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl, order, cats = _sky_setup(args.workload)
+    threads = os.cpu_count() or 1
+    if args.impl == "reference":
+        tot_pairs, tot_t = 0, 0.0
+        rows = args.sky_cpu_rows
+        for s in range(args.warmup + args.steps):
+            n, dt, _ = _sky_oracle_sample(wl, cats, 1e9, rows, threads, offset=s)
+            if s >= args.warmup:
+                tot_pairs += n
+                tot_t += dt
+        v = tot_pairs / tot_t
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded, in memory)", "config": _sky_describe(wl, rows),
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"about {rows} outer rows per pair type per step"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from corr_pc_gb300 import build as b
+    b.build()
+    from corr_pc_gb300 import _lib, metrics
+    p = wl.params
+    ctx = _lib.Context(p, table=wl.table)
+    for r, c in cats.items():
+        ctx.upload(SKY_SLOTS[r], c)
+    rows = args.sky_rows
+    strides = _sky_strides(cats, rows)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def step(k, engine="fast", mult=1):
+        nb = nw = 0
+        ms = 0.0
+        for (t, a, bb), st in zip(SKY_TERMS, strides):
+            st = st * mult
+            r = ctx.count(t, SKY_SLOTS[a], SKY_SLOTS[bb], engine=engine, row_stride=st,
+                          row_offset=k % st)
+            nb += r["n_binned"]
+            nw += r["n_window"]
+            ms += r["kernel_ms"]
+        return nb, nw, ms
+
+    for k in range(args.warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step(k)
+    l0 = ctx.launches()
+    n_bin = n_win = 0
+    tot_ms = 0.0
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            nb, nw, ms = step(args.warmup + k)
+            n_bin += nb
+            n_win += nw
+            tot_ms += ms
+    launches = ctx.launches() - l0
+    value = n_bin / (tot_ms * 1e-3)
+    # end to end: the four uploads (host windows, device sort) + one step
+    h2d = sum(8 * 9 * c.n + 4 * c.n + c.n for c in cats.values())
+    t0 = time.perf_counter()
+    for r, c in cats.items():
+        ctx.upload(SKY_SLOTS[r], c)
+    nb_e, _, _ = step(0)
+    e2e_t = time.perf_counter() - t0
+    nh, nbins, npb = ctx.shape
+    d2h = 4 * nh * nbins * npb * (8 + 8 * _lib.NF)
+    # plain FP64 sky kernel on an 8x sparser row sample
+    nb64, _, ms64 = step(0, engine="fp64", mult=8)
+    fp64 = {"value": nb64 / (ms64 * 1e-3), "unit": UNIT,
+            "sample": f"8x sparser row sample: {nb64} binned pairs in {ms64:.1f} ms"}
+    fp64["speedup_of_fast"] = value / fp64["value"]
+    cpu = None
+    if not args.no_cpu:
+        n, dt, _ = _sky_oracle_sample(wl, cats, args.cpu_budget, args.sky_cpu_rows, threads)
+        cpu = {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"about {args.sky_cpu_rows} outer rows per pair type: {n} binned "
+                         f"pairs in {dt:.2f} s"}
+    peaks = _peaks()
+    F = metrics.FLOPS_PER_PAIR[p.which_corr]
+    A = metrics.smem_updates_per_pair(p.which_corr, bool(p.do_jk))
+    achieved_flops = F * value
+    roofline = {"bound": "fp32", "achieved": achieved_flops / 1e12,
+                "peak": (peaks["ffma_flops"] or float("nan")) / 1e12, "unit": "TFLOP/s",
+                "frac": achieved_flops / peaks["ffma_flops"] if peaks["ffma_flops"] else None,
+                "traffic": None, "kernel": "sky_warp_kernel",
+                "kernel_ms_per_launch": tot_ms / (args.steps * len(SKY_TERMS)),
+                "work_per_pair": {"fp32_flops": F, "smem_atomic_updates": A},
+                "peak_source": "measured live in this run (FFMA microbenchmark)"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded generator, in memory)", "config": _sky_describe(wl, rows),
+            "n_binned_per_step": n_bin / args.steps, "n_window_per_step": n_win / args.steps,
+            "roofline": roofline, "cpu_baseline": cpu, "fp64_gpu": fp64,
+            "e2e": {"value": nb_e / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_t},
+            "gpu_launches": launches, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -214,7 +394,14 @@ def main() -> None:
     ap.add_argument("--ref-budget", type=float, default=8.0, help="seconds per reference step")
     ap.add_argument("--fp64-budget", type=float, default=3.0, help="seconds of FP64 kernel")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--sky-rows", type=int, default=20000,
+                    help="outer rows per pair type per step (sky workloads)")
+    ap.add_argument("--sky-cpu-rows", type=int, default=400,
+                    help="outer rows per pair type for the CPU baseline (sky workloads)")
     args = ap.parse_args()
+    if args.workload.startswith("sky"):
+        run_sky(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

@@ -4,7 +4,8 @@
 // reference's corr_pc (main.cpp:27-82).  The sequence follows do_corr for a
 // cross-correlation run (do_corr.cpp:24-161): read S, Rs, D, Rd in that order
 // (which fixes the glibc rand() jackknife draws), one GPU corels2 per pair
-// type, then the finalisation and output files.
+// type (SRd, RsRd, SD, DRs; SD alone in a periodic box), then the finalisation
+// and output files.
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -63,9 +64,15 @@ int main(int argc, char **argv) {
     return 1;
   }
   outp_data_info(d, d.out_file + "inp.info");
-  if (d.coordinates != 6 || d.estimator != 0 || d.which_corr > 2 || d.sig_crit) {
+  if ((d.coordinates != 6 && d.coordinates != 0) || d.estimator != 0 || d.which_corr > 2 ||
+      d.sig_crit) {
     std::cout << "this build runs cross correlations (estimator 0) of wgg/wg+/w++ in x,y,z "
-                 "coordinates (coordinates 6)" << std::endl;
+                 "(coordinates 6) or on the sky (coordinates 0)" << std::endl;
+    return 1;
+  }
+  if (d.RsRd_same && !d.periodic_box) {
+    std::cout << "without a periodic box this build needs separate density randoms "
+                 "(n_Drand > 0)" << std::endl;
     return 1;
   }
   Ctx ctx;

@@ -41,6 +41,8 @@ struct Info {
   double S_wt[2] = {0, 0}, D_wt[2] = {0, 0}, Rs_wt[2] = {0, 0}, Rd_wt[2] = {0, 0};
   double SD_wt[2] = {0, 0}, SRd_wt[2] = {0, 0}, DRs_wt[2] = {0, 0}, RsRd_wt[2] = {0, 0};
   double SS_wt = 0, SRs_wt = 0, RsRs_wt[2] = {0, 0}, DD_wt = 0;
+  // distance table (da_Z, initialization.cpp:23-60), read when not periodic
+  std::vector<double> H_z, dA_z, dC_z;
 };
 
 // 0 ok, nonzero: message in err
@@ -53,6 +55,7 @@ cpc_params to_params(const Info &d);
 struct Catalog {
   int64_t n = 0;
   std::vector<double> x, y, z, w, e1, e2, phi, jk_prob, include_prob;
+  std::vector<double> dc, da;  // table rows at floor(z/dz) (not periodic)
   std::vector<int32_t> jk;
   bool has_e = false;
   cpc_catalog view() const;

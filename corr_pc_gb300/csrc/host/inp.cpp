@@ -2,6 +2,7 @@
 // whitespace-separated "key value" pairs whose keys are ignored; the order is
 // the contract (the Gen_inp notebooks write exactly this order).  Plus the
 // settings data_ini derives from it for the paths this library implements.
+#include <algorithm>
 #include <cmath>
 #include <fstream>
 #include <sstream>
@@ -57,6 +58,35 @@ int read_inp(const std::string &path, Info &d, std::string &err) {
   return 0;
 }
 
+namespace {
+// da_Z (initialization.cpp:23-60): rows "z H D_A D_C D_T"; with use_comoving the
+// fifth column is stored as the transverse distance, else the third; reads at
+// most ceil((z_max+1)/dz)+1 rows and needs at least ceil(z_max/dz)+1.
+int read_distances(Info &d, std::string &err) {
+  std::ifstream in(d.distance_file);
+  if (!in.is_open()) {
+    err = "da_Z:: distances file (dA vs Z) not opened: " + d.distance_file;
+    return 1;
+  }
+  const int64_t want = (int64_t)std::ceil((d.z_max + 1) / d.dz) + 1;
+  const int64_t need = (int64_t)std::ceil(d.z_max / d.dz) + 1;
+  d.H_z.clear();
+  d.dA_z.clear();
+  d.dC_z.clear();
+  double z, h, c3, c4, c5;
+  while ((int64_t)d.H_z.size() < want && (in >> z >> h >> c3 >> c4 >> c5)) {
+    d.H_z.push_back(h);
+    d.dC_z.push_back(c4);
+    d.dA_z.push_back(d.use_comoving ? c5 : c3);
+  }
+  if ((int64_t)d.H_z.size() < need) {
+    err = "da_Z:: distances file (dA vs Z) ended unexpectedly";
+    return 1;
+  }
+  return 0;
+}
+}  // namespace
+
 // data_ini's derived settings (initialization.cpp:349-561).
 int derive_info(Info &d, std::string &err) {
   if (d.periodic_box) {
@@ -93,7 +123,16 @@ int derive_info(Info &d, std::string &err) {
     err = "dz=0";
     return 1;
   }
-  if (d.coordinates == 6) {
+  if (!d.periodic_box && read_distances(d, err)) return 1;
+  const int64_t z_idx = (int64_t)std::ceil(d.z_max / d.dz);
+  if (d.coordinates == 0) {
+    if (z_idx >= (int64_t)d.H_z.size()) {
+      err = "distances file shorter than z_max / dz";
+      return 1;
+    }
+    d.z_sep_max = d.p_max * d.H_z[z_idx] / 300000.0 + 0.001;
+    d.z_sep_min = d.p_min * d.H_z[z_idx] / 300000.0 - 0.001;
+  } else if (d.coordinates == 6) {
     d.z_sep_max = d.p_max + 1;
     d.z_sep_min = d.p_min - 1;
   } else if (d.coordinates == 7) {
@@ -133,6 +172,11 @@ cpc_params to_params(const Info &d) {
   p.z_max = d.z_max;
   p.dz = d.dz;
   p.z_sep_max = d.z_sep_max;
+  if (!d.periodic_box && !d.H_z.empty()) {
+    p.H_z = d.H_z.data();
+    p.dA_z = d.dA_z.data();
+    p.n_table = (int64_t)std::min(d.H_z.size(), d.dA_z.size());
+  }
   return p;
 }
 

@@ -4,7 +4,8 @@
 // loop reads: jk_prob (glibc rand()/(RAND_MAX+1.) in a periodic box, one draw
 // per galaxy in read order after srand(124693517); 1 otherwise, 0 without
 // jackknife), phi (elip_angle, or -10 without shapes), include_prob (a second
-// draw for random catalogues), and the weight totals.  Numbers are parsed with
+// draw for random catalogues), the table distances D_C and D_A of a non-periodic
+// run, and the weight totals.  Numbers are parsed with
 // std::from_chars, which rounds exactly as the reference's istream >> double.
 #include <charconv>
 #include <cmath>
@@ -72,6 +73,8 @@ cpc_catalog Catalog::view() const {
   c.phi = phi.data();
   c.jk = jk.empty() ? nullptr : jk.data();
   c.jk_prob = jk_prob.data();
+  c.dc = dc.empty() ? nullptr : dc.data();
+  c.da = da.empty() ? nullptr : da.data();
   return c;
 }
 
@@ -114,6 +117,7 @@ int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &er
   c.phi.assign(n_gal, -10.0); c.jk_prob.assign(n_gal, 1.0); c.include_prob.assign(n_gal, 0.0);
   if (read_jk) c.jk.assign(n_gal, -1);
   c.has_e = read_e;
+  if (!d.periodic_box) { c.dc.resize(n_gal); c.da.resize(n_gal); }
   if (read_e) { c.e1.resize(n_gal); c.e2.resize(n_gal); }
   for (int i = 0; i < n_gal; i++) {
     if (!fp.get(c.x[i]) || !fp.get(c.y[i]) || !fz.get(c.z[i])) {
@@ -128,6 +132,14 @@ int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &er
     if (d.periodic_box) {
       c.jk_prob[i] = rng.next() / (2147483647 + 1.);
       draws++;
+    } else {  // read_dat.cpp:247-251: table rows, no interpolation
+      const int64_t it = (int64_t)std::floor(c.z[i] / d.dz);
+      if (it < 0 || it >= (int64_t)d.dC_z.size()) {
+        err = "redshift beyond the distances table at row " + std::to_string(i);
+        return 1;
+      }
+      c.dc[i] = d.dC_z[it];
+      c.da[i] = d.dA_z[it];
     }
     if (d.do_jk == 0 || d.n_jk == 0) c.jk_prob[i] = 0;
     if (w_f != "0" && !fw.get(c.w[i])) { err = "wt file ended early"; return 1; }

@@ -25,3 +25,24 @@ def test_cli_output_files_match_reference(name, tmp_path):
         if fname.endswith(".info"):
             continue
         compare_files(open(out + fname).read(), ref, label=f"{name}:{fname}")
+
+
+@pytest.mark.parametrize("name", ["sky_wgp_jk", "sky_wgg_distinct_wrap"])
+def test_cli_sky_output_files_match_reference(name, tmp_path):
+    """A sky cross run through the command line: reads the four catalogues and
+    the distances file, counts SRd, RsRd, SD, DRs on the GPU, finalises with
+    Landy-Szalay and writes the reference's files."""
+    from helpers import SkyGolden
+    g = SkyGolden(name)
+    c = g.cats
+    wl = synth.SkyWorkload(name, g.params, g.table, c["S"], c["D"], c["Rs"], c["Rd"])
+    inp = synth.write_sky_run(str(tmp_path), wl, same_files=g.meta["same_files"])
+    r = subprocess.run([build.CLI, inp], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for t in g.terms:
+        assert f"pairs in={g.term(t)[2]}" in r.stdout, t
+    out = os.path.join(str(tmp_path), "out", "run_")
+    for fname, ref in g.files.items():
+        if fname.endswith(".info"):
+            continue
+        compare_files(open(out + fname).read(), ref, label=f"{name}:{fname}")

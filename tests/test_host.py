@@ -11,7 +11,7 @@ import pytest
 
 import oracle
 from corr_pc_gb300 import _lib, host, synth
-from helpers import Golden, compare_files, golden_names
+from helpers import Golden, SkyGolden, compare_files, golden_names, sky_golden_names
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -130,3 +130,27 @@ def test_finalisation_matches_reference_files(name, tmp_path):
         if fname.endswith(".info"):
             continue
         compare_files(got, ref, label=f"{name}:{fname}")
+
+
+@pytest.mark.parametrize("name", sky_golden_names())
+def test_sky_finalisation_matches_reference_files(name, tmp_path):
+    """Reference raw histograms of the four sky terms -> Landy-Szalay
+    finalisation -> the reference's own output files."""
+    g = SkyGolden(name)
+    p = g.params
+    p.out_file = str(tmp_path) + "/run_"
+    p.distance_file = str(tmp_path / "distances.dat")
+    g.table.write(p.distance_file)
+    inp = str(tmp_path / "run.inp")
+    p.write(inp)
+    terms = {t: g.term(t)[:2] for t in g.terms}
+    w = []
+    for role in ("S", "D", "Rs", "Rd"):
+        c = g.cats[role]
+        ww = np.ones(c.n) if c.w is None else c.w
+        w += [float(ww.sum()), float((ww * ww).sum())]
+    _lib.finalize_cross(inp, terms, w)
+    for fname, ref in g.files.items():
+        if fname.endswith(".info"):
+            continue
+        compare_files(open(p.out_file + fname).read(), ref, label=f"{name}:{fname}")
