@@ -85,7 +85,8 @@ struct Slot {
   // redshift-ordered catalogue; these the sky-only per-galaxy quantities
   bool sky = false;
   DevBuf<double> dc, da, sd, cd, rar, decr, win;
-  DevBuf<float4> sky_su, sky_sw;  // float unit vector + D_A; float RA, Dec, z, D_C
+  DevBuf<float4> sky_su, sky_sl, sky_sw, sky_sx, sky_ss;  // float views (SkyFast)
+  double dcmax = 0;  // largest |D_C| (error bound of the float Pi)
   // host copies in the same order for the host edge tier
   std::vector<double> hs_ra, hs_dec, hs_dc, hs_da, hs_w, hs_e1, hs_e2, hs_phi;
   std::vector<int32_t> hs_jk;
@@ -859,18 +860,31 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   CK(put(s.da, s.hs_da, n), "sky upload"); CK(put(s.sd, sds, n), "sky upload");
   CK(put(s.cd, cds, n), "sky upload"); CK(put(s.rar, rars, n), "sky upload");
   CK(put(s.decr, decrs, n), "sky upload"); CK(put(s.win, wins, 6 * (size_t)n), "sky upload");
-  // float views for the fast kernel's prefilters
-  std::vector<float4> su(n), sw(n);
+  // float views for the fast kernel: hi parts and the remainders
+  std::vector<float4> su(n), sl(n), sw(n), sx(n), ss(n);
+  auto hi = [](double v) { return (float)v; };
+  auto lo = [](double v) { return (float)(v - (double)(float)v); };
+  s.dcmax = 0;
   for (int64_t k = 0; k < n; k++) {
-    const double ca = std::cos(rars[k]), sa = std::sin(rars[k]);
-    su[k] = make_float4((float)(cds[k] * ca), (float)(cds[k] * sa), (float)sds[k], (float)s.hs_da[k]);
-    sw[k] = make_float4((float)s.hs_ra[k], (float)s.hs_dec[k], (float)zs[k], (float)s.hs_dc[k]);
+    const double ux = cds[k] * std::cos(rars[k]), uy = cds[k] * std::sin(rars[k]), uz = sds[k];
+    const double dcv = s.hs_dc[k];
+    s.dcmax = std::max(s.dcmax, std::fabs(dcv));
+    su[k] = make_float4(hi(ux), hi(uy), hi(uz), (float)s.hs_da[k]);
+    sl[k] = make_float4(lo(ux), lo(uy), lo(uz), lo(dcv));
+    sw[k] = make_float4(hi(s.hs_ra[k]), hi(s.hs_dec[k]), (float)zs[k], hi(dcv));
+    sx[k] = make_float4(lo(s.hs_ra[k]), lo(s.hs_dec[k]), (float)decrs[k], (float)s.hs_w[k]);
+    ss[k] = make_float4((float)s.hs_e1[k], (float)s.hs_e2[k], (float)s.hs_phi[k], 0.f);
   }
-  CK(s.sky_su.alloc(nn), "alloc"); CK(s.sky_sw.alloc(nn), "alloc");
+  DevBuf<float4> *fbufs[5] = {&s.sky_su, &s.sky_sl, &s.sky_sw, &s.sky_sx, &s.sky_ss};
+  const std::vector<float4> *fsrc[5] = {&su, &sl, &sw, &sx, &ss};
+  for (int q = 0; q < 5; q++) {
+    CK(fbufs[q]->alloc(nn), "alloc");
+    if (n > 0)
+      CK(cudaMemcpyAsync(fbufs[q]->p, fsrc[q]->data(), sizeof(float4) * n, cudaMemcpyHostToDevice,
+                         st), "H2D");
+  }
   CK(s.jk.alloc(nn), "alloc"); CK(s.keep.alloc(nn), "alloc"); CK(s.orig.alloc(nn), "alloc");
   if (n > 0) {
-    CK(cudaMemcpyAsync(s.sky_su.p, su.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(s.sky_sw.p, sw.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st), "H2D");
     CK(cudaMemcpyAsync(s.jk.p, s.hs_jk.data(), 4 * n, cudaMemcpyHostToDevice, st), "H2D");
     CK(cudaMemcpyAsync(s.keep.p, s.hs_keep.data(), n, cudaMemcpyHostToDevice, st), "H2D");
     CK(cudaMemcpyAsync(s.orig.p, orig.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
@@ -934,6 +948,36 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
   J.acc_num = c->d_num.p;
   J.acc_sums = c->d_sums.p;
   J.counters = c->d_counters.p;
+  // float bands of the mixed-precision path.  r_p bin k is certain when
+  // [rp - tol, rp + tol] lies inside [A_k, B_k) (the exact thresholds rounded
+  // inwards; tol is per pair).  The float Pi differs from the reference's by at
+  // most 2^-23 |Pi| + 2^-46 max|D_C|; the Pi bands are shrunk by twice that.
+  {
+    const int nrp = p.n_bins, npi = p.n_p_bin;
+    for (int k = 0; k < nrp; k++) {
+      J.A[k] = f_up(c->thr_rp[k]);
+      J.B[k] = f_down(c->thr_rp[k + 1]);
+    }
+    J.rej_lo = f_down(c->thr_rp[0]);
+    J.rej_hi = f_up(c->thr_rp[nrp]);
+    const double dcm = std::max(g1.dcmax, g2.dcmax);
+    auto gp = [&](double v) { return 2.4e-7 * std::fabs(v) + 4e-14 * dcm + 1e-30; };
+    for (int k = 0; k < npi; k++) {
+      const double lo = c->thr_pi[k], hi = c->thr_pi[k + 1];
+      J.PA[k] = f_up(lo + gp(lo));
+      J.PB[k] = f_down(hi - gp(hi));
+    }
+    J.pi_out_lo = f_down(c->thr_pi[0] - gp(c->thr_pi[0]));
+    J.pi_out_hi = f_up(c->thr_pi[npi] + gp(c->thr_pi[npi]));
+    J.inv_ps_f = (float)(1.0 / c->ps);
+    J.tp0 = (float)(-p.p_min / c->ps);
+    J.rmin_f = (float)p.bin_r_min;
+    J.inv_rsize_f = (float)(1.0 / c->rsize);
+    if (!p.lin_bin) {
+      J.l2rmin2 = (float)(2.0 * std::log2(p.bin_r_min));
+      J.inv_lw = (float)(1.0 / (2.0 * std::log2(p.bin_r_max / p.bin_r_min) / nrp));
+    }
+  }
   if ((st_ = ensure_scratch(c, 1, 1)) != CPC_OK) return st_;
   CK(c->d_hq.alloc(kSkyHostQueue), "alloc host queue");
   CK(c->d_hq_n.alloc(1), "alloc");
@@ -948,7 +992,8 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
     CK(launch_sky_fp64(c->d_jobs.p, sky_view(g1), sky_view(g2), c->d_hq.p, c->d_hq_n.p,
                        kSkyHostQueue, esum, c->st), "sky kernel");
   } else {
-    const SkyFast fa{g1.sky_su.p, g1.sky_sw.p}, fb{g2.sky_su.p, g2.sky_sw.p};
+    const SkyFast fa{g1.sky_su.p, g1.sky_sl.p, g1.sky_sw.p, g1.sky_sx.p, g1.sky_ss.p};
+    const SkyFast fb{g2.sky_su.p, g2.sky_sl.p, g2.sky_sw.p, g2.sky_sx.p, g2.sky_ss.p};
     const float rp_lo_f = f_down(c->thr_rp[0]), rp_hi_f = f_up(c->thr_rp[p.n_bins]);
     CK(launch_sky_warp(c->d_jobs.p, sky_view(g1), sky_view(g2), fa, fb, c->d_unit_ctr.p,
                        c->d_hq.p, c->d_hq_n.p, kSkyHostQueue, esum, rp_lo_f, rp_hi_f,

@@ -55,9 +55,14 @@ cudaError_t launch_plain_fp64(const JobDev *job, const DCat &a, const DCat &b, c
 // Sky pairs (coordinates 0) in FP64; pairs whose r_p may bin differently with
 // the C library's trigonometry are appended to hq (host edge tier).
 constexpr unsigned long long kSkyHostQueue = 1ull << 22;
+// float views of a sky catalogue for the fast kernel (hi = float(v),
+// lo = float(v - hi), so hi + lo carries about 48 bits of v)
 struct SkyFast {
-  const float4 *su;  // unit vector (cos d cos a, cos d sin a, sin d) and transverse distance
-  const float4 *sw;  // RA, Dec, redshift, comoving distance
+  const float4 *su;  // unit vector (cos d cos a, cos d sin a, sin d) hi parts, D_A
+  const float4 *sl;  // unit vector lo parts, D_C lo part
+  const float4 *sw;  // RA, Dec hi parts, redshift, D_C hi part
+  const float4 *sx;  // RA, Dec lo parts, Dec in radians, weight
+  const float4 *ss;  // e1, e2, phi, 0
 };
 cudaError_t launch_sky_warp(const JobDev *job, const SkyView &a, const SkyView &b,
                             const SkyFast &fa, const SkyFast &fb, unsigned int *row_ctr, int2 *hq,

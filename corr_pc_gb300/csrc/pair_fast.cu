@@ -1,25 +1,33 @@
 // pair_fast.cu -- the mixed-precision pair-counting kernel (sm_103a).
 //
 // One persistent launch drains a device work queue of "units".  A unit is a
-// tile of up to kTile g1 rows (one row per thread, held in registers) from a
-// single (column, jackknife region) bucket, paired with every g2 candidate of
-// the neighbouring columns inside the unit's shifted-z range.  Candidates are
-// staged through shared memory in batches of kTile and every thread tests its
-// row against every staged candidate (broadcast reads, no bank conflicts).
+// tile of up to kTile g1 rows from one (column, jackknife region) bucket and
+// z-chunk, paired with every g2 candidate of the neighbouring columns inside
+// the unit's shifted-z range.  A block of 256 threads holds the tile's rows
+// twice (two warp groups, one row per lane; the lanes of a warp are spread over
+// the tile) and the groups split each staged batch of 256 candidates.  Batches
+// are drawn as a coprime-stride permutation of the (partner region, image
+// shift) group, so simultaneous pairs of a warp fall in different bins.
 //
-// Precision: separations, r_p^2 and Pi are computed in FP32.  A pair is
-// resolved on this path only when it is farther than a rigorous error bound
-// from every decision boundary (the r_p / Pi window, every r_p and Pi bin
-// edge); otherwise it is appended to an edge queue and re-evaluated with the
-// reference's exact double-precision arithmetic (recheck_kernel), so integer
-// counts are bit-identical with the reference.
+// Light pass (every candidate): FP32 separations with the image shift applied
+// exactly, definite in / definite out tests of the reference's window, r^2
+// range test; binned pairs go to a per-warp queue.  Heavy step (32 queued
+// pairs, all lanes busy): exact r_p and Pi bins from an estimated index checked
+// against definite bands, shape values, histogram updates.
+//
+// Precision: a pair is resolved on this path only when it is farther than a
+// rigorous error bound from every decision boundary (the r_p / Pi window,
+// every r_p and Pi bin edge); otherwise it is appended to an edge queue and
+// re-evaluated with the reference's exact double-precision arithmetic
+// (recheck_kernel), so integer counts are bit-identical with the reference.
 //
 // Accumulation: block-private histograms over (r_p bin, block-local Pi window)
 // in shared memory -- the full sample ("main"), the tile's own jackknife region
 // ("X") and one other region ("Y", the partner's region for cross-region
-// pairs) -- with 32-bit counts and 64-bit fixed-point sums (exact integer
-// addition, order independent), flushed to the FP64 global histogram block
-// with one atomic per non-empty (bin, field) at the end of the unit.
+// pairs) -- with 32-bit counts and fixed-point sums split over two 32-bit
+// words per field (exact integer addition, order independent), flushed to the
+// FP64 global histogram block every kFlushCands staged candidates and at the
+// end of the unit.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <climits>

@@ -31,7 +31,9 @@
 //    reject pairs certainly outside the Pi range or certainly outside
 //    [thr_0, thr_nrp) in r_p (the chord |u1 - u2| of float unit vectors with a
 //    rigorous error bound); survivors are compacted into a per-warp queue and
-//    run through the FP64 path 32 at a time with every lane busy; the main
+//    evaluated 32 at a time with every lane busy: Pi and r_p in FP32 from hi+lo
+//    floats with per-pair error bounds, FP32 shape values when both bins are
+//    certain, the FP64 path (and behind it the host tier) otherwise.  The main
 //    histogram lives in shared memory (FP64 atomics) and is flushed once per
 //    block.
 #include <cuda_runtime.h>
@@ -138,10 +140,44 @@ struct SkyRow {
   int jk, keep;
 };
 
+// Add one binned pair's values to the histograms: the main histogram in shared
+// memory (SMEM) or global memory, the jackknife regions in global memory with
+// jk_check_sky (jk.cpp:53-57) and corel_jk1 (jk.cpp:138-171).
+template <bool SMEM, class T>
+__device__ __forceinline__ void sky_accumulate(const JobDev &J, const SkyRow &r, int r2, int keep2,
+                                               int64_t cell, const T *f,
+                                               unsigned long long *s_num, double *s_sums) {
+  const int nf = J.corel == COREL_DD ? 1 : kNF;
+  if (SMEM) {
+    atomicAdd(&s_num[cell], 1ull);
+    for (int q = 0; q < nf; q++)
+      if (f[q] != 0) atomicAdd(&s_sums[cell * kNF + q], (double)f[q]);
+  } else {
+    atomicAdd(&J.acc_num[cell], 1ull);
+    for (int q = 0; q < nf; q++)
+      if (f[q] != 0) atomicAdd(&J.acc_sums[cell * kNF + q], (double)f[q]);
+  }
+  if (!J.do_jk) return;
+  const int k1 = r.keep, k2 = (r2 == r.jk) ? 0 : keep2;
+  const int64_t hstride = (int64_t)J.nrp * J.npi;
+  const int rs[2] = {r.jk, r2};
+  const int ks[2] = {k1, k2};
+  for (int t = 0; t < 2; t++) {
+    if (!ks[t]) continue;
+    const int64_t hc = (int64_t)(1 + rs[t]) * hstride + cell;
+    atomicAdd(&J.acc_num[hc], 1ull);
+    double *sj = J.acc_sums + hc * kNF;
+    if (f[0] != 0) atomicAdd(&sj[0], (double)f[0]);
+    if (J.which_corr == 0 || nf == 1) continue;  // f holds nf values
+    for (int q = 1; q < kNF; q += 2)
+      if (f[q] != 0) atomicAdd(&sj[q], (double)f[q]);
+  }
+}
+
 // FP64 path of one window pair whose Pi and r_p may fall in the bins: exact
 // Pi bin, great-circle r_p, ambiguity test, values and accumulation.
 template <bool SMEM>
-__device__ __forceinline__ void sky_pair_fp64(const JobDev &J, const SkyRow &r, const SkyView &b,
+__device__ __noinline__ void sky_pair_fp64(const JobDev &J, const SkyRow &r, const SkyView &b,
                                               int64_t j, unsigned long long *s_num,
                                               double *s_sums, int2 *hq,
                                               unsigned long long *hq_n,
@@ -176,33 +212,131 @@ __device__ __forceinline__ void sky_pair_fp64(const JobDev &J, const SkyRow &r, 
   double f[kNF];
   pair_values(J.corel, J.gws, wt, theta, PairGal{r.e1, r.e2, r.phi},
               PairGal{b.d.e1[j], b.d.e2[j], b.d.phi[j]}, f);
-  const int64_t cell = (int64_t)(k - 1) * J.npi + (int)v2;
-  const int nf = J.corel == COREL_DD ? 1 : kNF;
-  if (SMEM) {
-    atomicAdd(&s_num[cell], 1ull);
-    for (int q = 0; q < nf; q++)
-      if (f[q] != 0.0) atomicAdd(&s_sums[cell * kNF + q], f[q]);
-  } else {
-    atomicAdd(&J.acc_num[cell], 1ull);
-    for (int q = 0; q < nf; q++)
-      if (f[q] != 0.0) atomicAdd(&J.acc_sums[cell * kNF + q], f[q]);
+  sky_accumulate<SMEM>(J, r, b.d.jk[j], b.d.keep[j], (int64_t)(k - 1) * J.npi + (int)v2, f,
+                       s_num, s_sums);
+}
+
+// the row's float quantities for the mixed-precision path
+struct SkyRowF {
+  float4 u, ul, w, x, sh;  // su, sl, sw, sx, ss of the row
+};
+
+// estimated bin index confirmed against definite bands: the bin, -1 certainly
+// outside, -2 undecided.  band k is [lo_k, hi_k) in the estimate's units.
+__device__ __forceinline__ int band_bin(float v, float tol, int est, int n, const float *lo,
+                                        const float *hi, float rej_lo, float rej_hi) {
+  if (v + tol < rej_lo || v - tol >= rej_hi) return -1;
+  est = min(max(est, 0), n - 1);
+  for (int d = 0; d < 3; d++) {
+    const int k = d == 0 ? est : d == 1 ? est - 1 : est + 1;
+    if (k < 0 || k >= n) continue;
+    if (v - tol >= lo[k] && v + tol < hi[k]) return k;
   }
-  if (!J.do_jk) return;
-  // jk_check_sky (jk.cpp:53-57) then corel_jk1 (jk.cpp:138-171)
-  const int r2 = b.d.jk[j];
-  const int k1 = r.keep, k2 = (r2 == r.jk) ? 0 : b.d.keep[j];
-  const int64_t hstride = (int64_t)J.nrp * J.npi;
-  const int rs[2] = {r.jk, r2};
-  const int ks[2] = {k1, k2};
-  for (int t = 0; t < 2; t++) {
-    if (!ks[t]) continue;
-    const int64_t hc = (int64_t)(1 + rs[t]) * hstride + cell;
-    atomicAdd(&J.acc_num[hc], 1ull);
-    double *sj = J.acc_sums + hc * kNF;
-    if (f[0] != 0.0) atomicAdd(&sj[0], f[0]);
-    if (J.which_corr == 0) continue;
-    for (int q = 1; q < kNF; q += 2)
-      if (f[q] != 0.0) atomicAdd(&sj[q], f[q]);
+  return -2;
+}
+
+// Mixed-precision evaluation of a pair that may bin.  Pi from hi+lo float
+// comoving distances, r_p = 2 asin(|u1 - u2| / 2) (D_A1 + D_A2) / 2 from hi+lo
+// float unit vectors, each with a bound on its difference from the
+// reference's double value; when both bins are certain the shape values are
+// computed in FP32 and accumulated, otherwise the pair takes the FP64 path.
+template <bool SMEM>
+__device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r, const SkyRowF &rf,
+                                               const SkyView &b, const SkyFast &fb, int64_t j,
+                                               unsigned long long *s_num, double *s_sums,
+                                               int2 *hq, unsigned long long *hq_n,
+                                               unsigned long long hq_cap, double esum,
+                                               const float *s_A, const float *s_B,
+                                               const float *s_PA, const float *s_PB) {
+  const float4 w2 = fb.sw[j], l2 = fb.sl[j], u2 = fb.su[j];
+  // Pi: (dc2_hi - dc1_hi) + (dc2_lo - dc1_lo); the bands carry the error bound
+  const float pf = (w2.w - rf.w.w) + (l2.w - rf.ul.w);
+  const int k2 = band_bin(pf, 0.0f, (int)floorf(fmaf(pf, J.inv_ps_f, J.tp0)), J.npi, s_PA, s_PB,
+                          J.pi_out_lo, J.pi_out_hi);
+  if (k2 == -1) return;
+  // chord of the unit vectors, then theta and r_p
+  const float dx = (rf.u.x - u2.x) + (rf.ul.x - l2.x);
+  const float dy = (rf.u.y - u2.y) + (rf.ul.y - l2.y);
+  const float dz = (rf.u.z - u2.z) + (rf.ul.z - l2.z);
+  const float c2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float c = sqrtf(c2);
+  int k1 = -2;
+  if (k2 >= 0 && c > 1.5e-5f) {  // below: near the clamp of dA_calc
+    // |rp - rp_ref| / rp: float chord, asinf and D_A sum (< 6e-7), the double
+    // unit vectors (3e-16 / c), and the reference's own sum = cos(theta)
+    // rounding through acos (< 1.2e-15 / theta^2), each with margin
+    const float rp = asinf(0.5f * c) * (rf.u.w + u2.w);
+    const float tol = rp * (1.5e-6f + 3e-14f / c + 4e-15f / c2);
+    const int est = J.lin_bin ? (int)floorf((rp - J.rmin_f) * J.inv_rsize_f)
+                              : (int)floorf((__log2f(rp * rp) - J.l2rmin2) * J.inv_lw);
+    k1 = band_bin(rp, tol, est, J.nrp, s_A, s_B, J.rej_lo, J.rej_hi);
+    if (k1 == -1) return;
+  }
+  if (k1 < 0 || k2 < 0) {
+    sky_pair_fp64<SMEM>(J, r, b, j, s_num, s_sums, hq, hq_n, hq_cap, esum);
+    return;
+  }
+  // values: theta = atan(dDec / (dRA cos(mean Dec))) (sky_calcs.cpp:13-22)
+  const float4 x2 = fb.sx[j];
+  const float wt = rf.x.w * x2.w;
+  const int64_t cell = (int64_t)k1 * J.npi + k2;
+  if (J.corel == COREL_DD) {
+    const float f0[1] = {wt};
+    sky_accumulate<SMEM>(J, r, b.d.jk[j], b.d.keep[j], cell, f0, s_num, s_sums);
+  } else {
+    const float4 sh2 = fb.ss[j];
+    const float dra = (w2.x - rf.w.x) + (x2.x - rf.x.x);
+    const float ddec = (w2.y - rf.w.y) + (x2.y - rf.x.y);
+    const float xx = dra * __cosf(0.5f * (rf.x.z + x2.z)), yy = ddec;
+    const float a = xx * xx, bb = yy * yy;
+    const float inv = 1.0f / (a + bb);
+    const float cs = (a - bb) * inv, sn = 2.0f * xx * yy * inv;
+    const float theta = atanf(yy / xx);
+    float v[kNF];
+    for (int q = 0; q < kNF; q++) v[q] = 0.0f;
+    v[0] = wt;
+    auto ephi = [&](float phi) {
+      float t = fabsf(phi - theta);
+      return t > 1.5707963267948966f ? 3.14159265358979f - t : t;
+    };
+    if (J.corel == COREL_SD) {
+      const float es0 = J.gws == 2 ? sh2.x : rf.sh.x, es1 = J.gws == 2 ? sh2.y : rf.sh.y;
+      const float ep = cs * es0 - sn * es1, ex = sn * es0 + cs * es1;
+      v[1] = wt * ep;
+      v[2] = v[1] * v[1];
+      v[3] = wt * ex;
+      v[4] = v[3] * v[3];
+      v[11] = ephi(rf.sh.z);
+      v[12] = v[11] * v[11];
+    } else {
+      const float ei0 = cs * rf.sh.x - sn * rf.sh.y, ei1 = sn * rf.sh.x + cs * rf.sh.y;
+      const float ej0 = cs * sh2.x - sn * sh2.y, ej1 = sn * sh2.x + cs * sh2.y;
+      if (J.corel == COREL_SS) {
+        const bool g2s = J.gws == 2;
+        v[1] = wt * (g2s ? ej0 : ei0);
+        v[2] = v[1] * v[1];
+        v[11] = ephi(g2s ? sh2.z : rf.sh.z);
+        v[12] = v[11] * v[11];
+      } else {
+        v[1] = wt * (ei0 + ej0) * 0.5f;
+        const float pa = wt * ei0 * 0.5f, pb = wt * ej0 * 0.5f;
+        v[2] = pa * pa + pb * pb;
+        v[3] = wt * (ei1 + ej1) * 0.5f;
+        const float qa = wt * ei1 * 0.5f, qb = wt * ej1 * 0.5f;
+        v[4] = qa * qa + qb * qb;
+        const float ta = ephi(rf.sh.z), tb = ephi(sh2.z);
+        v[11] = ta + tb;
+        v[12] = ta * ta + tb * tb;
+      }
+      v[5] = wt * (ei0 * ej0);
+      v[6] = v[5] * v[5];
+      v[7] = wt * (ei1 * ej1);
+      v[8] = v[7] * v[7];
+      v[9] = wt * (ei1 * ej0 + ei0 * ej1) * 0.5f;
+      const float xa = wt * (ei1 * ej0) * 0.5f, xb = wt * ei0 * ej1 * 0.5f;
+      v[10] = xa * xa + xb * xb;
+    }
+    sky_accumulate<SMEM>(J, r, b.d.jk[j], b.d.keep[j], cell, v, s_num, s_sums);
   }
 }
 
@@ -222,8 +356,12 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
                 int zero_bin) {
   extern __shared__ __align__(16) unsigned char sky_smem[];
   __shared__ int s_q[kSkyWarps][kSkyQ];
+  __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
   const JobDev &J = *jobp;
   const int ncell = J.nrp * J.npi;
+  for (int k = threadIdx.x; k < J.nrp; k += blockDim.x) { s_A[k] = J.A[k]; s_B[k] = J.B[k]; }
+  for (int k = threadIdx.x; k < J.npi; k += blockDim.x) { s_PA[k] = J.PA[k]; s_PB[k] = J.PB[k]; }
+  if (!SMEM) __syncthreads();
   unsigned long long *s_num = reinterpret_cast<unsigned long long *>(sky_smem);
   double *s_sums = reinterpret_cast<double *>(s_num + ncell);
   if (SMEM) {
@@ -258,6 +396,12 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
     const float de_lrd = __double2float_rd(dec_min), de_hru = __double2float_ru(dec_max);
     const float4 u1 = fa.su[i];
     const float dc1f = fa.sw[i].w;
+    SkyRowF rf;
+    rf.u = u1;
+    rf.ul = fa.sl[i];
+    rf.w = fa.sw[i];
+    rf.x = fa.sx[i];
+    rf.sh = fa.ss[i];
     // redshift range [lo, hi): z_min <= z <= z_max
     int64_t lo = 0, hi = n2;
     while (lo < hi) {
@@ -317,14 +461,17 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
       count += __popc(m);
       __syncwarp();
       if (count >= 32) {
-        sky_pair_fp64<SMEM>(J, r, b, q[lane], s_num, s_sums, hq, hq_n, hq_cap, esum);
+        sky_pair_mixed<SMEM>(J, r, rf, b, fb, q[lane], s_num, s_sums, hq, hq_n, hq_cap, esum, s_A,
+                             s_B, s_PA, s_PB);
         __syncwarp();
         if (lane < count - 32) q[lane] = q[lane + 32];
         count -= 32;
         __syncwarp();
       }
     }
-    if (lane < count) sky_pair_fp64<SMEM>(J, r, b, q[lane], s_num, s_sums, hq, hq_n, hq_cap, esum);
+    if (lane < count)
+      sky_pair_mixed<SMEM>(J, r, rf, b, fb, q[lane], s_num, s_sums, hq, hq_n, hq_cap, esum, s_A,
+                           s_B, s_PA, s_PB);
     __syncwarp();
   }
   if (nwin) atomicAdd(&J.counters[1], nwin);
