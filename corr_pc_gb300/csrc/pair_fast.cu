@@ -4,8 +4,9 @@
 // tile of up to kTile g1 rows from one (column, jackknife region) bucket and
 // z-chunk, paired with every g2 candidate of the neighbouring columns inside
 // the unit's shifted-z range.  A block of 256 threads holds the tile's rows
-// twice (two warp groups, one row per lane; the lanes of a warp are spread over
-// the tile) and the groups split each staged batch of 256 candidates.  Batches
+// in several warp groups (one row per lane; the lanes of a warp are spread over
+// the tile) and the groups split each staged batch of 256 candidates; a tile
+// of up to 32 W rows is held by 8 / W groups of W warps.  Batches
 // are drawn as a coprime-stride permutation of the (partner region, image
 // shift) group, so simultaneous pairs of a warp fall in different bins.
 //
@@ -254,10 +255,15 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     // tile (tile row q = lane * W + warp) so that simultaneous pairs of a warp
     // fall in different Pi bins; both warp groups hold the same rows and split
     // the candidates. ----
-    const int tr = t & (kTile - 1), grp = t / kTile;
+    // W warps hold the tile's rows (row q = lane * W + warp-in-group); the
+    // block's 8 warps form G = 8 / W such groups, each taking a share of every
+    // staged batch, so small tiles still keep every warp busy
     const int W = (U.g1_count + 31) >> 5;
-    const int q = (tr & 31) * W + (tr >> 5);
-    const bool has1 = (tr >> 5) < W && q < U.g1_count;
+    const int G = (kThreads / 32) / W;
+    const int grp = wid / W;
+    const int tr = (wid - grp * W) * 32 + lane;  // row slot in the tile (< 32 W)
+    const int q = lane * W + (wid - grp * W);
+    const bool has1 = grp < G && q < U.g1_count;
     const int64_t i1 = (int64_t)U.g1_start + (int64_t)q * U.g1_stride;
     float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f);
     bool valid = false;
@@ -455,10 +461,12 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
 
           // ---- light pass over the batch, binned pairs queued per warp; the
           // heavy step runs whenever 32 are queued (all lanes busy) ----
-          // group g takes batch slots [c0, c0 + nk); lane l at step s takes slot
-          // c0 + (s + l) mod nk, so a warp works on 32 different candidates
-          const int nk0 = (nb + 1) >> 1;
-          const int c0 = grp ? nk0 : 0, nk = grp ? nb - nk0 : nk0;
+          // lane l at step s takes slot c0 + (s + l) mod nk, so a warp works on
+          // 32 different candidates;
+          // group g takes batch slots [c0, c0 + nk); warps outside every group
+          // (8 % W of them) skip the pass
+          const int c0 = grp < G ? (grp * nb) / G : 0;
+          const int nk = grp < G ? ((grp + 1) * nb) / G - c0 : 0;
           int step = 0;
           int qhead = 0, qtail = 0;
           for (;;) {
