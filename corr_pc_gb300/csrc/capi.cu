@@ -381,8 +381,8 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
     J.l2rmin2 = (float)(2.0 * std::log2(p.bin_r_min));
     J.inv_lw = (float)(1.0 / (2.0 * std::log2(p.bin_r_max / p.bin_r_min) / nrp));
   }
-  // fixed-point scales: field f's terms are rint(v 2^S_f) + B with
-  // B = 2^26 >= max|v_f| 2^S_f (see pair_fast.cu); S_f from a bound on |v_f|
+  // fixed-point scales: field f's terms are rint(v 2^S_f) with
+  // |v_f| 2^S_f <= 2^26 (see pair_fast.cu); S_f from a bound on |v_f|
   {
     const double wm = std::max(g1.wmax, 1e-30) * std::max(g2.wmax, 1e-30);
     const double em = std::max({g1.emax, g2.emax, 1e-30});

@@ -77,7 +77,7 @@ struct JobDev {
   float rmin_f, inv_rsize_f;           // linear-bin estimate
   float rej_lo, rej_hi;                // definite r^2 rejection bounds
   float qscale[kNF];                   // per-field fixed-point scale 2^S_f
-  int qbias;                           // fixed-point bias B (> max |v_f| 2^S_f)
+  int qbias;                           // fixed-point bound: |v_f| 2^S_f <= qbias
   int unit_w;                          // every weight is 1: wt_num = count
   float A[kMaxRp], B[kMaxRp];          // definite r^2 band of r_p bin k
   float PA[kMaxPi], PB[kMaxPi];        // definite Pi band of Pi bin k

@@ -81,25 +81,26 @@ size_t fast_smem_bytes(int corel, int do_jk, int NB) {
   return b;
 }
 
-// Fixed-point sums in 32-bit shared words.  A term v of field f becomes
-// u = rint(v * 2^S_f) + B with B = 2^26 >= max|v| 2^S_f, so 0 <= u < 2^27; u is
-// split into a 14-bit low part and a 13-bit high part, each added to its own
-// 32-bit word with a plain reduction (no return value: no scoreboard wait, and
-// same-address adds of a warp are combined in hardware).  A block flushes its
-// histograms after every kFlushCands staged candidates, so a bin takes at most
-// kTile * kFlushCands = 2^18 terms between flushes and neither word can wrap.
+// Fixed-point sums in 32-bit shared words.  A term v of field f becomes the
+// integer u = rint(v * 2^S_f), |u| <= 2^26 (S_f from a bound on |v|); u is split
+// into its low 14 bits (0..16383) and the arithmetic shift u >> 14
+// (-2^12..2^12), each added to its own 32-bit word with a plain reduction (no
+// return value: no scoreboard wait, and same-address adds of a warp are
+// combined in hardware).  A block flushes its histograms after every
+// kFlushCands staged candidates, so a bin takes at most kTile * kFlushCands =
+// 2^18 terms between flushes: the low word stays below 2^32 and the high word,
+// read as a signed integer, within +-2^30.
 constexpr int kFlushCands = 2048;
 static_assert((long long)kTileThreads * kFlushCands <= (1ll << 18), "fixed-point word headroom");
-__device__ __forceinline__ unsigned to_fixed(float v, float scale, int bias) {
-  return (unsigned)(__float2int_rn(v * scale) + bias);
+__device__ __forceinline__ int to_fixed(float v, float scale) {
+  return __float2int_rn(v * scale);
 }
-__device__ __forceinline__ void red_split(unsigned *lo, unsigned *hi, unsigned u) {
-  atomicAdd(lo, u & 0x3FFFu);
-  atomicAdd(hi, u >> 14);
+__device__ __forceinline__ void red_split(unsigned *lo, unsigned *hi, int u) {
+  atomicAdd(lo, (unsigned)u & 0x3FFFu);
+  atomicAdd(hi, (unsigned)(u >> 14));
 }
-__device__ __forceinline__ double fixed_total(unsigned lw, unsigned hw, unsigned cnt, int bias,
-                                              double inv_scale) {
-  const long long tot = ((long long)hw << 14) + (long long)lw - (long long)cnt * (long long)bias;
+__device__ __forceinline__ double fixed_total(unsigned lw, unsigned hw, double inv_scale) {
+  const long long tot = (long long)(int)hw * 16384ll + (long long)lw;
   return (double)tot * inv_scale;
 }
 
@@ -167,7 +168,7 @@ __device__ __forceinline__ float ephi_f(float phi, float theta) {
 template <int NF, bool JKMAP, class FM>
 __device__ __forceinline__ void flush_hist(unsigned *cnt, unsigned *lo, unsigned *hi, int NB,
                                            int wpi, int npi, int nrp, int n2_base, int h, int f0,
-                                           int qbias, const double *s_iqs, const JobDev &J) {
+                                           const double *s_iqs, const JobDev &J) {
   const int64_t hb = (int64_t)h * nrp * npi;
   for (int lb = threadIdx.x; lb < NB; lb += kThreads) {
     const unsigned n = cnt[lb];
@@ -180,7 +181,7 @@ __device__ __forceinline__ void flush_hist(unsigned *cnt, unsigned *lo, unsigned
       const size_t o = (size_t)f * NB + lb;
       const int fld = JKMAP ? FM::j(f) : FM::m(f);
       if (f >= f0) {
-        const double v = fixed_total(lo[o], hi[o], n, qbias, s_iqs[fld]);
+        const double v = fixed_total(lo[o], hi[o], s_iqs[fld]);
         if (v != 0.0) atomicAdd(&J.acc_sums[cell * kNF + fld], v);
       }
       lo[o] = 0u;
@@ -248,7 +249,6 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     unsigned *s_ynum = s_xhi + (size_t)F::FJ * NB;
     unsigned *s_ylo = s_ynum + NB;
     unsigned *s_yhi = s_ylo + (size_t)F::FJ * NB;
-    const int qbias = J.qbias;
     const int f0 = J.unit_w ? 1 : 0;  // unit weights: wt_num = count, not accumulated
 
     // ---- this thread's g1 row.  The lanes of a warp are spread over the whole
@@ -294,7 +294,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     if (t < kNF) { s_qs[t] = J.qscale[t]; s_iqs[t] = J.inv_qscale[t]; }
     const float l2rmin2 = J.l2rmin2, inv_lw = J.inv_lw, rej_lo = J.rej_lo, rej_hi = J.rej_hi;
     const int n2_base = U.n2_base;
-    unsigned long long nwin = 0;
+    unsigned nwin = 0;  // window pairs of this thread's row in this unit
 
     // ---- enumerate candidate slots: (column, bucket, sz) overlapping the unit's z range ----
     const int ncxu = U.cx_hi - U.cx_lo + 1;
@@ -411,7 +411,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
           if (cur_y >= 0) {
             __syncthreads();
             flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
-                                       1 + cur_y, f0, qbias, s_iqs, J);
+                                       1 + cur_y, f0, s_iqs, J);
             __syncthreads();
           }
           cur_y = region2;
@@ -427,13 +427,13 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
           if (since_flush + nb > kFlushCands) {  // keep every word below 2^32
             __syncthreads();
             flush_hist<F::FM, false, F>(s_mnum, s_mlo, s_mhi, NB, wpi, npi, nrp, n2_base, 0, f0,
-                                        qbias, s_iqs, J);
+                                        s_iqs, J);
             if (JK) {
               flush_hist<F::FJ, true, F>(s_xnum, s_xlo, s_xhi, NB, wpi, npi, nrp, n2_base,
-                                         1 + U.region, f0, qbias, s_iqs, J);
+                                         1 + U.region, f0, s_iqs, J);
               if (cur_y >= 0)
                 flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
-                                           1 + cur_y, f0, qbias, s_iqs, J);
+                                           1 + cur_y, f0, s_iqs, J);
             }
             since_flush = 0;
           }
@@ -469,11 +469,9 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
           const int nk = grp < G ? ((grp + 1) * nb) / G - c0 : 0;
           int step = 0;
           int qhead = 0, qtail = 0;
+          int cr = nk > 0 ? lane % nk : 0;  // (step + lane) mod nk, kept incrementally
           for (;;) {
             while (step < nk && (qtail - qhead) < 32) {
-              int cr = step + lane;
-              if (cr >= nk) cr -= nk;
-              if (cr >= nk) cr %= nk;
               const int c = c0 + cr;
               const float4 p2 = s_pos[c];
               const float dz = p2.z - z1s;
@@ -496,6 +494,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                 s_wq[wid][(qtail + __popc(bm & lt_mask)) & (kQCap - 1)] = (unsigned)tr | ((unsigned)c << 7);
               qtail += __popc(bm);
               step++;
+              cr = (cr + 1 == nk) ? 0 : cr + 1;
             }
             const int avail = qtail - qhead;
             if (avail == 0) break;
@@ -553,7 +552,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                 const float a = dxr * dxr, b = dyr * dyr;
                 const float inv = __fdividef(1.0f, a + b);
                 const float c2 = (a - b) * inv, s2v = 2.0f * dxr * dyr * inv;
-                const float theta = atanf(dyr / dxr);
+                const float theta = atanf(__fdividef(dyr, dxr));
                 if (C == COREL_SD) {
                   const float es0 = gws == 2 ? s2.x : e1v.x, es1 = gws == 2 ? s2.y : e1v.y;
                   const float ep = c2 * es0 - s2v * es1, ex = s2v * es0 + c2 * es1;
@@ -597,7 +596,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               for (int f = 0; f < F::FM; f++)
                 if (f >= f0)
                   red_split(&s_mlo[(size_t)f * NB + lb], &s_mhi[(size_t)f * NB + lb],
-                            to_fixed(v[F::m(f)], s_qs[F::m(f)], qbias));
+                            to_fixed(v[F::m(f)], s_qs[F::m(f)]));
               if (JK) {
                 const bool k1 = s_rkeep[er] != 0;
                 const bool xc = same_region ? (box_same_keep || k1) : k1;
@@ -608,7 +607,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                   for (int f = 0; f < F::FJ; f++)
                     if (f >= f0)
                       red_split(&s_xlo[(size_t)f * NB + lb], &s_xhi[(size_t)f * NB + lb],
-                                to_fixed(v[F::j(f)], s_qs[F::j(f)], qbias));
+                                to_fixed(v[F::j(f)], s_qs[F::j(f)]));
                 }
                 if (yc) {
                   atomicAdd(&s_ynum[lb], 1u);
@@ -616,7 +615,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                   for (int f = 0; f < F::FJ; f++)
                     if (f >= f0)
                       red_split(&s_ylo[(size_t)f * NB + lb], &s_yhi[(size_t)f * NB + lb],
-                                to_fixed(v[F::j(f)], s_qs[F::j(f)], qbias));
+                                to_fixed(v[F::j(f)], s_qs[F::j(f)]));
                 }
               }
               }
@@ -634,18 +633,18 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
 
     // ---- flush main, X and the last Y ----
     __syncthreads();
-    flush_hist<F::FM, false, F>(s_mnum, s_mlo, s_mhi, NB, wpi, npi, nrp, n2_base, 0, f0, qbias,
+    flush_hist<F::FM, false, F>(s_mnum, s_mlo, s_mhi, NB, wpi, npi, nrp, n2_base, 0, f0,
                                 s_iqs, J);
     if (JK) {
       flush_hist<F::FJ, true, F>(s_xnum, s_xlo, s_xhi, NB, wpi, npi, nrp, n2_base, 1 + U.region,
-                                 f0, qbias, s_iqs, J);
+                                 f0, s_iqs, J);
       if (cur_y >= 0)
         flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y,
-                                   f0, qbias, s_iqs, J);
+                                   f0, s_iqs, J);
     }
     // window-pair counter
     {
-      unsigned long long v = nwin;
+      unsigned long long v = (unsigned long long)nwin;
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
       if (lane == 0) s_red[wid] = v;
       __syncthreads();
