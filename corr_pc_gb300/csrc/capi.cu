@@ -21,6 +21,12 @@
 
 using namespace cpc;
 
+// initial capacity of the FP64 edge queue (entries); it grows when a count
+// needs more
+#ifndef CPC_EDGE_QUEUE_INIT
+#define CPC_EDGE_QUEUE_INIT (1ull << 24)
+#endif
+
 namespace {
 
 std::mutex g_err_mu;
@@ -514,7 +520,7 @@ cpc_status ensure_scratch(cpc_ctx *c, size_t n_units, size_t n_jobs) {
   CK(c->d_unit_ctr.alloc(1), "alloc counter");
   CK(c->d_qcount.alloc(1), "alloc queue counter");
   if (!c->d_queue.p) {
-    c->qcap = 1ull << 24;
+    c->qcap = CPC_EDGE_QUEUE_INIT;
     cudaError_t e = c->d_queue.alloc(c->qcap);
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -633,7 +639,7 @@ cpc_status run_plain(JobPlan &jp) {
 }
 
 // fast engine over one or more jobs (one persistent launch per corel group)
-cpc_status run_fast(std::vector<JobPlan> &jobs) {
+cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt = 0) {
   cpc_ctx *c0 = jobs[0].c;
   cpc_ctx *c = c0;
   cudaStream_t st = c0->st;
@@ -707,11 +713,21 @@ cpc_status run_fast(std::vector<JobPlan> &jobs) {
   CK(cudaEventElapsedTime(&pms, c0->e0, c0->e2), "event time");
   unsigned long long qn = 0;
   CK(cudaMemcpy(&qn, c0->d_qcount.p, sizeof qn, cudaMemcpyDeviceToHost), "D2H");
+  if (qn > c0->qcap) {
+    // the edge queue overflowed: grow it to hold every queued pair and count
+    // again (the queued set does not depend on the order of execution)
+    if (grow_attempt) return fail(c, CPC_ERR_NOMEM, "edge queue overflow after growing it");
+    unsigned long long cap = c0->qcap;
+    while (cap < qn) cap *= 2;
+    c0->d_queue.reset();
+    CK(c0->d_queue.alloc(cap), "alloc edge queue");
+    c0->qcap = cap;
+    return run_fast(jobs, 1);
+  }
   for (size_t k = 0; k < jobs.size(); k++) {
     if ((s = fetch_accum(jobs[k].c, jobs[k].out, st, jobs[k].jd.unit_w)) != CPC_OK) return s;
     jobs[k].out->kernel_ms = ms;
     jobs[k].out->pair_kernel_ms = pms;
-    if (qn > c0->qcap) jobs[k].out->n_rechecked += (int64_t)(qn - c0->qcap);
   }
   return CPC_OK;
 }

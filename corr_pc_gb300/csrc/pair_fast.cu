@@ -128,22 +128,12 @@ __device__ __forceinline__ int lower_bound_f(const float *zf, int lo, int hi, fl
   return lo;
 }
 
-__device__ __noinline__ void fallback_exact(const JobDev &J, int64_t i1, int64_t j2, int code) {
-  int sx, sy, sz, n1, n2;
-  shift_decode(code & kShiftMask, sx, sy, sz);
-  const int r = exact_classify(J, J.d1, i1, J.d2, j2, sx, sy, sz, n1, n2);
-  if (r == 0) return;
-  if (!(code & kWindowCounted)) atomicAdd(&J.counters[1], 1ull);
-  if (r == 2) {
-    double f[kNF];
-    exact_values(J, J.d1, i1, J.d2, j2, f);
-    exact_accumulate(J, J.d1, i1, J.d2, j2, n1, n2, f);
-  }
-}
-
-__device__ __forceinline__ void enqueue(const JobDev &J, int job, int64_t i1, int64_t j2, int code,
-                                        QEntry *q, unsigned long long *qcount,
-                                        unsigned long long qcap) {
+// Append a pair to the FP64 edge queue.  Entries past the capacity are only
+// counted: the host then grows the queue and runs the job again (the set of
+// queued pairs is deterministic), so the kernel never needs an inline FP64
+// path of its own.
+__device__ __forceinline__ void enqueue(int job, int64_t i1, int64_t j2, int code, QEntry *q,
+                                        unsigned long long *qcount, unsigned long long qcap) {
   const unsigned long long pos = atomicAdd(qcount, 1ull);
   if (pos < qcap) {
     QEntry e;
@@ -152,8 +142,6 @@ __device__ __forceinline__ void enqueue(const JobDev &J, int job, int64_t i1, in
     e.j2 = (int)j2;
     e.shift = code;
     q[pos] = e;
-  } else {
-    fallback_exact(J, i1, j2, code);
   }
 }
 
@@ -191,6 +179,7 @@ __device__ __forceinline__ void flush_hist(unsigned *cnt, unsigned *lo, unsigned
 }
 
 constexpr int kQCap = 64;  // per-warp ring of binned pairs awaiting the heavy step
+constexpr unsigned kEdgeFlag = 0x8000u;  // queue entry: near the window edge
 
 template <int C, bool JK>
 __global__ void __launch_bounds__(kThreads, 2)
@@ -478,20 +467,23 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               const float dx = x1s - p2.x;
               const float dy = y1s - p2.y;
               const float m = fmaxf(fabsf(dx), fabsf(dy));
-              bool binned = false;
+              bool binned = false, edge = false;
               if (valid && dz >= pi_out_lo && dz <= pi_out_hi && m <= xy_out) {
                 if (!(dz >= pi_in_lo && dz <= pi_in_hi && m <= xy_in)) {
-                  // near the window edge: exact FP64 evaluation of the whole pair
-                  enqueue(J, U.job, i1, s_jidx[c], code, queue, qcount, qcap);
+                  // near the window edge: queued with a flag, the heavy step hands
+                  // it to the exact FP64 evaluation of the whole pair
+                  edge = true;
                 } else {
                   nwin++;
                   const float r2 = fmaf(dx, dx, dy * dy);
                   binned = r2 >= rej_lo && r2 < rej_hi;
                 }
               }
-              const unsigned bm = __ballot_sync(0xffffffffu, binned);
-              if (binned)
-                s_wq[wid][(qtail + __popc(bm & lt_mask)) & (kQCap - 1)] = (unsigned)tr | ((unsigned)c << 7);
+              const bool push = binned || edge;
+              const unsigned bm = __ballot_sync(0xffffffffu, push);
+              if (push)
+                s_wq[wid][(qtail + __popc(bm & lt_mask)) & (kQCap - 1)] =
+                    (unsigned)tr | ((unsigned)c << 7) | (edge ? kEdgeFlag : 0u);
               qtail += __popc(bm);
               step++;
               cr = (cr + 1 == nk) ? 0 : cr + 1;
@@ -504,6 +496,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               // ---- heavy step for one queued pair ----
               const unsigned e = s_wq[wid][(qhead + lane) & (kQCap - 1)];
               const int er = e & 127, ec = (e >> 7) & 255;
+              const bool edge = (e & kEdgeFlag) != 0;
               const float4 r1 = s_rpos[er];
               const float4 p2 = s_pos[ec];
               // exact bins: approximate index confirmed against the definite bands
@@ -529,11 +522,13 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               }
               const int elk = n2 - n2_base;
               if ((unsigned)elk >= (unsigned)wpi) amb = true;
-              if (amb) {
-                // near a bin edge: exact FP64 binning (window already counted)
+              if (amb || edge) {
+                // near the window edge (not yet counted) or a bin edge (window
+                // counted): exact FP64 evaluation
                 const int64_t gi1 = (int64_t)U.g1_start +
                                     (int64_t)(((er & 31) * W) + (er >> 5)) * U.g1_stride;
-                enqueue(J, U.job, gi1, s_jidx[ec], code | kWindowCounted, queue, qcount, qcap);
+                enqueue(U.job, gi1, s_jidx[ec], edge ? code : (code | kWindowCounted), queue,
+                        qcount, qcap);
               } else {
               const int lb = n1 * wpi + elk;
               float v[kNF];
