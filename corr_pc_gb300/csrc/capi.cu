@@ -134,7 +134,8 @@ struct cpc_ctx {
   DevBuf<uint64_t> d_keys, d_ktmp;
   DevBuf<uint32_t> d_vals, d_vtmp, d_hist, d_bucket;
   DevBuf<unsigned long long> d_census;
-  // sky host edge queue
+  // sky: fixed-point sums of the fast kernel, host edge queue
+  DevBuf<unsigned long long> d_fix;
   DevBuf<int2> d_hq;
   DevBuf<unsigned long long> d_hq_n;
   std::vector<UnitCache> unit_cache;
@@ -777,6 +778,10 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   std::vector<int32_t> jk(n, 0);
   std::vector<uint8_t> keep(n, 0);
   s.has_e = cat->e1 && cat->e2;
+  s.wmax = 0;
+  s.wmin = n > 0 ? 1e300 : 1.0;
+  s.emax = 0;
+  s.phimax = 0;
   for (int64_t i = 0; i < n; i++) {
     const double ra = cat->x[i], dec = cat->y[i], z = cat->z[i];
     if (!std::isfinite(ra) || !std::isfinite(dec) || !std::isfinite(z) ||
@@ -805,6 +810,10 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
       jk[i] = r;
     }
     if (cat->jk_prob) keep[i] = cat->jk_prob[i] >= 0.5 ? 1 : 0;
+    s.wmax = std::max(s.wmax, std::fabs(w[i]));
+    s.wmin = std::min(s.wmin, w[i]);
+    s.emax = std::max(s.emax, std::max(std::fabs(e1[i]), std::fabs(e2[i])));
+    s.phimax = std::max(s.phimax, std::fabs(phi[i]));
     sky_angles(ra, dec, &rar[i], &decr[i], &sd[i], &cd[i]);
     double wv[6];
     const int rc = sky_window(sp, ra, dec, z, wv);
@@ -994,6 +1003,37 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
       J.inv_lw = (float)(1.0 / (2.0 * std::log2(p.bin_r_max / p.bin_r_min) / nrp));
     }
   }
+  // fixed-point scales of the fast kernel: terms rint(v 2^S_f), |v| 2^S_f <= 2^28
+  // (64-bit integer sums; 2^35 terms per bin before any overflow)
+  {
+    const double wm = std::max(g1.wmax, 1e-30) * std::max(g2.wmax, 1e-30);
+    const double em = std::max({g1.emax, g2.emax, 1e-30});
+    const double tm = std::max(M_PI / 2, std::max(g1.phimax, g2.phimax) + M_PI);
+    const double tm2 = (rule.corel == COREL_SSA) ? 2 * tm : tm;
+    double vb[kNF];
+    vb[0] = wm;
+    vb[1] = vb[3] = wm * em;
+    vb[2] = vb[4] = wm * wm * em * em;
+    vb[5] = vb[7] = vb[9] = wm * em * em;
+    vb[6] = vb[8] = vb[10] = wm * wm * em * em * em * em;
+    vb[11] = tm2;
+    vb[12] = 2 * tm * tm;
+    for (int f = 0; f < kNF; f++) {
+      const double v = std::max(vb[f] * 1.0001, 1e-30);
+      int S = 28 - (int)std::ceil(std::log2(v));
+      S = std::min(60, std::max(-60, S));
+      J.qscale[f] = (float)std::ldexp(1.0, S);
+      J.inv_qscale[f] = std::ldexp(1.0, -S);
+    }
+    J.unit_w = (engine == CPC_ENGINE_FAST && g1.wmax == 1.0 && g1.wmin == 1.0 &&
+                g2.wmax == 1.0 && g2.wmin == 1.0) ? 1 : 0;
+  }
+  const size_t n_fix = (size_t)(1 + (p.do_jk ? p.n_jk : 0)) * p.n_bins * p.n_p_bin * kNF;
+  CK(c->d_fix.alloc(n_fix), "alloc fixed-point sums");
+  CK(cudaMemsetAsync(c->d_fix.p, 0, sizeof(unsigned long long) * n_fix, c->st), "memset");
+  J.acc_fix = c->d_fix.p;
+  J.sky1 = sky_view(g1);
+  J.sky2 = sky_view(g2);
   if ((st_ = ensure_scratch(c, 1, 1)) != CPC_OK) return st_;
   CK(c->d_hq.alloc(kSkyHostQueue), "alloc host queue");
   CK(c->d_hq_n.alloc(1), "alloc");
@@ -1015,10 +1055,13 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
                        c->d_hq.p, c->d_hq_n.p, kSkyHostQueue, esum, rp_lo_f, rp_hi_f,
                        c->thr_rp[0] <= 0.0 ? 1 : 0, p.n_bins, p.n_p_bin, c->sm_count, c->st),
        "sky kernel");
+    CK(launch_fix_to_sums((int64_t)n_fix, c->d_fix.p, c->d_sums.p, c->d_jobs.p, c->st),
+       "fixed-point sums");
+    c->launches += 1;
   }
   c->launches += 1;
   CK(cudaEventRecord(c->e1, c->st), "event");
-  if ((st_ = fetch_accum(c, out, c->st, 0)) != CPC_OK) return st_;
+  if ((st_ = fetch_accum(c, out, c->st, J.unit_w)) != CPC_OK) return st_;
   unsigned long long nq = 0;
   CK(cudaMemcpy(&nq, c->d_hq_n.p, sizeof nq, cudaMemcpyDeviceToHost), "D2H");
   if (nq > kSkyHostQueue)

@@ -34,17 +34,6 @@ struct DCat {
   const int64_t *orig;
 };
 
-// sky catalogue (coordinates 0) in redshift order: d.x = RA and d.y = Dec in
-// degrees, d.z = redshift, plus the per-galaxy quantities the pair loop reads
-struct SkyView {
-  DCat d;
-  const double *dc, *da;     // comoving (Pi) and transverse (r_p) distance
-  const double *sd, *cd;     // sin and cos of Dec in radians (host libm)
-  const double *rar, *decr;  // RA and Dec in radians (degrees / r2d)
-  const double *win;         // per-row windows, 6 blocks of n: z_min, z_max,
-                             // ra_min, ra_max, dec_min, dec_max (host libm)
-};
-
 // single-precision cell-list view (fast kernel)
 struct FCat {
   int64_t n;
@@ -57,6 +46,17 @@ struct FCat {
   const int *bk_start, *bk_end, *bk_region;
   const float *bk_zmin, *bk_zmax;
   const int *col_begin, *col_end;  // per column: range into the bucket list
+};
+
+// sky catalogue (coordinates 0) in redshift order: d.x = RA and d.y = Dec in
+// degrees, d.z = redshift, plus the per-galaxy quantities the pair loop reads
+struct SkyView {
+  DCat d;
+  const double *dc, *da;     // comoving (Pi) and transverse (r_p) distance
+  const double *sd, *cd;     // sin and cos of Dec in radians (host libm)
+  const double *rar, *decr;  // RA and Dec in radians (degrees / r2d)
+  const double *win;         // per-row windows, 6 blocks of n: z_min, z_max,
+                             // ra_min, ra_max, dec_min, dec_max (host libm)
 };
 
 struct JobDev {
@@ -89,6 +89,8 @@ struct JobDev {
   unsigned long long *acc_num;         // [n_hist][nrp][npi]
   double *acc_sums;                    // [n_hist][nrp][npi][kNF]
   unsigned long long *counters;        // [0] window (fast), [1] window (recheck), [2] rechecked
+  unsigned long long *acc_fix;         // sky fast path: fixed-point sums, layout of acc_sums
+  SkyView sky1, sky2;                  // sky catalogues g1, g2 (FP64 path of the fast kernel)
 };
 
 struct UnitDesc {

@@ -140,48 +140,87 @@ struct SkyRow {
   int jk, keep;
 };
 
-// Add one binned pair's values to the histograms: the main histogram in shared
-// memory (SMEM) or global memory, the jackknife regions in global memory with
-// jk_check_sky (jk.cpp:53-57) and corel_jk1 (jk.cpp:138-171).
-template <bool SMEM, class T>
-__device__ __forceinline__ void sky_accumulate(const JobDev &J, const SkyRow &r, int r2, int keep2,
-                                               int64_t cell, const T *f,
-                                               unsigned long long *s_num, double *s_sums) {
+// Jackknife attribution of a sky pair: jk_check_sky (jk.cpp:53-57), each
+// region whose galaxy has jk_prob >= 0.5 (same region: g1's only).
+__device__ __forceinline__ int sky_regions(int r1, int keep1, int r2, int keep2, int rs[2]) {
+  int n = 0;
+  if (keep1) rs[n++] = r1;
+  if (r2 != r1 && keep2) rs[n++] = r2;
+  return n;
+}
+
+// FP64 values of a pair from the FP64 path: global FP64 atomics (rare pairs),
+// corel_jk1 (jk.cpp:138-171) for the regions.
+__device__ __forceinline__ void sky_accumulate_exact(const JobDev &J, int r1, int keep1, int r2,
+                                                     int keep2, int64_t cell,
+                                                     const double f[kNF]) {
   const int nf = J.corel == COREL_DD ? 1 : kNF;
-  if (SMEM) {
-    atomicAdd(&s_num[cell], 1ull);
-    for (int q = 0; q < nf; q++)
-      if (f[q] != 0) atomicAdd(&s_sums[cell * kNF + q], (double)f[q]);
-  } else {
-    atomicAdd(&J.acc_num[cell], 1ull);
-    for (int q = 0; q < nf; q++)
-      if (f[q] != 0) atomicAdd(&J.acc_sums[cell * kNF + q], (double)f[q]);
-  }
+  atomicAdd(&J.acc_num[cell], 1ull);
+  for (int q = 0; q < nf; q++)
+    if (f[q] != 0) atomicAdd(&J.acc_sums[cell * kNF + q], f[q]);
   if (!J.do_jk) return;
-  const int k1 = r.keep, k2 = (r2 == r.jk) ? 0 : keep2;
   const int64_t hstride = (int64_t)J.nrp * J.npi;
-  const int rs[2] = {r.jk, r2};
-  const int ks[2] = {k1, k2};
-  for (int t = 0; t < 2; t++) {
-    if (!ks[t]) continue;
+  int rs[2];
+  const int nr = sky_regions(r1, keep1, r2, keep2, rs);
+  for (int t = 0; t < nr; t++) {
     const int64_t hc = (int64_t)(1 + rs[t]) * hstride + cell;
     atomicAdd(&J.acc_num[hc], 1ull);
     double *sj = J.acc_sums + hc * kNF;
-    if (f[0] != 0) atomicAdd(&sj[0], (double)f[0]);
-    if (J.which_corr == 0 || nf == 1) continue;  // f holds nf values
+    if (f[0] != 0) atomicAdd(&sj[0], f[0]);
+    if (J.which_corr == 0 || nf == 1) continue;
     for (int q = 1; q < kNF; q += 2)
-      if (f[q] != 0) atomicAdd(&sj[q], (double)f[q]);
+      if (f[q] != 0) atomicAdd(&sj[q], f[q]);
+  }
+}
+
+// FP32 values of a pair from the mixed-precision path as fixed-point integers
+// rint(v 2^S_f), |v| 2^S_f <= 2^28 (S_f from bounds on |v|), added as 64-bit
+// integers: the main histogram in shared memory (SMEM) or in the global
+// fixed-point block, the regions in the global fixed-point block.  Field 0
+// (the weight) is skipped when every weight is 1 (wt_num = count).
+template <bool SMEM>
+__device__ __forceinline__ void sky_accumulate_fixed(const JobDev &J, int r1, int keep1, int r2,
+                                                     int keep2, int64_t cell, const float *v,
+                                                     int nf, const float *s_qs,
+                                                     unsigned long long *s_num,
+                                                     unsigned long long *s_fix) {
+  const int f0 = J.unit_w ? 1 : 0;
+  auto fx = [&](int q) {
+    return (unsigned long long)(long long)__float2int_rn(v[q] * s_qs[q]);
+  };
+  unsigned long long *mfix = SMEM ? s_fix : J.acc_fix;
+  atomicAdd(SMEM ? &s_num[cell] : &J.acc_num[cell], 1ull);
+#pragma unroll
+  for (int q = 0; q < kNF; q++)  // constant indices: v stays in registers
+    if (q >= f0 && q < nf && v[q] != 0.0f) atomicAdd(&mfix[cell * kNF + q], fx(q));
+  if (!J.do_jk) return;
+  const int64_t hstride = (int64_t)J.nrp * J.npi;
+  int rs[2];
+  const int nr = sky_regions(r1, keep1, r2, keep2, rs);
+  for (int t = 0; t < nr; t++) {
+    const int64_t hc = (int64_t)(1 + rs[t]) * hstride + cell;
+    atomicAdd(&J.acc_num[hc], 1ull);
+    unsigned long long *sj = J.acc_fix + hc * kNF;
+    if (f0 == 0 && v[0] != 0.0f) atomicAdd(&sj[0], fx(0));
+    if (J.which_corr == 0 || nf == 1) continue;
+#pragma unroll
+    for (int q = 1; q < kNF; q += 2)
+      if (v[q] != 0.0f) atomicAdd(&sj[q], fx(q));
   }
 }
 
 // FP64 path of one window pair whose Pi and r_p may fall in the bins: exact
 // Pi bin, great-circle r_p, ambiguity test, values and accumulation.
-template <bool SMEM>
-__device__ __noinline__ void sky_pair_fp64(const JobDev &J, const SkyRow &r, const SkyView &b,
-                                              int64_t j, unsigned long long *s_num,
-                                              double *s_sums, int2 *hq,
-                                              unsigned long long *hq_n,
-                                              unsigned long long hq_cap, double esum) {
+__device__ __noinline__ void sky_pair_fp64(const JobDev &J, int64_t i, int64_t j, int2 *hq,
+                                           unsigned long long *hq_n, unsigned long long hq_cap,
+                                           double esum) {
+  const SkyView &a = J.sky1, &b = J.sky2;
+  SkyRow r;
+  r.i = i;
+  r.ra = a.d.x[i]; r.dec = a.d.y[i]; r.dc = a.dc[i]; r.da = a.da[i];
+  r.sd = a.sd[i]; r.cd = a.cd[i]; r.rar = a.rar[i]; r.decr = a.decr[i];
+  r.w = a.d.w[i]; r.e1 = a.d.e1[i]; r.e2 = a.d.e2[i]; r.phi = a.d.phi[i];
+  r.jk = a.d.jk[i]; r.keep = a.d.keep[i];
   const double dP = __dsub_rn(b.dc[j], r.dc);
   const double v2 = floor(__ddiv_rn(__dsub_rn(dP, J.pmin), J.ps));
   if (!(v2 >= 0.0) || v2 >= (double)J.npi) return;
@@ -212,8 +251,8 @@ __device__ __noinline__ void sky_pair_fp64(const JobDev &J, const SkyRow &r, con
   double f[kNF];
   pair_values(J.corel, J.gws, wt, theta, PairGal{r.e1, r.e2, r.phi},
               PairGal{b.d.e1[j], b.d.e2[j], b.d.phi[j]}, f);
-  sky_accumulate<SMEM>(J, r, b.d.jk[j], b.d.keep[j], (int64_t)(k - 1) * J.npi + (int)v2, f,
-                       s_num, s_sums);
+  sky_accumulate_exact(J, r.jk, r.keep, b.d.jk[j], b.d.keep[j], (int64_t)(k - 1) * J.npi + (int)v2,
+                       f);
 }
 
 // the row's float quantities for the mixed-precision path
@@ -243,7 +282,8 @@ __device__ __forceinline__ int band_bin(float v, float tol, int est, int n, cons
 template <bool SMEM>
 __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r, const SkyRowF &rf,
                                                const SkyView &b, const SkyFast &fb, int64_t j,
-                                               unsigned long long *s_num, double *s_sums,
+                                               unsigned long long *s_num,
+                                               unsigned long long *s_fix, const float *s_qs,
                                                int2 *hq, unsigned long long *hq_n,
                                                unsigned long long hq_cap, double esum,
                                                const float *s_A, const float *s_B,
@@ -273,7 +313,7 @@ __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r,
     if (k1 == -1) return;
   }
   if (k1 < 0 || k2 < 0) {
-    sky_pair_fp64<SMEM>(J, r, b, j, s_num, s_sums, hq, hq_n, hq_cap, esum);
+    sky_pair_fp64(J, r.i, j, hq, hq_n, hq_cap, esum);
     return;
   }
   // values: theta = atan(dDec / (dRA cos(mean Dec))) (sky_calcs.cpp:13-22)
@@ -282,7 +322,8 @@ __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r,
   const int64_t cell = (int64_t)k1 * J.npi + k2;
   if (J.corel == COREL_DD) {
     const float f0[1] = {wt};
-    sky_accumulate<SMEM>(J, r, b.d.jk[j], b.d.keep[j], cell, f0, s_num, s_sums);
+    sky_accumulate_fixed<SMEM>(J, r.jk, r.keep, b.d.jk[j], b.d.keep[j], cell, f0, 1, s_qs, s_num,
+                               s_fix);
   } else {
     const float4 sh2 = fb.ss[j];
     const float dra = (w2.x - rf.w.x) + (x2.x - rf.x.x);
@@ -336,7 +377,8 @@ __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r,
       const float xa = wt * (ei1 * ej0) * 0.5f, xb = wt * ei0 * ej1 * 0.5f;
       v[10] = xa * xa + xb * xb;
     }
-    sky_accumulate<SMEM>(J, r, b.d.jk[j], b.d.keep[j], cell, v, s_num, s_sums);
+    sky_accumulate_fixed<SMEM>(J, r.jk, r.keep, b.d.jk[j], b.d.keep[j], cell, v, kNF, s_qs, s_num,
+                               s_fix);
   }
 }
 
@@ -361,14 +403,15 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
   const int ncell = J.nrp * J.npi;
   for (int k = threadIdx.x; k < J.nrp; k += blockDim.x) { s_A[k] = J.A[k]; s_B[k] = J.B[k]; }
   for (int k = threadIdx.x; k < J.npi; k += blockDim.x) { s_PA[k] = J.PA[k]; s_PB[k] = J.PB[k]; }
-  if (!SMEM) __syncthreads();
+  __shared__ float s_qs[kNF];
+  if (threadIdx.x < kNF) s_qs[threadIdx.x] = J.qscale[threadIdx.x];
   unsigned long long *s_num = reinterpret_cast<unsigned long long *>(sky_smem);
-  double *s_sums = reinterpret_cast<double *>(s_num + ncell);
+  unsigned long long *s_fix = s_num + ncell;
   if (SMEM) {
     for (int c = threadIdx.x; c < ncell; c += blockDim.x) s_num[c] = 0ull;
-    for (int c = threadIdx.x; c < ncell * kNF; c += blockDim.x) s_sums[c] = 0.0;
-    __syncthreads();
+    for (int c = threadIdx.x; c < ncell * kNF; c += blockDim.x) s_fix[c] = 0ull;
   }
+  __syncthreads();  // bands, scales, zeroed histograms
   const unsigned FULL = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int *q = s_q[warp];
@@ -461,7 +504,7 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
       count += __popc(m);
       __syncwarp();
       if (count >= 32) {
-        sky_pair_mixed<SMEM>(J, r, rf, b, fb, q[lane], s_num, s_sums, hq, hq_n, hq_cap, esum, s_A,
+        sky_pair_mixed<SMEM>(J, r, rf, b, fb, q[lane], s_num, s_fix, s_qs, hq, hq_n, hq_cap, esum, s_A,
                              s_B, s_PA, s_PB);
         __syncwarp();
         if (lane < count - 32) q[lane] = q[lane + 32];
@@ -470,7 +513,7 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
       }
     }
     if (lane < count)
-      sky_pair_mixed<SMEM>(J, r, rf, b, fb, q[lane], s_num, s_sums, hq, hq_n, hq_cap, esum, s_A,
+      sky_pair_mixed<SMEM>(J, r, rf, b, fb, q[lane], s_num, s_fix, s_qs, hq, hq_n, hq_cap, esum, s_A,
                            s_B, s_PA, s_PB);
     __syncwarp();
   }
@@ -482,15 +525,34 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
       if (!v) continue;
       atomicAdd(&J.acc_num[c], v);
       for (int f = 0; f < kNF; f++) {
-        const double x = s_sums[c * kNF + f];
-        if (x != 0.0) atomicAdd(&J.acc_sums[c * kNF + f], x);
+        const unsigned long long x = s_fix[c * kNF + f];
+        if (x != 0ull) atomicAdd(&J.acc_fix[c * kNF + f], x);
       }
     }
   }
 }
 
 size_t sky_warp_smem_bytes(int nrp, int npi) {
-  return (size_t)nrp * npi * (sizeof(unsigned long long) + kNF * sizeof(double));
+  return (size_t)nrp * npi * (1 + kNF) * sizeof(unsigned long long);
+}
+
+// fixed-point block -> FP64 sums: sums[i] += fix[i] 2^-S_f, f = i mod kNF
+__global__ void fix_to_sums_kernel(int64_t n, const unsigned long long *__restrict__ fix,
+                                   double *__restrict__ sums, const JobDev *__restrict__ jobp) {
+  const JobDev &J = *jobp;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const long long v = (long long)fix[i];
+    if (v != 0) sums[i] += (double)v * J.inv_qscale[i % kNF];
+  }
+}
+
+cudaError_t launch_fix_to_sums(int64_t n, const unsigned long long *fix, double *sums,
+                               const JobDev *job, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4096);
+  fix_to_sums_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, fix, sums, job);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_sky_warp(const JobDev *job, const SkyView &a, const SkyView &b,
