@@ -47,7 +47,7 @@
 
 #define CPC_NF 13 /* wt, d1v,d1e, d2v,d2e, d3v,d3e, d4v,d4e, d5v,d5e, d6v,d6e */
 
-enum { ORC_SD = 0, ORC_SRD = 1, ORC_DRS = 2, ORC_RSRD = 3, ORC_RSRS = 4, ORC_SRS = 5 };
+enum { ORC_SD = 0, ORC_SRD = 1, ORC_DRS = 2, ORC_RSRD = 3, ORC_RSRS = 4, ORC_SRS = 5, ORC_SS = 6 };
 enum { COREL_DD = 0, COREL_SD = 1, COREL_SS = 2 };
 
 typedef struct {
@@ -401,6 +401,112 @@ int orc_corels2(const orc_params *p, int kind, const orc_cat *ga, const orc_cat 
               double yy = g2->y[j] + sy;
               if (yy > w.dec_max || yy < w.dec_min) continue;
               double xx = g2->x[j] + sx;
+              if (xx < w.ra_min || xx > w.ra_max) continue;
+              h.n_out += corel_pair(&c, &h, i, j, PBx, PBy, PBz);
+              h.n_total++;
+            }
+          }
+        }
+      }
+    }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+    {
+      for (int64_t t = 0; t < hsize; t++) num[t] += h.num[t];
+      for (int64_t t = 0; t < hsize * CPC_NF; t++) sums[t] += h.sums[t];
+    }
+    tot += h.n_total;
+    out += h.n_out;
+    free(h.num);
+    free(h.sums);
+  }
+  if (err) return -4;
+  counters[0] = tot;
+  counters[1] = tot - out;
+  return 0;
+}
+
+/* corels1 (corr.cpp:103-216): pairs within one catalogue, each counted once.
+ * For outer row i and each image (lim_calc as in corels2) the scan starts at
+ * j = i + 1, except that with data_sorted != 0 the +1 z image starts at j = 0
+ * (corr.cpp:171-178); with data_sorted 1 it stops at the first redshift
+ * failure (do_pair_sorted, corr.cpp:67-86: ret_z), so an image whose first
+ * scanned row already fails the lower redshift bound contributes nothing.
+ * g_with_shape = 1 (corr.cpp:112); corel: do_RsRs -> density_density, do_SS ->
+ * shape_shape for which_corr 1, 2 (initialization.cpp:490-520).
+ * kind: ORC_SS (do_SS) or ORC_RSRS (do_RsRs). */
+int orc_corels1(const orc_params *p, int kind, const orc_cat *g, int64_t *num, double *sums,
+                int64_t *counters) {
+  if (p->sig_crit != 0) return -2;
+  if (p->coordinates != 6 && p->coordinates != 0) return -2;
+  if (p->coordinates == 0 && p->periodic_box) return -2;
+  counters[0] = counters[1] = 0;
+  job_t job;
+  job.swapped = 0;
+  job.g_with_shape = 1;
+  if (kind == ORC_RSRS) job.corel = COREL_DD;
+  else if (kind == ORC_SS) job.corel = (p->which_corr == 0) ? COREL_DD : COREL_SS;
+  else return -1;
+  job.include_prob_max = (kind == ORC_RSRS) ? p->include_prob_rr : 1.0;
+  if (g->n == 0) return 0;
+  int n_hist = 1 + (p->do_jk ? p->n_jk : 0);
+  if (p->do_jk)
+    for (int64_t t = 0; t < g->n; t++) if (!g->jk || g->jk[t] < 0 || g->jk[t] >= p->n_jk) return -3;
+  ctx_t c;
+  c.p = p; c.job = &job; c.g1 = g; c.g2 = g; c.n_hist = n_hist;
+  c.p_size = (p->p_max - p->p_min) / (p->n_p_bin);
+  if (p->lin_bin) c.r_size = (p->bin_r_max - p->bin_r_min) / p->n_bins;
+  else c.r_size = (log10(p->bin_r_max) - log10(p->bin_r_min)) / p->n_bins;
+  int64_t hsize = (int64_t)n_hist * p->n_bins * p->n_p_bin;
+  memset(num, 0, sizeof(int64_t) * hsize);
+  memset(sums, 0, sizeof(double) * hsize * CPC_NF);
+  int64_t stride = p->row_stride > 0 ? p->row_stride : 1, off = p->row_offset;
+  int nthr = p->n_threads;
+#ifdef _OPENMP
+  if (nthr <= 0) nthr = omp_get_num_procs();
+#else
+  nthr = 1;
+#endif
+  int err = 0;
+  int64_t tot = 0, out = 0;
+  const int64_t n = g->n;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nthr) reduction(+ : tot, out)
+#endif
+  {
+    hist_t h;
+    h.num = (int64_t *)calloc(hsize, sizeof(int64_t));
+    h.sums = (double *)calloc(hsize * CPC_NF, sizeof(double));
+    h.n_total = h.n_out = 0;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 100)
+#endif
+    for (int64_t i = 0; i < n; i++) {
+      if (((i - off) % stride) != 0) continue;
+      if (g->include_prob && g->include_prob[i] > job.include_prob_max) continue;
+      window_t w;
+      if (p->coordinates == 6) lim_box(p, g->x[i], g->y[i], g->z[i], &w);
+      else if (lim_sky(p, g->x[i], g->y[i], g->z[i], &w) != 0) { err = 1; continue; }
+      int xt = w.PBx, yt = w.PBy, zt = w.PBz;
+      int PBx = xt > 0;
+      for (int xi = 0; xi <= abs(xt); xi++, PBx--) {
+        int PBy = yt > 0;
+        for (int yi = 0; yi <= abs(yt); yi++, PBy--) {
+          int PBz = zt > 0;
+          for (int zi = 0; zi <= abs(zt); zi++, PBz--) {
+            double sz = p->box * PBz, sy = p->box * PBy, sx = p->box * PBx;
+            if (p->coordinates != 6) sz = sy = sx = 0;
+            int64_t j = i + 1;
+            if (p->data_sorted != 0 && PBz > 0) j = 0;
+            const int sorted = p->data_sorted == 1;
+            for (; j < n; j++) {
+              if (g->include_prob && g->include_prob[j] > job.include_prob_max) continue;
+              double zz = g->z[j] + sz;
+              if (zz > w.z_max || zz < w.z_min) { if (sorted) break; continue; }
+              double yy = g->y[j] + sy;
+              if (yy > w.dec_max || yy < w.dec_min) continue;
+              double xx = g->x[j] + sx;
               if (xx < w.ra_min || xx > w.ra_max) continue;
               h.n_out += corel_pair(&c, &h, i, j, PBx, PBy, PBz);
               h.n_total++;

@@ -25,7 +25,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libcpc_oracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
 NF = 13  # wt, d1v, d1e, ..., d6v, d6e
-KIND = {"SD": 0, "SRd": 1, "DRs": 2, "RsRd": 3, "RsRs": 4, "SRs": 5}
+KIND = {"SD": 0, "SRd": 1, "DRs": 2, "RsRd": 3, "RsRs": 4, "SRs": 5, "SS": 6}
 JK_SEED = 124693517  # jk.cpp:40-43
 RAND_MAX = 2147483647
 
@@ -75,6 +75,10 @@ def lib():
         _lib.orc_corels2.argtypes = [ctypes.POINTER(_Params), ctypes.c_int,
                                      ctypes.POINTER(_Cat), ctypes.POINTER(_Cat),
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        _lib.orc_corels1.restype = ctypes.c_int
+        _lib.orc_corels1.argtypes = [ctypes.POINTER(_Params), ctypes.c_int,
+                                     ctypes.POINTER(_Cat), ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p]
         _lib.orc_elip_angle.restype = None
         _lib.orc_elip_angle.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p]
@@ -174,6 +178,46 @@ def read_like_reference(params, cats_in_read_order, table=None):
         out[role] = OracleCatalog(c.x, c.y, c.z, w=w, e1=e1, e2=e2, phi=phi, jk=jk,
                                   jk_prob=jkp, include_prob=inc, dc=dc, da=da)
     return out
+
+
+def _params_struct(p, n_threads, row_stride, row_offset, H_z, dA_z, z_sep_max):
+    P = _Params()
+    P.which_corr, P.coordinates, P.estimator = p.which_corr, p.coordinates, p.estimator
+    P.periodic_box, P.data_sorted, P.do_jk = int(p.periodic_box), p.data_sorted, p.do_jk
+    P.n_jk, P.lin_bin, P.n_bins, P.n_p_bin = p.n_jk_regions, int(p.lin_bin), p.n_bins, p.n_p_bin
+    P.sig_crit = p.sig_crit
+    P.bin_r_min, P.bin_r_max, P.p_min, P.p_max = p.bin_r_min, p.bin_r_max, p.p_min, p.p_max
+    P.box = p.periodic_box_size
+    P.include_prob_rr = 1.0
+    P.z_max_data, P.dz = p.z_max, p.dz
+    P.z_sep_max = p.z_sep_max if z_sep_max is None else z_sep_max
+    keep = []
+    if H_z is not None:
+        H_z = np.ascontiguousarray(H_z, dtype=np.float64)
+        dA_z = np.ascontiguousarray(dA_z, dtype=np.float64)
+        keep += [H_z, dA_z]
+        P.H_z, P.dA_z, P.n_table = H_z.ctypes.data, dA_z.ctypes.data, H_z.shape[0]
+    P.n_threads, P.row_stride, P.row_offset = n_threads, row_stride, row_offset
+    return P, keep
+
+
+def port_corels1(params, kind: str, g: OracleCatalog, *, n_threads: int = 0,
+                 row_stride: int = 1, row_offset: int = 0, H_z=None, dA_z=None,
+                 z_sep_max: float | None = None):
+    """The C restatement of corels1 (auto pairs of one catalogue); kind "SS"
+    (do_SS) or "RsRs" (do_RsRs).  Same return values as port_corels2."""
+    p = params
+    P, keep = _params_struct(p, n_threads, row_stride, row_offset, H_z, dA_z, z_sep_max)
+    n_hist = 1 + (p.n_jk_regions if p.do_jk else 0)
+    num = np.zeros((n_hist, p.n_bins, p.n_p_bin), dtype=np.int64)
+    sums = np.zeros((n_hist, p.n_bins, p.n_p_bin, NF), dtype=np.float64)
+    cnt = np.zeros(2, dtype=np.int64)
+    cg = g.cstruct()
+    rc = lib().orc_corels1(ctypes.byref(P), KIND[kind], ctypes.byref(cg), num.ctypes.data,
+                           sums.ctypes.data, cnt.ctypes.data)
+    if rc != 0:
+        raise ValueError(f"orc_corels1 failed with code {rc}")
+    return num, sums, int(cnt[0]), int(cnt[1])
 
 
 def port_corels2(params, kind: str, ga: OracleCatalog, gb: OracleCatalog, *,

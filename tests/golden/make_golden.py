@@ -31,7 +31,11 @@ from corr_pc_gb300 import synth  # noqa: E402
 KEEP_FILES = ["bins_cross_final.dat", "bins2D_cross_final.dat", "bins_cross_SD.dat",
               "bins2D_cross_SD.dat", "bins_cross_RR.dat", "bins2D_cross_RR.dat",
               "bins_cross_SR.dat", "bins_cross_jk0_final.dat", "bins2D_cross_jk0_SD.dat",
-              "bins_cross_jk_final.dat", "bins2D_cross_jk_final.dat", "inp2.info"]
+              "bins_cross_jk_final.dat", "bins2D_cross_jk_final.dat", "inp2.info",
+              "bins_auto_final.dat", "bins2D_auto_final.dat", "bins_auto_SS.dat",
+              "bins2D_auto_SS.dat", "bins_auto_RR.dat", "bins2D_auto_RR.dat", "bins_auto_SR.dat",
+              "bins_auto_jk0_final.dat", "bins2D_auto_jk0_SS.dat", "bins_auto_jk_final.dat",
+              "bins2D_auto_jk_final.dat"]
 
 
 def lattice(n, L, seed, jk_side):
@@ -220,6 +224,79 @@ def run_sky_case(name, wl, same):
     print(f"{name}: " + " ".join(f"{t}={dump[t]['n_in']}" for t in SKY_TERMS))
 
 
+def auto_cases():
+    """Auto-correlation runs (estimator 1: corels1 on S; estimator 2 adds the
+    Pi re-binning).  A periodic box counts SS only; the sky adds SRs and RsRs."""
+    out = []
+    c = synth.uniform_box(2500, 100.0, 51, nside_jk=2)
+    p = synth._box_params(which_corr=0, L=100.0, rmin=0.5, rmax=20.0, nrp=8, npi=12, pmax=30.0,
+                          njk=8, n=c.n)
+    p.estimator = 1
+    out.append(("auto_box_wgg", p, c, None, None))
+
+    c = synth.uniform_box(2000, 100.0, 52, nside_jk=2, with_shapes=True)
+    p = synth._box_params(which_corr=2, L=100.0, rmin=0.3, rmax=25.0, nrp=10, npi=10, pmax=30.0,
+                          njk=8, n=c.n)
+    p.estimator = 2
+    out.append(("auto_box_wpp_rebin", p, c, None, None))
+
+    c = synth.neyman_scott(30, 60.0, 2.0, 100.0, 53, nside_jk=2)
+    c = c.subset(np.random.default_rng(54).permutation(c.n))
+    p = synth._box_params(which_corr=1, L=100.0, rmin=0.2, rmax=25.0, nrp=10, npi=10, pmax=30.0,
+                          njk=8, n=c.n)
+    p.estimator = 1
+    p.data_sorted = 0
+    out.append(("auto_box_wgp_unsorted", p, c, None, None))
+
+    p = synth._sky_params(which_corr=1, rmin=0.3, rmax=30.0, nrp=8, npi=12, pmax=40.0, njk=9,
+                          z_max=0.5)
+    p.dz = 0.001
+    p.estimator = 1
+    t = synth.flat_lcdm_table(p.z_max, p.dz)
+    d = synth.sky_patch(1500, 55, t, ra_deg=6, dec_deg=6, chi_range=(500, 900), nside_jk=3,
+                        with_shapes=True, weights=True)
+    r = synth.sky_patch(4000, 56, t, ra_deg=6, dec_deg=6, chi_range=(500, 900), nside_jk=3)
+    out.append(("auto_sky_wgp", p, d, r, t))
+    return out
+
+
+def run_auto_case(name, p, S, R, table):
+    with tempfile.TemporaryDirectory() as tmp:
+        if table is None:
+            inp = synth.write_box_run(tmp, synth.Workload(name, p, S, S), same_files=True,
+                                      n_threads=1)
+        else:
+            inp = synth.write_sky_run(tmp, synth.SkyWorkload(name, p, table, S, S, R, R),
+                                      n_threads=1)
+        totals, _ = oracle.run_reference(inp, os.path.join(tmp, "dump.txt"), bining=True)
+        dump = oracle.parse_dump(os.path.join(tmp, "dump.txt"))
+        files = {}
+        for f in KEEP_FILES:
+            fp = os.path.join(tmp, "out", "run_" + f)
+            if os.path.exists(fp):
+                files[f] = open(fp).read()
+        params = {a: getattr(p, a) for _k, a, _t in synth.INP_KEYS}
+    terms = list(dump.keys())
+    arrays = {}
+    if table is not None:
+        arrays.update({"table_H": table.H, "table_DC": table.DC, "table_DA": table.DA})
+    for role, c in (("S", S), ("Rs", R)):
+        if c is None:
+            continue
+        for a in ("x", "y", "z", "w", "e1", "e2", "jk"):
+            v = getattr(c, a)
+            if v is not None:
+                arrays[f"{role}_{a}"] = v
+    for k, term in enumerate(terms):
+        arrays[f"{term}_raw_num"] = dump[term]["raw_num"]
+        arrays[f"{term}_raw_sums"] = dump[term]["raw_sums"]
+        arrays[f"{term}_n_in"] = np.array(dump[term]["n_in"])
+        arrays[f"{term}_n_total"] = np.array(totals[k][0])
+    meta = {"name": name, "params": params, "files": files, "terms": terms}
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **arrays)
+    print(f"{name}: " + " ".join(f"{t}={dump[t]['n_in']}" for t in terms))
+
+
 def main():
     oracle.build_reference()
     only = sys.argv[1:]
@@ -229,6 +306,9 @@ def main():
     for name, wl, same in sky_cases():
         if not only or name in only:
             run_sky_case(name, wl, same)
+    for name, p, S, R, table in auto_cases():
+        if not only or name in only:
+            run_auto_case(name, p, S, R, table)
 
 
 if __name__ == "__main__":

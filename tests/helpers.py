@@ -24,6 +24,46 @@ def sky_golden_names():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "sky_*.npz")))
 
 
+def auto_golden_names():
+    """Auto-correlation fixtures (estimator 1/2: SS by corels1; the sky also SRs
+    by corels2 and RsRs by corels1)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "auto_*.npz")))
+
+
+class AutoGolden:
+    """An auto-correlation run as the reference computed it."""
+
+    def __init__(self, name):
+        z = np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False)
+        self.meta = json.loads(str(z["meta"]))
+        self.arr = {k: z[k] for k in z.files if k != "meta"}
+        p = synth.InpParams()
+        for k, v in self.meta["params"].items():
+            setattr(p, k, v)
+        self.params = p
+        a = self.arr
+        self.table = None
+        if "table_H" in a:
+            self.table = synth.DistanceTable(p.dz * np.arange(a["table_H"].shape[0]),
+                                             a["table_H"], a["table_DA"], a["table_DC"])
+        self.cats = {}
+        for r in ("S", "Rs"):
+            if f"{r}_x" in a:
+                g = lambda q: a.get(f"{r}_{q}")
+                self.cats[r] = synth.Catalog(g("x"), g("y"), g("z"), g("w"), g("e1"), g("e2"),
+                                             g("jk"))
+        self.terms = self.meta["terms"]
+        self.files = self.meta["files"]
+
+    def read_order(self):
+        return [(r, self.cats[r]) for r in ("S", "Rs") if r in self.cats]
+
+    def term(self, t):
+        a = self.arr
+        return (a[f"{t}_raw_num"], a[f"{t}_raw_sums"], int(a[f"{t}_n_in"]),
+                int(a[f"{t}_n_total"]))
+
+
 class SkyGolden:
     """A sky cross run as the reference computed it: four catalogues, the
     distances table and, per term, the raw histograms and pair counters.  The

@@ -7,7 +7,7 @@ import oracle
 import copy
 
 from corr_pc_gb300 import synth
-from helpers import Golden, SkyGolden, golden_names, sky_golden_names
+from helpers import AutoGolden, Golden, SkyGolden, auto_golden_names, golden_names, sky_golden_names
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -74,6 +74,34 @@ def test_port_matches_reference_sky(name):
         num, sums, n_total, n_in = oracle.port_corels2(pp, kind, cats[a], cats[b], n_threads=2,
                                                        H_z=g.table.H, dA_z=g.table.transverse,
                                                        z_sep_max=zsep)
+        rnum, rsums, rin, rtot = g.term(t)
+        assert (n_in, n_total) == (rin, rtot), t
+        assert np.array_equal(num, rnum), t
+        scale = np.abs(rsums).max(axis=(0, 1, 2)) + 1e-300
+        assert (np.abs(sums - rsums) / scale).max() < 1e-12, t
+
+
+@pytest.mark.parametrize("name", auto_golden_names())
+def test_port_corels1_matches_reference(name):
+    """corels1 (one catalogue, each pair once by index order, the +1 z image
+    from row 0 when sorted) and the auto run's other terms."""
+    g = AutoGolden(name)
+    p = g.params
+    cats = oracle.read_like_reference(p, g.read_order(), table=g.table)
+    kw = {}
+    if g.table is not None:
+        kw = dict(H_z=g.table.H, dA_z=g.table.transverse,
+                  z_sep_max=synth.derived_z_sep(p, g.table)[0])
+    for t in g.terms:
+        if t == "SS":
+            res = oracle.port_corels1(p, "SS", cats["S"], n_threads=2, **kw)
+        elif t == "RsRs":
+            res = oracle.port_corels1(p, "RsRs", cats["Rs"], n_threads=2, **kw)
+        elif t == "SRs":
+            res = oracle.port_corels2(p, "SRs", cats["Rs"], cats["S"], n_threads=2, **kw)
+        else:
+            raise AssertionError(t)
+        num, sums, n_total, n_in = res
         rnum, rsums, rin, rtot = g.term(t)
         assert (n_in, n_total) == (rin, rtot), t
         assert np.array_equal(num, rnum), t
