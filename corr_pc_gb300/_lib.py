@@ -19,7 +19,7 @@ STATUS_NAMES = {0: "CPC_OK", 1: "CPC_ERR_INVALID", 2: "CPC_ERR_CUDA", 3: "CPC_ER
                 4: "CPC_ERR_TIMEOUT", 5: "CPC_ERR_STATE", 6: "CPC_ERR_RANGE",
                 7: "CPC_ERR_NODEVICE"}
 # cpc_pair_kind (the data_info.do_* flag of each corels2 call)
-PAIR = {"SD": 0, "SRd": 1, "DRs": 2, "RsRd": 3, "RsRs": 4, "SRs": 5}
+PAIR = {"SD": 0, "SRd": 1, "DRs": 2, "RsRd": 3, "RsRs": 4, "SRs": 5, "SS": 6}
 ENGINE = {"fast": 0, "fp64": 1}
 NF = 13
 
@@ -83,6 +83,7 @@ def load() -> ctypes.CDLL:
     lib.cpc_destroy.argtypes = [V]
     lib.cpc_upload.argtypes = [V, I, P(cpc_catalog)]
     lib.cpc_count.argtypes = [V, I, I, I, I, I64, I64, P(cpc_accum)]
+    lib.cpc_count_auto.argtypes = [V, I, I, I, I64, I64, P(cpc_accum)]
     lib.cpc_accum_shape.argtypes = [V, P(I), P(I), P(I)]
     lib.cpc_count_batch.argtypes = [I, P(V), P(I), P(I), P(I), P(cpc_accum)]
     lib.cpc_set_tuning.argtypes = [V, I, I, I]
@@ -96,7 +97,8 @@ def load() -> ctypes.CDLL:
                                            P(cpc_device_catalog), V, V, P(I64), P(I64), V,
                                            ctypes.c_char_p, ctypes.c_size_t]
     lib.cpc_count_fp64_noalloc.restype = I
-    for fn in ("cpc_create", "cpc_destroy", "cpc_upload", "cpc_count", "cpc_accum_shape",
+    for fn in ("cpc_create", "cpc_destroy", "cpc_upload", "cpc_count", "cpc_count_auto",
+               "cpc_accum_shape",
                "cpc_count_batch", "cpc_set_tuning", "cpc_host_rand_uniform",
                "cpc_host_elip_angle", "cpc_host_rp_thresholds", "cpc_host_pi_thresholds",
                "cpc_launch_count", "cpc_host_finalize_cross"):
@@ -219,6 +221,18 @@ class Context:
         acc, num, sums = self.new_accum()
         check(self.lib.cpc_count(self.h, PAIR[kind], slot_g1, slot_g2, ENGINE[engine],
                                  row_stride, row_offset, ctypes.byref(acc)), self.h)
+        return {"num": num, "sums": sums, "n_window": acc.n_window, "n_binned": acc.n_binned,
+                "n_rechecked": acc.n_rechecked, "kernel_ms": acc.kernel_ms,
+                "pair_kernel_ms": acc.pair_kernel_ms}
+
+
+    def count_auto(self, kind: str, slot: int, engine: str = "fast", row_stride: int = 1,
+                   row_offset: int = 0) -> dict:
+        """One corels1 call (auto pairs of the catalogue in `slot`), kind "SS"
+        or "RsRs": RAW region sums like count()."""
+        acc, num, sums = self.new_accum()
+        check(self.lib.cpc_count_auto(self.h, PAIR[kind], slot, ENGINE[engine], row_stride,
+                                      row_offset, ctypes.byref(acc)), self.h)
         return {"num": num, "sums": sums, "n_window": acc.n_window, "n_binned": acc.n_binned,
                 "n_rechecked": acc.n_rechecked, "kernel_ms": acc.kernel_ms,
                 "pair_kernel_ms": acc.pair_kernel_ms}

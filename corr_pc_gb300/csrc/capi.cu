@@ -76,6 +76,7 @@ struct Slot {
   DevBuf<int32_t> jk;
   DevBuf<uint8_t> keep;
   DevBuf<int64_t> orig;
+  DevBuf<uint8_t> aflag;  // corels1 scan-start flags of each row (cell order)
   DevBuf<int> bk_start, bk_end, bk_region, col_begin, col_end;
   DevBuf<float> bk_zmin, bk_zmax;
   // host copies used to build work units
@@ -85,7 +86,7 @@ struct Slot {
   bool zbuilt = false;
   DevBuf<double> zx, zy, zz, zw, ze1, ze2, zphi;
   DevBuf<int32_t> zjk;
-  DevBuf<uint8_t> zkeep;
+  DevBuf<uint8_t> zkeep, zaflag;
   DevBuf<int64_t> zorig;
   // sky (coordinates 0): x, y, z, w, e1, e2, phi, jk, keep, orig above hold the
   // redshift-ordered catalogue; these the sky-only per-galaxy quantities
@@ -240,6 +241,20 @@ int job_rule(const cpc_params &p, cpc_pair_kind kind, int64_t n1, int64_t n2, Jo
   return 0;
 }
 
+// corels1's rules (corr.cpp:103-216): g_with_shape = 1, no swap; corel by
+// choose_corel_func (initialization.cpp:490-520) with do_RsRs or do_SS set.
+int job_rule_auto(const cpc_params &p, cpc_pair_kind kind, JobRule &r) {
+  int corel;
+  if (kind == CPC_PAIR_RSRS) corel = COREL_DD;
+  else if (kind == CPC_PAIR_SS) corel = p.which_corr == 0 ? COREL_DD : COREL_SS;
+  else return -1;
+  if (corel == COREL_SS && p.estimator != 0) corel = COREL_SSA;
+  r.swapped = 0;
+  r.corel = corel;
+  r.gws = 1;
+  return 0;
+}
+
 void fill_views(Slot &s, FCat &f, DCat &d) {
   f.n = s.n;
   f.pos = s.pos.p;
@@ -247,6 +262,7 @@ void fill_views(Slot &s, FCat &f, DCat &d) {
   f.lo = s.lo.p;
   f.zf = s.zf.p;
   f.keep = s.keep.p;
+  f.aflag = s.aflag.p;
   f.bk_start = s.bk_start.p;
   f.bk_end = s.bk_end.p;
   f.bk_region = s.bk_region.p;
@@ -257,7 +273,7 @@ void fill_views(Slot &s, FCat &f, DCat &d) {
   d.n = s.n;
   d.x = s.x.p; d.y = s.y.p; d.z = s.z.p; d.w = s.w.p;
   d.e1 = s.e1.p; d.e2 = s.e2.p; d.phi = s.phi.p;
-  d.jk = s.jk.p; d.keep = s.keep.p; d.orig = s.orig.p;
+  d.jk = s.jk.p; d.keep = s.keep.p; d.orig = s.orig.p; d.aflag = s.aflag.p;
 }
 
 // error bound (absolute, per coordinate difference) of the FP32 separations
@@ -285,7 +301,7 @@ struct JobPlan {
 };
 
 cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, int64_t rs,
-                    int64_t ro, cpc_accum *out, JobPlan &jp) {
+                    int64_t ro, cpc_accum *out, JobPlan &jp, int auto_mode = 0) {
   if (slot_g1 < 0 || slot_g1 >= kMaxSlots || slot_g2 < 0 || slot_g2 >= kMaxSlots)
     return fail(c, CPC_ERR_INVALID, "slot out of range");
   Slot &A = c->slots[slot_g1], &B = c->slots[slot_g2];
@@ -297,7 +313,8 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   jp.out = out;
   jp.row_stride = rs > 1 ? rs : 1;
   jp.row_offset = ro;
-  if (job_rule(p, kind, A.n, B.n, jp.rule) != 0) return fail(c, CPC_ERR_INVALID, "bad pair kind");
+  if ((auto_mode ? job_rule_auto(p, kind, jp.rule) : job_rule(p, kind, A.n, B.n, jp.rule)) != 0)
+    return fail(c, CPC_ERR_INVALID, "bad pair kind");
   jp.s1 = jp.rule.swapped ? slot_g2 : slot_g1;
   jp.s2 = jp.rule.swapped ? slot_g1 : slot_g2;
   Slot &g1 = c->slots[jp.s1], &g2 = c->slots[jp.s2];
@@ -334,6 +351,7 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   J.wpi = wpi;
   J.lin_bin = p.lin_bin ? 1 : 0;
   J.box_same_keep = 1;  // jk_check_PB (jk.cpp:64-71) for coordinates 6
+  J.auto_mode = auto_mode;
   J.has_lo = (g1.exact_f32 && g2.exact_f32) ? 0 : 1;
   J.ncx = g1.ncx;
   J.ncy = g1.ncy;
@@ -596,6 +614,9 @@ cpc_status build_zorder(cpc_ctx *c, Slot &s) {
   out.e1 = s.ze1.p; out.e2 = s.ze2.p; out.phi = s.zphi.p; out.jk = s.zjk.p;
   out.keep = s.zkeep.p; out.orig = s.zorig.p; out.orig_in = s.orig.p;
   CK(launch_gather(n, c->d_keys.p, c->d_vals.p, in, out, st), "z gather");
+  CK(s.zaflag.alloc(n), "alloc");
+  CK(launch_gather_u8(n, c->d_vals.p, s.aflag.p, s.zaflag.p, st), "z gather");
+  c->launches += 1;
   CK(cudaStreamSynchronize(st), "sync");
   s.zbuilt = true;
   return CPC_OK;
@@ -606,7 +627,7 @@ DCat zview(Slot &s) {
   d.n = s.n;
   d.x = s.zx.p; d.y = s.zy.p; d.z = s.zz.p; d.w = s.zw.p;
   d.e1 = s.ze1.p; d.e2 = s.ze2.p; d.phi = s.zphi.p;
-  d.jk = s.zjk.p; d.keep = s.zkeep.p; d.orig = s.zorig.p;
+  d.jk = s.zjk.p; d.keep = s.zkeep.p; d.orig = s.zorig.p; d.aflag = s.zaflag.p;
   return d;
 }
 
@@ -866,12 +887,15 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   s.hs_keep.resize(n);
   std::vector<int64_t> orig(n);
   std::vector<double> wins(6 * (size_t)n);
+  std::vector<uint8_t> aflag(n);
   for (int64_t k = 0; k < n; k++) {
     const uint32_t o = perm[k];
     s.hs_jk[k] = jk[o];
     s.hs_keep[k] = keep[o];
     orig[k] = o;
     for (int q = 0; q < 6; q++) wins[(size_t)q * n + k] = win[(size_t)q * n + o];
+    // corels1 scan start: row o + 1 (input order) against z_min of row o
+    aflag[k] = (o + 1 < (uint32_t)n && !(cat->z[o + 1] < win[o])) ? kAutoStart0 : 0;
   }
   auto put = [&](DevBuf<double> &d, const std::vector<double> &h, size_t cnt) -> cudaError_t {
     cudaError_t e = d.alloc(std::max<size_t>(cnt, 1));
@@ -909,7 +933,9 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
                          st), "H2D");
   }
   CK(s.jk.alloc(nn), "alloc"); CK(s.keep.alloc(nn), "alloc"); CK(s.orig.alloc(nn), "alloc");
+  CK(s.aflag.alloc(nn), "alloc");
   if (n > 0) {
+    CK(cudaMemcpyAsync(s.aflag.p, aflag.data(), n, cudaMemcpyHostToDevice, st), "H2D");
     CK(cudaMemcpyAsync(s.jk.p, s.hs_jk.data(), 4 * n, cudaMemcpyHostToDevice, st), "H2D");
     CK(cudaMemcpyAsync(s.keep.p, s.hs_keep.data(), n, cudaMemcpyHostToDevice, st), "H2D");
     CK(cudaMemcpyAsync(s.orig.p, orig.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
@@ -924,7 +950,7 @@ SkyView sky_view(Slot &s) {
   v.d.n = s.n;
   v.d.x = s.x.p; v.d.y = s.y.p; v.d.z = s.z.p; v.d.w = s.w.p;
   v.d.e1 = s.e1.p; v.d.e2 = s.e2.p; v.d.phi = s.phi.p;
-  v.d.jk = s.jk.p; v.d.keep = s.keep.p; v.d.orig = s.orig.p;
+  v.d.jk = s.jk.p; v.d.keep = s.keep.p; v.d.orig = s.orig.p; v.d.aflag = s.aflag.p;
   v.dc = s.dc.p; v.da = s.da.p; v.sd = s.sd.p; v.cd = s.cd.p;
   v.rar = s.rar.p; v.decr = s.decr.p; v.win = s.win.p;
   return v;
@@ -932,7 +958,7 @@ SkyView sky_view(Slot &s) {
 
 // one sky corels2 call: GPU FP64 kernel, then the host edge tier
 cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, int64_t rs,
-                     int64_t ro, cpc_engine engine, cpc_accum *out) {
+                     int64_t ro, cpc_engine engine, cpc_accum *out, int auto_mode = 0) {
   if (slot_g1 < 0 || slot_g1 >= kMaxSlots || slot_g2 < 0 || slot_g2 >= kMaxSlots)
     return fail(c, CPC_ERR_INVALID, "slot out of range");
   Slot &A = c->slots[slot_g1], &B = c->slots[slot_g2];
@@ -940,7 +966,8 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
   if (!out || !out->num || !out->sums) return fail(c, CPC_ERR_INVALID, "null output arrays");
   const cpc_params &p = c->p;
   JobRule rule;
-  if (job_rule(p, kind, A.n, B.n, rule) != 0) return fail(c, CPC_ERR_INVALID, "bad pair kind");
+  if ((auto_mode ? job_rule_auto(p, kind, rule) : job_rule(p, kind, A.n, B.n, rule)) != 0)
+    return fail(c, CPC_ERR_INVALID, "bad pair kind");
   const int s1 = rule.swapped ? slot_g2 : slot_g1, s2 = rule.swapped ? slot_g1 : slot_g2;
   Slot &g1 = c->slots[s1], &g2 = c->slots[s2];
   cpc_status st_;
@@ -961,6 +988,7 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
   J.npi = p.n_p_bin;
   J.lin_bin = p.lin_bin ? 1 : 0;
   J.box_same_keep = 0;  // jk_check_sky (jk.cpp:53-57)
+  J.auto_mode = auto_mode;
   J.row_stride = rs > 1 ? rs : 1;
   J.row_offset = ro;
   J.rmin = p.bin_r_min;
@@ -1251,6 +1279,22 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
     }
     if (cat->jk_prob) keep[i] = cat->jk_prob[i] >= 0.5 ? 1 : 0;
   }
+  // corels1 scan starts (corr.cpp:165-180 with do_pair_sorted's redshift test):
+  // does the first row of each image's scan pass z >= z_min = z_i + p_min
+  // (lim_calc_PB / lim_calc_xyz)?  0 image: row i + 1; -1 image: row i + 1
+  // shifted by -L; +1 image: row 0 shifted by +L.
+  std::vector<uint8_t> aflag(n, 0);
+  for (int64_t i = 0; i < n; i++) {
+    const double zmin = cat->z[i] + p.p_min;
+    uint8_t f = 0;
+    if (i + 1 < n) {
+      const double zn = cat->z[i + 1];
+      if (!((zn + L * 0.0) < zmin)) f |= kAutoStart0;
+      if (!((zn + L * -1.0) < zmin)) f |= kAutoStartM;
+    }
+    if (!((cat->z[0] + L * 1.0) < zmin)) f |= kAutoStartP;
+    aflag[i] = f;
+  }
   // grid: columns of width >= r_max / k over [0, box)
   const int k = c->tune_k > 0 ? c->tune_k : 2;
   int nc = (int)std::floor(L / (p.bin_r_max / k));
@@ -1301,6 +1345,17 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   go.x = s.x.p; go.y = s.y.p; go.z = s.z.p; go.w = s.w.p; go.e1 = s.e1.p; go.e2 = s.e2.p;
   go.phi = s.phi.p; go.jk = s.jk.p; go.keep = s.keep.p; go.orig = s.orig.p; go.orig_in = nullptr;
   CK(launch_gather(n, c->d_keys.p, c->d_vals.p, in, go, st), "gather");
+  {
+    DevBuf<uint8_t> oflag;
+    CK(oflag.alloc(nn), "alloc");
+    CK(s.aflag.alloc(nn), "alloc");
+    if (n > 0) {
+      CK(cudaMemcpyAsync(oflag.p, aflag.data(), n, cudaMemcpyHostToDevice, st), "H2D");
+      CK(launch_gather_u8(n, c->d_vals.p, oflag.p, s.aflag.p, st), "gather");
+      c->launches += 1;
+    }
+    CK(cudaStreamSynchronize(st), "upload");
+  }
   // buckets on the host
   std::vector<uint32_t> hb(n);
   s.h_pos.resize(n);
@@ -1355,6 +1410,8 @@ cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, c
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
   if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
     return fail(c, CPC_ERR_INVALID, "unknown engine");
+  if (kind == CPC_PAIR_SS)
+    return fail(c, CPC_ERR_INVALID, "CPC_PAIR_SS pairs one catalogue: use cpc_count_auto");
   // sky: FP32-prefiltered warp kernel (fast) or plain FP64 kernel, both with
   // the FP64 path and the host edge tier for the pairs that can bin
   if (c->p.coordinates == 0)
@@ -1364,6 +1421,25 @@ cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, c
   if (s != CPC_OK) return s;
   if (engine == CPC_ENGINE_FP64) return run_plain(jobs[0]);
   if (engine != CPC_ENGINE_FAST) return fail(c, CPC_ERR_INVALID, "unknown engine");
+  return run_fast(jobs);
+}
+
+cpc_status cpc_count_auto(cpc_ctx *c, cpc_pair_kind kind, int slot, cpc_engine engine,
+                          int64_t row_stride, int64_t row_offset, cpc_accum *out) {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
+    return fail(c, CPC_ERR_INVALID, "unknown engine");
+  if (kind != CPC_PAIR_SS && kind != CPC_PAIR_RSRS)
+    return fail(c, CPC_ERR_INVALID, "auto pairs: kind must be CPC_PAIR_SS or CPC_PAIR_RSRS");
+  if (c->p.data_sorted != 0 && c->p.data_sorted != 1)
+    return fail(c, CPC_ERR_INVALID, "auto pairs: data_sorted must be 0 or 1");
+  const int mode = c->p.data_sorted == 1 ? 2 : 1;
+  if (c->p.coordinates == 0)
+    return sky_count(c, kind, slot, slot, row_stride, row_offset, engine, out, mode);
+  std::vector<JobPlan> jobs(1);
+  cpc_status s = plan_job(c, kind, slot, slot, row_stride, row_offset, out, jobs[0], mode);
+  if (s != CPC_OK) return s;
+  if (engine == CPC_ENGINE_FP64) return run_plain(jobs[0]);
   return run_fast(jobs);
 }
 

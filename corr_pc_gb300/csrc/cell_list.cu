@@ -254,4 +254,17 @@ cudaError_t launch_gather(int64_t n, const uint64_t *keys, const uint32_t *perm,
   return cudaGetLastError();
 }
 
+__global__ void gather_u8_kernel(int64_t n, const uint32_t *__restrict__ perm,
+                                 const uint8_t *__restrict__ in, uint8_t *__restrict__ out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = in[perm[k]];
+}
+
+cudaError_t launch_gather_u8(int64_t n, const uint32_t *perm, const uint8_t *in, uint8_t *out,
+                             cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  gather_u8_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, perm, in, out);
+  return cudaGetLastError();
+}
+
 }  // namespace cpc

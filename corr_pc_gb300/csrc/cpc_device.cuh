@@ -32,6 +32,7 @@ struct DCat {
   const int32_t *jk;
   const uint8_t *keep;
   const int64_t *orig;
+  const uint8_t *aflag;  // corels1 scan starts of this row (kAuto* bits)
 };
 
 // single-precision cell-list view (fast kernel)
@@ -42,6 +43,7 @@ struct FCat {
   const float2 *lo;   // x - (float)x, y - (float)y (non-float32 inputs)
   const float *zf;
   const uint8_t *keep;
+  const uint8_t *aflag;  // corels1 scan starts of this row (kAuto* bits)
   // non-empty buckets (column-major, region-minor)
   const int *bk_start, *bk_end, *bk_region;
   const float *bk_zmin, *bk_zmax;
@@ -65,6 +67,7 @@ struct JobDev {
   int corel, gws, which_corr, estimator, do_jk, n_jk;
   int periodic, coordinates, nrp, npi, wpi, lin_bin;
   int box_same_keep;        // 1 for the box (jk_check_PB), 0 for the sky
+  int auto_mode;            // 0 corels2; corels1: 1 unsorted, 2 z-sorted scan
   int has_lo;               // positions are not float32-exact: use hi+lo for theta
   int ncx, ncy;
   int64_t row_stride, row_offset;
@@ -92,6 +95,25 @@ struct JobDev {
   unsigned long long *acc_fix;         // sky fast path: fixed-point sums, layout of acc_sums
   SkyView sky1, sky2;                  // sky catalogues g1, g2 (FP64 path of the fast kernel)
 };
+
+// corels1 (corr.cpp:103-216).  The scan of row i starts at j = i + 1 (j = 0 for
+// the +1 z image when the data are sorted) and, sorted, stops at its first
+// redshift failure: an image contributes nothing when its first scanned row
+// already fails the lower bound.  Per row: whether that first row passes, for
+// the 0, -1 and +1 z images.
+constexpr uint8_t kAutoStart0 = 1, kAutoStartM = 2, kAutoStartP = 4;
+
+// Whether corels1 counts (i, j) in z image sz: auto_mode 1 (unsorted) j > i;
+// auto_mode 2 (sorted) the +1 image every j if its scan start passes, the 0
+// and -1 images j > i if theirs does.
+__host__ __device__ inline bool auto_image_all(int auto_mode, int sz, uint8_t af) {
+  return auto_mode == 0 || (auto_mode == 2 && sz == 1 && (af & kAutoStartP));
+}
+__host__ __device__ inline bool auto_image_gt(int auto_mode, int sz, uint8_t af) {
+  if (auto_mode == 1) return true;
+  if (auto_mode != 2 || sz == 1) return false;
+  return (af & (sz == 0 ? kAutoStart0 : kAutoStartM)) != 0;
+}
 
 struct UnitDesc {
   int job;

@@ -37,6 +37,9 @@ cudaError_t launch_z_keys(int64_t n, const double *z, uint64_t *keys, uint32_t *
 cudaError_t launch_gather(int64_t n, const uint64_t *keys, const uint32_t *perm, const GatherIn &in,
                           const GatherOut &out, cudaStream_t st);
 
+cudaError_t launch_gather_u8(int64_t n, const uint32_t *perm, const uint8_t *in, uint8_t *out,
+                             cudaStream_t st);
+
 // pair_fast.cu
 constexpr int kTileThreads = 128;  // g1 rows per tile (the block has 2 warp groups over them)
 size_t fast_smem_bytes(int corel, int do_jk, int NB);

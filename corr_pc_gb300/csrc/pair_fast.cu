@@ -200,6 +200,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   __shared__ int s_seg_a[kMaxSeg], s_seg_len[kMaxSeg], s_seg_key[kMaxSeg];
   __shared__ int s_order[kMaxSeg], s_pre[kMaxSeg + 1];
   __shared__ int s_jidx[kBatch];
+  __shared__ int s_orig[kBatch];  // input index of each staged candidate (corels1)
   __shared__ unsigned char s_keep[kBatch];
   __shared__ float2 s_lo[kBatch];
   __shared__ unsigned long long s_red[kThreads / 32];
@@ -256,12 +257,18 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     const int64_t i1 = (int64_t)U.g1_start + (int64_t)q * U.g1_stride;
     float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f);
     bool valid = false;
+    int oi = 0;       // input index of the row (corels1)
+    uint8_t af = 0;   // its corels1 scan-start flags
     const bool has_lo = C != COREL_DD && J.has_lo;
     const int gws = J.gws, lin_bin = J.lin_bin, box_same_keep = J.box_same_keep;
     const float rmin_f = J.rmin_f, inv_rsize_f = J.inv_rsize_f;
     if (has1) {
       p1 = J.f1.pos[i1];
       valid = true;
+      if (J.auto_mode) {
+        oi = (int)J.d1.orig[i1];
+        af = J.f1.aflag[i1];
+      }
       if (J.row_stride > 1) {
         const int64_t o = J.d1.orig[i1] - J.row_offset;
         valid = (o % J.row_stride) == 0;
@@ -387,6 +394,10 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         int sx, sy, sz;
         shift_decode(code, sx, sy, sz);
         const bool same_region = region2 == U.region;
+        // corels1: this image counts every partner, or only partners after the
+        // row in input order, or none
+        const bool a_all = auto_image_all(J.auto_mode, sz, af);
+        const bool a_gt = !a_all && auto_image_gt(J.auto_mode, sz, af);
         // staging order: position (i * ks) mod N over the group's N candidates,
         // ks coprime with N and ~0.618 N, so a batch is a spread-out sample of
         // the group's columns and z range (decorrelated bins, fewer collisions)
@@ -444,6 +455,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             if (C != COREL_DD) s_shp[t] = J.f2.shp[j2];
             if (has_lo) s_lo[t] = J.f2.lo[j2];
             s_jidx[t] = j2;
+            if (J.auto_mode) s_orig[t] = (int)J.d2.orig[j2];
             if (JK) s_keep[t] = J.f2.keep[j2];
           }
           __syncthreads();
@@ -468,7 +480,8 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               const float dy = y1s - p2.y;
               const float m = fmaxf(fabsf(dx), fabsf(dy));
               bool binned = false, edge = false;
-              if (valid && dz >= pi_out_lo && dz <= pi_out_hi && m <= xy_out) {
+              if (valid && (a_all || (a_gt && s_orig[c] > oi)) && dz >= pi_out_lo &&
+                  dz <= pi_out_hi && m <= xy_out) {
                 if (!(dz >= pi_in_lo && dz <= pi_in_hi && m <= xy_in)) {
                   // near the window edge: queued with a flag, the heavy step hands
                   // it to the exact FP64 evaluation of the whole pair

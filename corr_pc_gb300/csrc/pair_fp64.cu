@@ -42,6 +42,12 @@ plain_fp64_kernel(const JobDev *__restrict__ jobp, DCat a, DCat b) {
     for (int xi = 0; xi <= abs(PBx); xi++, sx--) {
       int sz = PBz > 0;
       for (int zi = 0; zi <= abs(PBz); zi++, sz--) {
+        // corels1 (corr.cpp:165-180): every partner, partners after row i in
+        // input order, or none
+        const uint8_t af = J.auto_mode ? a.aflag[i] : 0;
+        const bool a_all = auto_image_all(J.auto_mode, sz, af);
+        const bool a_gt = !a_all && auto_image_gt(J.auto_mode, sz, af);
+        if (!a_all && !a_gt) continue;
         const double Lsx = J.L * sx, Lsy = J.L * sy, Lsz = J.L * sz;
         // first b row with z + L*sz >= z_min (b is z-sorted)
         int64_t lo = 0, hi = b.n;
@@ -52,6 +58,7 @@ plain_fp64_kernel(const JobDev *__restrict__ jobp, DCat a, DCat b) {
         for (int64_t j = lo; j < b.n; j++) {
           const double z2s = __dadd_rn(b.z[j], Lsz);
           if (z2s > z_max) break;
+          if (!a_all && !(b.orig[j] > a.orig[i])) continue;
           const double y2s = __dadd_rn(b.y[j], Lsy);
           if (y2s > dec_max || y2s < dec_min) continue;
           const double x2s = __dadd_rn(b.x[j], Lsx);

@@ -65,6 +65,9 @@ sky_fp64_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, int2 *hq,
   const int64_t n1 = a.d.n, n2 = b.d.n;
   if (i >= n1) return;
   if (J.row_stride > 1 && ((a.d.orig[i] - J.row_offset) % J.row_stride) != 0) return;
+  // corels1: the scan from row i + 1 must pass the lower redshift bound (sorted)
+  if (J.auto_mode == 2 && !(a.d.aflag[i] & kAutoStart0)) return;
+  const int64_t oi = a.d.orig[i];
   const double z_min = a.win[i], z_max = a.win[n1 + i];
   const double ra_min = a.win[2 * n1 + i], ra_max = a.win[3 * n1 + i];
   const double dec_min = a.win[4 * n1 + i], dec_max = a.win[5 * n1 + i];
@@ -83,6 +86,7 @@ sky_fp64_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, int2 *hq,
   for (int64_t j = lo; j < n2; j++) {
     const double z2 = b.d.z[j];
     if (z2 > z_max) break;
+    if (J.auto_mode && !(b.d.orig[j] > oi)) continue;  // corels1: partners after row i
     const double dec2 = b.d.y[j];
     if (dec2 > dec_max || dec2 < dec_min) continue;
     const double ra2 = b.d.x[j];
@@ -424,6 +428,8 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
     i = __shfl_sync(FULL, i, 0);
     if (i >= n1) break;
     if (J.row_stride > 1 && ((a.d.orig[i] - J.row_offset) % J.row_stride) != 0) continue;
+    if (J.auto_mode == 2 && !(a.d.aflag[i] & kAutoStart0)) continue;  // corels1, sorted
+    const int64_t oi = a.d.orig[i];
     SkyRow r;
     r.i = i;
     r.ra = a.d.x[i]; r.dec = a.d.y[i]; r.dc = a.dc[i]; r.da = a.da[i];
@@ -460,7 +466,7 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
     for (int64_t base = lo; base < end; base += 32) {
       const int64_t j = base + lane;
       bool need = false;
-      if (j < end) {
+      if (j < end && (!J.auto_mode || b.d.orig[j] > oi)) {  // corels1: partners after i
         const float4 w2 = fb.sw[j];
         int in = fwin(w2.y, de_lru, de_hrd, de_lrd, de_hru);
         if (in < 0) {

@@ -48,7 +48,8 @@ typedef enum {
   CPC_PAIR_DRS = 2,  /* do_DRs  : corels2(grand_shape, gdensity, ...)   */
   CPC_PAIR_RSRD = 3, /* do_RsRd : corels2(grand_density, grand_shape)   */
   CPC_PAIR_RSRS = 4, /* do_RsRs : corels2(grand_shape, grand_shape)     */
-  CPC_PAIR_SRS = 5   /* do_SRs  : corels2(grand_shape, gshape, ...)     */
+  CPC_PAIR_SRS = 5,  /* do_SRs  : corels2(grand_shape, gshape, ...)     */
+  CPC_PAIR_SS = 6    /* do_SS   : corels1(gshape, ...) (cpc_count_auto only) */
 } cpc_pair_kind;
 
 /* which kernel counts the pairs */
@@ -148,6 +149,18 @@ cpc_status cpc_upload(cpc_ctx *ctx, int slot, const cpc_catalog *cat);
 cpc_status cpc_count(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_g2,
                      cpc_engine engine, int64_t row_stride, int64_t row_offset,
                      cpc_accum *out);
+
+/* Auto pairs of one catalogue: the reference's
+ *     long corels1(gal g1[], bin_jk &bjk, data_info &data_inf)
+ *     (corr.cpp:103-216; do_corr.cpp:63 with do_SS, :76 with do_RsRs)
+ * for the catalogue in slot `slot`, kind CPC_PAIR_SS or CPC_PAIR_RSRS.  Each
+ * pair is taken once by input order (row i with rows j > i), except that with
+ * data_sorted 1 the +1 z image of a periodic box pairs row i with every row,
+ * and an image whose first scanned row fails the lower redshift bound adds
+ * nothing (the reference's sorted scan).  data_sorted 1 expects input sorted
+ * by z, as the reference does.  Same output block as cpc_count. */
+cpc_status cpc_count_auto(cpc_ctx *ctx, cpc_pair_kind kind, int slot, cpc_engine engine,
+                          int64_t row_stride, int64_t row_offset, cpc_accum *out);
 
 /* Histogram shape for this context: n_hist, n_bins, n_p_bin. */
 cpc_status cpc_accum_shape(const cpc_ctx *ctx, int *n_hist, int *n_bins, int *n_p_bin);
