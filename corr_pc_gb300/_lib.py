@@ -93,6 +93,8 @@ def load() -> ctypes.CDLL:
     lib.cpc_host_pi_thresholds.argtypes = [P(cpc_params), V]
     lib.cpc_launch_count.argtypes = [V, P(I64)]
     lib.cpc_host_finalize_cross.argtypes = [ctypes.c_char_p] + [V] * 9
+    lib.cpc_host_finalize_auto.argtypes = [ctypes.c_char_p] + [V] * 7
+    lib.cpc_host_finalize_auto.restype = I
     lib.cpc_count_fp64_noalloc.argtypes = [P(cpc_params), I, P(cpc_device_catalog),
                                            P(cpc_device_catalog), V, V, P(I64), P(I64), V,
                                            ctypes.c_char_p, ctypes.c_size_t]
@@ -302,6 +304,23 @@ def finalize_cross(inp_path: str, terms: dict, weights) -> None:
             args += [None, None]
     w = np.ascontiguousarray(weights, dtype=np.float64)
     check(load().cpc_host_finalize_cross(inp_path.encode(), *args, w.ctypes.data))
+
+
+def finalize_auto(inp_path: str, terms: dict, weights) -> None:
+    """Auto-correlation finalisation + output files from RAW blocks.  terms: keys
+    among SS, SRs, RsRs -> (num, sums); weights: 8 totals (S and Rs used)."""
+    args = []
+    for k in ("SS", "SRs", "RsRs"):
+        if k in terms:
+            n, s = terms[k]
+            n = np.ascontiguousarray(n, dtype=np.int64)
+            s = np.ascontiguousarray(s, dtype=np.float64)
+            terms[k] = (n, s)
+            args += [n.ctypes.data, s.ctypes.data]
+        else:
+            args += [None, None]
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    check(load().cpc_host_finalize_auto(inp_path.encode(), *args, w.ctypes.data))
 
 
 def count_fp64_noalloc(inp_params, kind: str, g1: dict, g2: dict, d_num: int, d_sums: int,

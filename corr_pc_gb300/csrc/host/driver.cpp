@@ -1,11 +1,12 @@
 // driver.cpp -- the corr_pc command line on the GPU pair loop:
 //     corr_pc_gb300 <file.inp> [--engine fast|fp64]
 // Same argument, same parameter file, same input and output files as the
-// reference's corr_pc (main.cpp:27-82).  The sequence follows do_corr for a
-// cross-correlation run (do_corr.cpp:24-161): read S, Rs, D, Rd in that order
-// (which fixes the glibc rand() jackknife draws), one GPU corels2 per pair
-// type (SRd, RsRd, SD, DRs; SD alone in a periodic box), then the finalisation
-// and output files.
+// reference's corr_pc (main.cpp:27-82).  The sequence follows do_corr
+// (do_corr.cpp:24-161): read S, Rs, D, Rd in that order (which fixes the glibc
+// rand() jackknife draws); the auto pair types (SS by corels1; SRs and RsRs
+// without a periodic box) for estimators 1-3; the cross pair types (SRd, RsRd,
+// SD, DRs; SD alone in a periodic box) for estimators 0 and 3; then the
+// finalisation and output files.
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -23,7 +24,8 @@ struct Ctx {
   ~Ctx() { cpc_destroy(c); }
 };
 
-int count_term(Ctx &ctx, Info &d, cpc_pair_kind kind, int s1, int s2, Bins &out, cpc_engine eng) {
+int count_term(Ctx &ctx, Info &d, cpc_pair_kind kind, int s1, int s2, Bins &out, cpc_engine eng,
+               bool auto_pairs = false) {
   int nh, nb, np;
   cpc_accum_shape(ctx.c, &nh, &nb, &np);
   std::vector<int64_t> num((size_t)nh * nb * np);
@@ -32,14 +34,16 @@ int count_term(Ctx &ctx, Info &d, cpc_pair_kind kind, int s1, int s2, Bins &out,
   acc.num = num.data();
   acc.sums = sums.data();
   const auto t0 = std::chrono::steady_clock::now();
-  const cpc_status s = cpc_count(ctx.c, kind, s1, s2, eng, 1, 0, &acc);
+  const cpc_status s = auto_pairs ? cpc_count_auto(ctx.c, kind, s1, eng, 1, 0, &acc)
+                                  : cpc_count(ctx.c, kind, s1, s2, eng, 1, 0, &acc);
   const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (s != CPC_OK) {
     std::cout << "corels2 on the GPU failed: " << cpc_last_error(ctx.c) << std::endl;
     return 1;
   }
   add_count(out, d, num.data(), sums.data());
-  std::cout << "corel2 ends::time: " << dt << "  total pair= " << acc.n_window
+  std::cout << (auto_pairs ? "corel 1 ends: time:" : "corel2 ends::time: ") << dt
+            << "  total pair= " << acc.n_window
             << "\tpairs out= " << acc.n_window - acc.n_binned << "   pairs in=" << acc.n_binned
             << "    PB=0" << std::endl;
   return 0;
@@ -64,15 +68,10 @@ int main(int argc, char **argv) {
     return 1;
   }
   outp_data_info(d, d.out_file + "inp.info");
-  if ((d.coordinates != 6 && d.coordinates != 0) || d.estimator != 0 || d.which_corr > 2 ||
-      d.sig_crit) {
-    std::cout << "this build runs cross correlations (estimator 0) of wgg/wg+/w++ in x,y,z "
+  if ((d.coordinates != 6 && d.coordinates != 0) || d.estimator < 0 || d.estimator > 3 ||
+      d.which_corr > 2 || d.sig_crit) {
+    std::cout << "this build runs wgg/wg+/w++ (which_corr 0-2) with estimators 0-3 in x,y,z "
                  "(coordinates 6) or on the sky (coordinates 0)" << std::endl;
-    return 1;
-  }
-  if (d.RsRd_same && !d.periodic_box) {
-    std::cout << "without a periodic box this build needs separate density randoms "
-                 "(n_Drand > 0)" << std::endl;
     return 1;
   }
   Ctx ctx;
@@ -81,36 +80,61 @@ int main(int argc, char **argv) {
     std::cout << "GPU context: " << cpc_last_error(nullptr) << std::endl;
     return 1;
   }
-  // do_corr.cpp:40-96: read order S, Rs, D, Rd; slots 0..3
+  const bool box = d.periodic_box != 0;
+  const bool read_rs = !box || d.n_jk > 0;
+  const int nh = 1 + (d.do_jk ? d.n_jk : 0);
+  Bins SS, SRs, RsRs, SD, SRd, DRs, RsRd;
+  for (Bins *b : {&SS, &SRs, &RsRs, &SD, &SRd, &DRs, &RsRd}) b->init(d, nh);
+  // do_corr.cpp:40-52: S, then the shape randoms; slots S 0, Rs 1, D 2, Rd 3
   int64_t draws = 0;
   Catalog S, Rs, D, Rd;
-  if (read_catalog(d, ROLE_S, S, draws, err)) { std::cout << err << std::endl; return 1; }
-  if (!d.periodic_box || d.n_jk > 0)
-    if (read_catalog(d, ROLE_RS, Rs, draws, err)) { std::cout << err << std::endl; return 1; }
-  if (read_catalog(d, ROLE_D, D, draws, err)) { std::cout << err << std::endl; return 1; }
-  if (!d.RsRd_same)
-    if (read_catalog(d, ROLE_RD, Rd, draws, err)) { std::cout << err << std::endl; return 1; }
-  const Catalog *cats[4] = {&S, &Rs, &D, &Rd};
-  for (int k = 0; k < 4; k++) {
-    if (k == 3 && d.RsRd_same) continue;
-    cpc_catalog v = cats[k]->view();
-    if (cpc_upload(ctx.c, k, &v) != CPC_OK) {
+  auto upload = [&](int slot, const Catalog &c) {
+    cpc_catalog v = c.view();
+    if (cpc_upload(ctx.c, slot, &v) != CPC_OK) {
       std::cout << "upload: " << cpc_last_error(ctx.c) << std::endl;
       return 1;
     }
+    return 0;
+  };
+  if (read_catalog(d, ROLE_S, S, draws, err)) { std::cout << err << std::endl; return 1; }
+  if (upload(0, S)) return 1;
+  if (read_rs) {
+    if (read_catalog(d, ROLE_RS, Rs, draws, err)) { std::cout << err << std::endl; return 1; }
+    if (upload(1, Rs)) return 1;
   }
-  const int nh = 1 + (d.do_jk ? d.n_jk : 0);
-  Bins SD, SRd, DRs, RsRd;
-  SD.init(d, nh); SRd.init(d, nh); DRs.init(d, nh); RsRd.init(d, nh);
-  const int rd_slot = d.RsRd_same ? 1 : 3;
-  if (!d.RsRd_same) {
-    if (count_term(ctx, d, CPC_PAIR_SRD, rd_slot, 0, SRd, eng)) return 1;
-    if (count_term(ctx, d, CPC_PAIR_RSRD, rd_slot, 1, RsRd, eng)) return 1;
+  // do_corr.cpp:56-81: auto pair types
+  if (d.do_auto_corr)
+    if (count_term(ctx, d, CPC_PAIR_SS, 0, 0, SS, eng, true)) return 1;
+  if ((d.do_auto_corr || d.RsRd_same) && !box) {
+    if (count_term(ctx, d, CPC_PAIR_SRS, 1, 0, SRs, eng)) return 1;
+    if (!d.RsRd_same) {
+      if (count_term(ctx, d, CPC_PAIR_RSRS, 1, 1, RsRs, eng, true)) return 1;
+    } else {
+      if (count_term(ctx, d, CPC_PAIR_RSRS, 1, 1, RsRd, eng)) return 1;
+    }
   }
-  if (count_term(ctx, d, CPC_PAIR_SD, 2, 0, SD, eng)) return 1;
-  if (!d.periodic_box)
-    if (count_term(ctx, d, CPC_PAIR_DRS, 1, 2, DRs, eng)) return 1;
-  if (do_bining_cross(d, SD, SRd, DRs, RsRd, err)) {
+  // do_corr.cpp:83-133: cross pair types
+  if (d.do_cross_corr) {
+    if (read_catalog(d, ROLE_D, D, draws, err)) { std::cout << err << std::endl; return 1; }
+    if (upload(2, D)) return 1;
+    if (!d.RsRd_same) {
+      if (read_catalog(d, ROLE_RD, Rd, draws, err)) { std::cout << err << std::endl; return 1; }
+      if (upload(3, Rd)) return 1;
+      if (count_term(ctx, d, CPC_PAIR_SRD, 3, 0, SRd, eng)) return 1;
+      if (count_term(ctx, d, CPC_PAIR_RSRD, 3, 1, RsRd, eng)) return 1;
+    }
+    if (count_term(ctx, d, CPC_PAIR_SD, 2, 0, SD, eng)) return 1;
+    if (!box)
+      if (count_term(ctx, d, CPC_PAIR_DRS, 1, 2, DRs, eng)) return 1;
+  }
+  // do_corr.cpp:135-155: with one random sample the auto terms feed the cross ones
+  if (d.RsRd_same && !box) {
+    add_bins(RsRs, RsRd);
+    add_bins(SRd, SRs);
+    d.Rd_wt[0] = d.Rs_wt[0];
+    d.Rd_wt[1] = d.Rs_wt[1];
+  }
+  if (do_bining(d, SS, SRs, RsRs, SD, SRd, DRs, RsRd, err)) {
     std::cout << err << std::endl;
     return 1;
   }

@@ -1,5 +1,5 @@
-// finalize.cpp -- bin trees and the estimator finalisation of a cross run
-// (do_corr.cpp:326-431 with bins_calcs.cpp:30-52, 94-256, 331-462 and the
+// finalize.cpp -- bin trees and the estimator finalisation of cross and auto
+// runs (do_corr.cpp:203-433 with bins_calcs.cpp:30-91, 94-256, 331-530 and the
 // analytic periodic-box RR of PB_calcs.cpp:63-85).  Bin edges are formed in
 // single precision exactly as the reference's initialisers do
 // (initialization.cpp:357-444), because they are printed in the outputs.
@@ -220,15 +220,162 @@ void jk_final(Bins &out, Bins &fin, const Info &d) {
   }
 }
 
+// re_bin (bins_calcs.cpp:465-530): fold each negative-Pi bin of sample h onto
+// its mirror bin (estimators 2, 3), with the reference's edge checks
+void re_bin(Bins &b, int h, const Info &d) {
+  if (d.n_p_bin <= 1) return;
+  for (int i = 0; i < b.nb; i++) {
+    for (int k = 0; k < b.np; k++) {
+      if (b.p_min[k] >= 0) break;  // only negative bins move
+      const double p_val = 0.0 - (b.p_min[k] + b.p_max[k]) / 2.0;
+      int p = (int)std::floor((p_val - d.p_min) / d.p_size);
+      bool found = false;
+      for (;;) {
+        if (p < 0 || p >= d.n_p_bin) break;
+        if (p_val < b.p_min[p]) p--;
+        else if (p_val > b.p_max[p]) p++;
+        else { found = true; break; }
+      }
+      if (!found) break;  // the reference leaves the Pi loop here
+      if (std::fabs(b.p_min[k] + b.p_max[p]) > (d.p_size / 100.) ||
+          std::fabs(b.p_max[k] + b.p_min[p]) > (d.p_size / 100.) || b.p_max[p] < 0)
+        continue;  // "rebinning problem": bin left in place
+      const size_t from = b.pi(h, i, k), to = b.pi(h, i, p);
+      b.pnum[to] += b.pnum[from];
+      b.pnum[from] = 0;
+      b.pwt[to] += b.pwt[from];
+      b.pwt[from] = 0;
+      b.pls[to] += b.pls[from];
+      b.pls[from] = 0;
+      for (int j = 0; j < 7; j++)
+        for (int e = 0; e < 2; e++) {
+          b.pd(h, i, p, j, e) += b.pd(h, i, k, j, e);
+          b.pd(h, i, k, j, e) = 0;
+        }
+    }
+  }
+}
+
+// final_calc_auto (bins_calcs.cpp:54-91) for sample h: SS normalised by
+// S_wt^2 / 2, SR by S_wt Rs_wt, RR by Rs_wt^2 (halved when the randoms pairs
+// were counted once by corels1) or the analytic periodic RR
+void final_calc_auto(Info &d, Bins &ss, Bins &sr, Bins &rr, Bins &fin, int h) {
+  auto rel = [](const double *w) { return w[1] / std::pow(w[0], 2); };
+  const double SS_wt = d.S_wt[0] * d.S_wt[0] / 2.0;
+  const double SS_err = SS_wt * std::sqrt(rel(d.S_wt) + rel(d.S_wt));
+  const double SR_wt = d.S_wt[0] * d.Rs_wt[0];
+  const double SR_err = SR_wt * std::sqrt(rel(d.S_wt) + rel(d.Rs_wt));
+  double RR_wt = d.Rs_wt[0] * d.Rs_wt[0] * d.include_prob_RR * d.include_prob_RR;
+  double RR_err = RR_wt * std::sqrt(rel(d.Rs_wt) + rel(d.Rs_wt));
+  if (!d.RsRd_same) {
+    RR_wt /= 2.0;
+    RR_err /= 2.0;
+  }
+  if (d.periodic_box) {
+    RR_wt = 1;
+    RR_err = 0;
+    rr_periodic(rr, h, d);
+    if (d.do_auto_rebin) re_bin(rr, h, d);
+  }
+  d.SD_wt[0] = SS_wt; d.SD_wt[1] = SS_err;
+  d.SRd_wt[0] = SR_wt; d.SRd_wt[1] = SR_err;
+  d.RsRd_wt[0] = RR_wt; d.RsRd_wt[1] = RR_err;
+  d.DRs_wt[0] = SR_wt; d.DRs_wt[1] = SR_err;
+  final_bins(ss, sr, sr, rr, fin, h, d);  // DR = SR (bins_calcs.cpp:88)
+  integrate(ss, h, d);
+  integrate(rr, h, d);
+  integrate(sr, h, d);
+  integrate(fin, h, d);
+}
+
 }  // namespace
+
+// do_bining's auto part (do_corr.cpp:220-324)
+int do_bining_auto(Info &d, Bins &SS, Bins &SRs, Bins &RsRs, std::string &err) {
+  const std::string &o = d.out_file;
+  int bad = 0;
+  if (d.do_auto_rebin) {
+    re_bin(SS, 0, d);
+    re_bin(SRs, 0, d);
+    re_bin(RsRs, 0, d);
+    bad |= outp_2Dbins(SRs, 0, o + "bins_auto_SR2.temp");
+  }
+  Bins fin;
+  fin.init(d, SS.nh);
+  final_calc_auto(d, SS, SRs, RsRs, fin, 0);
+  bad |= outp_bins(fin, 0, o + "bins_auto_final.dat");
+  bad |= outp_bins(SS, 0, o + "bins_auto_SS.dat");
+  bad |= outp_bins(SRs, 0, o + "bins_auto_SR.dat");
+  bad |= outp_bins(RsRs, 0, o + "bins_auto_RR.dat");
+  bad |= outp_2Dbins(fin, 0, o + "bins2D_auto_final.dat");
+  bad |= outp_2Dbins(SS, 0, o + "bins2D_auto_SS.dat");
+  bad |= outp_2Dbins(SRs, 0, o + "bins2D_auto_SR.dat");
+  bad |= outp_2Dbins(RsRs, 0, o + "bins2D_auto_RR.dat");
+  if (d.do_jk) {
+    for (int r = 0; r < d.n_jk; r++) {
+      const int h = r + 1;
+      if (d.do_auto_rebin) {
+        re_bin(SS, h, d);
+        re_bin(RsRs, h, d);
+        re_bin(SRs, h, d);
+      }
+      final_calc_auto(d, SS, SRs, RsRs, fin, h);
+      const std::string s = o + "bins_auto_jk" + std::to_string(r);
+      const std::string s2 = o + "bins2D_auto_jk" + std::to_string(r);
+      bad |= outp_bins(SS, h, s + "_SS.dat");
+      bad |= outp_bins(RsRs, h, s + "_RR.dat");
+      bad |= outp_bins(SRs, h, s + "_SR.dat");
+      bad |= outp_bins(fin, h, s + "_final.dat");
+      bad |= outp_2Dbins(fin, h, s2 + "_final.dat");
+      bad |= outp_2Dbins(SS, h, s2 + "_SS.dat");
+      bad |= outp_2Dbins(RsRs, h, s2 + "_RR.dat");
+      bad |= outp_2Dbins(SRs, h, s2 + "_SR.dat");
+    }
+    if (d.do_jk == 1) {
+      Bins jk;
+      jk.init(d, 1);
+      jk_final(jk, fin, d);
+      bad |= outp_bins(jk, 0, o + "bins_auto_jk_final.dat");
+      bad |= outp_2Dbins(jk, 0, o + "bins2D_auto_jk_final.dat");
+    }
+  }
+  if (bad) {
+    err = "could not write output files with prefix " + o;
+    return 1;
+  }
+  return 0;
+}
+
+// add_bins of do_corr.cpp:135-155: b += a over every sample and field
+void add_bins(Bins &b, const Bins &a) {
+  for (size_t k = 0; k < b.bnum.size(); k++) b.bnum[k] += a.bnum[k];
+  for (size_t k = 0; k < b.bwt.size(); k++) b.bwt[k] += a.bwt[k];
+  for (size_t k = 0; k < b.bdat.size(); k++) b.bdat[k] += a.bdat[k];
+  for (size_t k = 0; k < b.bls.size(); k++) b.bls[k] += a.bls[k];
+  for (size_t k = 0; k < b.bsig.size(); k++) b.bsig[k] += a.bsig[k];
+  for (size_t k = 0; k < b.pnum.size(); k++) b.pnum[k] += a.pnum[k];
+  for (size_t k = 0; k < b.pwt.size(); k++) b.pwt[k] += a.pwt[k];
+  for (size_t k = 0; k < b.pdat.size(); k++) b.pdat[k] += a.pdat[k];
+  for (size_t k = 0; k < b.pls.size(); k++) b.pls[k] += a.pls[k];
+}
+
+// do_bining (do_corr.cpp:203-433): the temporary SR files, then the auto and
+// the cross parts as the estimator asks
+int do_bining(Info &d, Bins &SS, Bins &SRs, Bins &RsRs, Bins &SD, Bins &SRd, Bins &DRs,
+              Bins &RsRd, std::string &err) {
+  const std::string &o = d.out_file;
+  if (outp_2Dbins(SRs, 0, o + "bins_auto_SR.temp") || outp_2Dbins(SRd, 0, o + "bins_cross_SR.temp")) {
+    err = "could not write output files with prefix " + o;
+    return 1;
+  }
+  if (d.do_auto_corr && do_bining_auto(d, SS, SRs, RsRs, err)) return 1;
+  if (d.do_cross_corr && do_bining_cross(d, SD, SRd, DRs, RsRd, err)) return 1;
+  return 0;
+}
 
 int do_bining_cross(Info &d, Bins &SD, Bins &SRd, Bins &DRs, Bins &RsRd, std::string &err) {
   const std::string &o = d.out_file;
-  Bins SRs;  // the auto-term histogram, never filled in a cross run
-  SRs.init(d, 1);
   int bad = 0;
-  bad |= outp_2Dbins(SRs, 0, o + "bins_auto_SR.temp");
-  bad |= outp_2Dbins(SRd, 0, o + "bins_cross_SR.temp");
   Bins fin;
   fin.init(d, SD.nh);
   final_calc(d, SD, SRd, DRs, RsRd, fin, 0);
@@ -300,7 +447,37 @@ extern "C" cpc_status cpc_host_finalize_cross(const char *inp_path, const int64_
   for (int k = 0; k < 4; k++)
     if (nums[k] && sums[k]) add_count(*terms[k], d, nums[k], sums[k]);
   outp_data_info(d, d.out_file + "inp.info");
-  if (do_bining_cross(d, SD, SRd, DRs, RsRd, err)) return CPC_ERR_INVALID;
+  Bins SS, SRs, RsRs;
+  SS.init(d, nh); SRs.init(d, nh); RsRs.init(d, nh);
+  d.do_auto_corr = 0;
+  d.do_cross_corr = 1;
+  if (do_bining(d, SS, SRs, RsRs, SD, SRd, DRs, RsRd, err)) return CPC_ERR_INVALID;
+  outp_data_info(d, d.out_file + "inp2.info");
+  return CPC_OK;
+}
+
+// C ABI: finalisation and output files of an auto-correlation run (the auto
+// part of do_bining) from RAW histogram blocks of SS (corels1), SRs and RsRs
+// (corels1, or corels2 of the randoms with themselves when RsRd_same).
+extern "C" cpc_status cpc_host_finalize_auto(const char *inp_path, const int64_t *ss_num,
+                                             const double *ss_sums, const int64_t *srs_num,
+                                             const double *srs_sums, const int64_t *rsrs_num,
+                                             const double *rsrs_sums, const double *weights) {
+  using namespace cpch;
+  if (!inp_path || !weights) return CPC_ERR_INVALID;
+  Info d;
+  std::string err;
+  if (read_inp(inp_path, d, err) || derive_info(d, err)) return CPC_ERR_INVALID;
+  d.S_wt[0] = weights[0]; d.S_wt[1] = weights[1];
+  d.Rs_wt[0] = weights[4]; d.Rs_wt[1] = weights[5];
+  const int nh = 1 + (d.do_jk ? d.n_jk : 0);
+  Bins SS, SRs, RsRs;
+  SS.init(d, nh); SRs.init(d, nh); RsRs.init(d, nh);
+  if (ss_num && ss_sums) add_count(SS, d, ss_num, ss_sums);
+  if (srs_num && srs_sums) add_count(SRs, d, srs_num, srs_sums);
+  if (rsrs_num && rsrs_sums) add_count(RsRs, d, rsrs_num, rsrs_sums);
+  outp_data_info(d, d.out_file + "inp.info");
+  if (do_bining_auto(d, SS, SRs, RsRs, err)) return CPC_ERR_INVALID;
   outp_data_info(d, d.out_file + "inp2.info");
   return CPC_OK;
 }

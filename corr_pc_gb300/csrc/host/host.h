@@ -92,8 +92,13 @@ struct Bins {
 // corels2's end: add the GPU histogram block (raw region sums) into the tree
 // and apply final_jk_bins (jk.cpp:74-81).
 void add_count(Bins &b, const Info &d, const int64_t *num, const double *sums);
-// do_corr's finalisation and output files (do_corr.cpp:203-433, cross part)
+// do_corr's finalisation and output files (do_corr.cpp:203-433): both parts,
+// the cross part, the auto part; and add_bins (b += a, every sample)
+int do_bining(Info &d, Bins &SS, Bins &SRs, Bins &RsRs, Bins &SD, Bins &SRd, Bins &DRs,
+              Bins &RsRd, std::string &err);
 int do_bining_cross(Info &d, Bins &SD, Bins &SRd, Bins &DRs, Bins &RsRd, std::string &err);
+int do_bining_auto(Info &d, Bins &SS, Bins &SRs, Bins &RsRs, std::string &err);
+void add_bins(Bins &b, const Bins &a);
 int outp_data_info(const Info &d, const std::string &path);
 
 }  // namespace cpch

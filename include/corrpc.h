@@ -213,6 +213,16 @@ cpc_status cpc_host_finalize_cross(const char *inp_path, const int64_t *sd_num,
                                    const double *drs_sums, const int64_t *rsrd_num,
                                    const double *rsrd_sums, const double *weights);
 
+/* Finalisation of an auto-correlation run (do_corr.cpp:220-324: re_bin for
+ * estimators 2 and 3, final_calc_auto, int_calc, jk_final) and its bins_auto_*
+ * output files, from the RAW blocks of SS (corels1), SRs and RsRs (NULL = empty
+ * term; the delete-one conversion is applied here).  weights as for
+ * cpc_host_finalize_cross (S and Rs totals are used). */
+cpc_status cpc_host_finalize_auto(const char *inp_path, const int64_t *ss_num,
+                                  const double *ss_sums, const int64_t *srs_num,
+                                  const double *srs_sums, const int64_t *rsrs_num,
+                                  const double *rsrs_sums, const double *weights);
+
 /* ---- counting without any GPU allocation (no counterpart in the reference) ----
  *
  * For callers that cannot allocate GPU memory themselves -- code embedded in a

@@ -46,3 +46,30 @@ def test_cli_sky_output_files_match_reference(name, tmp_path):
         if fname.endswith(".info"):
             continue
         compare_files(open(out + fname).read(), ref, label=f"{name}:{fname}")
+
+
+@pytest.mark.parametrize("name", ["auto_box_wgg", "auto_box_wpp_rebin", "auto_box_wgp_unsorted",
+                                  "auto_sky_wgp"])
+def test_cli_auto_output_files_match_reference(name, tmp_path):
+    """Auto-correlation runs (estimators 1 and 2) through the command line:
+    corels1 on the GPU, final_calc_auto (re_bin for estimator 2), the
+    reference's bins_auto_* files."""
+    from helpers import AutoGolden
+    g = AutoGolden(name)
+    S = g.cats["S"]
+    if g.table is None:
+        inp = synth.write_box_run(str(tmp_path), synth.Workload(name, g.params, S, S),
+                                  same_files=True)
+    else:
+        R = g.cats["Rs"]
+        inp = synth.write_sky_run(str(tmp_path), synth.SkyWorkload(name, g.params, g.table, S, S,
+                                                                   R, R))
+    r = subprocess.run([build.CLI, inp], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for t in g.terms:
+        assert f"pairs in={g.term(t)[2]}" in r.stdout, t
+    out = os.path.join(str(tmp_path), "out", "run_")
+    for fname, ref in g.files.items():
+        if fname.endswith(".info"):
+            continue
+        compare_files(open(out + fname).read(), ref, label=f"{name}:{fname}")

@@ -11,7 +11,8 @@ import pytest
 
 import oracle
 from corr_pc_gb300 import _lib, host, synth
-from helpers import Golden, SkyGolden, compare_files, golden_names, sky_golden_names
+from helpers import (AutoGolden, Golden, SkyGolden, auto_golden_names, compare_files,
+                     golden_names, sky_golden_names)
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -150,6 +151,35 @@ def test_sky_finalisation_matches_reference_files(name, tmp_path):
         ww = np.ones(c.n) if c.w is None else c.w
         w += [float(ww.sum()), float((ww * ww).sum())]
     _lib.finalize_cross(inp, terms, w)
+    for fname, ref in g.files.items():
+        if fname.endswith(".info"):
+            continue
+        compare_files(open(p.out_file + fname).read(), ref, label=f"{name}:{fname}")
+
+
+@pytest.mark.parametrize("name", auto_golden_names())
+def test_auto_finalisation_matches_reference_files(name, tmp_path):
+    """Reference raw histograms of an auto run (SS; SRs and RsRs on the sky) ->
+    final_calc_auto (with re_bin for estimator 2) -> the reference's files."""
+    g = AutoGolden(name)
+    p = g.params
+    p.out_file = str(tmp_path) + "/run_"
+    if g.table is not None:
+        p.distance_file = str(tmp_path / "distances.dat")
+        g.table.write(p.distance_file)
+    inp = str(tmp_path / "run.inp")
+    p.write(inp)
+    terms = {t: g.term(t)[:2] for t in g.terms}
+    w = []
+    for role in ("S", "S", "Rs", "Rs"):
+        c = g.cats.get(role)
+        if c is None:
+            w += [0.0, 0.0]
+            continue
+        ww = np.ones(c.n) if c.w is None else c.w
+        w += [float(ww.sum()), float((ww * ww).sum())]
+    _lib.finalize_auto(inp, terms, w)
+    assert g.files
     for fname, ref in g.files.items():
         if fname.endswith(".info"):
             continue
