@@ -135,6 +135,12 @@ struct cpc_ctx {
   DevBuf<uint64_t> d_keys, d_ktmp;
   DevBuf<uint32_t> d_vals, d_vtmp, d_hist, d_bucket;
   DevBuf<unsigned long long> d_census;
+  // upload scratch: a catalogue in input order, its checks and statistics
+  DevBuf<double> u_x, u_y, u_z, u_w, u_e1, u_e2, u_phi, u_prob;
+  DevBuf<int32_t> u_jk;
+  DevBuf<uint8_t> u_keep, u_flag;
+  DevBuf<UploadStats> d_ustats;
+  UploadStats h_ustats{};
   // sky: fixed-point sums of the fast kernel, host edge queue
   DevBuf<unsigned long long> d_fix;
   DevBuf<int2> d_hq;
@@ -1235,66 +1241,7 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   s.n = n;
   s.version = ++c->version_ctr;
   const double L = p.periodic_box_size;
-  // host-side validation and derived per-galaxy arrays
-  std::vector<double> w(n, 1.0), e1(n, 0.0), e2(n, 0.0), phi(n, -10.0);
-  std::vector<int32_t> jk(n, 0);
-  std::vector<uint8_t> keep(n, 0);
   s.has_e = cat->e1 && cat->e2;
-  s.exact_f32 = true;
-  s.wmax = 0;
-  s.phimax = 0.0;
-  s.wmin = n > 0 ? 1e300 : 1.0;
-  s.emax = 0;
-  s.cmax = 0;
-  for (int64_t i = 0; i < n; i++) {
-    const double x = cat->x[i], y = cat->y[i], z = cat->z[i];
-    if (!std::isfinite(x) || !std::isfinite(y) || !std::isfinite(z))
-      return fail(c, CPC_ERR_RANGE, "non-finite position at row " + std::to_string(i));
-    if (x < 0 || y < 0 || z < 0 || x > L || y > L || z > L)
-      return fail(c, CPC_ERR_RANGE, "position outside [0, box_size] at row " + std::to_string(i));
-    if ((double)(float)x != x || (double)(float)y != y || (double)(float)z != z) s.exact_f32 = false;
-    s.cmax = std::max(s.cmax, std::max(x, std::max(y, z)));
-    if (cat->w) {
-      if (!std::isfinite(cat->w[i])) return fail(c, CPC_ERR_RANGE, "non-finite weight");
-      w[i] = cat->w[i];
-    }
-    s.wmax = std::max(s.wmax, std::fabs(w[i]));
-    s.wmin = std::min(s.wmin, w[i]);
-    if (s.has_e) {
-      if (!std::isfinite(cat->e1[i]) || !std::isfinite(cat->e2[i])) return fail(c, CPC_ERR_RANGE, "non-finite ellipticity");
-      e1[i] = cat->e1[i];
-      e2[i] = cat->e2[i];
-      s.emax = std::max(s.emax, std::max(std::fabs(e1[i]), std::fabs(e2[i])));
-    }
-    if (cat->phi) {
-      if (!std::isfinite(cat->phi[i])) return fail(c, CPC_ERR_RANGE, "non-finite phi");
-      phi[i] = cat->phi[i];
-    }
-    s.phimax = std::max(s.phimax, std::fabs(phi[i]));
-    if (p.do_jk) {
-      const int r = cat->jk[i];
-      if (r < 0 || r >= p.n_jk)
-        return fail(c, CPC_ERR_RANGE, "jackknife label out of range at row " + std::to_string(i));
-      jk[i] = r;
-    }
-    if (cat->jk_prob) keep[i] = cat->jk_prob[i] >= 0.5 ? 1 : 0;
-  }
-  // corels1 scan starts (corr.cpp:165-180 with do_pair_sorted's redshift test):
-  // does the first row of each image's scan pass z >= z_min = z_i + p_min
-  // (lim_calc_PB / lim_calc_xyz)?  0 image: row i + 1; -1 image: row i + 1
-  // shifted by -L; +1 image: row 0 shifted by +L.
-  std::vector<uint8_t> aflag(n, 0);
-  for (int64_t i = 0; i < n; i++) {
-    const double zmin = cat->z[i] + p.p_min;
-    uint8_t f = 0;
-    if (i + 1 < n) {
-      const double zn = cat->z[i + 1];
-      if (!((zn + L * 0.0) < zmin)) f |= kAutoStart0;
-      if (!((zn + L * -1.0) < zmin)) f |= kAutoStartM;
-    }
-    if (!((cat->z[0] + L * 1.0) < zmin)) f |= kAutoStartP;
-    aflag[i] = f;
-  }
   // grid: columns of width >= r_max / k over [0, box)
   const int k = c->tune_k > 0 ? c->tune_k : 2;
   int nc = (int)std::floor(L / (p.bin_r_max / k));
@@ -1304,24 +1251,57 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   s.n_reg = p.do_jk ? p.n_jk : 1;
   if ((double)nc * nc * s.n_reg >= 4294967295.0) return fail(c, CPC_ERR_INVALID, "too many cell buckets");
   cudaStream_t st = c->st;
-  // device originals (temporary) + sort scratch
-  DevBuf<double> ox, oy, oz, ow, oe1, oe2, ophi;
-  DevBuf<int32_t> ojk;
-  DevBuf<uint8_t> okeep;
+  // the caller's arrays, in input order, in context buffers reused by every
+  // upload; absent optional arrays get the reference's defaults on the device
+  // (w 1, e 0, phi -10, region 0)
   const size_t nn = std::max<int64_t>(n, 1);
+  DevBuf<double> &ox = c->u_x, &oy = c->u_y, &oz = c->u_z, &ow = c->u_w, &oe1 = c->u_e1,
+                 &oe2 = c->u_e2, &ophi = c->u_phi, &oprob = c->u_prob;
+  DevBuf<int32_t> &ojk = c->u_jk;
+  DevBuf<uint8_t> &okeep = c->u_keep, &oflag = c->u_flag;
   CK(ox.alloc(nn), "alloc"); CK(oy.alloc(nn), "alloc"); CK(oz.alloc(nn), "alloc");
   CK(ow.alloc(nn), "alloc"); CK(oe1.alloc(nn), "alloc"); CK(oe2.alloc(nn), "alloc");
-  CK(ophi.alloc(nn), "alloc"); CK(ojk.alloc(nn), "alloc"); CK(okeep.alloc(nn), "alloc");
+  CK(ophi.alloc(nn), "alloc"); CK(oprob.alloc(nn), "alloc"); CK(ojk.alloc(nn), "alloc");
+  CK(okeep.alloc(nn), "alloc"); CK(oflag.alloc(nn), "alloc");
+  CK(c->d_ustats.alloc(1), "alloc");
+  UploadStats init;
+  for (int q = 0; q < 4; q++) init.bad_row[q] = ~0ull;
+  init.cmax_bits = init.wmax_bits = init.emax_bits = init.phimax_bits = 0;
+  init.wmin_key = ~0ull;
+  init.not_f32 = 0;
+  c->h_ustats = init;
   if (n > 0) {
-    CK(cudaMemcpyAsync(ox.p, cat->x, 8 * n, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(oy.p, cat->y, 8 * n, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(oz.p, cat->z, 8 * n, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(ow.p, w.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(oe1.p, e1.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(oe2.p, e2.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(ophi.p, phi.data(), 8 * n, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(ojk.p, jk.data(), 4 * n, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(okeep.p, keep.data(), n, cudaMemcpyHostToDevice, st), "H2D");
+    auto h2d = [&](void *d, const void *h, size_t bytes) {
+      return cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st);
+    };
+    CK(h2d(ox.p, cat->x, 8 * n), "H2D");
+    CK(h2d(oy.p, cat->y, 8 * n), "H2D");
+    CK(h2d(oz.p, cat->z, 8 * n), "H2D");
+    CK(cat->w ? h2d(ow.p, cat->w, 8 * n) : launch_fill_f64(n, 1.0, ow.p, st), "weights");
+    if (s.has_e) {
+      CK(h2d(oe1.p, cat->e1, 8 * n), "H2D");
+      CK(h2d(oe2.p, cat->e2, 8 * n), "H2D");
+    } else {
+      CK(cudaMemsetAsync(oe1.p, 0, 8 * n, st), "memset");
+      CK(cudaMemsetAsync(oe2.p, 0, 8 * n, st), "memset");
+    }
+    CK(cat->phi ? h2d(ophi.p, cat->phi, 8 * n) : launch_fill_f64(n, -10.0, ophi.p, st), "phi");
+    CK(p.do_jk ? h2d(ojk.p, cat->jk, 4 * n) : cudaMemsetAsync(ojk.p, 0, 4 * n, st), "labels");
+    if (cat->jk_prob) CK(h2d(oprob.p, cat->jk_prob, 8 * n), "H2D");
+    CK(h2d(c->d_ustats.p, &c->h_ustats, sizeof(UploadStats)), "H2D");
+    PrepIn pin;
+    pin.n = n;
+    pin.x = ox.p; pin.y = oy.p; pin.z = oz.p; pin.w = cat->w ? ow.p : nullptr;
+    pin.e1 = s.has_e ? oe1.p : nullptr; pin.e2 = s.has_e ? oe2.p : nullptr;
+    pin.phi = cat->phi ? ophi.p : nullptr; pin.jk_prob = cat->jk_prob ? oprob.p : nullptr;
+    pin.jk = p.do_jk ? ojk.p : nullptr;
+    pin.L = L;
+    pin.p_min = p.p_min;
+    pin.n_jk = p.n_jk;
+    CK(launch_prep_catalog(pin, okeep.p, oflag.p, c->d_ustats.p, st), "catalogue checks");
+    c->launches += 1;
+    CK(cudaMemcpyAsync(&c->h_ustats, c->d_ustats.p, sizeof(UploadStats), cudaMemcpyDeviceToHost,
+                       st), "D2H");
   }
   CK(c->d_keys.alloc(nn), "alloc"); CK(c->d_ktmp.alloc(nn), "alloc");
   CK(c->d_vals.alloc(nn), "alloc"); CK(c->d_vtmp.alloc(nn), "alloc");
@@ -1345,16 +1325,10 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   go.x = s.x.p; go.y = s.y.p; go.z = s.z.p; go.w = s.w.p; go.e1 = s.e1.p; go.e2 = s.e2.p;
   go.phi = s.phi.p; go.jk = s.jk.p; go.keep = s.keep.p; go.orig = s.orig.p; go.orig_in = nullptr;
   CK(launch_gather(n, c->d_keys.p, c->d_vals.p, in, go, st), "gather");
-  {
-    DevBuf<uint8_t> oflag;
-    CK(oflag.alloc(nn), "alloc");
-    CK(s.aflag.alloc(nn), "alloc");
-    if (n > 0) {
-      CK(cudaMemcpyAsync(oflag.p, aflag.data(), n, cudaMemcpyHostToDevice, st), "H2D");
-      CK(launch_gather_u8(n, c->d_vals.p, oflag.p, s.aflag.p, st), "gather");
-      c->launches += 1;
-    }
-    CK(cudaStreamSynchronize(st), "upload");
+  CK(s.aflag.alloc(nn), "alloc");
+  if (n > 0) {
+    CK(launch_gather_u8(n, c->d_vals.p, oflag.p, s.aflag.p, st), "gather");
+    c->launches += 1;
   }
   // buckets on the host
   std::vector<uint32_t> hb(n);
@@ -1364,6 +1338,25 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
     CK(cudaMemcpyAsync(s.h_pos.data(), s.pos.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, st), "D2H");
   }
   CK(cudaStreamSynchronize(st), "upload");
+  {  // the device checks (first failing row of each kind) and statistics
+    const UploadStats &u = c->h_ustats;
+    static const char *what[4] = {"non-finite position", "position outside [0, box_size]",
+                                  "non-finite weight, ellipticity or phi",
+                                  "jackknife label out of range"};
+    int kind = -1;
+    for (int q = 0; q < 4; q++)
+      if (u.bad_row[q] != ~0ull && (kind < 0 || u.bad_row[q] < u.bad_row[kind])) kind = q;
+    if (kind >= 0)
+      return fail(c, CPC_ERR_RANGE,
+                  std::string(what[kind]) + " at row " + std::to_string(u.bad_row[kind]));
+    double v;
+    std::memcpy(&v, &u.cmax_bits, 8); s.cmax = v;
+    std::memcpy(&v, &u.wmax_bits, 8); s.wmax = v;
+    std::memcpy(&v, &u.emax_bits, 8); s.emax = v;
+    std::memcpy(&v, &u.phimax_bits, 8); s.phimax = v;
+    s.wmin = n > 0 ? from_orderable_key(u.wmin_key) : 1.0;
+    s.exact_f32 = u.not_f32 == 0;
+  }
   s.h_bk_start.clear(); s.h_bk_end.clear(); s.h_bk_region.clear();
   std::vector<float> bz0, bz1;
   const int ncol = s.ncx * s.ncy;

@@ -12,6 +12,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+#include <cstring>
+
 #include "kernels.h"
 
 namespace cpc {
@@ -251,6 +254,120 @@ cudaError_t launch_gather(int64_t n, const uint64_t *keys, const uint32_t *perm,
                           const GatherOut &out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   gather_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, keys, perm, in, out);
+  return cudaGetLastError();
+}
+
+__global__ void fill_f64_kernel(int64_t n, double v, double *__restrict__ out) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = v;
+}
+
+cudaError_t launch_fill_f64(int64_t n, double v, double *out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4096);
+  fill_f64_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, v, out);
+  return cudaGetLastError();
+}
+
+unsigned long long orderable_key(double v) {
+  unsigned long long u;
+  std::memcpy(&u, &v, 8);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+double from_orderable_key(unsigned long long k) {
+  const unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  double v;
+  std::memcpy(&v, &u, 8);
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+// bit pattern of a non-negative double: ordered like the values
+__device__ __forceinline__ unsigned long long nonneg_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v);
+}
+
+// One pass over a catalogue in input order (the host checks of the reference's
+// read path plus what the pair kernels need): see UploadStats.  The corels1
+// scan starts compare, as do_pair_sorted does, z + L*PBz with z_min = z_i + p_min
+// (lim_calc_PB): row i + 1 for the 0 and -1 images, row 0 for the +1 image.
+__global__ void prep_catalog_kernel(PrepIn in, uint8_t *__restrict__ keep,
+                                    uint8_t *__restrict__ aflag, UploadStats *__restrict__ st) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long cm = 0, wm = 0, em = 0, pm = 0, wk = ~0ull;
+  unsigned int nf = 0;
+  if (i < in.n) {
+    const double x = in.x[i], y = in.y[i], z = in.z[i];
+    const double L = in.L;
+    if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicMin(&st->bad_row[0], (unsigned long long)i);
+    else if (x < 0 || y < 0 || z < 0 || x > L || y > L || z > L)
+      atomicMin(&st->bad_row[1], (unsigned long long)i);
+    if ((double)(float)x != x || (double)(float)y != y || (double)(float)z != z) nf = 1u;
+    cm = nonneg_bits(fmax(fmax(fmax(x, y), z), 0.0));
+    const double w = in.w ? in.w[i] : 1.0;
+    bool bad = !isfinite(w);
+    wm = nonneg_bits(fabs(w));
+    // orderable key of w for the minimum
+    const unsigned long long u = (unsigned long long)__double_as_longlong(w);
+    wk = (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+    if (in.e1) {
+      const double a = in.e1[i], b = in.e2[i];
+      bad |= !isfinite(a) || !isfinite(b);
+      em = nonneg_bits(fmax(fabs(a), fabs(b)));
+    }
+    const double ph = in.phi ? in.phi[i] : -10.0;
+    bad |= !isfinite(ph);
+    pm = nonneg_bits(fabs(ph));
+    if (bad) atomicMin(&st->bad_row[2], (unsigned long long)i);
+    if (in.jk) {
+      const int r = in.jk[i];
+      if (r < 0 || r >= in.n_jk) atomicMin(&st->bad_row[3], (unsigned long long)i);
+    }
+    keep[i] = (in.jk_prob && in.jk_prob[i] >= 0.5) ? 1 : 0;
+    const double zmin = __dadd_rn(z, in.p_min);
+    uint8_t f = 0;
+    if (i + 1 < in.n) {
+      const double zn = in.z[i + 1];
+      if (!(__dadd_rn(zn, __dmul_rn(L, 0.0)) < zmin)) f |= kAutoStart0;
+      if (!(__dadd_rn(zn, __dmul_rn(L, -1.0)) < zmin)) f |= kAutoStartM;
+    }
+    if (!(__dadd_rn(in.z[0], __dmul_rn(L, 1.0)) < zmin)) f |= kAutoStartP;
+    aflag[i] = f;
+  }
+  cm = warp_max_u64(cm);
+  wm = warp_max_u64(wm);
+  em = warp_max_u64(em);
+  pm = warp_max_u64(pm);
+  wk = warp_min_u64(wk);
+  nf = __any_sync(0xffffffffu, nf != 0u) ? 1u : 0u;
+  if ((threadIdx.x & 31) == 0) {
+    if (cm) atomicMax(&st->cmax_bits, cm);
+    if (wm) atomicMax(&st->wmax_bits, wm);
+    if (em) atomicMax(&st->emax_bits, em);
+    if (pm) atomicMax(&st->phimax_bits, pm);
+    if (wk != ~0ull) atomicMin(&st->wmin_key, wk);
+    if (nf) atomicOr(&st->not_f32, 1u);
+  }
+}
+
+cudaError_t launch_prep_catalog(const PrepIn &in, uint8_t *keep, uint8_t *aflag,
+                                UploadStats *stats, cudaStream_t st) {
+  if (in.n == 0) return cudaSuccess;
+  prep_catalog_kernel<<<(unsigned)((in.n + 255) / 256), 256, 0, st>>>(in, keep, aflag, stats);
   return cudaGetLastError();
 }
 

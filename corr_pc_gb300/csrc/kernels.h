@@ -40,6 +40,29 @@ cudaError_t launch_gather(int64_t n, const uint64_t *keys, const uint32_t *perm,
 cudaError_t launch_gather_u8(int64_t n, const uint32_t *perm, const uint8_t *in, uint8_t *out,
                              cudaStream_t st);
 
+// Checks and derived per-row data of a box catalogue (input order), on the
+// device: the first failing row of each check, the statistics the error bounds
+// and fixed-point scales need, the keep flags and the corels1 scan starts.
+struct UploadStats {
+  unsigned long long bad_row[4];  // first row: 0 non-finite position, 1 outside
+                                  // [0, L], 2 non-finite w/e/phi, 3 label range
+  unsigned long long cmax_bits, wmax_bits, emax_bits, phimax_bits;  // non-negative
+  unsigned long long wmin_key;    // orderable key of min w
+  unsigned int not_f32;           // a position is not a float32 value
+};
+struct PrepIn {
+  int64_t n;
+  const double *x, *y, *z, *w, *e1, *e2, *phi, *jk_prob;  // w, e1, e2, phi, jk_prob may be null
+  const int32_t *jk;  // null without jackknife
+  double L, p_min;
+  int n_jk;
+};
+cudaError_t launch_fill_f64(int64_t n, double v, double *out, cudaStream_t st);
+cudaError_t launch_prep_catalog(const PrepIn &in, uint8_t *keep, uint8_t *aflag,
+                                UploadStats *stats, cudaStream_t st);
+unsigned long long orderable_key(double v);
+double from_orderable_key(unsigned long long k);
+
 // pair_fast.cu
 constexpr int kTileThreads = 128;  // g1 rows per tile (the block has 2 warp groups over them)
 size_t fast_smem_bytes(int corel, int do_jk, int NB);
