@@ -394,6 +394,7 @@ def main() -> None:
     ap.add_argument("--ref-budget", type=float, default=8.0, help="seconds per reference step")
     ap.add_argument("--fp64-budget", type=float, default=3.0, help="seconds of FP64 kernel")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")
     ap.add_argument("--sky-rows", type=int, default=20000,
                     help="outer rows per pair type per step (sky workloads)")
     ap.add_argument("--sky-cpu-rows", type=int, default=400,
@@ -425,6 +426,11 @@ def main() -> None:
     for c, cat in zip(ctxs, preps):
         c.upload(0, cat["D"])
         c.upload(1, cat["S"])
+    tuning = None
+    if len(ctxs) == 1 and not args.no_tune:  # outside the timed region
+        n_rows = wls[0].density.n
+        k, w = ctxs[0].autotune("SD", 0, 1, sample_stride=max(1, n_rows // 25000))
+        tuning = {"cells_per_rmax": k, "pi_window": w, "by": "cpc_autotune on a row sample"}
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
     def step():
@@ -541,7 +547,7 @@ def main() -> None:
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64", "data": "synthetic (seeded generator, in memory)",
-            "config": _describe(wls), "n_binned_per_step": n_per_step,
+            "config": dict(_describe(wls), tuning=tuning), "n_binned_per_step": n_per_step,
             "n_window_per_step": n_win / args.steps,
             "roofline": roofline, "cpu_baseline": cpu, "fp64_gpu": fp64,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,

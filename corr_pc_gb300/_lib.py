@@ -87,6 +87,8 @@ def load() -> ctypes.CDLL:
     lib.cpc_accum_shape.argtypes = [V, P(I), P(I), P(I)]
     lib.cpc_count_batch.argtypes = [I, P(V), P(I), P(I), P(I), P(cpc_accum)]
     lib.cpc_set_tuning.argtypes = [V, I, I, I]
+    lib.cpc_autotune.argtypes = [V, I, I, I, I64, P(I), P(I)]
+    lib.cpc_autotune.restype = I
     lib.cpc_host_rand_uniform.argtypes = [ctypes.c_uint32, I64, I64, V]
     lib.cpc_host_elip_angle.argtypes = [I64, V, V, V]
     lib.cpc_host_rp_thresholds.argtypes = [P(cpc_params), V]
@@ -179,6 +181,14 @@ class Context:
 
     def set_tuning(self, cells_per_rmax=0, pi_window=0, tile=0):
         check(self.lib.cpc_set_tuning(self.h, cells_per_rmax, pi_window, tile), self.h)
+
+    def autotune(self, kind: str, slot_g1: int, slot_g2: int, sample_stride: int = 8):
+        """Pick the fastest cell width and Pi window for this pair type on a row
+        sample; returns (cells_per_rmax, pi_window)."""
+        k, w = ctypes.c_int(), ctypes.c_int()
+        check(self.lib.cpc_autotune(self.h, PAIR[kind], slot_g1, slot_g2, sample_stride,
+                                    ctypes.byref(k), ctypes.byref(w)), self.h)
+        return k.value, w.value
 
     def upload(self, slot: int, cat) -> None:
         """cat: object with x, y, z and optional w, e1, e2, phi, jk, jk_prob

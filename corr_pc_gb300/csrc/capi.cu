@@ -66,7 +66,7 @@ struct Slot {
   double wmax = 1.0, wmin = 1.0, emax = 0.0, cmax = 0.0, phimax = 0.0;
   uint64_t version = 0;
   // grid this cell list was built with
-  int ncx = 0, ncy = 0, n_reg = 1;
+  int ncx = 0, ncy = 0, n_reg = 1, kcells = 0;
   double cw_x = 0, cw_y = 0;
   // device, cell order
   DevBuf<float4> pos, shp;
@@ -139,6 +139,7 @@ struct cpc_ctx {
   DevBuf<double> u_x, u_y, u_z, u_w, u_e1, u_e2, u_phi, u_prob;
   DevBuf<int32_t> u_jk;
   DevBuf<uint8_t> u_keep, u_flag;
+  DevBuf<int64_t> u_orig;
   DevBuf<UploadStats> d_ustats;
   UploadStats h_ustats{};
   // sky: fixed-point sums of the fast kernel, host edge queue
@@ -760,6 +761,150 @@ cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt = 0) {
   return CPC_OK;
 }
 
+// Cell list of slot s from a catalogue held in the context's upload buffers
+// (u_x .. u_flag; orig_in maps their rows to input rows, null = identity):
+// grid of columns r_max / k wide, keys, radix sort, gather into the slot, the
+// bucket and column tables.  check_stats: the upload's device checks must pass.
+cpc_status build_cells(cpc_ctx *c, Slot &s, int64_t n, int k, const int64_t *orig_in,
+                       bool check_stats) {
+  const cpc_params &p = c->p;
+  const double L = p.periodic_box_size;
+  const size_t nn = std::max<int64_t>(n, 1);
+  cudaStream_t st = c->st;
+  DevBuf<double> &ox = c->u_x, &oy = c->u_y, &oz = c->u_z, &ow = c->u_w, &oe1 = c->u_e1,
+                 &oe2 = c->u_e2, &ophi = c->u_phi;
+  DevBuf<int32_t> &ojk = c->u_jk;
+  DevBuf<uint8_t> &okeep = c->u_keep, &oflag = c->u_flag;
+  // grid: columns of width >= r_max / k over [0, box)
+  int nc = (int)std::floor(L / (p.bin_r_max / k));
+  nc = std::max(1, std::min(nc, 2048));
+  s.ncx = s.ncy = nc;
+  s.cw_x = s.cw_y = L / nc;
+  s.kcells = k;
+  s.n_reg = p.do_jk ? p.n_jk : 1;
+  if ((double)nc * nc * s.n_reg >= 4294967295.0) return fail(c, CPC_ERR_INVALID, "too many cell buckets");
+  CK(c->d_keys.alloc(nn), "alloc"); CK(c->d_ktmp.alloc(nn), "alloc");
+  CK(c->d_vals.alloc(nn), "alloc"); CK(c->d_vtmp.alloc(nn), "alloc");
+  CK(c->d_hist.alloc(radix_hist_words(nn)), "alloc");
+  CK(c->d_census.alloc(8 * 256), "alloc");
+  CK(c->d_bucket.alloc(nn), "alloc");
+  CK(s.pos.alloc(nn), "alloc"); CK(s.shp.alloc(nn), "alloc"); CK(s.zf.alloc(nn), "alloc");
+  CK(s.lo.alloc(nn), "alloc");
+  CK(s.x.alloc(nn), "alloc"); CK(s.y.alloc(nn), "alloc"); CK(s.z.alloc(nn), "alloc");
+  CK(s.w.alloc(nn), "alloc"); CK(s.e1.alloc(nn), "alloc"); CK(s.e2.alloc(nn), "alloc");
+  CK(s.phi.alloc(nn), "alloc"); CK(s.jk.alloc(nn), "alloc"); CK(s.keep.alloc(nn), "alloc");
+  CK(s.orig.alloc(nn), "alloc");
+  CK(launch_cell_keys(n, ox.p, oy.p, oz.p, ojk.p, 1.0 / s.cw_x, 1.0 / s.cw_y, s.ncx, s.ncy, s.n_reg,
+                      c->d_keys.p, c->d_vals.p, st), "cell keys");
+  CK(radix_sort_pairs(n, c->d_keys.p, c->d_vals.p, c->d_ktmp.p, c->d_vtmp.p, c->d_hist.p,
+                      c->d_census.p, st, &c->launches), "radix sort");
+  if (n > 0) c->launches += 2;  // cell keys + gather
+  GatherIn in{ox.p, oy.p, oz.p, ow.p, oe1.p, oe2.p, ophi.p, ojk.p, okeep.p};
+  GatherOut go{};
+  go.pos = s.pos.p; go.shp = s.shp.p; go.lo = s.lo.p; go.zf = s.zf.p; go.bucket = c->d_bucket.p;
+  go.x = s.x.p; go.y = s.y.p; go.z = s.z.p; go.w = s.w.p; go.e1 = s.e1.p; go.e2 = s.e2.p;
+  go.phi = s.phi.p; go.jk = s.jk.p; go.keep = s.keep.p; go.orig = s.orig.p; go.orig_in = orig_in;
+  CK(launch_gather(n, c->d_keys.p, c->d_vals.p, in, go, st), "gather");
+  CK(s.aflag.alloc(nn), "alloc");
+  if (n > 0) {
+    CK(launch_gather_u8(n, c->d_vals.p, oflag.p, s.aflag.p, st), "gather");
+    c->launches += 1;
+  }
+  // buckets on the host
+  std::vector<uint32_t> hb(n);
+  s.h_pos.resize(n);
+  if (n > 0) {
+    CK(cudaMemcpyAsync(hb.data(), c->d_bucket.p, 4 * n, cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(s.h_pos.data(), s.pos.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, st), "D2H");
+  }
+  CK(cudaStreamSynchronize(st), "upload");
+  if (check_stats) {  // the device checks (first failing row of each kind) and statistics
+    const UploadStats &u = c->h_ustats;
+    static const char *what[4] = {"non-finite position", "position outside [0, box_size]",
+                                  "non-finite weight, ellipticity or phi",
+                                  "jackknife label out of range"};
+    int kind = -1;
+    for (int q = 0; q < 4; q++)
+      if (u.bad_row[q] != ~0ull && (kind < 0 || u.bad_row[q] < u.bad_row[kind])) kind = q;
+    if (kind >= 0)
+      return fail(c, CPC_ERR_RANGE,
+                  std::string(what[kind]) + " at row " + std::to_string(u.bad_row[kind]));
+    double v;
+    std::memcpy(&v, &u.cmax_bits, 8); s.cmax = v;
+    std::memcpy(&v, &u.wmax_bits, 8); s.wmax = v;
+    std::memcpy(&v, &u.emax_bits, 8); s.emax = v;
+    std::memcpy(&v, &u.phimax_bits, 8); s.phimax = v;
+    s.wmin = n > 0 ? from_orderable_key(u.wmin_key) : 1.0;
+    s.exact_f32 = u.not_f32 == 0;
+  }
+  s.h_bk_start.clear(); s.h_bk_end.clear(); s.h_bk_region.clear();
+  std::vector<float> bz0, bz1;
+  const int ncol = s.ncx * s.ncy;
+  std::vector<int> cb(ncol, 0), ce(ncol, 0);
+  for (int64_t i = 0; i < n;) {
+    int64_t j = i + 1;
+    while (j < n && hb[j] == hb[i]) j++;
+    const int b = (int)s.h_bk_start.size();
+    const int col = (int)(hb[i] / s.n_reg), reg = (int)(hb[i] % s.n_reg);
+    if (ce[col] == 0 && cb[col] == 0) cb[col] = b;
+    ce[col] = b + 1;
+    s.h_bk_start.push_back((int)i);
+    s.h_bk_end.push_back((int)j);
+    s.h_bk_region.push_back(reg);
+    bz0.push_back(s.h_pos[i].z);
+    bz1.push_back(s.h_pos[j - 1].z);
+    i = j;
+  }
+  // columns with no bucket: empty range
+  for (int q = 0; q < ncol; q++)
+    if (ce[q] == 0) cb[q] = 0;
+  const size_t nbk = std::max<size_t>(1, s.h_bk_start.size());
+  CK(s.bk_start.alloc(nbk), "alloc"); CK(s.bk_end.alloc(nbk), "alloc");
+  CK(s.bk_region.alloc(nbk), "alloc"); CK(s.bk_zmin.alloc(nbk), "alloc");
+  CK(s.bk_zmax.alloc(nbk), "alloc"); CK(s.col_begin.alloc(ncol), "alloc");
+  CK(s.col_end.alloc(ncol), "alloc");
+  const size_t nb = s.h_bk_start.size();
+  if (nb) {
+    CK(cudaMemcpyAsync(s.bk_start.p, s.h_bk_start.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.bk_end.p, s.h_bk_end.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.bk_region.p, s.h_bk_region.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.bk_zmin.p, bz0.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaMemcpyAsync(s.bk_zmax.p, bz1.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
+  }
+  CK(cudaMemcpyAsync(s.col_begin.p, cb.data(), 4 * ncol, cudaMemcpyHostToDevice, st), "H2D");
+  CK(cudaMemcpyAsync(s.col_end.p, ce.data(), 4 * ncol, cudaMemcpyHostToDevice, st), "H2D");
+  CK(cudaStreamSynchronize(st), "upload");
+  s.valid = true;
+  return CPC_OK;
+}
+
+// Rebuild a box slot's cell list with columns r_max / k wide from its own
+// device arrays (the autotuner's cell-size candidates).
+cpc_status rebuild_cells(cpc_ctx *c, Slot &s, int k) {
+  const int64_t n = s.n;
+  const size_t nn = std::max<int64_t>(n, 1);
+  cudaStream_t st = c->st;
+  CK(c->u_x.alloc(nn), "alloc"); CK(c->u_y.alloc(nn), "alloc"); CK(c->u_z.alloc(nn), "alloc");
+  CK(c->u_w.alloc(nn), "alloc"); CK(c->u_e1.alloc(nn), "alloc"); CK(c->u_e2.alloc(nn), "alloc");
+  CK(c->u_phi.alloc(nn), "alloc"); CK(c->u_jk.alloc(nn), "alloc"); CK(c->u_keep.alloc(nn), "alloc");
+  CK(c->u_flag.alloc(nn), "alloc"); CK(c->u_orig.alloc(nn), "alloc");
+  if (n > 0) {
+    auto d2d = [&](void *d, const void *h, size_t bytes) {
+      return cudaMemcpyAsync(d, h, bytes, cudaMemcpyDeviceToDevice, st);
+    };
+    CK(d2d(c->u_x.p, s.x.p, 8 * n), "D2D"); CK(d2d(c->u_y.p, s.y.p, 8 * n), "D2D");
+    CK(d2d(c->u_z.p, s.z.p, 8 * n), "D2D"); CK(d2d(c->u_w.p, s.w.p, 8 * n), "D2D");
+    CK(d2d(c->u_e1.p, s.e1.p, 8 * n), "D2D"); CK(d2d(c->u_e2.p, s.e2.p, 8 * n), "D2D");
+    CK(d2d(c->u_phi.p, s.phi.p, 8 * n), "D2D"); CK(d2d(c->u_jk.p, s.jk.p, 4 * n), "D2D");
+    CK(d2d(c->u_keep.p, s.keep.p, n), "D2D"); CK(d2d(c->u_flag.p, s.aflag.p, n), "D2D");
+    CK(d2d(c->u_orig.p, s.orig.p, 8 * n), "D2D");
+  }
+  s.valid = false;
+  s.zbuilt = false;
+  s.version = ++c->version_ctr;
+  return build_cells(c, s, n, k, c->u_orig.p, false);
+}
+
 // ---------------------------------------------------------------------------
 // sky path (coordinates 0)
 // ---------------------------------------------------------------------------
@@ -1242,14 +1387,6 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   s.version = ++c->version_ctr;
   const double L = p.periodic_box_size;
   s.has_e = cat->e1 && cat->e2;
-  // grid: columns of width >= r_max / k over [0, box)
-  const int k = c->tune_k > 0 ? c->tune_k : 2;
-  int nc = (int)std::floor(L / (p.bin_r_max / k));
-  nc = std::max(1, std::min(nc, 2048));
-  s.ncx = s.ncy = nc;
-  s.cw_x = s.cw_y = L / nc;
-  s.n_reg = p.do_jk ? p.n_jk : 1;
-  if ((double)nc * nc * s.n_reg >= 4294967295.0) return fail(c, CPC_ERR_INVALID, "too many cell buckets");
   cudaStream_t st = c->st;
   // the caller's arrays, in input order, in context buffers reused by every
   // upload; absent optional arrays get the reference's defaults on the device
@@ -1303,99 +1440,7 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
     CK(cudaMemcpyAsync(&c->h_ustats, c->d_ustats.p, sizeof(UploadStats), cudaMemcpyDeviceToHost,
                        st), "D2H");
   }
-  CK(c->d_keys.alloc(nn), "alloc"); CK(c->d_ktmp.alloc(nn), "alloc");
-  CK(c->d_vals.alloc(nn), "alloc"); CK(c->d_vtmp.alloc(nn), "alloc");
-  CK(c->d_hist.alloc(radix_hist_words(nn)), "alloc");
-  CK(c->d_census.alloc(8 * 256), "alloc");
-  CK(c->d_bucket.alloc(nn), "alloc");
-  CK(s.pos.alloc(nn), "alloc"); CK(s.shp.alloc(nn), "alloc"); CK(s.zf.alloc(nn), "alloc");
-  CK(s.lo.alloc(nn), "alloc");
-  CK(s.x.alloc(nn), "alloc"); CK(s.y.alloc(nn), "alloc"); CK(s.z.alloc(nn), "alloc");
-  CK(s.w.alloc(nn), "alloc"); CK(s.e1.alloc(nn), "alloc"); CK(s.e2.alloc(nn), "alloc");
-  CK(s.phi.alloc(nn), "alloc"); CK(s.jk.alloc(nn), "alloc"); CK(s.keep.alloc(nn), "alloc");
-  CK(s.orig.alloc(nn), "alloc");
-  CK(launch_cell_keys(n, ox.p, oy.p, oz.p, ojk.p, 1.0 / s.cw_x, 1.0 / s.cw_y, s.ncx, s.ncy, s.n_reg,
-                      c->d_keys.p, c->d_vals.p, st), "cell keys");
-  CK(radix_sort_pairs(n, c->d_keys.p, c->d_vals.p, c->d_ktmp.p, c->d_vtmp.p, c->d_hist.p,
-                      c->d_census.p, st, &c->launches), "radix sort");
-  if (n > 0) c->launches += 2;  // cell keys + gather
-  GatherIn in{ox.p, oy.p, oz.p, ow.p, oe1.p, oe2.p, ophi.p, ojk.p, okeep.p};
-  GatherOut go{};
-  go.pos = s.pos.p; go.shp = s.shp.p; go.lo = s.lo.p; go.zf = s.zf.p; go.bucket = c->d_bucket.p;
-  go.x = s.x.p; go.y = s.y.p; go.z = s.z.p; go.w = s.w.p; go.e1 = s.e1.p; go.e2 = s.e2.p;
-  go.phi = s.phi.p; go.jk = s.jk.p; go.keep = s.keep.p; go.orig = s.orig.p; go.orig_in = nullptr;
-  CK(launch_gather(n, c->d_keys.p, c->d_vals.p, in, go, st), "gather");
-  CK(s.aflag.alloc(nn), "alloc");
-  if (n > 0) {
-    CK(launch_gather_u8(n, c->d_vals.p, oflag.p, s.aflag.p, st), "gather");
-    c->launches += 1;
-  }
-  // buckets on the host
-  std::vector<uint32_t> hb(n);
-  s.h_pos.resize(n);
-  if (n > 0) {
-    CK(cudaMemcpyAsync(hb.data(), c->d_bucket.p, 4 * n, cudaMemcpyDeviceToHost, st), "D2H");
-    CK(cudaMemcpyAsync(s.h_pos.data(), s.pos.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, st), "D2H");
-  }
-  CK(cudaStreamSynchronize(st), "upload");
-  {  // the device checks (first failing row of each kind) and statistics
-    const UploadStats &u = c->h_ustats;
-    static const char *what[4] = {"non-finite position", "position outside [0, box_size]",
-                                  "non-finite weight, ellipticity or phi",
-                                  "jackknife label out of range"};
-    int kind = -1;
-    for (int q = 0; q < 4; q++)
-      if (u.bad_row[q] != ~0ull && (kind < 0 || u.bad_row[q] < u.bad_row[kind])) kind = q;
-    if (kind >= 0)
-      return fail(c, CPC_ERR_RANGE,
-                  std::string(what[kind]) + " at row " + std::to_string(u.bad_row[kind]));
-    double v;
-    std::memcpy(&v, &u.cmax_bits, 8); s.cmax = v;
-    std::memcpy(&v, &u.wmax_bits, 8); s.wmax = v;
-    std::memcpy(&v, &u.emax_bits, 8); s.emax = v;
-    std::memcpy(&v, &u.phimax_bits, 8); s.phimax = v;
-    s.wmin = n > 0 ? from_orderable_key(u.wmin_key) : 1.0;
-    s.exact_f32 = u.not_f32 == 0;
-  }
-  s.h_bk_start.clear(); s.h_bk_end.clear(); s.h_bk_region.clear();
-  std::vector<float> bz0, bz1;
-  const int ncol = s.ncx * s.ncy;
-  std::vector<int> cb(ncol, 0), ce(ncol, 0);
-  for (int64_t i = 0; i < n;) {
-    int64_t j = i + 1;
-    while (j < n && hb[j] == hb[i]) j++;
-    const int b = (int)s.h_bk_start.size();
-    const int col = (int)(hb[i] / s.n_reg), reg = (int)(hb[i] % s.n_reg);
-    if (ce[col] == 0 && cb[col] == 0) cb[col] = b;
-    ce[col] = b + 1;
-    s.h_bk_start.push_back((int)i);
-    s.h_bk_end.push_back((int)j);
-    s.h_bk_region.push_back(reg);
-    bz0.push_back(s.h_pos[i].z);
-    bz1.push_back(s.h_pos[j - 1].z);
-    i = j;
-  }
-  // columns with no bucket: empty range
-  for (int q = 0; q < ncol; q++)
-    if (ce[q] == 0) cb[q] = 0;
-  const size_t nbk = std::max<size_t>(1, s.h_bk_start.size());
-  CK(s.bk_start.alloc(nbk), "alloc"); CK(s.bk_end.alloc(nbk), "alloc");
-  CK(s.bk_region.alloc(nbk), "alloc"); CK(s.bk_zmin.alloc(nbk), "alloc");
-  CK(s.bk_zmax.alloc(nbk), "alloc"); CK(s.col_begin.alloc(ncol), "alloc");
-  CK(s.col_end.alloc(ncol), "alloc");
-  const size_t nb = s.h_bk_start.size();
-  if (nb) {
-    CK(cudaMemcpyAsync(s.bk_start.p, s.h_bk_start.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(s.bk_end.p, s.h_bk_end.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(s.bk_region.p, s.h_bk_region.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(s.bk_zmin.p, bz0.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
-    CK(cudaMemcpyAsync(s.bk_zmax.p, bz1.data(), 4 * nb, cudaMemcpyHostToDevice, st), "H2D");
-  }
-  CK(cudaMemcpyAsync(s.col_begin.p, cb.data(), 4 * ncol, cudaMemcpyHostToDevice, st), "H2D");
-  CK(cudaMemcpyAsync(s.col_end.p, ce.data(), 4 * ncol, cudaMemcpyHostToDevice, st), "H2D");
-  CK(cudaStreamSynchronize(st), "upload");
-  s.valid = true;
-  return CPC_OK;
+  return build_cells(c, s, n, c->tune_k > 0 ? c->tune_k : 2, nullptr, true);
 }
 
 cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, cpc_engine engine,
@@ -1434,6 +1479,66 @@ cpc_status cpc_count_auto(cpc_ctx *c, cpc_pair_kind kind, int slot, cpc_engine e
   if (s != CPC_OK) return s;
   if (engine == CPC_ENGINE_FP64) return run_plain(jobs[0]);
   return run_fast(jobs);
+}
+
+cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2,
+                        int64_t sample_stride, int *cells_per_rmax, int *pi_window) {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  const cpc_params &p = c->p;
+  if (slot_g1 < 0 || slot_g1 >= kMaxSlots || slot_g2 < 0 || slot_g2 >= kMaxSlots)
+    return fail(c, CPC_ERR_INVALID, "slot out of range");
+  if (!c->slots[slot_g1].valid || !c->slots[slot_g2].valid)
+    return fail(c, CPC_ERR_STATE, "autotune before upload");
+  if (p.coordinates != 6) {  // the sky kernel has no cell or window knobs
+    if (cells_per_rmax) *cells_per_rmax = 0;
+    if (pi_window) *pi_window = 0;
+    return CPC_OK;
+  }
+  int nh, nb, npb;
+  cpc_accum_shape(c, &nh, &nb, &npb);
+  std::vector<int64_t> num((size_t)nh * nb * npb);
+  std::vector<double> sums(num.size() * kNF);
+  cpc_accum acc{};
+  acc.num = num.data();
+  acc.sums = sums.data();
+  const int ks[3] = {2, 3, 4};
+  const int ws[4] = {0, 16, 24, 32};
+  const int64_t stride = std::max<int64_t>(1, sample_stride);
+  double best = INFINITY;
+  int bk = c->slots[slot_g1].kcells, bw = c->tune_wpi;
+  for (int k : ks) {
+    cpc_status s;
+    if (c->slots[slot_g1].kcells != k && (s = rebuild_cells(c, c->slots[slot_g1], k)) != CPC_OK)
+      return s;
+    if (slot_g2 != slot_g1 && c->slots[slot_g2].kcells != k &&
+        (s = rebuild_cells(c, c->slots[slot_g2], k)) != CPC_OK)
+      return s;
+    for (int w : ws) {
+      if (w > p.n_p_bin) continue;
+      c->tune_wpi = w;
+      // first run builds the work units, the second is timed
+      if (cpc_count(c, kind, slot_g1, slot_g2, CPC_ENGINE_FAST, stride, 0, &acc) != CPC_OK) continue;
+      if (cpc_count(c, kind, slot_g1, slot_g2, CPC_ENGINE_FAST, stride, 0, &acc) != CPC_OK) continue;
+      if (acc.pair_kernel_ms < best) {
+        best = acc.pair_kernel_ms;
+        bk = k;
+        bw = w;
+      }
+    }
+  }
+  // keep the best: every box slot on the chosen grid (counts pair slots of one grid)
+  c->tune_k = bk;
+  c->tune_wpi = bw;
+  for (int q = 0; q < kMaxSlots; q++) {
+    Slot &sl = c->slots[q];
+    if (sl.valid && !sl.sky && sl.kcells != bk) {
+      const cpc_status s = rebuild_cells(c, sl, bk);
+      if (s != CPC_OK) return s;
+    }
+  }
+  if (cells_per_rmax) *cells_per_rmax = bk;
+  if (pi_window) *pi_window = bw;
+  return CPC_OK;
 }
 
 cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind *kinds,

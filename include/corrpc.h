@@ -178,6 +178,15 @@ cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind
  * block (64 or 128). */
 cpc_status cpc_set_tuning(cpc_ctx *ctx, int cells_per_rmax, int pi_window, int tile);
 
+/* Autotuner: times the fast kernel on every `sample_stride`-th outer row of
+ * this pair type for cell widths r_max / k (k = 2, 3, 4; the cell lists are
+ * rebuilt on the device) and block-local Pi windows (automatic, 16, 24, 32
+ * bins), keeps the fastest for this context (as cpc_set_tuning would) and
+ * returns it.  Results never depend on the choice.  Box runs only (sky runs
+ * return zeros). */
+cpc_status cpc_autotune(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_g2,
+                        int64_t sample_stride, int *cells_per_rmax, int *pi_window);
+
 /* Number of GPU kernels this context has launched so far (all entry points;
  * for a batch, counted on the first job's context). */
 cpc_status cpc_launch_count(const cpc_ctx *ctx, int64_t *launches);

@@ -130,3 +130,25 @@ def test_bad_inputs_are_rejected_with_status():
     with pytest.raises(_lib.CpcError) as e:
         ctx.count("SD", 0, 1)
     assert e.value.status == 5  # CPC_ERR_STATE: count before upload
+
+
+def test_autotune_keeps_results_identical():
+    """The autotuner rebuilds the cell lists on the device for several cell
+    widths and Pi windows, keeps the fastest; the counts stay the reference's."""
+    g = Golden("box_wgp_clustered")
+    p = g.params
+    cats = host.prepare(p, [("S", g.S), ("D", g.D)])
+    ctx = _lib.Context(p)
+    ctx.upload(0, cats["D"])
+    ctx.upload(1, cats["S"])
+    k, w = ctx.autotune("SD", 0, 1, sample_stride=2)
+    assert k in (2, 3, 4) and w in (0, 16, 24, 32)
+    r = ctx.count("SD", 0, 1)
+    assert r["n_binned"] == g.n_in and r["n_window"] == g.n_total
+    assert np.array_equal(r["num"], g.raw_num)
+    check_sums(r["sums"], g.raw_sums)
+    # a later upload uses the tuned grid and pairs with the rebuilt slot
+    ctx.upload(0, cats["D"])
+    r2 = ctx.count("SD", 0, 1)
+    assert np.array_equal(r2["num"], g.raw_num)
+    ctx.close()
