@@ -535,6 +535,20 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               }
               const int elk = n2 - n2_base;
               if ((unsigned)elk >= (unsigned)wpi) amb = true;
+              // raw (un-shifted) separation for the orientation angle
+              // (angle_orient_axis_PB); coincident positions give atan(0/0) in
+              // the reference: those pairs take the exact path
+              float dxr = 0.f, dyr = 0.f;
+              if (C != COREL_DD) {
+                dxr = (p2.x + g2sx) - r1.x;
+                dyr = (p2.y + g2sy) - r1.y;
+                if (has_lo) {
+                  const float2 lo1 = s_rlo[er], lo2 = s_lo[ec];
+                  dxr += lo2.x - lo1.x;
+                  dyr += lo2.y - lo1.y;
+                }
+                if (dxr == 0.0f && dyr == 0.0f) amb = true;
+              }
               if (amb || edge) {
                 // near the window edge (not yet counted) or a bin edge (window
                 // counted): exact FP64 evaluation
@@ -550,13 +564,6 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               if (C != COREL_DD) {
                 const float4 e1v = s_rshp[er];
                 const float4 s2 = s_shp[ec];
-                float dxr = (p2.x + g2sx) - r1.x;
-                float dyr = (p2.y + g2sy) - r1.y;
-                if (has_lo) {
-                  const float2 lo1 = s_rlo[er], lo2 = s_lo[ec];
-                  dxr += lo2.x - lo1.x;
-                  dyr += lo2.y - lo1.y;
-                }
                 const float a = dxr * dxr, b = dyr * dyr;
                 const float inv = __fdividef(1.0f, a + b);
                 const float c2 = (a - b) * inv, s2v = 2.0f * dxr * dyr * inv;

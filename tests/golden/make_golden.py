@@ -191,7 +191,40 @@ def sky_cases():
     r = synth.sky_patch(1500, 40, t, ra_deg=4, dec_deg=4, chi_range=(600, 900), nside_jk=2)
     out.append(("sky_twins_clamp", synth.SkyWorkload("sky_twins_clamp", p, t, both, both, r, r),
                 True))
+
+    # a box without periodic images (coordinates 6, periodic_box 0: lim_calc_xyz,
+    # Landy-Szalay with randoms); the distances file is read but unused.  No
+    # jackknife: lim_calc_xyz never sets the row's region (ct.gjk[0]) and the
+    # reference crashes in corel_jk1 with do_jk on.
+    p = _nbox_params(which_corr=1, njk=0)
+    t = synth.flat_lcdm_table(p.z_max, p.dz)
+    d = _nbox_clustered(57)
+    r = synth.uniform_box(3000, 100.0, 58, nside_jk=2)
+    out.append(("nbox_wgp_ls", synth.SkyWorkload("nbox_wgp_ls", p, t, d, d, r, r), True))
     return out
+
+
+def _nbox_params(*, which_corr, njk):
+    p = synth._box_params(which_corr=which_corr, L=100.0, rmin=0.3, rmax=20.0, nrp=8, npi=10,
+                          pmax=25.0, njk=njk, n=0)
+    p.periodic_box = 0
+    p.dz = 1.0
+    p.z_max = 100.0
+    return p
+
+
+def _nbox_clustered(seed):
+    """Neyman-Scott points inside [0, 100)^3 without wrapping (parents kept
+    away from the faces)."""
+    rng = np.random.default_rng(seed)
+    parents = rng.uniform(10.0, 90.0, size=(40, 3))
+    counts = rng.poisson(40, 40)
+    pos = np.repeat(parents, counts, axis=0) + rng.normal(0.0, 2.0, size=(int(counts.sum()), 3))
+    pos = np.clip(pos, 0.0, 99.999)
+    e1, e2 = synth.shapes(rng, pos.shape[0])
+    jk = synth.jk_cubes(pos[:, 0], pos[:, 1], pos[:, 2], 100.0, 2)
+    return synth.Catalog(pos[:, 0].copy(), pos[:, 1].copy(), pos[:, 2].copy(), None, e1, e2,
+                         jk).sorted_by_z()
 
 
 def run_sky_case(name, wl, same):
@@ -257,6 +290,12 @@ def auto_cases():
                         with_shapes=True, weights=True)
     r = synth.sky_patch(4000, 56, t, ra_deg=6, dec_deg=6, chi_range=(500, 900), nside_jk=3)
     out.append(("auto_sky_wgp", p, d, r, t))
+
+    p = _nbox_params(which_corr=0, njk=0)
+    p.estimator = 1
+    t = synth.flat_lcdm_table(p.z_max, p.dz)
+    out.append(("auto_nbox_wgg", p, _nbox_clustered(59),
+                synth.uniform_box(2500, 100.0, 60, nside_jk=2), t))
     return out
 
 

@@ -20,8 +20,10 @@ def golden_names():
 
 
 def sky_golden_names():
-    """Sky fixtures (four terms each: SRd, RsRd, SD, DRs)."""
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "sky_*.npz")))
+    """Cross runs with randoms and a distances table (four terms each: SRd, RsRd,
+    SD, DRs): the sky fixtures and the box without periodic images."""
+    return sorted(os.path.basename(p)[:-4] for pat in ("sky_*.npz", "nbox_*.npz")
+                  for p in glob.glob(os.path.join(GOLDEN, pat)))
 
 
 def auto_golden_names():
@@ -65,8 +67,9 @@ class AutoGolden:
 
 
 class SkyGolden:
-    """A sky cross run as the reference computed it: four catalogues, the
-    distances table and, per term, the raw histograms and pair counters.  The
+    """A cross run with randoms (sky, or a box without periodic images) as the
+    reference computed it: four catalogues, the distances table and, per term,
+    the raw histograms and pair counters.  The
     reference's DRs term was run as a density-density count (its wg+ DRs term
     crashes), so only its counts and weights are compared."""
 

@@ -27,7 +27,7 @@ def test_cli_output_files_match_reference(name, tmp_path):
         compare_files(open(out + fname).read(), ref, label=f"{name}:{fname}")
 
 
-@pytest.mark.parametrize("name", ["sky_wgp_jk", "sky_wgg_distinct_wrap"])
+@pytest.mark.parametrize("name", ["sky_wgp_jk", "sky_wgg_distinct_wrap", "nbox_wgp_ls"])
 def test_cli_sky_output_files_match_reference(name, tmp_path):
     """A sky cross run through the command line: reads the four catalogues and
     the distances file, counts SRd, RsRd, SD, DRs on the GPU, finalises with
@@ -49,7 +49,7 @@ def test_cli_sky_output_files_match_reference(name, tmp_path):
 
 
 @pytest.mark.parametrize("name", ["auto_box_wgg", "auto_box_wpp_rebin", "auto_box_wgp_unsorted",
-                                  "auto_sky_wgp"])
+                                  "auto_sky_wgp", "auto_nbox_wgg"])
 def test_cli_auto_output_files_match_reference(name, tmp_path):
     """Auto-correlation runs (estimators 1 and 2) through the command line:
     corels1 on the GPU, final_calc_auto (re_bin for estimator 2), the
