@@ -48,7 +48,7 @@ class cpc_params(ctypes.Structure):
 
 class cpc_catalog(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64)] + [(n, ctypes.c_void_p) for n in (
-        "x", "y", "z", "w", "e1", "e2", "phi", "jk", "jk_prob", "dc", "da")]
+        "x", "y", "z", "w", "e1", "e2", "phi", "jk", "jk_prob", "dc", "da", "e3")]
 
 
 class cpc_device_catalog(ctypes.Structure):
@@ -191,8 +191,9 @@ class Context:
         return k.value, w.value
 
     def upload(self, slot: int, cat) -> None:
-        """cat: object with x, y, z and optional w, e1, e2, phi, jk, jk_prob
-        (and dc, da for sky catalogues)."""
+        """cat: object with x, y, z and optional w, e1, e2, phi, jk, jk_prob, e3
+        (kappa as e1 for which_corr 3, 4; the ED orientation as e1, e2, e3 for
+        which_corr 5; dc, da for sky catalogues)."""
         keep = []
 
         def ptr(a, dt=np.float64):
@@ -211,6 +212,7 @@ class Context:
         c.jk = ptr(getattr(cat, "jk", None), np.int32)
         c.jk_prob = ptr(getattr(cat, "jk_prob", None))
         c.dc, c.da = ptr(getattr(cat, "dc", None)), ptr(getattr(cat, "da", None))
+        c.e3 = ptr(getattr(cat, "e3", None))
         check(self.lib.cpc_upload(self.h, slot, ctypes.byref(c)), self.h)
         self.sizes[slot] = c.n
 

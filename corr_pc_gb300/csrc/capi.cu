@@ -71,8 +71,8 @@ struct Slot {
   // device, cell order
   DevBuf<float4> pos, shp;
   DevBuf<float2> lo;
-  DevBuf<float> zf;
-  DevBuf<double> x, y, z, w, e1, e2, phi;
+  DevBuf<float> zlo, zf;
+  DevBuf<double> x, y, z, w, e1, e2, phi, e3;
   DevBuf<int32_t> jk;
   DevBuf<uint8_t> keep;
   DevBuf<int64_t> orig;
@@ -84,7 +84,7 @@ struct Slot {
   std::vector<int> h_bk_start, h_bk_end, h_bk_region;
   // z-ordered FP64 copy for the plain kernel (built on first use)
   bool zbuilt = false;
-  DevBuf<double> zx, zy, zz, zw, ze1, ze2, zphi;
+  DevBuf<double> zx, zy, zz, zw, ze1, ze2, zphi, ze3;
   DevBuf<int32_t> zjk;
   DevBuf<uint8_t> zkeep, zaflag;
   DevBuf<int64_t> zorig;
@@ -136,7 +136,7 @@ struct cpc_ctx {
   DevBuf<uint32_t> d_vals, d_vtmp, d_hist, d_bucket;
   DevBuf<unsigned long long> d_census;
   // upload scratch: a catalogue in input order, its checks and statistics
-  DevBuf<double> u_x, u_y, u_z, u_w, u_e1, u_e2, u_phi, u_prob;
+  DevBuf<double> u_x, u_y, u_z, u_w, u_e1, u_e2, u_phi, u_prob, u_e3;
   DevBuf<int32_t> u_jk;
   DevBuf<uint8_t> u_keep, u_flag;
   DevBuf<int64_t> u_orig;
@@ -191,10 +191,16 @@ float f_down(double v) {
 }
 
 cpc_status validate_params(cpc_ctx *c, const cpc_params &p) {
-  if (p.coordinates != 6 && p.coordinates != 0)
+  if (p.coordinates != 6 && p.coordinates != 7 && p.coordinates != 0)
     return fail(c, CPC_ERR_INVALID,
-                "coordinates: 6 (x,y,z with r_p, Pi) and 0 (sky, r_p and Pi) are supported");
-  if (p.which_corr < 0 || p.which_corr > 2) return fail(c, CPC_ERR_INVALID, "which_corr must be 0, 1 or 2");
+                "coordinates: 6 (x,y,z with r_p, Pi), 7 (x,y,z with r, mu) and 0 (sky, r_p and "
+                "Pi) are supported");
+  if (p.which_corr < 0 || p.which_corr > 5)
+    return fail(c, CPC_ERR_INVALID, "which_corr must be in 0..5");
+  // coordinates 7 outside a periodic box takes the sky window (lim_calc_sky,
+  // corr.cpp:311-324) in the reference: not a box computation
+  if (p.coordinates == 7 && !p.periodic_box)
+    return fail(c, CPC_ERR_INVALID, "coordinates 7 (r, mu) needs a periodic box");
   if (p.sig_crit != 0) return fail(c, CPC_ERR_INVALID, "sig_crit weights are not supported");
   if (p.rand_subsample != 0) return fail(c, CPC_ERR_INVALID, "rand_subsample is not supported");
   if (p.do_jk != 0 && p.do_jk != 1) return fail(c, CPC_ERR_INVALID, "do_jk must be 0 or 1");
@@ -206,6 +212,8 @@ cpc_status validate_params(cpc_ctx *c, const cpc_params &p) {
   if (!(p.p_max > p.p_min)) return fail(c, CPC_ERR_INVALID, "bad Pi bin limits");
   if (p.coordinates == 0) {
     if (p.periodic_box) return fail(c, CPC_ERR_INVALID, "coordinates 0 (sky) cannot be periodic");
+    if (p.which_corr > 2)
+      return fail(c, CPC_ERR_INVALID, "which_corr 3-5 (kappa, ED) run in x,y,z (coordinates 6, 7)");
     if (!p.H_z || !p.dA_z || p.n_table < 2)
       return fail(c, CPC_ERR_INVALID, "sky runs need the distance table (H_z, dA_z, n_table)");
     if (!(p.dz > 0) || !(p.z_max > 0) || !std::isfinite(p.z_sep_max))
@@ -215,7 +223,8 @@ cpc_status validate_params(cpc_ctx *c, const cpc_params &p) {
   if (!(p.periodic_box_size > 0)) return fail(c, CPC_ERR_INVALID, "box size must be > 0");
   if (p.periodic_box) {
     const double L = p.periodic_box_size;
-    if (p.bin_r_max > L || p.p_max > L || -p.p_min > L)
+    const bool rmu = p.coordinates == 7;  // p_min, p_max bound mu there
+    if (p.bin_r_max > L || (!rmu && (p.p_max > L || -p.p_min > L)))
       return fail(c, CPC_ERR_INVALID, "bin limits larger than the periodic box");
   }
   return CPC_OK;
@@ -236,7 +245,8 @@ int job_rule(const cpc_params &p, cpc_pair_kind kind, int64_t n1, int64_t n2, Jo
   int corel;
   if (kind == CPC_PAIR_RSRS || kind == CPC_PAIR_RSRD || p.which_corr == 0) corel = COREL_DD;
   else if (p.which_corr == 1) corel = COREL_SD;
-  else corel = (kind == CPC_PAIR_SD) ? COREL_SS : COREL_SD;
+  else if (p.which_corr == 2) corel = (kind == CPC_PAIR_SD) ? COREL_SS : COREL_SD;
+  else corel = COREL_DK + (p.which_corr - 3);  // 3 DK, 4 SK, 5 ED
   if (corel == COREL_SS && p.estimator != 0) corel = COREL_SSA;
   r.swapped = 0;
   if (n2 > n1) {
@@ -253,7 +263,8 @@ int job_rule(const cpc_params &p, cpc_pair_kind kind, int64_t n1, int64_t n2, Jo
 int job_rule_auto(const cpc_params &p, cpc_pair_kind kind, JobRule &r) {
   int corel;
   if (kind == CPC_PAIR_RSRS) corel = COREL_DD;
-  else if (kind == CPC_PAIR_SS) corel = p.which_corr == 0 ? COREL_DD : COREL_SS;
+  else if (kind == CPC_PAIR_SS)
+    corel = p.which_corr == 0 ? COREL_DD : p.which_corr <= 2 ? COREL_SS : COREL_DK + (p.which_corr - 3);
   else return -1;
   if (corel == COREL_SS && p.estimator != 0) corel = COREL_SSA;
   r.swapped = 0;
@@ -267,6 +278,7 @@ void fill_views(Slot &s, FCat &f, DCat &d) {
   f.pos = s.pos.p;
   f.shp = s.shp.p;
   f.lo = s.lo.p;
+  f.zlo = s.zlo.p;
   f.zf = s.zf.p;
   f.keep = s.keep.p;
   f.aflag = s.aflag.p;
@@ -279,9 +291,14 @@ void fill_views(Slot &s, FCat &f, DCat &d) {
   f.col_end = s.col_end.p;
   d.n = s.n;
   d.x = s.x.p; d.y = s.y.p; d.z = s.z.p; d.w = s.w.p;
-  d.e1 = s.e1.p; d.e2 = s.e2.p; d.phi = s.phi.p;
+  d.e1 = s.e1.p; d.e2 = s.e2.p; d.phi = s.phi.p; d.e3 = s.e3.p;
   d.jk = s.jk.p; d.keep = s.keep.p; d.orig = s.orig.p; d.aflag = s.aflag.p;
 }
+
+// z window offsets of lim_calc_xyz (PB_calcs.cpp:12-28): [p_min, p_max], or
+// [-r_max, r_max] for coordinates 7 (p_min, p_max then bound mu)
+double wz_lo(const cpc_params &p) { return p.coordinates == 7 ? -p.bin_r_max : p.p_min; }
+double wz_hi(const cpc_params &p) { return p.coordinates == 7 ? p.bin_r_max : p.p_max; }
 
 // error bound (absolute, per coordinate difference) of the FP32 separations
 double eps_abs(const cpc_ctx *c, const Slot &a, const Slot &b) {
@@ -290,7 +307,7 @@ double eps_abs(const cpc_ctx *c, const Slot &a, const Slot &b) {
   const double cmax = std::max({a.cmax, b.cmax, L});
   double e = 0;
   if (!(a.exact_f32 && b.exact_f32)) e += ulpf(cmax);
-  const double wmax = std::max({p.bin_r_max, p.p_max, -p.p_min});
+  const double wmax = std::max({p.bin_r_max, wz_hi(p), -wz_lo(p)});
   if (p.periodic_box && !(wmax <= 0.45 * L)) e += ulpf(2 * cmax);
   return e;
 }
@@ -330,14 +347,17 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   jp.empty = (A.n == 0 || B.n == 0);
   const int nrp = p.n_bins, npi = p.n_p_bin;
   const int jk = p.do_jk ? 1 : 0;
-  // block-local Pi window: as many Pi bins as fit two blocks per SM
+  // block-local Pi window: as many Pi bins as fit two blocks per SM.  With
+  // coordinates 7 the mu bins have no locality in z: a block holds every mu bin
+  // when they fit (else the units are repeated over slices of wpi mu bins)
+  const bool rmu = p.coordinates == 7;
   const size_t static_b = fast_static_smem_bytes();
   const size_t budget = (size_t)(227 * 1024) / 2 - static_b - 1024;
   int wpi = npi;
-  if (c->tune_wpi > 0) wpi = std::min(npi, c->tune_wpi);
+  if (c->tune_wpi > 0 && !rmu) wpi = std::min(npi, c->tune_wpi);
   else
-    while (wpi > 8 && fast_smem_bytes(jp.rule.corel, jk, nrp * wpi) > budget) wpi--;
-  if (wpi < npi && wpi < 8) wpi = std::min(npi, 8);
+    while (wpi > (rmu ? 1 : 8) && fast_smem_bytes(jp.rule.corel, jk, nrp * wpi) > budget) wpi--;
+  if (!rmu && wpi < npi && wpi < 8) wpi = std::min(npi, 8);
   jp.wpi = wpi;
   jp.tile = kTileThreads;
 
@@ -360,6 +380,7 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   J.box_same_keep = 1;  // jk_check_PB (jk.cpp:64-71) for coordinates 6
   J.auto_mode = auto_mode;
   J.has_lo = (g1.exact_f32 && g2.exact_f32) ? 0 : 1;
+  J.rmu = rmu ? 1 : 0;
   J.ncx = g1.ncx;
   J.ncy = g1.ncy;
   J.row_stride = jp.row_stride;
@@ -371,6 +392,8 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   J.rmax = p.bin_r_max;
   J.pmin = p.p_min;
   J.pmax = p.p_max;
+  J.wz_lo = wz_lo(p);
+  J.wz_hi = wz_hi(p);
   J.ps = c->ps;
   J.rsize = c->rsize;
   for (int k = 0; k <= nrp; k++) J.thr[k] = c->thr_rp[k];
@@ -378,24 +401,41 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   // difference, 2^-20 on r^2, plus the absolute representation/wrap error.
   const double ea = eps_abs(c, g1, g2);
   const double crel = std::ldexp(1.0, -21);
-  const double dtiny = 1e-12 * (L + std::max({p.bin_r_max, p.p_max, -p.p_min}));
+  const double zlo_w = J.wz_lo, zhi_w = J.wz_hi;
+  const double dtiny = 1e-12 * (L + std::max({p.bin_r_max, zhi_w, -zlo_w}));
   const double gxy = crel * p.bin_r_max + 2 * ea + dtiny;
   J.xy_in = f_down(p.bin_r_max - gxy);
   J.xy_out = f_up(p.bin_r_max + gxy);
   auto gp = [&](double v) { return crel * std::fabs(v) + 2 * ea + dtiny + 1e-30; };
-  J.pi_in_lo = f_up(p.p_min + gp(p.p_min));
-  J.pi_out_lo = f_down(p.p_min - gp(p.p_min));
-  J.pi_in_hi = f_down(p.p_max - gp(p.p_max));
-  J.pi_out_hi = f_up(p.p_max + gp(p.p_max));
-  for (int k = 0; k < npi; k++) {
-    const double lo = c->thr_pi[k], hi = c->thr_pi[k + 1];
-    J.PA[k] = f_up(lo + gp(lo));
-    J.PB[k] = f_down(hi - gp(hi));
+  J.pi_in_lo = f_up(zlo_w + gp(zlo_w));
+  J.pi_out_lo = f_down(zlo_w - gp(zlo_w));
+  J.pi_in_hi = f_down(zhi_w - gp(zhi_w));
+  J.pi_out_hi = f_up(zhi_w + gp(zhi_w));
+  if (!rmu) {
+    for (int k = 0; k < npi; k++) {
+      const double lo = c->thr_pi[k], hi = c->thr_pi[k + 1];
+      J.PA[k] = f_up(lo + gp(lo));
+      J.PB[k] = f_down(hi - gp(hi));
+    }
+  } else {
+    // mu bins: the edges themselves (nearest float); a pair is inside bin k when
+    // dz - PA[k] r >= mu_rel r + mu_abs and PB[k] r - dz > mu_rel r + mu_abs,
+    // which covers the float errors of dz, r, the edge and the products
+    for (int k = 0; k < npi; k++) {
+      J.PA[k] = (float)c->thr_pi[k];
+      J.PB[k] = (float)c->thr_pi[k + 1];
+    }
+    const double tmax = std::max({1.0, std::fabs(p.p_min), std::fabs(p.p_max)});
+    J.mu_rel = (float)(std::ldexp(1.0, -19) * tmax);
+    J.mu_abs = (float)(8 * ea * tmax + dtiny + 1e-30);
   }
   J.inv_ps_f = (float)(1.0 / c->ps);
   J.tp0 = (float)(-p.p_min / c->ps);
+  // r^2 error bound: two squared differences (r_p), three for coordinates 7 (r)
+  const double nterm = rmu ? 3.0 : 2.0;
   auto gr = [&](double T) {
-    return std::ldexp(1.0, -20) * T * T + 2.0 * std::sqrt(2.0) * T * ea + 2 * ea * ea + 1e-12 * T * T;
+    return std::ldexp(1.0, -20) * T * T + 2.0 * std::sqrt(nterm) * T * ea + nterm * ea * ea +
+           1e-12 * T * T;
   };
   for (int k = 0; k < nrp; k++) {
     const double lo = c->thr_rp[k], hi = c->thr_rp[k + 1];
@@ -430,6 +470,10 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
     vb[6] = vb[8] = vb[10] = wm * wm * em * em * em * em;
     vb[11] = tm2;
     vb[12] = 2 * tm * tm;
+    if (jp.rule.corel == COREL_ED) {  // cos^2 <= |e|^2 <= 3 max|e_k|^2
+      vb[11] = std::max(1.0, 3 * em * em);
+      vb[12] = vb[11] * vb[11];
+    }
     for (int f = 0; f < kNF; f++) {
       const double v = std::max(vb[f] * 1.0001, 1e-30);
       int S = 26 - (int)std::ceil(std::log2(v));
@@ -466,12 +510,16 @@ const std::vector<UnitDesc> &build_units(JobPlan &jp) {
   const int npi = p.n_p_bin, wpi = jp.wpi;
   const double cmax = std::max(g1.cmax, L);
   const double ea = eps_abs(c, g1, c->slots[jp.s2]);
-  const double guard = 4 * ulpf(2 * cmax) + 2 * ea + std::ldexp(1.0, -20) * (std::fabs(p.p_min) + std::fabs(p.p_max) + p.bin_r_max);
+  const bool rmu = p.coordinates == 7;
+  const double zw0 = wz_lo(p), zw1 = wz_hi(p);
+  const double guard = 4 * ulpf(2 * cmax) + 2 * ea + std::ldexp(1.0, -20) * (std::fabs(zw0) + std::fabs(zw1) + p.bin_r_max);
   // tile z-extent: wide enough that the 32 lanes of a warp (spread over the
   // tile) see different Pi bins, small enough to fit the block-local window
-  double Emax = 0.25 * (p.p_max - p.p_min);
-  if (wpi < npi) Emax = std::min(Emax, (wpi - 6) * ps / 2.0);
-  Emax = std::max(Emax, std::min(2.0 * ps, 0.25 * (p.p_max - p.p_min)));
+  double Emax = 0.25 * (zw1 - zw0);
+  if (!rmu) {
+    if (wpi < npi) Emax = std::min(Emax, (wpi - 6) * ps / 2.0);
+    Emax = std::max(Emax, std::min(2.0 * ps, 0.25 * (p.p_max - p.p_min)));
+  }
   const int ncx = g1.ncx, ncy = g1.ncy;
   const double inv_cwx = 1.0 / g1.cw_x, inv_cwy = 1.0 / g1.cw_y;
   std::vector<UnitDesc> &units = uc.units;
@@ -505,7 +553,7 @@ const std::vector<UnitDesc> &build_units(JobPlan &jp) {
         cx0 = std::max(cx0, 0); cx1 = std::min(cx1, ncx - 1);
         cy0 = std::max(cy0, 0); cy1 = std::min(cy1, ncy - 1);
       }
-      const double Zlo = zt0 + p.p_min - guard, Zhi = zt1 + p.p_max + guard;
+      const double Zlo = zt0 + zw0 - guard, Zhi = zt1 + zw1 + guard;
       for (int k = 0; k < nt; k++) {
         UnitDesc u;
         std::memset(&u, 0, sizeof u);
@@ -514,11 +562,15 @@ const std::vector<UnitDesc> &build_units(JobPlan &jp) {
         u.g1_count = (m - k + nt - 1) / nt;
         u.region = g1.h_bk_region[b];
         u.cx_lo = cx0; u.cx_hi = cx1; u.cy_lo = cy0; u.cy_hi = cy1;
-        if (wpi >= npi) {
-          u.n2_base = 0;
+        if (wpi >= npi || rmu) {
+          // coordinates 7: one unit per slice of wpi mu bins; each pair is
+          // taken by the slice holding its estimated bin (pair_fast.cu)
           u.zlo = Zlo;
           u.zhi = Zhi;
-          units.push_back(u);
+          for (int base = 0; base < npi; base += wpi) {
+            u.n2_base = base;
+            units.push_back(u);
+          }
         } else {
           const double span = std::max(ps, (wpi - 4) * ps - (zt1 - zt0));
           const int U = std::max(1, (int)std::ceil((Zhi - Zlo) / span));
@@ -614,11 +666,11 @@ cpc_status build_zorder(cpc_ctx *c, Slot &s) {
   CK(s.zx.alloc(n), "alloc"); CK(s.zy.alloc(n), "alloc"); CK(s.zz.alloc(n), "alloc");
   CK(s.zw.alloc(n), "alloc"); CK(s.ze1.alloc(n), "alloc"); CK(s.ze2.alloc(n), "alloc");
   CK(s.zphi.alloc(n), "alloc"); CK(s.zjk.alloc(n), "alloc"); CK(s.zkeep.alloc(n), "alloc");
-  CK(s.zorig.alloc(n), "alloc");
-  GatherIn in{s.x.p, s.y.p, s.z.p, s.w.p, s.e1.p, s.e2.p, s.phi.p, s.jk.p, s.keep.p};
+  CK(s.zorig.alloc(n), "alloc"); CK(s.ze3.alloc(n), "alloc");
+  GatherIn in{s.x.p, s.y.p, s.z.p, s.w.p, s.e1.p, s.e2.p, s.phi.p, s.jk.p, s.keep.p, s.e3.p};
   GatherOut out{};
   out.x = s.zx.p; out.y = s.zy.p; out.z = s.zz.p; out.w = s.zw.p;
-  out.e1 = s.ze1.p; out.e2 = s.ze2.p; out.phi = s.zphi.p; out.jk = s.zjk.p;
+  out.e1 = s.ze1.p; out.e2 = s.ze2.p; out.phi = s.zphi.p; out.e3 = s.ze3.p; out.jk = s.zjk.p;
   out.keep = s.zkeep.p; out.orig = s.zorig.p; out.orig_in = s.orig.p;
   CK(launch_gather(n, c->d_keys.p, c->d_vals.p, in, out, st), "z gather");
   CK(s.zaflag.alloc(n), "alloc");
@@ -633,7 +685,7 @@ DCat zview(Slot &s) {
   DCat d;
   d.n = s.n;
   d.x = s.zx.p; d.y = s.zy.p; d.z = s.zz.p; d.w = s.zw.p;
-  d.e1 = s.ze1.p; d.e2 = s.ze2.p; d.phi = s.zphi.p;
+  d.e1 = s.ze1.p; d.e2 = s.ze2.p; d.phi = s.zphi.p; d.e3 = s.ze3.p;
   d.jk = s.zjk.p; d.keep = s.zkeep.p; d.orig = s.zorig.p; d.aflag = s.zaflag.p;
   return d;
 }
@@ -772,7 +824,7 @@ cpc_status build_cells(cpc_ctx *c, Slot &s, int64_t n, int k, const int64_t *ori
   const size_t nn = std::max<int64_t>(n, 1);
   cudaStream_t st = c->st;
   DevBuf<double> &ox = c->u_x, &oy = c->u_y, &oz = c->u_z, &ow = c->u_w, &oe1 = c->u_e1,
-                 &oe2 = c->u_e2, &ophi = c->u_phi;
+                 &oe2 = c->u_e2, &ophi = c->u_phi, &oe3 = c->u_e3;
   DevBuf<int32_t> &ojk = c->u_jk;
   DevBuf<uint8_t> &okeep = c->u_keep, &oflag = c->u_flag;
   // grid: columns of width >= r_max / k over [0, box)
@@ -789,7 +841,7 @@ cpc_status build_cells(cpc_ctx *c, Slot &s, int64_t n, int k, const int64_t *ori
   CK(c->d_census.alloc(8 * 256), "alloc");
   CK(c->d_bucket.alloc(nn), "alloc");
   CK(s.pos.alloc(nn), "alloc"); CK(s.shp.alloc(nn), "alloc"); CK(s.zf.alloc(nn), "alloc");
-  CK(s.lo.alloc(nn), "alloc");
+  CK(s.lo.alloc(nn), "alloc"); CK(s.zlo.alloc(nn), "alloc"); CK(s.e3.alloc(nn), "alloc");
   CK(s.x.alloc(nn), "alloc"); CK(s.y.alloc(nn), "alloc"); CK(s.z.alloc(nn), "alloc");
   CK(s.w.alloc(nn), "alloc"); CK(s.e1.alloc(nn), "alloc"); CK(s.e2.alloc(nn), "alloc");
   CK(s.phi.alloc(nn), "alloc"); CK(s.jk.alloc(nn), "alloc"); CK(s.keep.alloc(nn), "alloc");
@@ -799,10 +851,12 @@ cpc_status build_cells(cpc_ctx *c, Slot &s, int64_t n, int k, const int64_t *ori
   CK(radix_sort_pairs(n, c->d_keys.p, c->d_vals.p, c->d_ktmp.p, c->d_vtmp.p, c->d_hist.p,
                       c->d_census.p, st, &c->launches), "radix sort");
   if (n > 0) c->launches += 2;  // cell keys + gather
-  GatherIn in{ox.p, oy.p, oz.p, ow.p, oe1.p, oe2.p, ophi.p, ojk.p, okeep.p};
+  GatherIn in{ox.p, oy.p, oz.p, ow.p, oe1.p, oe2.p, ophi.p, ojk.p, okeep.p, oe3.p};
   GatherOut go{};
-  go.pos = s.pos.p; go.shp = s.shp.p; go.lo = s.lo.p; go.zf = s.zf.p; go.bucket = c->d_bucket.p;
+  go.pos = s.pos.p; go.shp = s.shp.p; go.lo = s.lo.p; go.zlo = s.zlo.p; go.zf = s.zf.p;
+  go.bucket = c->d_bucket.p;
   go.x = s.x.p; go.y = s.y.p; go.z = s.z.p; go.w = s.w.p; go.e1 = s.e1.p; go.e2 = s.e2.p;
+  go.e3 = s.e3.p;
   go.phi = s.phi.p; go.jk = s.jk.p; go.keep = s.keep.p; go.orig = s.orig.p; go.orig_in = orig_in;
   CK(launch_gather(n, c->d_keys.p, c->d_vals.p, in, go, st), "gather");
   CK(s.aflag.alloc(nn), "alloc");
@@ -887,7 +941,7 @@ cpc_status rebuild_cells(cpc_ctx *c, Slot &s, int k) {
   CK(c->u_x.alloc(nn), "alloc"); CK(c->u_y.alloc(nn), "alloc"); CK(c->u_z.alloc(nn), "alloc");
   CK(c->u_w.alloc(nn), "alloc"); CK(c->u_e1.alloc(nn), "alloc"); CK(c->u_e2.alloc(nn), "alloc");
   CK(c->u_phi.alloc(nn), "alloc"); CK(c->u_jk.alloc(nn), "alloc"); CK(c->u_keep.alloc(nn), "alloc");
-  CK(c->u_flag.alloc(nn), "alloc"); CK(c->u_orig.alloc(nn), "alloc");
+  CK(c->u_flag.alloc(nn), "alloc"); CK(c->u_orig.alloc(nn), "alloc"); CK(c->u_e3.alloc(nn), "alloc");
   if (n > 0) {
     auto d2d = [&](void *d, const void *h, size_t bytes) {
       return cudaMemcpyAsync(d, h, bytes, cudaMemcpyDeviceToDevice, st);
@@ -898,6 +952,7 @@ cpc_status rebuild_cells(cpc_ctx *c, Slot &s, int k) {
     CK(d2d(c->u_phi.p, s.phi.p, 8 * n), "D2D"); CK(d2d(c->u_jk.p, s.jk.p, 4 * n), "D2D");
     CK(d2d(c->u_keep.p, s.keep.p, n), "D2D"); CK(d2d(c->u_flag.p, s.aflag.p, n), "D2D");
     CK(d2d(c->u_orig.p, s.orig.p, 8 * n), "D2D");
+    CK(d2d(c->u_e3.p, s.e3.p, 8 * n), "D2D");
   }
   s.valid = false;
   s.zbuilt = false;
@@ -1386,16 +1441,17 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   s.n = n;
   s.version = ++c->version_ctr;
   const double L = p.periodic_box_size;
-  s.has_e = cat->e1 && cat->e2;
+  s.has_e = cat->e1 || cat->e2 || cat->e3;
   cudaStream_t st = c->st;
   // the caller's arrays, in input order, in context buffers reused by every
   // upload; absent optional arrays get the reference's defaults on the device
   // (w 1, e 0, phi -10, region 0)
   const size_t nn = std::max<int64_t>(n, 1);
   DevBuf<double> &ox = c->u_x, &oy = c->u_y, &oz = c->u_z, &ow = c->u_w, &oe1 = c->u_e1,
-                 &oe2 = c->u_e2, &ophi = c->u_phi, &oprob = c->u_prob;
+                 &oe2 = c->u_e2, &ophi = c->u_phi, &oprob = c->u_prob, &oe3 = c->u_e3;
   DevBuf<int32_t> &ojk = c->u_jk;
   DevBuf<uint8_t> &okeep = c->u_keep, &oflag = c->u_flag;
+  CK(oe3.alloc(nn), "alloc");
   CK(ox.alloc(nn), "alloc"); CK(oy.alloc(nn), "alloc"); CK(oz.alloc(nn), "alloc");
   CK(ow.alloc(nn), "alloc"); CK(oe1.alloc(nn), "alloc"); CK(oe2.alloc(nn), "alloc");
   CK(ophi.alloc(nn), "alloc"); CK(oprob.alloc(nn), "alloc"); CK(ojk.alloc(nn), "alloc");
@@ -1415,14 +1471,11 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
     CK(h2d(oy.p, cat->y, 8 * n), "H2D");
     CK(h2d(oz.p, cat->z, 8 * n), "H2D");
     CK(cat->w ? h2d(ow.p, cat->w, 8 * n) : launch_fill_f64(n, 1.0, ow.p, st), "weights");
-    if (s.has_e) {
-      CK(h2d(oe1.p, cat->e1, 8 * n), "H2D");
-      CK(h2d(oe2.p, cat->e2, 8 * n), "H2D");
-    } else {
-      CK(cudaMemsetAsync(oe1.p, 0, 8 * n, st), "memset");
-      CK(cudaMemsetAsync(oe2.p, 0, 8 * n, st), "memset");
-    }
+    // e1 alone carries kappa (which_corr 3, 4)
+    CK(cat->e1 ? h2d(oe1.p, cat->e1, 8 * n) : cudaMemsetAsync(oe1.p, 0, 8 * n, st), "e1");
+    CK(cat->e2 ? h2d(oe2.p, cat->e2, 8 * n) : cudaMemsetAsync(oe2.p, 0, 8 * n, st), "e2");
     CK(cat->phi ? h2d(ophi.p, cat->phi, 8 * n) : launch_fill_f64(n, -10.0, ophi.p, st), "phi");
+    CK(cat->e3 ? h2d(oe3.p, cat->e3, 8 * n) : cudaMemsetAsync(oe3.p, 0, 8 * n, st), "e3");
     CK(p.do_jk ? h2d(ojk.p, cat->jk, 4 * n) : cudaMemsetAsync(ojk.p, 0, 4 * n, st), "labels");
     if (cat->jk_prob) CK(h2d(oprob.p, cat->jk_prob, 8 * n), "H2D");
     CK(h2d(c->d_ustats.p, &c->h_ustats, sizeof(UploadStats)), "H2D");
@@ -1432,8 +1485,9 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
     pin.e1 = s.has_e ? oe1.p : nullptr; pin.e2 = s.has_e ? oe2.p : nullptr;
     pin.phi = cat->phi ? ophi.p : nullptr; pin.jk_prob = cat->jk_prob ? oprob.p : nullptr;
     pin.jk = p.do_jk ? ojk.p : nullptr;
+    pin.e3 = cat->e3 ? oe3.p : nullptr;
     pin.L = L;
-    pin.p_min = p.p_min;
+    pin.wz_lo = wz_lo(p);
     pin.n_jk = p.n_jk;
     CK(launch_prep_catalog(pin, okeep.p, oflag.p, c->d_ustats.p, st), "catalogue checks");
     c->launches += 1;

@@ -230,12 +230,13 @@ __global__ void gather_kernel(int64_t n, const uint64_t *__restrict__ keys,
   if (k >= n) return;
   const uint32_t i = perm[k];
   const double x = in.x[i], y = in.y[i], z = in.z[i], w = in.w[i];
-  const double e1 = in.e1[i], e2 = in.e2[i], phi = in.phi[i];
+  const double e1 = in.e1[i], e2 = in.e2[i], phi = in.phi[i], e3 = in.e3[i];
   if (out.pos) {
     out.pos[k] = make_float4((float)x, (float)y, (float)z, (float)w);
-    out.shp[k] = make_float4((float)e1, (float)e2, (float)phi, 0.f);
+    out.shp[k] = make_float4((float)e1, (float)e2, (float)phi, (float)e3);
     out.zf[k] = (float)z;
     out.lo[k] = make_float2((float)(x - (double)(float)x), (float)(y - (double)(float)y));
+    out.zlo[k] = (float)(z - (double)(float)z);
   }
   if (out.bucket) out.bucket[k] = (uint32_t)(keys[k] >> 32);
   out.x[k] = x;
@@ -245,6 +246,7 @@ __global__ void gather_kernel(int64_t n, const uint64_t *__restrict__ keys,
   out.e1[k] = e1;
   out.e2[k] = e2;
   out.phi[k] = phi;
+  out.e3[k] = e3;
   out.jk[k] = in.jk[i];
   out.keep[k] = in.keep[i];
   out.orig[k] = out.orig_in ? out.orig_in[i] : (int64_t)i;
@@ -304,7 +306,8 @@ __device__ __forceinline__ unsigned long long nonneg_bits(double v) {
 // One pass over a catalogue in input order (the host checks of the reference's
 // read path plus what the pair kernels need): see UploadStats.  The corels1
 // scan starts compare, as do_pair_sorted does, z + L*PBz with z_min = z_i + p_min
-// (lim_calc_PB): row i + 1 for the 0 and -1 images, row 0 for the +1 image.
+// (lim_calc_PB; z_i - r_max for coordinates 7): row i + 1 for the 0 and -1
+// images, row 0 for the +1 image.
 __global__ void prep_catalog_kernel(PrepIn in, uint8_t *__restrict__ keep,
                                     uint8_t *__restrict__ aflag, UploadStats *__restrict__ st) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -329,6 +332,12 @@ __global__ void prep_catalog_kernel(PrepIn in, uint8_t *__restrict__ keep,
       bad |= !isfinite(a) || !isfinite(b);
       em = nonneg_bits(fmax(fabs(a), fabs(b)));
     }
+    if (in.e3) {
+      const double c3 = in.e3[i];
+      bad |= !isfinite(c3);
+      const double m3 = fabs(c3);
+      if (nonneg_bits(m3) > em) em = nonneg_bits(m3);
+    }
     const double ph = in.phi ? in.phi[i] : -10.0;
     bad |= !isfinite(ph);
     pm = nonneg_bits(fabs(ph));
@@ -338,7 +347,7 @@ __global__ void prep_catalog_kernel(PrepIn in, uint8_t *__restrict__ keep,
       if (r < 0 || r >= in.n_jk) atomicMin(&st->bad_row[3], (unsigned long long)i);
     }
     keep[i] = (in.jk_prob && in.jk_prob[i] >= 0.5) ? 1 : 0;
-    const double zmin = __dadd_rn(z, in.p_min);
+    const double zmin = __dadd_rn(z, in.wz_lo);
     uint8_t f = 0;
     if (i + 1 < in.n) {
       const double zn = in.z[i + 1];

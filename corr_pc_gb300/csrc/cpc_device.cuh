@@ -22,13 +22,24 @@ constexpr int kMaxRp = 64;     // r_p bins supported
 constexpr int kMaxPi = 128;    // Pi bins supported
 constexpr int kMaxSlots = 8;
 
-enum Corel { COREL_DD = 0, COREL_SD = 1, COREL_SS = 2, COREL_SSA = 3 };
+// corel functions (initialization.cpp:490-538): density_density, shape_density,
+// shape_shape (estimator 0 branch / other estimators), density_convergence,
+// shape_convergence, ED_corel
+enum Corel {
+  COREL_DD = 0, COREL_SD = 1, COREL_SS = 2, COREL_SSA = 3,
+  COREL_DK = 4, COREL_SK = 5, COREL_ED = 6
+};
+// the corel uses the orientation angle of the pair (angle_orient_axis)
+__host__ __device__ inline bool corel_has_theta(int c) {
+  return c == COREL_SD || c == COREL_SS || c == COREL_SSA || c == COREL_SK;
+}
 static_assert(kNF == kPairFields, "field count");
 
 // double-precision catalogue view (recheck and plain FP64 kernel)
 struct DCat {
   int64_t n;
   const double *x, *y, *z, *w, *e1, *e2, *phi;
+  const double *e3;      // third orientation component (ED_corel)
   const int32_t *jk;
   const uint8_t *keep;
   const int64_t *orig;
@@ -41,6 +52,7 @@ struct FCat {
   const float4 *pos;
   const float4 *shp;
   const float2 *lo;   // x - (float)x, y - (float)y (non-float32 inputs)
+  const float *zlo;   // z - (float)z (non-float32 inputs)
   const float *zf;
   const uint8_t *keep;
   const uint8_t *aflag;  // corels1 scan starts of this row (kAuto* bits)
@@ -69,6 +81,7 @@ struct JobDev {
   int box_same_keep;        // 1 for the box (jk_check_PB), 0 for the sky
   int auto_mode;            // 0 corels2; corels1: 1 unsorted, 2 z-sorted scan
   int has_lo;               // positions are not float32-exact: use hi+lo for theta
+  int rmu;                  // coordinates 7: bins of r = |(dx, dy, Pi)| and mu = Pi / r
   int ncx, ncy;
   int64_t row_stride, row_offset;
   // ---- fast-path single precision constants ----
@@ -79,6 +92,7 @@ struct JobDev {
   float l2rmin2, inv_lw;               // log2(r_min^2), 1/(log2 width in r^2)
   float rmin_f, inv_rsize_f;           // linear-bin estimate
   float rej_lo, rej_hi;                // definite r^2 rejection bounds
+  float mu_rel, mu_abs;                // coordinates 7: mu-bin margin mu_rel r + mu_abs (dz units)
   float qscale[kNF];                   // per-field fixed-point scale 2^S_f
   int qbias;                           // fixed-point bound: |v_f| 2^S_f <= qbias
   int unit_w;                          // every weight is 1: wt_num = count
@@ -86,6 +100,8 @@ struct JobDev {
   float PA[kMaxPi], PB[kMaxPi];        // definite Pi band of Pi bin k
   // ---- FP64 exact constants ----
   double L, rmin, rmax, pmin, pmax, ps, rsize;
+  double wz_lo, wz_hi;                 // z window offsets: p_min, p_max (coordinates 6)
+                                       // or -r_max, r_max (coordinates 7)
   double inv_qscale[kNF];
   double thr[kMaxRp + 1];              // exact r_p thresholds (host libm)
   // ---- outputs ----
@@ -140,45 +156,25 @@ __host__ __device__ inline void shift_decode(int c, int &sx, int &sy, int &sz) {
 }
 
 // ---------------------------------------------------------------------------
-// Exact evaluation of one (g1, g2, image) triple with the reference's double
-// arithmetic: no contraction into FMA (explicit _rn intrinsics), same operation
-// order.  Window predicates: PB_calcs.cpp:12-61 and corr.cpp:67-86; binning:
-// corels.cpp:21-46 with PB_calcs.cpp:87-98; r_p bin from the host-computed
-// exact thresholds of floor(log10(r/r_min)/r_size).
-// Returns: 0 not a window pair, 1 window pair outside the bins, 2 binned.
+// Binning of one window pair with the reference's double arithmetic (no
+// contraction into FMA: explicit _rn intrinsics, same operation order):
+// corel_bin (corels.cpp:21-46) with pi_calc_PB / rp_calc_PB (PB_calcs.cpp:87-98)
+// and, for coordinates 7, r_mu_calc (calcs.cpp:135-140): r = sqrt(r_p^2 + Pi^2)
+// from the already rounded r_p, mu = Pi / r in place of Pi.  The r (or r_p) bin
+// comes from the host-computed exact thresholds of floor(log10(r/r_min)/r_size).
+// Returns 1 for a window pair outside the bins, 2 binned (n1, n2 set).
 // ---------------------------------------------------------------------------
-__device__ inline int exact_classify(const JobDev &J, const DCat &g1, int64_t i,
-                                     const DCat &g2, int64_t j, int sx, int sy, int sz,
-                                     int &n1, int &n2) {
-  const double x1 = g1.x[i], y1 = g1.y[i], z1 = g1.z[i];
-  const double x2 = g2.x[j], y2 = g2.y[j], z2 = g2.z[j];
-  // lim_calc_xyz / lim_calc_PB
-  const double z_max = __dadd_rn(z1, J.pmax), z_min = __dadd_rn(z1, J.pmin);
-  const double ra_max = __dadd_rn(x1, J.rmax), ra_min = __dsub_rn(x1, J.rmax);
-  const double dec_max = __dadd_rn(y1, J.rmax), dec_min = __dsub_rn(y1, J.rmax);
-  if (J.periodic) {
-    if (sz == 1 && !(z_max > J.L)) return 0;
-    if (sz == -1 && !(z_min < 0)) return 0;
-    if (sx == 1 && !(ra_max > J.L)) return 0;
-    if (sx == -1 && !(ra_min < 0)) return 0;
-    if (sy == 1 && !(dec_max > J.L)) return 0;
-    if (sy == -1 && !(dec_min < 0)) return 0;
-  } else if (sx | sy | sz) {
-    return 0;
+__device__ inline int exact_bin(const JobDev &J, double x1, double y1, double z1, double x2s,
+                                double y2s, double z2s, int &n1, int &n2) {
+  double dP = __dsub_rn(z2s, z1);
+  const double t0 = __dsub_rn(x1, x2s), t1 = __dsub_rn(y1, y2s);
+  double rp = __dsqrt_rn(__dadd_rn(__dmul_rn(t0, t0), __dmul_rn(t1, t1)));
+  if (J.rmu) {
+    rp = __dsqrt_rn(__dadd_rn(__dmul_rn(rp, rp), __dmul_rn(dP, dP)));
+    dP = __ddiv_rn(dP, rp);
   }
-  const double Lsx = J.L * sx, Lsy = J.L * sy, Lsz = J.L * sz;  // exact (s in -1..1)
-  const double z2s = __dadd_rn(z2, Lsz);
-  if (z2s > z_max || z2s < z_min) return 0;
-  const double y2s = __dadd_rn(y2, Lsy);
-  if (y2s > dec_max || y2s < dec_min) return 0;
-  const double x2s = __dadd_rn(x2, Lsx);
-  if (x2s < ra_min || x2s > ra_max) return 0;
-  // corel_bin
-  const double dP = __dsub_rn(z2s, z1);
   const double v2 = floor(__ddiv_rn(__dsub_rn(dP, J.pmin), J.ps));
   if (!(v2 >= 0.0) || v2 >= (double)J.npi) return 1;
-  const double t0 = __dsub_rn(x1, x2s), t1 = __dsub_rn(y1, y2s);
-  const double rp = __dsqrt_rn(__dadd_rn(__dmul_rn(t0, t0), __dmul_rn(t1, t1)));
   int k1;
   if (J.lin_bin) {
     const double v1 = floor(__ddiv_rn(__dsub_rn(rp, J.rmin), J.rsize));
@@ -198,16 +194,58 @@ __device__ inline int exact_classify(const JobDev &J, const DCat &g1, int64_t i,
   return 2;
 }
 
-// Per-pair accumulator values in double (corels.cpp:48-77, 122-244; calcs.cpp
-// 54-64, 97-105) for a binned pair of the box: theta from the raw, un-shifted
-// positions (angle_orient_axis_PB).  f[0..12] as in the output layout.
+// Exact evaluation of one (g1, g2, image) triple: window predicates of
+// PB_calcs.cpp:12-61 (lim_calc_xyz, lim_calc_PB: z window [z1 + p_min, z1 +
+// p_max], or [z1 - r_max, z1 + r_max] for coordinates 7) and corr.cpp:67-86,
+// then exact_bin.  Returns: 0 not a window pair, 1 window pair outside the
+// bins, 2 binned.
+__device__ inline int exact_classify(const JobDev &J, const DCat &g1, int64_t i,
+                                     const DCat &g2, int64_t j, int sx, int sy, int sz,
+                                     int &n1, int &n2) {
+  const double x1 = g1.x[i], y1 = g1.y[i], z1 = g1.z[i];
+  const double x2 = g2.x[j], y2 = g2.y[j], z2 = g2.z[j];
+  // lim_calc_xyz / lim_calc_PB
+  const double z_max = __dadd_rn(z1, J.wz_hi), z_min = __dadd_rn(z1, J.wz_lo);
+  const double ra_max = __dadd_rn(x1, J.rmax), ra_min = __dsub_rn(x1, J.rmax);
+  const double dec_max = __dadd_rn(y1, J.rmax), dec_min = __dsub_rn(y1, J.rmax);
+  if (J.periodic) {
+    if (sz == 1 && !(z_max > J.L)) return 0;
+    if (sz == -1 && !(z_min < 0)) return 0;
+    if (sx == 1 && !(ra_max > J.L)) return 0;
+    if (sx == -1 && !(ra_min < 0)) return 0;
+    if (sy == 1 && !(dec_max > J.L)) return 0;
+    if (sy == -1 && !(dec_min < 0)) return 0;
+  } else if (sx | sy | sz) {
+    return 0;
+  }
+  const double Lsx = J.L * sx, Lsy = J.L * sy, Lsz = J.L * sz;  // exact (s in -1..1)
+  const double z2s = __dadd_rn(z2, Lsz);
+  if (z2s > z_max || z2s < z_min) return 0;
+  const double y2s = __dadd_rn(y2, Lsy);
+  if (y2s > dec_max || y2s < dec_min) return 0;
+  const double x2s = __dadd_rn(x2, Lsx);
+  if (x2s < ra_min || x2s > ra_max) return 0;
+  return exact_bin(J, x1, y1, z1, x2s, y2s, z2s, n1, n2);
+}
+
+// Per-pair accumulator values in double (corels.cpp:48-262; calcs.cpp 54-64,
+// 97-105; PB_calcs.cpp:101-134) for a binned pair of the box in image (sx, sy,
+// sz): theta from the raw, un-shifted positions (angle_orient_axis_PB), the ED
+// separation g1 - (g2 + L*shift) (ED_calc_PB).  f[0..12] as in the output
+// layout.
 __device__ inline void exact_values(const JobDev &J, const DCat &g1, int64_t i, const DCat &g2,
-                                    int64_t j, double f[kNF]) {
+                                    int64_t j, int sx, int sy, int sz, double f[kNF]) {
   const double wt = __dmul_rn(g1.w[i], g2.w[j]);
   double theta = 0.0;
-  if (J.corel != COREL_DD) theta = atan((g2.y[j] - g1.y[i]) / (g2.x[j] - g1.x[i]));
-  pair_values(J.corel, J.gws, wt, theta, PairGal{g1.e1[i], g1.e2[i], g1.phi[i]},
-              PairGal{g2.e1[j], g2.e2[j], g2.phi[j]}, f);
+  if (corel_has_theta(J.corel)) theta = atan((g2.y[j] - g1.y[i]) / (g2.x[j] - g1.x[i]));
+  double sep[3] = {0.0, 0.0, 0.0};
+  if (J.corel == COREL_ED) {
+    sep[0] = __dsub_rn(g1.x[i], __dadd_rn(g2.x[j], J.L * sx));
+    sep[1] = __dsub_rn(g1.y[i], __dadd_rn(g2.y[j], J.L * sy));
+    sep[2] = __dsub_rn(g1.z[i], __dadd_rn(g2.z[j], J.L * sz));
+  }
+  pair_values(J.corel, J.gws, wt, theta, PairGal{g1.e1[i], g1.e2[i], g1.phi[i], g1.e3[i]},
+              PairGal{g2.e1[j], g2.e2[j], g2.phi[j], g2.e3[j]}, f, sep);
 }
 
 // Add one binned pair (FP64 values) to the global accumulators, including the

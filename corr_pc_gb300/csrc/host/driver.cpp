@@ -68,10 +68,12 @@ int main(int argc, char **argv) {
     return 1;
   }
   outp_data_info(d, d.out_file + "inp.info");
-  if ((d.coordinates != 6 && d.coordinates != 0) || d.estimator < 0 || d.estimator > 3 ||
-      d.which_corr > 2 || d.sig_crit) {
-    std::cout << "this build runs wgg/wg+/w++ (which_corr 0-2) with estimators 0-3 in x,y,z "
-                 "(coordinates 6) or on the sky (coordinates 0)" << std::endl;
+  if ((d.coordinates != 6 && d.coordinates != 7 && d.coordinates != 0) || d.estimator < 0 ||
+      d.estimator > 3 || d.which_corr < 0 || d.which_corr > 5 || d.sig_crit ||
+      (d.coordinates == 7 && !d.periodic_box) || (d.coordinates == 0 && d.which_corr > 2)) {
+    std::cout << "this build runs which_corr 0-5 with estimators 0-3 in x,y,z (coordinates 6; "
+                 "7 in a periodic box) and which_corr 0-2 on the sky (coordinates 0)"
+              << std::endl;
     return 1;
   }
   Ctx ctx;

@@ -91,16 +91,22 @@ void add_count(Bins &b, const Info &d, const int64_t *num, const double *sums) {
 
 namespace {
 
-// RR_PB_calc: expected pair fraction per (r_p, Pi) bin in a periodic box
+// RR_PB_calc (PB_calcs.cpp:63-85): expected pair fraction per (r_p, Pi) bin in
+// a periodic box; per (r, mu) bin for coordinates 7 (shell volume times the
+// mu-bin width over 2)
 void rr_periodic(Bins &rr, int h, const Info &d) {
   const double total_volume = std::pow(d.periodic_box_size, 3);
   for (int i = 0; i < rr.nb; i++) {
     double area = 0;
     if (d.coordinates == 6) area = M_PI * (rr.b_max[i] * rr.b_max[i] - rr.b_min[i] * rr.b_min[i]);
+    else if (d.coordinates == 7)
+      area = 4. / 3. * M_PI *
+             (rr.b_max[i] * rr.b_max[i] * rr.b_max[i] - rr.b_min[i] * rr.b_min[i] * rr.b_min[i]);
     rr.bnum[rr.bi(h, i)] = 1;
     for (int k = 0; k < rr.np; k++) {
       double volume = 0;
       if (d.coordinates == 6) volume = area * (rr.p_max[k] - rr.p_min[k]);
+      else if (d.coordinates == 7) volume = area / 2 * (rr.p_max[k] - rr.p_min[k]);
       rr.pwt[rr.pi(h, i, k)] = volume / total_volume;
       rr.pnum[rr.pi(h, i, k)] = 1;
     }
@@ -131,8 +137,14 @@ void final_bins(Bins &sd, Bins &sr, Bins &dr, Bins &rr, Bins &fin, int h, const 
       if (d.which_corr == 0) continue;
       for (int j = 1; j < 7; j++) {
         const double sd_val = sd.pd(h, i, k, j, 0), sr_val = sr.pd(h, i, k, j, 0);
-        const double sd_norm = (sd_val / rr_w) * (RR_wt / SD_wt);
-        const double sr_norm = (sr_val / rr_w) * (RR_wt / SR_wt);
+        double sd_norm = 0, sr_norm = 0;
+        if (d.which_corr == 5 && j == 6) {  // ED: mean cos^2 minus its isotropic 1/3
+          if (sd_num > 0) sd_norm = sd_val / sd_w;
+          sd_norm -= 1. / 3;
+        } else {
+          sd_norm = (sd_val / rr_w) * (RR_wt / SD_wt);
+          sr_norm = (sr_val / rr_w) * (RR_wt / SR_wt);
+        }
         double val = sd_norm - sr_norm;
         if (sd_num == 0 || sr_num == 0 || rr_num == 0) {
           val = 0;

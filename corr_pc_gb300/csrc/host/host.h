@@ -54,10 +54,11 @@ cpc_params to_params(const Info &d);
 // One catalogue as read_data leaves it (flattened gal[]).
 struct Catalog {
   int64_t n = 0;
-  std::vector<double> x, y, z, w, e1, e2, phi, jk_prob, include_prob;
+  std::vector<double> x, y, z, w, e1, e2, e3, phi, jk_prob, include_prob;
   std::vector<double> dc, da;  // table rows at floor(z/dz) (not periodic)
   std::vector<int32_t> jk;
-  bool has_e = false;
+  bool has_e = false;   // e1, e2 hold e (or kappa in e1, e2 = 0)
+  bool has_e3 = false;  // the ED orientation's third component
   cpc_catalog view() const;
 };
 enum Role { ROLE_S = 0, ROLE_D = 1, ROLE_RS = 2, ROLE_RD = 3 };

@@ -1,6 +1,7 @@
 // reader.cpp -- the reference's catalogue input format (read_dat.cpp:18-347):
-// <prefix>_pos.dat (two columns), _z.dat, _e.dat (e1 e2), _wt.dat, _jk.dat
-// (integer labels), "0" meaning "absent".  Per galaxy it derives what the pair
+// <prefix>_pos.dat (two columns), _z.dat, _e.dat (e1 e2; one column of kappa
+// or phi, or three of the ED orientation, depending on which_corr and the file
+// name), _wt.dat, _jk.dat (integer labels), "0" meaning "absent".  Per galaxy it derives what the pair
 // loop reads: jk_prob (glibc rand()/(RAND_MAX+1.) in a periodic box, one draw
 // per galaxy in read order after srand(124693517); 1 otherwise, 0 without
 // jackknife), phi (elip_angle, or -10 without shapes), include_prob (a second
@@ -59,6 +60,53 @@ struct TextCols {
   }
 };
 
+// What a sample reads from its e file (read_dat.cpp:27-205): the which_corr
+// switch (case 5 falls through into case 8), the per-sample overrides, then
+// the file-name rule ("phi" or "kappa" in the name selects a one-column read).
+struct EFlags {
+  bool e = false, kappa = false, phi = false, e3 = false;
+  std::string file;
+  bool any() const { return e || kappa || phi || e3; }
+};
+
+EFlags e_flags(const Info &d, Role role) {
+  EFlags f;
+  f.e = true;
+  bool css = false;  // cross_shape_shape: the density sample reads density_e
+  switch (d.which_corr) {
+    case 0: f.e = false; break;
+    case 3: css = false; f.e = false; f.kappa = true; break;
+    case 4:
+      f.e = role == ROLE_S;
+      f.kappa = role != ROLE_S;
+      css = true;
+      break;
+    case 5:
+      f.e = false;
+      if (role == ROLE_S) f.e3 = true;
+      f.kappa = false;  // falls through into case 8
+      css = true;
+      break;
+    case 2: css = true; break;
+    default: css = false; break;
+  }
+  if (role == ROLE_S) {
+    f.file = d.shape_e;
+    if (d.which_corr == 4) { f.e = true; f.kappa = false; }
+  } else if (role == ROLE_D) {
+    if (css) f.file = d.density_e;
+    else f.e = f.kappa = f.phi = f.e3 = false;
+  } else {
+    f.e = f.kappa = f.phi = false;
+    if (role == ROLE_RS || role == ROLE_RD) f.e3 = false;
+  }
+  if (f.any()) {
+    if (f.file.find("phi") != std::string::npos || f.phi) { f.phi = true; f.e = false; f.kappa = false; }
+    if (f.file.find("kappa") != std::string::npos || f.kappa) { f.kappa = true; f.e = false; f.phi = false; }
+  }
+  return f;
+}
+
 }  // namespace
 
 cpc_catalog Catalog::view() const {
@@ -70,6 +118,7 @@ cpc_catalog Catalog::view() const {
   c.w = w.data();
   c.e1 = has_e ? e1.data() : nullptr;
   c.e2 = has_e ? e2.data() : nullptr;
+  c.e3 = has_e3 ? e3.data() : nullptr;
   c.phi = phi.data();
   c.jk = jk.empty() ? nullptr : jk.data();
   c.jk_prob = jk_prob.data();
@@ -79,25 +128,23 @@ cpc_catalog Catalog::view() const {
 }
 
 int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &err) {
-  // which samples read ellipticities (read_dat.cpp:27-150)
-  bool read_e = d.which_corr == 1 || d.which_corr == 2;
-  const bool cross_shape_shape = d.which_corr == 2;
-  std::string p_f, z_f, e_f, w_f, jk_f;
+  const EFlags ef = e_flags(d, role);
+  std::string p_f, z_f, w_f, jk_f;
+  const std::string &e_f = ef.file;
   double *wt = nullptr;
   int n_gal = 0;
   if (role == ROLE_S) {
-    p_f = d.shape_pos; z_f = d.shape_z; e_f = d.shape_e; w_f = d.shape_wt; jk_f = d.shape_jk;
+    p_f = d.shape_pos; z_f = d.shape_z; w_f = d.shape_wt; jk_f = d.shape_jk;
     n_gal = d.n_shape; wt = d.S_wt;
   } else if (role == ROLE_D) {
     p_f = d.density_pos; z_f = d.density_z; w_f = d.density_wt; jk_f = d.density_jk;
     n_gal = d.n_density; wt = d.D_wt;
-    if (cross_shape_shape) e_f = d.density_e; else read_e = false;
   } else if (role == ROLE_RS) {
     p_f = d.srand_pos; z_f = d.srand_z; w_f = d.srand_wt; jk_f = d.srand_jk;
-    n_gal = d.n_shape_rand; wt = d.Rs_wt; read_e = false;
+    n_gal = d.n_shape_rand; wt = d.Rs_wt;
   } else {
     p_f = d.drand_pos; z_f = d.drand_z; w_f = d.drand_wt; jk_f = d.drand_jk;
-    n_gal = d.n_density_rand; wt = d.Rd_wt; read_e = false;
+    n_gal = d.n_density_rand; wt = d.Rd_wt;
   }
   c = Catalog();
   if (n_gal == 0) return 0;  // read_dat.cpp:152-156: nothing read, no draws
@@ -108,7 +155,7 @@ int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &er
   if (!fz.open(z_f)) { err = "z file not open: " + z_f; return 1; }
   if (w_f != "0" && !fw.open(w_f)) { err = "wt file not open: " + w_f; return 1; }
   if (read_jk && !fj.open(jk_f)) { err = "jk file not open: " + jk_f; return 1; }
-  if (read_e && !fe.open(e_f)) { err = "e file not open: " + e_f; return 1; }
+  if (ef.any() && !fe.open(e_f)) { err = "e file not open: " + e_f; return 1; }
   const uint32_t seed = d.periodic_box ? 124693517u : 1u;  // srand only in a box
   cpc::GlibcRand rng(seed);
   for (int64_t s = 0; s < draws; s++) rng.next();
@@ -116,9 +163,14 @@ int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &er
   c.x.resize(n_gal); c.y.resize(n_gal); c.z.resize(n_gal); c.w.assign(n_gal, 1.0);
   c.phi.assign(n_gal, -10.0); c.jk_prob.assign(n_gal, 1.0); c.include_prob.assign(n_gal, 0.0);
   if (read_jk) c.jk.assign(n_gal, -1);
-  c.has_e = read_e;
+  const bool two = ef.e && !ef.kappa && !ef.phi;     // e1 e2, then elip_angle
+  const bool one_phi = !ef.e && ef.phi && !ef.kappa;  // phi
+  const bool one_kappa = ef.kappa && !ef.e && !ef.phi;  // kappa into e[0]
+  c.has_e = two || ef.e3 || one_kappa;
+  c.has_e3 = ef.e3;
   if (!d.periodic_box) { c.dc.resize(n_gal); c.da.resize(n_gal); }
-  if (read_e) { c.e1.resize(n_gal); c.e2.resize(n_gal); }
+  if (c.has_e) { c.e1.assign(n_gal, 0.0); c.e2.assign(n_gal, 0.0); }
+  if (c.has_e3) c.e3.assign(n_gal, 0.0);
   for (int i = 0; i < n_gal; i++) {
     if (!fp.get(c.x[i]) || !fp.get(c.y[i]) || !fz.get(c.z[i])) {
       err = "gal data reading ended unexpectedly at row " + std::to_string(i) + " of " + p_f;
@@ -144,10 +196,24 @@ int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &er
     if (d.do_jk == 0 || d.n_jk == 0) c.jk_prob[i] = 0;
     if (w_f != "0" && !fw.get(c.w[i])) { err = "wt file ended early"; return 1; }
     if (read_jk && !fj.get(c.jk[i])) { err = "jk file ended early"; return 1; }
-    if (read_e) {
+    if (two) {
       if (!fe.get(c.e1[i]) || !fe.get(c.e2[i])) { err = "e file ended early"; return 1; }
       c.phi[i] = cpc::elip_angle(c.e1[i], c.e2[i]);
     }
+    if (ef.e3) {  // read_dat.cpp:282-293: normalised to unit length when non-zero
+      if (!fe.get(c.e1[i]) || !fe.get(c.e2[i]) || !fe.get(c.e3[i])) {
+        err = "e file ended early";
+        return 1;
+      }
+      const double en = std::sqrt(c.e1[i] * c.e1[i] + c.e2[i] * c.e2[i] + c.e3[i] * c.e3[i]);
+      if (en > 0) {
+        c.e1[i] /= en;
+        c.e2[i] /= en;
+        c.e3[i] /= en;
+      }
+    }
+    if (one_phi && !fe.get(c.phi[i])) { err = "phi file ended early"; return 1; }
+    if (one_kappa && !fe.get(c.e1[i])) { err = "kappa file ended early"; return 1; }
     if (randoms) {
       c.include_prob[i] = rng.next() / (2147483647 + 1.);
       draws++;

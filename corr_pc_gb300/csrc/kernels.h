@@ -11,13 +11,15 @@ struct GatherIn {
   const double *x, *y, *z, *w, *e1, *e2, *phi;
   const int32_t *jk;
   const uint8_t *keep;
+  const double *e3;
 };
 struct GatherOut {
-  float4 *pos, *shp;  // null for the z-ordered (FP64) copy
+  float4 *pos, *shp;  // null for the z-ordered (FP64) copy; shp = (e1, e2, phi, e3)
   float2 *lo;
+  float *zlo;
   float *zf;
   uint32_t *bucket;   // null for the z-ordered copy
-  double *x, *y, *z, *w, *e1, *e2, *phi;
+  double *x, *y, *z, *w, *e1, *e2, *phi, *e3;
   int32_t *jk;
   uint8_t *keep;
   int64_t *orig;
@@ -53,8 +55,9 @@ struct UploadStats {
 struct PrepIn {
   int64_t n;
   const double *x, *y, *z, *w, *e1, *e2, *phi, *jk_prob;  // w, e1, e2, phi, jk_prob may be null
+  const double *e3;   // may be null
   const int32_t *jk;  // null without jackknife
-  double L, p_min;
+  double L, wz_lo;    // box size, lower z-window offset (p_min, or -r_max for coordinates 7)
   int n_jk;
 };
 cudaError_t launch_fill_f64(int64_t n, double v, double *out, cudaStream_t st);

@@ -68,6 +68,24 @@ template <> struct FieldMap<COREL_SSA> {
   __device__ static constexpr int m(int k) { return k; }
   __device__ static constexpr int j(int k) { return k == 0 ? 0 : 2 * k - 1; }
 };
+// density_convergence: wt, data[1].val
+template <> struct FieldMap<COREL_DK> {
+  static constexpr int FM = 2, FJ = 2;
+  __device__ static constexpr int m(int k) { return k; }
+  __device__ static constexpr int j(int k) { return k; }
+};
+// shape_convergence: wt, data[1].val, data[3].val, data[5].val
+template <> struct FieldMap<COREL_SK> {
+  static constexpr int FM = 4, FJ = 4;
+  __device__ static constexpr int m(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 5 : 9; }
+  __device__ static constexpr int j(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 5 : 9; }
+};
+// ED: wt, data[6].val, data[6].err (regions: wt, data[6].val)
+template <> struct FieldMap<COREL_ED> {
+  static constexpr int FM = 3, FJ = 2;
+  __device__ static constexpr int m(int k) { return k == 0 ? 0 : k == 1 ? 11 : 12; }
+  __device__ static constexpr int j(int k) { return k == 0 ? 0 : 11; }
+};
 
 // Shared-memory bytes a block needs for a job with NB = nrp * wpi local bins.
 size_t fast_smem_bytes(int corel, int do_jk, int NB) {
@@ -75,6 +93,9 @@ size_t fast_smem_bytes(int corel, int do_jk, int NB) {
   if (corel == COREL_SD) { FM = 7; FJ = 4; }
   if (corel == COREL_SS) { FM = 11; FJ = 6; }
   if (corel == COREL_SSA) { FM = 13; FJ = 7; }
+  if (corel == COREL_DK) { FM = 2; FJ = 2; }
+  if (corel == COREL_SK) { FM = 4; FJ = 4; }
+  if (corel == COREL_ED) { FM = 3; FJ = 2; }
   size_t b = sizeof(float4) * 2 * kBatch;                // staging
   b += 8ull * FM * NB + 4ull * NB;
   if (do_jk) b += 2 * (8ull * FJ * NB + 4ull * NB);
@@ -210,6 +231,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   // the tile's g1 rows, for the heavy step (any lane may process any row)
   __shared__ float4 s_rpos[kTile], s_rshp[kTile];
   __shared__ float2 s_rlo[kTile];
+  __shared__ float s_rzlo[kTile], s_zlo[kBatch];  // z lo parts (ED separations)
   __shared__ unsigned char s_rkeep[kTile];
   __shared__ unsigned s_wq[kThreads / 32][kQCap];
 
@@ -259,7 +281,11 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     bool valid = false;
     int oi = 0;       // input index of the row (corels1)
     uint8_t af = 0;   // its corels1 scan-start flags
-    const bool has_lo = C != COREL_DD && J.has_lo;
+    // hi + lo positions for the orientation angle (raw separations) and the ED
+    // separation
+    constexpr bool kTheta = C == COREL_SD || C == COREL_SS || C == COREL_SSA || C == COREL_SK;
+    const bool has_lo = (kTheta || C == COREL_ED) && J.has_lo;
+    const int rmu = J.rmu;
     const int gws = J.gws, lin_bin = J.lin_bin, box_same_keep = J.box_same_keep;
     const float rmin_f = J.rmin_f, inv_rsize_f = J.inv_rsize_f;
     if (has1) {
@@ -277,6 +303,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         s_rpos[tr] = p1;
         if (C != COREL_DD) s_rshp[tr] = J.f1.shp[i1];
         if (has_lo) s_rlo[tr] = J.f1.lo[i1];
+        if (C == COREL_ED && has_lo) s_rzlo[tr] = J.f1.zlo[i1];
         if (JK) s_rkeep[tr] = J.f1.keep[i1];
       }
     }
@@ -285,6 +312,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     const float pi_in_lo = J.pi_in_lo, pi_in_hi = J.pi_in_hi;
     const float pi_out_lo = J.pi_out_lo, pi_out_hi = J.pi_out_hi;
     const float inv_ps = J.inv_ps_f, tp0 = J.tp0;
+    const float mu_rel = J.mu_rel, mu_abs = J.mu_abs;
     for (int k = t; k < nrp; k += kThreads) { s_A[k] = J.A[k]; s_B[k] = J.B[k]; }
     for (int k = t; k < npi; k += kThreads) { s_PA[k] = J.PA[k]; s_PB[k] = J.PB[k]; }
     if (t < kNF) { s_qs[t] = J.qscale[t]; s_iqs[t] = J.inv_qscale[t]; }
@@ -454,6 +482,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             s_pos[t] = q2;
             if (C != COREL_DD) s_shp[t] = J.f2.shp[j2];
             if (has_lo) s_lo[t] = J.f2.lo[j2];
+            if (C == COREL_ED && has_lo) s_zlo[t] = J.f2.zlo[j2];
             s_jidx[t] = j2;
             if (J.auto_mode) s_orig[t] = (int)J.d2.orig[j2];
             if (JK) s_keep[t] = J.f2.keep[j2];
@@ -488,7 +517,9 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                   edge = true;
                 } else {
                   nwin++;
-                  const float r2 = fmaf(dx, dx, dy * dy);
+                  // r_p^2, or r^2 = r_p^2 + dz^2 for coordinates 7
+                  float r2 = fmaf(dx, dx, dy * dy);
+                  if (rmu) r2 = fmaf(dz, dz, r2);
                   binned = r2 >= rej_lo && r2 < rej_hi;
                 }
               }
@@ -516,14 +547,37 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               const float hdz = p2.z - (sz == 1 ? r1.z - Lf : r1.z);
               const float hdx = (sx == 1 ? r1.x - Lf : r1.x) - p2.x;
               const float hdy = (sy == 1 ? r1.y - Lf : r1.y) - p2.y;
-              const float r2 = fmaf(hdx, hdx, hdy * hdy);
-              bool amb = false;
-              int n2 = (int)floorf(fmaf(hdz, inv_ps, tp0));
-              n2 = min(max(n2, 0), npi - 1);
-              if (!(hdz >= s_PA[n2] && hdz < s_PB[n2])) {
-                if (n2 > 0 && hdz >= s_PA[n2 - 1] && hdz < s_PB[n2 - 1]) n2--;
-                else if (n2 + 1 < npi && hdz >= s_PA[n2 + 1] && hdz < s_PB[n2 + 1]) n2++;
-                else amb = true;
+              float r2 = fmaf(hdx, hdx, hdy * hdy);
+              bool amb = false, own = true;
+              int n2;
+              if (!rmu) {
+                n2 = (int)floorf(fmaf(hdz, inv_ps, tp0));
+                n2 = min(max(n2, 0), npi - 1);
+                if (!(hdz >= s_PA[n2] && hdz < s_PB[n2])) {
+                  if (n2 > 0 && hdz >= s_PA[n2 - 1] && hdz < s_PB[n2 - 1]) n2--;
+                  else if (n2 + 1 < npi && hdz >= s_PA[n2 + 1] && hdz < s_PB[n2 + 1]) n2++;
+                  else amb = true;
+                }
+              } else {
+                // coordinates 7: r = |(dx, dy, dz)|, mu = dz / r (r_mu_calc); the
+                // mu bin is certain when dz is farther than mu_rel r + mu_abs from
+                // both edges scaled by r.  A block holds the mu bins
+                // [n2_base, n2_base + wpi): each pair belongs to the unit whose
+                // slice holds its estimated bin, the others skip it
+                r2 = fmaf(hdz, hdz, r2);
+                const float r = sqrtf(r2);
+                n2 = r2 > 0.0f ? (int)floorf(fmaf(__fdividef(hdz, r), inv_ps, tp0)) : 0;
+                n2 = min(max(n2, 0), npi - 1);
+                own = n2 >= n2_base && n2 < n2_base + wpi;
+                const float mg = fmaf(r, mu_rel, mu_abs);
+                auto in_mu = [&](int k) {
+                  return hdz - s_PA[k] * r >= mg && s_PB[k] * r - hdz > mg;
+                };
+                if (!in_mu(n2)) {
+                  if (n2 > 0 && in_mu(n2 - 1)) n2--;
+                  else if (n2 + 1 < npi && in_mu(n2 + 1)) n2++;
+                  else amb = true;
+                }
               }
               int n1 = lin_bin ? (int)floorf((sqrtf(r2) - rmin_f) * inv_rsize_f)
                                : (int)floorf((__log2f(r2) - l2rmin2) * inv_lw);
@@ -539,7 +593,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               // (angle_orient_axis_PB); coincident positions give atan(0/0) in
               // the reference: those pairs take the exact path
               float dxr = 0.f, dyr = 0.f;
-              if (C != COREL_DD) {
+              if (kTheta) {
                 dxr = (p2.x + g2sx) - r1.x;
                 dyr = (p2.y + g2sy) - r1.y;
                 if (has_lo) {
@@ -549,7 +603,25 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                 }
                 if (dxr == 0.0f && dyr == 0.0f) amb = true;
               }
-              if (amb || edge) {
+              // ED: the shifted separation g1 - (g2 + L*PB) (ED_calc_PB) from
+              // hi + lo positions; a zero separation gives 0/0 in the reference
+              float sxe = 0.f, sye = 0.f, sze = 0.f, see = 1.f;
+              if (C == COREL_ED) {
+                sxe = hdx;
+                sye = hdy;
+                sze = -hdz;
+                if (has_lo) {
+                  const float2 lo1 = s_rlo[er], lo2 = s_lo[ec];
+                  sxe += lo1.x - lo2.x;
+                  sye += lo1.y - lo2.y;
+                  sze += s_rzlo[er] - s_zlo[ec];
+                }
+                see = fmaf(sxe, sxe, fmaf(sye, sye, sze * sze));
+                if (!(see > 0.0f)) amb = true;
+              }
+              if (!own) {
+                // another mu slice's pair
+              } else if (amb || edge) {
                 // near the window edge (not yet counted) or a bin edge (window
                 // counted): exact FP64 evaluation
                 const int64_t gi1 = (int64_t)U.g1_start +
@@ -561,14 +633,34 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               float v[kNF];
               const float w = r1.w * p2.w;
               v[0] = w;
-              if (C != COREL_DD) {
+              if (C == COREL_DK) {  // the shape holder's kappa (e[0])
+                v[1] = gws == 1 ? w * s_rshp[er].x : gws == 2 ? w * s_shp[ec].x : 0.0f;
+              } else if (C == COREL_ED) {
+                const float4 es = gws == 2 ? s_shp[ec] : s_rshp[er];
+                const float dot = fmaf(es.x, sxe, fmaf(es.y, sye, es.w * sze));
+                v[11] = __fdividef(dot * dot, see);
+                v[12] = v[11] * v[11];
+              } else if (C != COREL_DD) {
                 const float4 e1v = s_rshp[er];
                 const float4 s2 = s_shp[ec];
                 const float a = dxr * dxr, b = dyr * dyr;
                 const float inv = __fdividef(1.0f, a + b);
                 const float c2 = (a - b) * inv, s2v = 2.0f * dxr * dyr * inv;
                 const float theta = atanf(__fdividef(dyr, dxr));
-                if (C == COREL_SD) {
+                if (C == COREL_SK) {
+                  // rotate the shape holder's e, weight by the other's kappa
+                  if (gws == 1 || gws == 2) {
+                    const float4 es = gws == 2 ? s2 : e1v;
+                    const float kap = gws == 2 ? e1v.x : s2.x;
+                    const float en0 = c2 * es.x - s2v * es.y, en1 = s2v * es.x + c2 * es.y;
+                    const float ep = w * kap;
+                    v[1] = ep;
+                    v[5] = ep * en0;
+                    v[9] = ep * en1;
+                  } else {
+                    v[1] = v[5] = v[9] = 0.0f;
+                  }
+                } else if (C == COREL_SD) {
                   const float es0 = gws == 2 ? s2.x : e1v.x, es1 = gws == 2 ? s2.y : e1v.y;
                   const float ep = c2 * es0 - s2v * es1, ex = s2v * es0 + c2 * es1;
                   v[1] = w * ep;
@@ -657,9 +749,9 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y,
                                    f0, s_iqs, J);
     }
-    // window-pair counter
+    // window-pair counter (once per pair: mu slices other than the first skip it)
     {
-      unsigned long long v = (unsigned long long)nwin;
+      unsigned long long v = (rmu && n2_base != 0) ? 0ull : (unsigned long long)nwin;
       for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
       if (lane == 0) s_red[wid] = v;
       __syncthreads();
@@ -690,7 +782,7 @@ __global__ void recheck_kernel(const JobDev *__restrict__ jobs, const QEntry *__
     if (!(e.shift & kWindowCounted)) atomicAdd(&J.counters[1], 1ull);
     if (r == 2) {
       double f[kNF];
-      exact_values(J, J.d1, e.i1, J.d2, e.j2, f);
+      exact_values(J, J.d1, e.i1, J.d2, e.j2, sx, sy, sz, f);
       exact_accumulate(J, J.d1, e.i1, J.d2, e.j2, n1, n2, f);
     }
   }
@@ -724,6 +816,9 @@ cudaError_t launch_fast(int corel, int jk, const JobDev *jobs, const UnitDesc *u
   CPC_CASE(COREL_SD)
   CPC_CASE(COREL_SS)
   CPC_CASE(COREL_SSA)
+  CPC_CASE(COREL_DK)
+  CPC_CASE(COREL_SK)
+  CPC_CASE(COREL_ED)
 #undef CPC_CASE
   return cudaErrorInvalidValue;
 }
@@ -745,6 +840,9 @@ int fast_blocks_per_sm(int corel, int jk, size_t smem) {
   CPC_OCC(COREL_SD)
   CPC_OCC(COREL_SS)
   CPC_OCC(COREL_SSA)
+  CPC_OCC(COREL_DK)
+  CPC_OCC(COREL_SK)
+  CPC_OCC(COREL_ED)
 #undef CPC_OCC
   return e == cudaSuccess ? nb : 0;
 }

@@ -23,7 +23,7 @@ plain_fp64_kernel(const JobDev *__restrict__ jobp, DCat a, DCat b) {
   if (J.row_stride > 1 && ((a.orig[i] - J.row_offset) % J.row_stride) != 0) return;
   const double x1 = a.x[i], y1 = a.y[i], z1 = a.z[i];
   // lim_calc_xyz / lim_calc_PB (PB_calcs.cpp:12-61)
-  const double z_max = __dadd_rn(z1, J.pmax), z_min = __dadd_rn(z1, J.pmin);
+  const double z_max = __dadd_rn(z1, J.wz_hi), z_min = __dadd_rn(z1, J.wz_lo);
   const double ra_max = __dadd_rn(x1, J.rmax), ra_min = __dsub_rn(x1, J.rmax);
   const double dec_max = __dadd_rn(y1, J.rmax), dec_min = __dsub_rn(y1, J.rmax);
   int PBx = 0, PBy = 0, PBz = 0;
@@ -65,28 +65,11 @@ plain_fp64_kernel(const JobDev *__restrict__ jobp, DCat a, DCat b) {
           if (x2s < ra_min || x2s > ra_max) continue;
           nwin++;
           // corel_bin (corels.cpp:21-46)
-          const double dP = __dsub_rn(z2s, z1);
-          const double v2 = floor(__ddiv_rn(__dsub_rn(dP, J.pmin), J.ps));
-          if (!(v2 >= 0.0) || v2 >= (double)J.npi) continue;
-          const double t0 = __dsub_rn(x1, x2s), t1 = __dsub_rn(y1, y2s);
-          const double rp = __dsqrt_rn(__dadd_rn(__dmul_rn(t0, t0), __dmul_rn(t1, t1)));
-          int n1;
-          if (J.lin_bin) {
-            const double v1 = floor(__ddiv_rn(__dsub_rn(rp, J.rmin), J.rsize));
-            if (!(v1 >= 0.0) || v1 >= (double)J.nrp) continue;
-            n1 = (int)v1;
-          } else {
-            if (!(rp >= J.thr[0]) || rp >= J.thr[J.nrp]) continue;
-            int l = 0, h = J.nrp;
-            while (h - l > 1) {
-              const int mid = (l + h) >> 1;
-              if (rp >= J.thr[mid]) l = mid; else h = mid;
-            }
-            n1 = l;
-          }
+          int n1, n2;
+          if (exact_bin(J, x1, y1, z1, x2s, y2s, z2s, n1, n2) != 2) continue;
           double f[kNF];
-          exact_values(J, a, i, b, j, f);
-          exact_accumulate(J, a, i, b, j, n1, (int)v2, f);
+          exact_values(J, a, i, b, j, sx, sy, sz, f);
+          exact_accumulate(J, a, i, b, j, n1, n2, f);
         }
       }
     }

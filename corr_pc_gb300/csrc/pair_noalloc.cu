@@ -286,6 +286,8 @@ extern "C" cpc_status cpc_count_fp64_noalloc(const cpc_params *p, cpc_pair_kind 
   J.rmax = p->bin_r_max;
   J.pmin = p->p_min;
   J.pmax = p->p_max;
+  J.wz_lo = p->p_min;  // coordinates 6: z window [z + p_min, z + p_max]
+  J.wz_hi = p->p_max;
   J.ps = (p->p_max - p->p_min) / (p->n_p_bin);
   J.rsize = p->lin_bin ? (p->bin_r_max - p->bin_r_min) / p->n_bins
                        : (std::log10(p->bin_r_max) - std::log10(p->bin_r_min)) / p->n_bins;

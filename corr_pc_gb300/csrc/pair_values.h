@@ -10,8 +10,17 @@
 //   shape_shape_corel    corels.cpp:122-204  (COREL_SS: estimator 0 branch,
 //                                             e-cross never assigned;
 //                                             COREL_SSA: the other estimators)
+//   density_convergence_corel corels.cpp:79-90  (COREL_DK: data[1] += w kappa)
+//   shape_convergence_corel   corels.cpp:92-120 (COREL_SK: kappa of the other
+//                                               galaxy times the rotated e)
+//   ED_corel                  corels.cpp:246-262 with ED_calc_PB
+//                                               (PB_calcs.cpp:101-134)
 // with the rotation of calcs.cpp:60-64 and the folded angle |phi - theta| of
-// ephi_calc (calcs.cpp:97-105).
+// ephi_calc (calcs.cpp:97-105).  kappa is read into e[0] (read_dat.cpp:300-304),
+// so it is e1 here; the ED orientation is (e1, e2, e3), normalised at read
+// (read_dat.cpp:282-293).  sep is the shifted separation g1 - (g2 + L*PB)
+// that ED_calc_PB projects (ED only).  The convergence weights take the
+// reference's default sig_crit = 1 (initialization.cpp:787).
 #pragma once
 
 #ifdef __CUDACC__
@@ -27,14 +36,29 @@ namespace cpc {
 constexpr int kPairFields = 13;
 
 struct PairGal {
-  double e1, e2, phi;
+  double e1, e2, phi, e3 = 0.0;
 };
 
 CPC_HD inline void pair_values(int corel, int gws, double wt, double theta, const PairGal &g1,
-                               const PairGal &g2, double f[kPairFields]) {
+                               const PairGal &g2, double f[kPairFields],
+                               const double *sep = nullptr) {
   for (int q = 0; q < kPairFields; q++) f[q] = 0.0;
   f[0] = wt;
   if (corel == 0) return;
+  if (corel == 4) {  // only the shape holder's kappa is assigned
+    if (gws == 1) f[1] = wt * g1.e1;
+    else if (gws == 2) f[1] = wt * g2.e1;
+    return;
+  }
+  if (corel == 6) {  // ED_calc_PB: shape holder g2 if g_with_shape == 2, else g1
+    const PairGal &gs = (gws == 2) ? g2 : g1;
+    const double norm = sqrt(sep[0] * sep[0] + sep[1] * sep[1] + sep[2] * sep[2]);
+    double ca = gs.e1 * sep[0] + gs.e2 * sep[1] + gs.e3 * sep[2];
+    ca /= norm;
+    f[11] = ca * ca;
+    f[12] = f[11] * f[11];
+    return;
+  }
   const double c2 = cos(2.0 * theta), s2 = sin(2.0 * theta);
   const double kpi = 3.141592653589793;
   auto ephi = [&](double phi) {
@@ -42,6 +66,16 @@ CPC_HD inline void pair_values(int corel, int gws, double wt, double theta, cons
     if (t > kpi / 2.0) t = kpi - t;
     return t;
   };
+  if (corel == 5) {  // rotate the shape holder's e, weight by the other's kappa
+    if (gws != 1 && gws != 2) return;
+    const PairGal &gs = (gws == 2) ? g2 : g1, &gk = (gws == 2) ? g1 : g2;
+    const double en0 = c2 * gs.e1 - s2 * gs.e2, en1 = s2 * gs.e1 + c2 * gs.e2;
+    const double ep = wt * gk.e1;
+    f[1] = ep;
+    f[5] = ep * en0;
+    f[9] = ep * en1;
+    return;
+  }
   if (corel == 1) {
     const PairGal &gs = (gws == 2) ? g2 : g1;
     const double e0 = gs.e1, e1 = gs.e2;

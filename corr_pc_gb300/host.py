@@ -5,7 +5,7 @@
   ``srand(124693517)``, one draw per galaxy in read order, read_dat.cpp:241-246),
   the orientation ``phi`` (elip_angle, read_dat.cpp:275-280) or -10, unit
   weights, the ``include_prob`` draw of random catalogues, and which samples
-  read ellipticities (read_dat.cpp:27-133).
+  read ellipticities, kappa or the ED orientation (read_dat.cpp:27-133).
 * ``corels2``  -- the reference's ``long corels2(gal g1[], gal g2[], bin_jk&,
   data_info&)`` (corr.cpp:219-459) on the GPU: counts one pair type through the
   C ABI and returns the bin_jk contents after the delete-one conversion
@@ -39,19 +39,29 @@ class Galaxies:
     include_prob: np.ndarray
     dc: np.ndarray | None = None  # sky: comoving distance (table row of z)
     da: np.ndarray | None = None  # sky: transverse distance (table row of z)
+    e3: np.ndarray | None = None  # ED orientation e[2] (which_corr 5)
 
     @property
     def n(self) -> int:
         return int(self.x.shape[0])
 
 
-def reads_e(params, role: str) -> bool:
-    """Which samples read ellipticities (read_dat.cpp:27-113)."""
+def e_columns(params, role: str):
+    """What a sample's e file holds for the pair loop (read_dat.cpp:27-113):
+    "e" (e1, e2; phi from elip_angle), "kappa" (one column stored as e[0]),
+    "e3" (the 3-D ED orientation, normalised to unit length at read,
+    read_dat.cpp:282-293) or None (nothing read).  which_corr 5 falls through
+    into case 8 (read_dat.cpp:50-58), so its density sample reads nothing."""
     if role == "S":
-        return params.which_corr in (1, 2)
+        return {1: "e", 2: "e", 3: "kappa", 4: "e", 5: "e3"}.get(params.which_corr)
     if role == "D":
-        return params.which_corr == 2
-    return False
+        return {2: "e", 4: "kappa"}.get(params.which_corr)
+    return None
+
+
+def reads_e(params, role: str) -> bool:
+    """Whether a sample reads ellipticities e1, e2."""
+    return e_columns(params, role) == "e"
 
 
 def prepare(params, cats_in_read_order, table=None) -> dict:
@@ -78,10 +88,21 @@ def prepare(params, cats_in_read_order, table=None) -> dict:
             inc = r.copy()
         if params.do_jk == 0 or params.n_jk_regions == 0:
             jkp = np.zeros(n)
-        re = reads_e(params, role) and getattr(c, "e1", None) is not None
-        e1 = np.ascontiguousarray(c.e1, dtype=np.float64) if re else None
-        e2 = np.ascontiguousarray(c.e2, dtype=np.float64) if re else None
-        phi = _lib.elip_angle(e1, e2) if re else np.full(n, -10.0)
+        mode = e_columns(params, role) if getattr(c, "e1", None) is not None else None
+        e1 = e2 = e3 = None
+        phi = np.full(n, -10.0)
+        if mode == "e":
+            e1 = np.ascontiguousarray(c.e1, dtype=np.float64)
+            e2 = np.ascontiguousarray(c.e2, dtype=np.float64)
+            phi = _lib.elip_angle(e1, e2)
+        elif mode == "kappa":
+            e1 = np.ascontiguousarray(c.e1, dtype=np.float64)
+        elif mode == "e3":
+            e1, e2, e3 = (np.array(v, dtype=np.float64) for v in (c.e1, c.e2, c.e3))
+            norm = np.sqrt(e1 * e1 + e2 * e2 + e3 * e3)
+            nz = norm > 0
+            for v in (e1, e2, e3):
+                v[nz] /= norm[nz]
         w = getattr(c, "w", None)
         w = np.ones(n) if w is None else np.ascontiguousarray(w, dtype=np.float64)
         jk = getattr(c, "jk", None) if params.do_jk else None
@@ -94,7 +115,7 @@ def prepare(params, cats_in_read_order, table=None) -> dict:
                              np.ascontiguousarray(c.y, dtype=np.float64),
                              np.ascontiguousarray(c.z, dtype=np.float64), w, e1, e2, phi,
                              None if jk is None else np.ascontiguousarray(jk, dtype=np.int32),
-                             jkp, inc, dc, da)
+                             jkp, inc, dc, da, e3)
     return out
 
 

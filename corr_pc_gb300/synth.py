@@ -190,9 +190,10 @@ class Catalog:
     y: np.ndarray
     z: np.ndarray
     w: np.ndarray | None = None
-    e1: np.ndarray | None = None
+    e1: np.ndarray | None = None   # e1, or kappa (which_corr 3, 4) with e2 None
     e2: np.ndarray | None = None
     jk: np.ndarray | None = None
+    e3: np.ndarray | None = None   # third orientation component (which_corr 5)
 
     @property
     def n(self) -> int:
@@ -200,14 +201,12 @@ class Catalog:
 
     def sorted_by_z(self) -> "Catalog":
         o = np.argsort(self.z, kind="stable")
-        take = lambda a: None if a is None else np.ascontiguousarray(a[o])
-        return Catalog(take(self.x), take(self.y), take(self.z), take(self.w),
-                       take(self.e1), take(self.e2), take(self.jk))
+        return self.subset(o)
 
     def subset(self, idx) -> "Catalog":
         take = lambda a: None if a is None else np.ascontiguousarray(a[idx])
         return Catalog(take(self.x), take(self.y), take(self.z), take(self.w),
-                       take(self.e1), take(self.e2), take(self.jk))
+                       take(self.e1), take(self.e2), take(self.jk), take(self.e3))
 
 
 def _wrap(v: np.ndarray, L: float) -> np.ndarray:
@@ -258,6 +257,24 @@ def uniform_box(n: int, L: float, seed: int, *, nside_jk: int = 0,
         e1, e2 = shapes(rng, n)
     jk = jk_cubes(x, y, z, L, nside_jk) if nside_jk else None
     return Catalog(x, y, z, None, e1, e2, jk).sorted_by_z()
+
+
+def with_kappa(cat: Catalog, seed: int) -> Catalog:
+    """A copy carrying a per-galaxy scalar (kappa, or a mean-subtracted log mass as
+    in the size notebook) in e1, e2 absent: one column in the e file."""
+    rng = np.random.default_rng(seed)
+    k = np.log10(rng.lognormal(0.0, 1.0, cat.n))
+    k -= k.mean()
+    return Catalog(cat.x, cat.y, cat.z, cat.w, k, None, cat.jk)
+
+
+def with_orientation(cat: Catalog, seed: int) -> Catalog:
+    """A copy carrying an un-normalised 3-D orientation (e1, e2, e3) -- the ED
+    notebook's dark-matter axis -- with random lengths and a few zero vectors."""
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=(3, cat.n)) * rng.uniform(0.2, 3.0, cat.n)
+    v[:, :: max(1, cat.n // 7)] = 0.0
+    return Catalog(cat.x, cat.y, cat.z, cat.w, v[0].copy(), v[1].copy(), cat.jk, v[2].copy())
 
 
 def neyman_scott(n_parents: int, mean_children: float, sigma: float, L: float,
@@ -368,8 +385,10 @@ def write_catalog(prefix: str, cat: Catalog, *, write_e: bool = True,
         names["jk"] = prefix + "_jk.dat"
         np.savetxt(names["jk"], cat.jk, fmt="%i")
     if write_e and cat.e1 is not None:
+        # one column (kappa), two (e1, e2) or three (the ED orientation)
         names["e"] = prefix + "_e.dat"
-        np.savetxt(names["e"], np.column_stack((cat.e1, cat.e2)))
+        cols = [c for c in (cat.e1, cat.e2, cat.e3) if c is not None]
+        np.savetxt(names["e"], np.column_stack(cols))
     if write_w and cat.w is not None:
         names["wt"] = prefix + "_wt.dat"
         np.savetxt(names["wt"], cat.w)

@@ -61,8 +61,10 @@ typedef enum {
 /* Parameters: the data_info fields the pair loop reads (data_def.h:46-96),
  * with the values data_ini computes (initialization.cpp:62-352). */
 typedef struct {
-  int which_corr;    /* 0 wgg, 1 wg+, 2 w++ */
-  int coordinates;   /* 6: x,y,z (r_p, Pi); 0: sky ra,dec,z (r_p, Pi) */
+  int which_corr;    /* 0 wgg, 1 wg+, 2 w++, 3 kappa-density, 4 shape-kappa,
+                        5 ED (cos^2 of the 3-D orientation angle); 3-5 box only */
+  int coordinates;   /* 6: x,y,z (r_p, Pi); 7: x,y,z (r, mu; periodic box);
+                        0: sky ra,dec,z (r_p, Pi) */
   int estimator;     /* 0..3 (affects the shape-shape accumulators only) */
   int periodic_box;  /* 1: periodic images (coordinates 6 only) */
   int data_sorted;   /* 0/1: as in the .inp (results follow set semantics) */
@@ -72,7 +74,7 @@ typedef struct {
   int rand_subsample;/* must be 0 */
   int n_bins;        /* r_p bins */
   int lin_bin;       /* 1 linear, 0 log10 */
-  int n_p_bin;       /* Pi bins */
+  int n_p_bin;       /* Pi bins (mu bins for coordinates 7, p_min..p_max in mu) */
   double bin_r_min, bin_r_max;
   double p_min, p_max;
   double periodic_box_size;
@@ -88,7 +90,10 @@ typedef struct {
  * degrees, y = Dec degrees, z = redshift, plus dc/da.  Optional arrays may be
  * NULL: w (weights 1), e1/e2 (no shapes: treated as 0), phi (-10, the
  * reference's value for galaxies read without e), jk (required when do_jk),
- * jk_prob (0), dc/da (sky only). */
+ * jk_prob (0), dc/da (sky only), e3 (0).  which_corr 3 and 4 read kappa into
+ * e[0] (read_dat.cpp:300-304): pass it as e1 (e2 may be NULL then); which_corr 5
+ * reads a 3-D orientation normalised to unit length (read_dat.cpp:282-293):
+ * pass it as e1, e2, e3. */
 typedef struct {
   int64_t n;
   const double *x, *y, *z;
@@ -98,6 +103,7 @@ typedef struct {
   const int32_t *jk;
   const double *jk_prob;
   const double *dc, *da;
+  const double *e3;
 } cpc_catalog;
 
 #define CPC_NF 13 /* wt_num, data[1..6].val, data[1..6].err interleaved */

@@ -15,6 +15,8 @@
  *   - per-pair binning                        corels.cpp:21-46, PB_calcs.cpp:87-98,
  *                                             calcs.cpp:126-132, sky_calcs.cpp:24-31,91-96
  *   - density/shape accumulators              corels.cpp:48-77,122-244, calcs.cpp:54-105
+ *   - convergence and ED accumulators         corels.cpp:79-120,246-262, PB_calcs.cpp:101-134
+ *   - r-mu binning (coordinates 7)            calcs.cpp:135-140, PB_calcs.cpp:12-28
  *   - jackknife attribution                   jk.cpp:53-71,138-171,201-223
  * with OpenMP threads over the outer rows and thread-private histograms
  * merged at the end (corr.cpp:329-442), as the reference does.
@@ -35,7 +37,8 @@
  *     which depends on the OpenMP schedule and is not reproduced.
  *   - a galaxy without ellipticities is treated as e = (0, 0) (the reference
  *     reads an uninitialised pointer there, corels.cpp:216-219).
- *   - sig_crit (lensing) and coordinates other than 0 and 6 are rejected.
+ *   - sig_crit (lensing) and coordinates other than 0, 6 and 7 (periodic) are
+ *     rejected.
  */
 #include <math.h>
 #include <stdint.h>
@@ -48,7 +51,7 @@
 #define CPC_NF 13 /* wt, d1v,d1e, d2v,d2e, d3v,d3e, d4v,d4e, d5v,d5e, d6v,d6e */
 
 enum { ORC_SD = 0, ORC_SRD = 1, ORC_DRS = 2, ORC_RSRD = 3, ORC_RSRS = 4, ORC_SRS = 5, ORC_SS = 6 };
-enum { COREL_DD = 0, COREL_SD = 1, COREL_SS = 2 };
+enum { COREL_DD = 0, COREL_SD = 1, COREL_SS = 2, COREL_DK = 4, COREL_SK = 5, COREL_ED = 6 };
 
 typedef struct {
   int64_t n;
@@ -60,6 +63,7 @@ typedef struct {
   const double *jk_prob;     /* NULL: 0 */
   const double *include_prob;/* NULL: 0 */
   const double *dc, *da;     /* sky: comoving / transverse distance per galaxy */
+  const double *e3;          /* NULL: 0 (third ED orientation component, e[2]) */
 } orc_cat;
 
 typedef struct {
@@ -97,6 +101,9 @@ static int setup_job(const orc_params *p, int kind, int64_t n1, int64_t n2, job_
   else if (p->which_corr == 0) corel = COREL_DD;
   else if (p->which_corr == 1) corel = COREL_SD;
   else if (p->which_corr == 2) corel = (kind == ORC_SD) ? COREL_SS : COREL_SD;
+  else if (p->which_corr == 3) corel = COREL_DK;
+  else if (p->which_corr == 4) corel = COREL_SK;
+  else if (p->which_corr == 5) corel = COREL_ED;
   else return -1;
   j->corel = corel;
   j->swapped = 0;
@@ -195,6 +202,7 @@ static inline double cat_w(const orc_cat *c, int64_t i) { return c->w ? c->w[i] 
 static inline double cat_e1(const orc_cat *c, int64_t i) { return c->e1 ? c->e1[i] : 0.0; }
 static inline double cat_e2(const orc_cat *c, int64_t i) { return c->e2 ? c->e2[i] : 0.0; }
 static inline double cat_phi(const orc_cat *c, int64_t i) { return c->phi ? c->phi[i] : -10.0; }
+static inline double cat_e3(const orc_cat *c, int64_t i) { return c->e3 ? c->e3[i] : 0.0; }
 static inline int cat_jk(const orc_cat *c, int64_t i) { return c->jk ? c->jk[i] : -1; }
 static inline double cat_jkp(const orc_cat *c, int64_t i) { return c->jk_prob ? c->jk_prob[i] : 0.0; }
 
@@ -205,12 +213,16 @@ static int corel_pair(const ctx_t *c, hist_t *h, int64_t i, int64_t j, int PBx, 
   const orc_cat *g1 = c->g1, *g2 = c->g2;
   double d_P, da_R;
   /* corel_bin corels.cpp:21-46 */
-  if (p->coordinates == 6) {
+  if (p->coordinates != 0) {
     /* pi_calc_PB / rp_calc_PB, PB_calcs.cpp:87-98 */
     d_P = ((g2->z[j] + p->box * PBz) - g1->z[i]);
     double t0 = g1->x[i] - (g2->x[j] + p->box * PBx);
     double t1 = g1->y[i] - (g2->y[j] + p->box * PBy);
     da_R = sqrt(t0 * t0 + t1 * t1);
+    if (p->coordinates == 7) { /* r_mu_calc calcs.cpp:135-140 */
+      da_R = sqrt(da_R * da_R + d_P * d_P);
+      d_P /= da_R;
+    }
   } else {
     /* pi_calc calcs.cpp:126-132; rp_calc_sky sky_calcs.cpp:91-96; dA_calc :24-31 */
     d_P = g2->dc[j] - g1->dc[i];
@@ -233,15 +245,43 @@ static int corel_pair(const ctx_t *c, hist_t *h, int64_t i, int64_t j, int PBx, 
   memset(f, 0, sizeof f);
   f[0] = wt;
   int corel = c->job->corel, gws = c->job->g_with_shape;
-  if (corel != COREL_DD) {
+  if (corel == COREL_DK) { /* density_convergence_corel corels.cpp:79-90, sig_crit 1 */
+    if (gws == 1) f[1] = wt * cat_e1(g1, i) * 1.0;
+    else if (gws == 2) f[1] = wt * cat_e1(g2, j) * 1.0;
+  } else if (corel == COREL_ED) { /* ED_corel corels.cpp:246-262, ED_calc_PB PB_calcs.cpp:101-134 */
+    double xyz[3];
+    xyz[0] = g1->x[i] - (g2->x[j] + p->box * PBx);
+    xyz[1] = g1->y[i] - (g2->y[j] + p->box * PBy);
+    xyz[2] = g1->z[i] - (g2->z[j] + p->box * PBz);
+    double xyz_norm = sqrt(xyz[0] * xyz[0] + xyz[1] * xyz[1] + xyz[2] * xyz[2]);
+    double cos_ang;
+    if (gws == 2)
+      cos_ang = cat_e1(g2, j) * xyz[0] + cat_e2(g2, j) * xyz[1] + cat_e3(g2, j) * xyz[2];
+    else
+      cos_ang = cat_e1(g1, i) * xyz[0] + cat_e2(g1, i) * xyz[1] + cat_e3(g1, i) * xyz[2];
+    cos_ang /= xyz_norm;
+    f[11] = cos_ang * cos_ang;
+    f[12] = pow(f[11], 2.0);
+  } else if (corel != COREL_DD) {
     double theta;
-    if (p->coordinates == 6) /* calcs.cpp:54-57 (raw, un-shifted positions) */
+    if (p->coordinates != 0) /* calcs.cpp:54-57 (raw, un-shifted positions) */
       theta = atan((g2->y[j] - g1->y[i]) / (g2->x[j] - g1->x[i]));
     else /* sky_calcs.cpp:13-22 */
       theta = atan((g2->y[j] - g1->y[i]) /
                    ((g2->x[j] - g1->x[i]) * cos((g1->y[i] / r2d + g2->y[j] / r2d) / 2.0)));
     double c2 = cos(2.0 * theta), s2 = sin(2.0 * theta);
-    if (corel == COREL_SD) { /* corels.cpp:206-244 */
+    if (corel == COREL_SK) { /* shape_convergence_corel corels.cpp:92-120, sig_crit 1 */
+      if (gws == 1 || gws == 2) {
+        const orc_cat *gs = (gws == 2) ? g2 : g1, *gk = (gws == 2) ? g1 : g2;
+        int64_t is = (gws == 2) ? j : i, ik = (gws == 2) ? i : j;
+        double en0 = c2 * cat_e1(gs, is) - s2 * cat_e2(gs, is); /* elip_rotate calcs.cpp:60-64 */
+        double en1 = s2 * cat_e1(gs, is) + c2 * cat_e2(gs, is);
+        double ep = wt * cat_e1(gk, ik) * 1.0;
+        f[1] = ep;
+        f[5] = ep * en0;
+        f[9] = ep * en1;
+      }
+    } else if (corel == COREL_SD) { /* corels.cpp:206-244 */
       const orc_cat *gs = (gws == 2) ? g2 : g1;
       int64_t is = (gws == 2) ? j : i;
       double e0 = cat_e1(gs, is), e1 = cat_e2(gs, is);
@@ -301,7 +341,7 @@ static int corel_pair(const ctx_t *c, hist_t *h, int64_t i, int64_t j, int PBx, 
   int r1 = cat_jk(g1, i), r2 = cat_jk(g2, j);
   double q1 = cat_jkp(g1, i), q2 = cat_jkp(g2, j);
   if (r1 == r2) {
-    if (p->coordinates == 6) q1 = 1;
+    if (p->coordinates != 0) q1 = 1; /* jk_check_PB: periodic box or coordinates 6 */
     q2 = 0;
   }
   int rs[2] = {r1, r2};
@@ -333,8 +373,10 @@ static int64_t lower_bound_z(const double *z, int64_t n, double shift, double zl
 int orc_corels2(const orc_params *p, int kind, const orc_cat *ga, const orc_cat *gb,
                 int64_t *num, double *sums, int64_t *counters) {
   if (p->sig_crit != 0) return -2;
-  if (p->coordinates != 6 && p->coordinates != 0) return -2;
+  if (p->coordinates != 6 && p->coordinates != 0 && p->coordinates != 7) return -2;
   if (p->coordinates == 0 && p->periodic_box) return -2;
+  if (p->coordinates == 7 && !p->periodic_box) return -2;
+  if (p->coordinates == 0 && p->which_corr > 2) return -2;
   counters[0] = counters[1] = 0;
   job_t job;
   if (setup_job(p, kind, ga->n, gb->n, &job) != 0) return -1;
@@ -379,7 +421,7 @@ int orc_corels2(const orc_params *p, int kind, const orc_cat *ga, const orc_cat 
       if (((i - off) % stride) != 0) continue;
       if (g1->include_prob && g1->include_prob[i] > job.include_prob_max) continue;
       window_t w;
-      if (p->coordinates == 6) lim_box(p, g1->x[i], g1->y[i], g1->z[i], &w);
+      if (p->coordinates != 0) lim_box(p, g1->x[i], g1->y[i], g1->z[i], &w);
       else if (lim_sky(p, g1->x[i], g1->y[i], g1->z[i], &w) != 0) { err = 1; continue; }
       int xt = w.PBx, yt = w.PBy, zt = w.PBz;
       int PBy = yt > 0;
@@ -389,7 +431,7 @@ int orc_corels2(const orc_params *p, int kind, const orc_cat *ga, const orc_cat 
           int PBz = zt > 0;
           for (int zi = 0; zi <= abs(zt); zi++, PBz--) {
             double sz = p->box * PBz, sy = p->box * PBy, sx = p->box * PBx;
-            if (p->coordinates != 6) sz = sy = sx = 0;
+            if (p->coordinates == 0) sz = sy = sx = 0;
             int64_t j = 0;
             int sorted = p->data_sorted == 1;
             if (sorted && PBz <= 0) j = lower_bound_z(g2->z, g2->n, sz, w.z_min);
@@ -439,14 +481,18 @@ int orc_corels2(const orc_params *p, int kind, const orc_cat *ga, const orc_cat 
 int orc_corels1(const orc_params *p, int kind, const orc_cat *g, int64_t *num, double *sums,
                 int64_t *counters) {
   if (p->sig_crit != 0) return -2;
-  if (p->coordinates != 6 && p->coordinates != 0) return -2;
+  if (p->coordinates != 6 && p->coordinates != 0 && p->coordinates != 7) return -2;
   if (p->coordinates == 0 && p->periodic_box) return -2;
+  if (p->coordinates == 7 && !p->periodic_box) return -2;
+  if (p->coordinates == 0 && p->which_corr > 2) return -2;
   counters[0] = counters[1] = 0;
   job_t job;
   job.swapped = 0;
   job.g_with_shape = 1;
   if (kind == ORC_RSRS) job.corel = COREL_DD;
-  else if (kind == ORC_SS) job.corel = (p->which_corr == 0) ? COREL_DD : COREL_SS;
+  else if (kind == ORC_SS)
+    job.corel = p->which_corr == 0 ? COREL_DD : p->which_corr <= 2 ? COREL_SS
+              : p->which_corr == 3 ? COREL_DK : p->which_corr == 4 ? COREL_SK : COREL_ED;
   else return -1;
   job.include_prob_max = (kind == ORC_RSRS) ? p->include_prob_rr : 1.0;
   if (g->n == 0) return 0;
@@ -486,7 +532,7 @@ int orc_corels1(const orc_params *p, int kind, const orc_cat *g, int64_t *num, d
       if (((i - off) % stride) != 0) continue;
       if (g->include_prob && g->include_prob[i] > job.include_prob_max) continue;
       window_t w;
-      if (p->coordinates == 6) lim_box(p, g->x[i], g->y[i], g->z[i], &w);
+      if (p->coordinates != 0) lim_box(p, g->x[i], g->y[i], g->z[i], &w);
       else if (lim_sky(p, g->x[i], g->y[i], g->z[i], &w) != 0) { err = 1; continue; }
       int xt = w.PBx, yt = w.PBy, zt = w.PBz;
       int PBx = xt > 0;
@@ -496,7 +542,7 @@ int orc_corels1(const orc_params *p, int kind, const orc_cat *g, int64_t *num, d
           int PBz = zt > 0;
           for (int zi = 0; zi <= abs(zt); zi++, PBz--) {
             double sz = p->box * PBz, sy = p->box * PBy, sx = p->box * PBx;
-            if (p->coordinates != 6) sz = sy = sx = 0;
+            if (p->coordinates == 0) sz = sy = sx = 0;
             int64_t j = i + 1;
             if (p->data_sorted != 0 && PBz > 0) j = 0;
             const int sorted = p->data_sorted == 1;

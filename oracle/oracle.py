@@ -47,7 +47,8 @@ def build_reference() -> str | None:
 class _Cat(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64)] + [
         (nm, ctypes.c_void_p) for nm in
-        ("x", "y", "z", "w", "e1", "e2", "phi", "jk", "jk_prob", "include_prob", "dc", "da")]
+        ("x", "y", "z", "w", "e1", "e2", "phi", "jk", "jk_prob", "include_prob", "dc", "da",
+         "e3")]
 
 
 class _Params(ctypes.Structure):
@@ -102,10 +103,11 @@ class OracleCatalog:
     """A catalogue with the per-galaxy attributes the pair loop reads."""
 
     def __init__(self, x, y, z, *, w=None, e1=None, e2=None, phi=None, jk=None,
-                 jk_prob=None, include_prob=None, dc=None, da=None):
+                 jk_prob=None, include_prob=None, dc=None, da=None, e3=None):
         f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
         self.x, self.y, self.z = f(x), f(y), f(z)
         self.w, self.e1, self.e2, self.phi = f(w), f(e1), f(e2), f(phi)
+        self.e3 = f(e3)
         self.jk = None if jk is None else np.ascontiguousarray(jk, dtype=np.int32)
         self.jk_prob, self.include_prob = f(jk_prob), f(include_prob)
         self.dc, self.da = f(dc), f(da)
@@ -115,7 +117,7 @@ class OracleCatalog:
         c = _Cat()
         c.n = self.n
         for nm in ("x", "y", "z", "w", "e1", "e2", "phi", "jk", "jk_prob",
-                   "include_prob", "dc", "da"):
+                   "include_prob", "dc", "da", "e3"):
             setattr(c, nm, _ptr(getattr(self, nm)))
         return c
 
@@ -129,6 +131,19 @@ def elip_angle(e1, e2):
     out = np.empty_like(e1)
     lib().orc_elip_angle(e1.shape[0], e1.ctypes.data, e2.ctypes.data, out.ctypes.data)
     return out
+
+
+def e_columns(which_corr, role):
+    """What read_data reads from a sample's e file (read_dat.cpp:27-113):
+    "e" (e1 e2, then elip_angle), "kappa" (one column into e[0]), "e3" (three
+    columns, normalised to unit length, read_dat.cpp:282-293) or None.  Note the
+    fall-through of which_corr 5 into case 8 (read_dat.cpp:50-58): the density
+    sample reads nothing there."""
+    if role == "S":
+        return {1: "e", 2: "e", 3: "kappa", 4: "e", 5: "e3"}.get(which_corr)
+    if role == "D":
+        return {2: "e", 4: "kappa"}.get(which_corr)
+    return None
 
 
 def read_like_reference(params, cats_in_read_order, table=None):
@@ -164,10 +179,22 @@ def read_like_reference(params, cats_in_read_order, table=None):
             inc = r / (RAND_MAX + 1.0)
         if p.do_jk == 0 or p.n_jk_regions == 0:
             jkp = np.zeros(n)
-        read_e = role == "S" and p.which_corr in (1, 2) or (role == "D" and p.which_corr == 2)
-        e1 = c.e1 if read_e else None
-        e2 = c.e2 if read_e else None
-        phi = elip_angle(e1, e2) if read_e else np.full(n, -10.0)
+        mode = e_columns(p.which_corr, role) if getattr(c, "e1", None) is not None else None
+        e1 = e2 = e3 = None
+        phi = np.full(n, -10.0)
+        if mode == "e":
+            e1, e2 = c.e1, c.e2
+            phi = elip_angle(e1, e2)
+        elif mode == "kappa":
+            e1 = c.e1
+        elif mode == "e3":
+            a, b, d = (np.asarray(v, dtype=np.float64) for v in (c.e1, c.e2, c.e3))
+            nrm = np.sqrt(a * a + b * b + d * d)
+            nz = nrm > 0
+            e1, e2, e3 = a.copy(), b.copy(), d.copy()
+            e1[nz] /= nrm[nz]
+            e2[nz] /= nrm[nz]
+            e3[nz] /= nrm[nz]
         w = c.w if c.w is not None else np.ones(n)
         jk = c.jk if (p.do_jk and c.jk is not None) else None
         dc = da = None
@@ -176,7 +203,7 @@ def read_like_reference(params, cats_in_read_order, table=None):
             dc = table.DC[it]
             da = (table.transverse if p.use_comoving else table.DA)[it]
         out[role] = OracleCatalog(c.x, c.y, c.z, w=w, e1=e1, e2=e2, phi=phi, jk=jk,
-                                  jk_prob=jkp, include_prob=inc, dc=dc, da=da)
+                                  jk_prob=jkp, include_prob=inc, dc=dc, da=da, e3=e3)
     return out
 
 

@@ -99,6 +99,42 @@ def cases():
                           njk=8, n=c.n)
     p.data_sorted = 0
     out.append(("box_wgp_unsorted", p, c, c, True))
+
+    # the variants: kappa-density (which_corr 3), shape-kappa (4), ED (5), and
+    # r-mu binning (coordinates 7) -- the ED and size notebooks' settings
+    c = synth.with_orientation(synth.neyman_scott(30, 40.0, 2.0, 75.0, 31, nside_jk=2), 32)
+    p = synth._box_params(which_corr=5, L=75.0, rmin=0.1, rmax=10.0, nrp=10, npi=4, pmax=1.0,
+                          njk=8, n=c.n)
+    p.coordinates = 7
+    out.append(("box_ed_rmu", p, c, c, True))
+
+    c = synth.with_orientation(synth.uniform_box(2500, 80.0, 33, nside_jk=2), 34)
+    p = synth._box_params(which_corr=5, L=80.0, rmin=0.3, rmax=15.0, nrp=8, npi=10, pmax=20.0,
+                          njk=8, n=c.n)
+    out.append(("box_ed_rppi", p, c, c, True))
+
+    c = synth.neyman_scott(30, 50.0, 2.0, 75.0, 35, nside_jk=3)
+    c = synth.with_kappa(c.subset(np.random.default_rng(36).permutation(c.n)), 37)
+    p = synth._box_params(which_corr=3, L=75.0, rmin=0.1, rmax=10.0, nrp=10, npi=20, pmax=25.0,
+                          njk=27, n=c.n)
+    p.data_sorted = 0
+    out.append(("box_kappa_unsorted", p, c, c, True))
+
+    rng = np.random.default_rng(38)
+    s = synth.uniform_box(1800, 80.0, 39, nside_jk=2, with_shapes=True)
+    d = synth.with_kappa(synth.uniform_box(2400, 80.0, 40, nside_jk=2), 41)
+    s.w = rng.uniform(0.5, 1.5, s.n)
+    p = synth._box_params(which_corr=4, L=80.0, rmin=0.3, rmax=15.0, nrp=8, npi=10, pmax=20.0,
+                          njk=8, n=0)
+    p.n_shape, p.n_density = s.n, d.n
+    out.append(("box_sk_distinct", p, s, d, False))
+
+    c = synth.uniform_box(2500, 90.0, 42, nside_jk=2, with_shapes=True)
+    p = synth._box_params(which_corr=2, L=90.0, rmin=0.0, rmax=18.0, nrp=9, npi=10, pmax=1.0,
+                          njk=8, n=c.n)
+    p.coordinates = 7
+    p.lin_bin = 1
+    out.append(("box_wpp_rmu_linear", p, c, c, True))
     return out
 
 
@@ -121,7 +157,7 @@ def run_case(name, p, S, D, same):
         "n_in": np.array(sd["n_in"]), "n_total": np.array(totals[-1][0]),
     }
     for role, c in (("S", S), ("D", D)):
-        for a in ("w", "e1", "e2", "jk"):
+        for a in ("w", "e1", "e2", "e3", "jk"):
             v = getattr(c, a)
             if v is not None:
                 arrays[f"{role}_{a}"] = v
@@ -281,6 +317,14 @@ def auto_cases():
     p.data_sorted = 0
     out.append(("auto_box_wgp_unsorted", p, c, None, None))
 
+    # ED auto-correlation in r-mu (corels1 with ED_corel, g_with_shape 1)
+    c = synth.with_orientation(synth.neyman_scott(25, 50.0, 2.0, 60.0, 57, nside_jk=2), 58)
+    p = synth._box_params(which_corr=5, L=60.0, rmin=0.2, rmax=12.0, nrp=8, npi=6, pmax=1.0,
+                          njk=8, n=c.n)
+    p.coordinates = 7
+    p.estimator = 1
+    out.append(("auto_box_ed_rmu", p, c, None, None))
+
     p = synth._sky_params(which_corr=1, rmin=0.3, rmax=30.0, nrp=8, npi=12, pmax=40.0, njk=9,
                           z_max=0.5)
     p.dz = 0.001
@@ -322,7 +366,7 @@ def run_auto_case(name, p, S, R, table):
     for role, c in (("S", S), ("Rs", R)):
         if c is None:
             continue
-        for a in ("x", "y", "z", "w", "e1", "e2", "jk"):
+        for a in ("x", "y", "z", "w", "e1", "e2", "e3", "jk"):
             v = getattr(c, a)
             if v is not None:
                 arrays[f"{role}_{a}"] = v

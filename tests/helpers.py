@@ -53,7 +53,7 @@ class AutoGolden:
             if f"{r}_x" in a:
                 g = lambda q: a.get(f"{r}_{q}")
                 self.cats[r] = synth.Catalog(g("x"), g("y"), g("z"), g("w"), g("e1"), g("e2"),
-                                             g("jk"))
+                                             g("jk"), g("e3"))
         self.terms = self.meta["terms"]
         self.files = self.meta["files"]
 
@@ -93,7 +93,7 @@ class SkyGolden:
 
     def _cat(self, role):
         g = lambda a: self.arr.get(f"{role}_{a}")
-        return synth.Catalog(g("x"), g("y"), g("z"), g("w"), g("e1"), g("e2"), g("jk"))
+        return synth.Catalog(g("x"), g("y"), g("z"), g("w"), g("e1"), g("e2"), g("jk"), g("e3"))
 
     def read_order(self):
         return [(r, self.cats[r]) for r in ("S", "Rs", "D", "Rd")]
@@ -123,7 +123,7 @@ class Golden:
 
     def _cat(self, role):
         g = lambda a: self.arr.get(f"{role}_{a}")
-        return synth.Catalog(g("x"), g("y"), g("z"), g("w"), g("e1"), g("e2"), g("jk"))
+        return synth.Catalog(g("x"), g("y"), g("z"), g("w"), g("e1"), g("e2"), g("jk"), g("e3"))
 
     def weights(self):
         w = []

@@ -12,7 +12,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name", ["box_wgg_uniform", "box_wgp_clustered", "box_wpp_weighted_distinct",
-                                  "box_wgp_swap", "box_linear_bins_nojk"])
+                                  "box_wgp_swap", "box_linear_bins_nojk", "box_ed_rmu",
+                                  "box_kappa_unsorted", "box_sk_distinct", "box_wpp_rmu_linear"])
 def test_cli_output_files_match_reference(name, tmp_path):
     g = Golden(name)
     wl = synth.Workload(name, g.params, g.S, g.D)
@@ -49,7 +50,7 @@ def test_cli_sky_output_files_match_reference(name, tmp_path):
 
 
 @pytest.mark.parametrize("name", ["auto_box_wgg", "auto_box_wpp_rebin", "auto_box_wgp_unsorted",
-                                  "auto_sky_wgp", "auto_nbox_wgg"])
+                                  "auto_sky_wgp", "auto_nbox_wgg", "auto_box_ed_rmu"])
 def test_cli_auto_output_files_match_reference(name, tmp_path):
     """Auto-correlation runs (estimators 1 and 2) through the command line:
     corels1 on the GPU, final_calc_auto (re_bin for estimator 2), the

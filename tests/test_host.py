@@ -90,14 +90,23 @@ def test_inp_round_trip(tmp_path):
         assert getattr(p, a) == getattr(q, a), a
 
 
-def test_prepare_matches_reference_read_path():
-    g = Golden("box_wpp_weighted_distinct")
+@pytest.mark.parametrize("name", ["box_wpp_weighted_distinct", "box_ed_rmu", "box_kappa_unsorted",
+                                  "box_sk_distinct"])
+def test_prepare_matches_reference_read_path(name):
+    """The host read path (jackknife draws, phi, weights, and which samples carry
+    e, kappa or the normalised ED orientation) equals the oracle's."""
+    g = Golden(name)
     a = host.prepare(g.params, [("S", g.S), ("D", g.D)])
     b = oracle.read_like_reference(g.params, [("S", g.S), ("D", g.D)])
     for role in ("S", "D"):
         assert np.array_equal(a[role].jk_prob, b[role].jk_prob)
         assert np.array_equal(a[role].phi, b[role].phi)
         assert np.array_equal(a[role].w, b[role].w)
+        for f in ("e1", "e2", "e3"):
+            u, v = getattr(a[role], f), getattr(b[role], f)
+            assert (u is None) == (v is None), (role, f)
+            if u is not None:
+                assert np.array_equal(u, v), (role, f)
 
 
 def test_create_rejects_bad_parameters():
@@ -112,6 +121,14 @@ def test_create_rejects_bad_parameters():
         _lib.Context(p)
     p = synth.box_uniform_wgg().params
     p.coordinates = 3
+    with pytest.raises(_lib.CpcError):
+        _lib.Context(p)
+    p = synth.box_uniform_wgg().params
+    p.which_corr = 6
+    with pytest.raises(_lib.CpcError):
+        _lib.Context(p)
+    p = synth.box_uniform_wgg().params
+    p.coordinates, p.periodic_box = 7, 0  # r-mu outside a periodic box
     with pytest.raises(_lib.CpcError):
         _lib.Context(p)
 
