@@ -5,7 +5,9 @@ Default workload: the 200,000-galaxy Neyman-Scott periodic box with shapes
 (wg+ and wgg, 64 jackknife cubes, 20 log r_p x 40 Pi bins) -- the workload the
 headline metric "binned pairs/s (wgg+wg+ w/ jackknife)" is quoted on.  Other
 workloads: --workload box_uniform_wgg_20k | box_ns_wpp_20M | box_batch_wpp_64 |
-sky_wgp_500k_5M | sky_wgp_50k_500k (sky survey: SRd, RsRd, SD, DRs on a row sample).
+box_ns_ed_rmu_200k | box_ns_kappa_200k (the same box with the ED and kappa
+variants) | sky_wgp_500k_5M | sky_wgp_50k_500k (sky survey: SRd, RsRd, SD, DRs
+on a row sample).
 
 One step = one corels2 call (the SD pair type these runs use) over the whole
 catalogue.  `value` times the device work with the catalogues resident in HBM
@@ -48,14 +50,18 @@ def _workload(name: str):
         return [synth.box_ns_large_wpp()]
     if name == "box_batch_wpp_64":
         return synth.box_batch_wpp()
+    if name == "box_ns_ed_rmu_200k":
+        return [synth.box_ns_ed_rmu()]
+    if name == "box_ns_kappa_200k":
+        return [synth.box_ns_kappa()]
     raise SystemExit(f"unknown workload {name}")
 
 
 def _describe(wls) -> dict:
     p = wls[0].params
     d = {"workload": wls[0].name if len(wls) == 1 else "box_batch_wpp_64",
-         "which_corr": p.which_corr, "n_jk": p.n_jk_regions, "rp_bins": p.n_bins,
-         "pi_bins": p.n_p_bin, "rp_range": [p.bin_r_min, p.bin_r_max],
+         "which_corr": p.which_corr, "coordinates": p.coordinates, "n_jk": p.n_jk_regions,
+         "rp_bins": p.n_bins, "pi_bins": p.n_p_bin, "rp_range": [p.bin_r_min, p.bin_r_max],
          "pi_range": [p.p_min, p.p_max], "box": p.periodic_box_size,
          "n_points": int(sum(w.shape.n for w in wls)), "n_catalogs": len(wls),
          "pair_type": "SD (shape x density, S and D the same points)",
@@ -361,7 +367,7 @@ def run_sky(args) -> None:
                "sample": f"about {args.sky_cpu_rows} outer rows per pair type: {n} binned "
                          f"pairs in {dt:.2f} s"}
     peaks = _peaks()
-    F = metrics.FLOPS_PER_PAIR[p.which_corr]
+    F = metrics.flops_per_pair(p.which_corr, p.coordinates)
     A = metrics.smem_updates_per_pair(p.which_corr, bool(p.do_jk))
     achieved_flops = F * value
     roofline = {"bound": "fp32", "achieved": achieved_flops / 1e12,
@@ -499,7 +505,7 @@ def main() -> None:
         return
     p = wls[0].params
     peaks = _peaks()
-    F = metrics.FLOPS_PER_PAIR[p.which_corr]
+    F = metrics.flops_per_pair(p.which_corr, p.coordinates)
     A = metrics.smem_updates_per_pair(p.which_corr, bool(p.do_jk))
     pair_s = tot_pair_ms / args.steps * 1e-3
     n_per_step = n_bin / args.steps

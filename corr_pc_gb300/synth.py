@@ -339,6 +339,27 @@ def box_ns_wgp(seed: int = 0, n_parents: int = 2000) -> Workload:
     return Workload("box_ns_wgp_200k", p, cat, cat)
 
 
+def box_ns_ed_rmu(seed: int = 0, n_parents: int = 2000) -> Workload:
+    """The 200k clustered box with 3-D orientations: ED (which_corr 5) in r-mu
+    (coordinates 7), 20 log r bins 0.1-60, 10 mu bins, 64 jackknife cubes."""
+    L = 500.0
+    cat = with_orientation(neyman_scott(n_parents, 100.0, 2.0, L, seed, nside_jk=4), seed + 1)
+    p = _box_params(which_corr=5, L=L, rmin=0.1, rmax=60.0, nrp=20, npi=10, pmax=1.0,
+                    njk=64, n=cat.n)
+    p.coordinates = 7
+    return Workload("box_ns_ed_rmu_200k", p, cat, cat)
+
+
+def box_ns_kappa(seed: int = 0, n_parents: int = 2000) -> Workload:
+    """The 200k clustered box with a per-galaxy scalar: kappa-density
+    (which_corr 3), the headline binning."""
+    L = 500.0
+    cat = with_kappa(neyman_scott(n_parents, 100.0, 2.0, L, seed, nside_jk=4), seed + 1)
+    p = _box_params(which_corr=3, L=L, rmin=0.1, rmax=60.0, nrp=20, npi=40, pmax=100.0,
+                    njk=64, n=cat.n)
+    return Workload("box_ns_kappa_200k", p, cat, cat)
+
+
 def box_ns_large_wpp(seed: int = 0, n_parents: int = 200000) -> Workload:
     L = 1000.0
     cat = neyman_scott(n_parents, 100.0, 3.0, L, seed, nside_jk=5)
