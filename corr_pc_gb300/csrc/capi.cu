@@ -347,12 +347,12 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   jp.empty = (A.n == 0 || B.n == 0);
   const int nrp = p.n_bins, npi = p.n_p_bin;
   const int jk = p.do_jk ? 1 : 0;
-  // block-local Pi window: as many Pi bins as fit two blocks per SM.  With
+  // block-local Pi window: as many Pi bins as fit kFastBlocksPerSM blocks per SM.  With
   // coordinates 7 the mu bins have no locality in z: a block holds every mu bin
   // when they fit (else the units are repeated over slices of wpi mu bins)
   const bool rmu = p.coordinates == 7;
   const size_t static_b = fast_static_smem_bytes();
-  const size_t budget = (size_t)(227 * 1024) / 2 - static_b - 1024;
+  const size_t budget = (size_t)(228 * 1024) / kFastBlocksPerSM - static_b - 1024;
   int wpi = npi;
   if (c->tune_wpi > 0 && !rmu) wpi = std::min(npi, c->tune_wpi);
   else

@@ -68,6 +68,7 @@ double from_orderable_key(unsigned long long k);
 
 // pair_fast.cu
 constexpr int kTileThreads = 128;  // g1 rows per tile (the block has 2 warp groups over them)
+constexpr int kFastBlocksPerSM = 3;  // occupancy target: registers and shared memory sized for it
 size_t fast_smem_bytes(int corel, int do_jk, int NB);
 size_t fast_static_smem_bytes();
 int fast_blocks_per_sm(int corel, int jk, size_t smem);

@@ -203,7 +203,7 @@ constexpr int kQCap = 64;  // per-warp ring of binned pairs awaiting the heavy s
 constexpr unsigned kEdgeFlag = 0x8000u;  // queue entry: near the window edge
 
 template <int C, bool JK>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, kFastBlocksPerSM)
 fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ units,
                   int n_units, unsigned int *__restrict__ unit_ctr, QEntry *__restrict__ queue,
                   unsigned long long *__restrict__ qcount, unsigned long long qcap,
