@@ -401,6 +401,8 @@ def main() -> None:
     ap.add_argument("--fp64-budget", type=float, default=3.0, help="seconds of FP64 kernel")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")
+    ap.add_argument("--tune", default=None,
+                    help="K,W: fixed cell width r_max/K and Pi window W (instead of the autotuner)")
     ap.add_argument("--sky-rows", type=int, default=20000,
                     help="outer rows per pair type per step (sky workloads)")
     ap.add_argument("--sky-cpu-rows", type=int, default=400,
@@ -429,11 +431,16 @@ def main() -> None:
     wls = _workload(args.workload)
     preps = [host.prepare(w.params, [("S", w.shape), ("D", w.density)]) for w in wls]
     ctxs = [_lib.Context(w.params) for w in wls]
+    tuning = None
+    if args.tune:
+        tk, tw = (int(v) for v in args.tune.split(","))
+        for c in ctxs:
+            c.set_tuning(tk, tw)
+        tuning = {"cells_per_rmax": tk, "pi_window": tw, "by": "--tune"}
     for c, cat in zip(ctxs, preps):
         c.upload(0, cat["D"])
         c.upload(1, cat["S"])
-    tuning = None
-    if len(ctxs) == 1 and not args.no_tune:  # outside the timed region
+    if len(ctxs) == 1 and not args.no_tune and not args.tune:  # outside the timed region
         n_rows = wls[0].density.n
         k, w = ctxs[0].autotune("SD", 0, 1, sample_stride=max(1, n_rows // 25000))
         tuning = {"cells_per_rmax": k, "pi_window": w, "by": "cpc_autotune on a row sample"}
