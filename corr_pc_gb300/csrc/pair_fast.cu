@@ -23,12 +23,13 @@
 // (recheck_kernel), so integer counts are bit-identical with the reference.
 //
 // Accumulation: block-private histograms over (r_p bin, block-local Pi window)
-// in shared memory -- the full sample ("main"), the tile's own jackknife region
-// ("X") and one other region ("Y", the partner's region for cross-region
-// pairs) -- with 32-bit counts and fixed-point sums split over two 32-bit
-// words per field (exact integer addition, order independent), flushed to the
-// FP64 global histogram block every kFlushCands staged candidates and at the
-// end of the unit.
+// in shared memory -- the full sample ("main"), the cross-region pairs that the
+// tile's own jackknife region does NOT take ("NX": that region's sums are main
+// minus NX, so the pairs it takes, most of them, cost no update of their own) and
+// one other region ("Y", the partner's region for cross-region pairs) -- with
+// 32-bit counts and fixed-point sums split over two 32-bit words per field
+// (exact integer addition, order independent), flushed to the FP64 global
+// histogram block every kFlushCands staged candidates and at the end of the unit.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <climits>
@@ -86,6 +87,14 @@ template <> struct FieldMap<COREL_ED> {
   __device__ static constexpr int m(int k) { return k == 0 ? 0 : k == 1 ? 11 : 12; }
   __device__ static constexpr int j(int k) { return k == 0 ? 0 : 11; }
 };
+
+// main-histogram slot of jackknife field g (FM::j(g) is one of the FM::m fields)
+template <class FM>
+__device__ constexpr int jk_in_main(int g) {
+  int k = 0;
+  while (FM::m(k) != FM::j(g)) k++;
+  return k;
+}
 
 // Shared-memory bytes a block needs for a job with NB = nrp * wpi local bins.
 size_t fast_smem_bytes(int corel, int do_jk, int NB) {
@@ -199,6 +208,50 @@ __device__ __forceinline__ void flush_hist(unsigned *cnt, unsigned *lo, unsigned
   }
 }
 
+// Flush the main histogram (into h = 0) and the tile's region (into hx): the
+// region takes main minus NX, in exact integer arithmetic; zero both.
+template <int FM, int FJ, class FMAP>
+__device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsigned *mhi,
+                                             unsigned *ncnt, unsigned *nlo, unsigned *nhi, int NB,
+                                             int wpi, int npi, int nrp, int n2_base, int hx,
+                                             bool jk, int f0, const double *s_iqs,
+                                             const JobDev &J) {
+  const int64_t hsz = (int64_t)nrp * npi;
+  for (int lb = threadIdx.x; lb < NB; lb += kThreads) {
+    const unsigned n = mcnt[lb];
+    if (!n) continue;  // no pair in this bin since the last flush: every word is 0
+    const int64_t cell = (int64_t)(lb / wpi) * npi + n2_base + lb % wpi;
+    atomicAdd(&J.acc_num[cell], (unsigned long long)n);
+    mcnt[lb] = 0u;
+    long long tm[FM];
+#pragma unroll
+    for (int f = 0; f < FM; f++) {
+      const size_t o = (size_t)f * NB + lb;
+      tm[f] = (long long)(int)mhi[o] * 16384ll + (long long)mlo[o];
+      const int fld = FMAP::m(f);
+      if (f >= f0 && tm[f] != 0)
+        atomicAdd(&J.acc_sums[cell * kNF + fld], (double)tm[f] * s_iqs[fld]);
+      mlo[o] = 0u;
+      mhi[o] = 0u;
+    }
+    if (!jk) continue;
+    const int64_t xc = (int64_t)hx * hsz + cell;
+    const unsigned nx = ncnt[lb];
+    ncnt[lb] = 0u;
+    if (n - nx) atomicAdd(&J.acc_num[xc], (unsigned long long)(n - nx));
+#pragma unroll
+    for (int g = 0; g < FJ; g++) {
+      const size_t o = (size_t)g * NB + lb;
+      const long long tn = (long long)(int)nhi[o] * 16384ll + (long long)nlo[o];
+      nlo[o] = 0u;
+      nhi[o] = 0u;
+      const long long tx = tm[jk_in_main<FMAP>(g)] - tn;
+      const int fld = FMAP::j(g);
+      if (g >= f0 && tx != 0) atomicAdd(&J.acc_sums[xc * kNF + fld], (double)tx * s_iqs[fld]);
+    }
+  }
+}
+
 constexpr int kQCap = 64;  // per-warp ring of binned pairs awaiting the heavy step
 constexpr unsigned kEdgeFlag = 0x8000u;  // queue entry: near the window edge
 
@@ -286,7 +339,9 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     constexpr bool kTheta = C == COREL_SD || C == COREL_SS || C == COREL_SSA || C == COREL_SK;
     const bool has_lo = (kTheta || C == COREL_ED) && J.has_lo;
     const int rmu = J.rmu;
-    const int gws = J.gws, lin_bin = J.lin_bin, box_same_keep = J.box_same_keep;
+    // jackknife attribution: jk_check_PB (the box's rule; this kernel runs box
+    // jobs only)
+    const int gws = J.gws, lin_bin = J.lin_bin;
     const float rmin_f = J.rmin_f, inv_rsize_f = J.inv_rsize_f;
     if (has1) {
       p1 = J.f1.pos[i1];
@@ -454,15 +509,11 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
           const int nb = min(kBatch, gN - base);
           if (since_flush + nb > kFlushCands) {  // keep every word below 2^32
             __syncthreads();
-            flush_hist<F::FM, false, F>(s_mnum, s_mlo, s_mhi, NB, wpi, npi, nrp, n2_base, 0, f0,
-                                        s_iqs, J);
-            if (JK) {
-              flush_hist<F::FJ, true, F>(s_xnum, s_xlo, s_xhi, NB, wpi, npi, nrp, n2_base,
-                                         1 + U.region, f0, s_iqs, J);
-              if (cur_y >= 0)
-                flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
-                                           1 + cur_y, f0, s_iqs, J);
-            }
+            flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_xnum, s_xlo, s_xhi, NB, wpi,
+                                          npi, nrp, n2_base, 1 + U.region, JK, f0, s_iqs, J);
+            if (JK && cur_y >= 0)
+              flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
+                                         1 + cur_y, f0, s_iqs, J);
             since_flush = 0;
           }
           since_flush += nb;
@@ -705,10 +756,12 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                   red_split(&s_mlo[(size_t)f * NB + lb], &s_mhi[(size_t)f * NB + lb],
                             to_fixed(v[F::m(f)], s_qs[F::m(f)]));
               if (JK) {
-                const bool k1 = s_rkeep[er] != 0;
-                const bool xc = same_region ? (box_same_keep || k1) : k1;
+                // jk_check_PB (jk.cpp:64-71): the tile's region takes a same-region
+                // pair and a cross-region pair whose row is kept (main - NX); the
+                // partner's region takes a cross-region pair whose partner is kept
+                const bool nxc = !same_region && !s_rkeep[er];
                 const bool yc = !same_region && s_keep[ec];
-                if (xc) {
+                if (nxc) {
                   atomicAdd(&s_xnum[lb], 1u);
 #pragma unroll
                   for (int f = 0; f < F::FJ; f++)
@@ -740,15 +793,11 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
 
     // ---- flush main, X and the last Y ----
     __syncthreads();
-    flush_hist<F::FM, false, F>(s_mnum, s_mlo, s_mhi, NB, wpi, npi, nrp, n2_base, 0, f0,
-                                s_iqs, J);
-    if (JK) {
-      flush_hist<F::FJ, true, F>(s_xnum, s_xlo, s_xhi, NB, wpi, npi, nrp, n2_base, 1 + U.region,
-                                 f0, s_iqs, J);
-      if (cur_y >= 0)
-        flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y,
-                                   f0, s_iqs, J);
-    }
+    flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_xnum, s_xlo, s_xhi, NB, wpi, npi, nrp,
+                                  n2_base, 1 + U.region, JK, f0, s_iqs, J);
+    if (JK && cur_y >= 0)
+      flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y, f0,
+                                 s_iqs, J);
     // window-pair counter (once per pair: mu slices other than the first skip it)
     {
       unsigned long long v = (rmu && n2_base != 0) ? 0ull : (unsigned long long)nwin;
