@@ -96,6 +96,10 @@ __device__ constexpr int jk_in_main(int g) {
   return k;
 }
 
+// Padding that puts the high-word array (FW * NB words after the low words)
+// 16 banks away from the low-word array.
+__host__ __device__ constexpr int hi_pad(int words) { return (16 - (words & 31) + 32) & 31; }
+
 // Shared-memory bytes a block needs for a job with NB = nrp * wpi local bins.
 size_t fast_smem_bytes(int corel, int do_jk, int NB) {
   int FM = 1, FJ = 1;
@@ -106,8 +110,8 @@ size_t fast_smem_bytes(int corel, int do_jk, int NB) {
   if (corel == COREL_SK) { FM = 4; FJ = 4; }
   if (corel == COREL_ED) { FM = 3; FJ = 2; }
   size_t b = sizeof(float4) * 2 * kBatch;                // staging
-  b += 8ull * FM * NB + 4ull * NB;
-  if (do_jk) b += 2 * (8ull * FJ * NB + 4ull * NB);
+  b += 8ull * FM * NB + 4ull * NB + 4ull * hi_pad(FM * NB);
+  if (do_jk) b += 2 * (8ull * FJ * NB + 4ull * NB + 4ull * hi_pad(FJ * NB));
   return b;
 }
 
@@ -115,8 +119,8 @@ size_t fast_smem_bytes(int corel, int do_jk, int NB) {
 // integer u = rint(v * 2^S_f), |u| <= 2^26 (S_f from a bound on |v|); u is split
 // into its low 14 bits (0..16383) and the arithmetic shift u >> 14
 // (-2^12..2^12), each added to its own 32-bit word with a plain reduction (no
-// return value: no scoreboard wait, and same-address adds of a warp are
-// combined in hardware).  A block flushes its histograms after every
+// return value: no scoreboard wait; lanes of one instruction that hit the same
+// word are serialised, which red_pair halves).  A block flushes its histograms after every
 // kFlushCands staged candidates, so a bin takes at most kTile * kFlushCands =
 // 2^18 terms between flushes: the low word stays below 2^32 and the high word,
 // read as a signed integer, within +-2^30.
@@ -125,9 +129,14 @@ static_assert((long long)kTileThreads * kFlushCands <= (1ll << 18), "fixed-point
 __device__ __forceinline__ int to_fixed(float v, float scale) {
   return __float2int_rn(v * scale);
 }
-__device__ __forceinline__ void red_split(unsigned *lo, unsigned *hi, int u) {
-  atomicAdd(lo, (unsigned)u & 0x3FFFu);
-  atomicAdd(hi, (unsigned)(u >> 14));
+// The two reductions of one term, even lanes taking the low word first and odd
+// lanes the high word first: lanes of one instruction that hit the same bin then
+// split over two addresses 16 banks apart (same-address shared reductions are
+// serialised), halving those collisions.
+__device__ __forceinline__ void red_pair(unsigned *lo, unsigned *hi, int u, bool odd) {
+  const unsigned a = (unsigned)u & 0x3FFFu, b = (unsigned)(u >> 14);
+  atomicAdd(odd ? hi : lo, odd ? b : a);
+  atomicAdd(odd ? lo : hi, odd ? a : b);
 }
 __device__ __forceinline__ double fixed_total(unsigned lw, unsigned hw, double inv_scale) {
   const long long tot = (long long)(int)hw * 16384ll + (long long)lw;
@@ -306,14 +315,16 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     const int nrp = J.nrp, wpi = J.wpi, npi = J.npi, NB = nrp * wpi;
     // per histogram: count[NB], low words [F][NB], high words [F][NB]
     unsigned *s_mnum = reinterpret_cast<unsigned *>(hist_base);
+    // the high words sit hi_pad words after a 32-word-aligned offset from the low
+    // words, so the low and high word of one bin are 16 banks apart (red_pair)
     unsigned *s_mlo = s_mnum + NB;
-    unsigned *s_mhi = s_mlo + (size_t)F::FM * NB;
+    unsigned *s_mhi = s_mlo + (size_t)F::FM * NB + hi_pad(F::FM * NB);
     unsigned *s_xnum = s_mhi + (size_t)F::FM * NB;
     unsigned *s_xlo = s_xnum + NB;
-    unsigned *s_xhi = s_xlo + (size_t)F::FJ * NB;
+    unsigned *s_xhi = s_xlo + (size_t)F::FJ * NB + hi_pad(F::FJ * NB);
     unsigned *s_ynum = s_xhi + (size_t)F::FJ * NB;
     unsigned *s_ylo = s_ynum + NB;
-    unsigned *s_yhi = s_ylo + (size_t)F::FJ * NB;
+    unsigned *s_yhi = s_ylo + (size_t)F::FJ * NB + hi_pad(F::FJ * NB);
     const int f0 = J.unit_w ? 1 : 0;  // unit weights: wt_num = count, not accumulated
 
     // ---- this thread's g1 row.  The lanes of a warp are spread over the whole
@@ -749,12 +760,13 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                   v[10] = xa * xa + xb * xb;
                 }
               }
+              const bool odd_lane = (lane & 1) != 0;
               atomicAdd(&s_mnum[lb], 1u);
 #pragma unroll
               for (int f = 0; f < F::FM; f++)
                 if (f >= f0)
-                  red_split(&s_mlo[(size_t)f * NB + lb], &s_mhi[(size_t)f * NB + lb],
-                            to_fixed(v[F::m(f)], s_qs[F::m(f)]));
+                  red_pair(&s_mlo[(size_t)f * NB + lb], &s_mhi[(size_t)f * NB + lb],
+                            to_fixed(v[F::m(f)], s_qs[F::m(f)]), odd_lane);
               if (JK) {
                 // jk_check_PB (jk.cpp:64-71): the tile's region takes a same-region
                 // pair and a cross-region pair whose row is kept (main - NX); the
@@ -766,16 +778,16 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
 #pragma unroll
                   for (int f = 0; f < F::FJ; f++)
                     if (f >= f0)
-                      red_split(&s_xlo[(size_t)f * NB + lb], &s_xhi[(size_t)f * NB + lb],
-                                to_fixed(v[F::j(f)], s_qs[F::j(f)]));
+                      red_pair(&s_xlo[(size_t)f * NB + lb], &s_xhi[(size_t)f * NB + lb],
+                                to_fixed(v[F::j(f)], s_qs[F::j(f)]), odd_lane);
                 }
                 if (yc) {
                   atomicAdd(&s_ynum[lb], 1u);
 #pragma unroll
                   for (int f = 0; f < F::FJ; f++)
                     if (f >= f0)
-                      red_split(&s_ylo[(size_t)f * NB + lb], &s_yhi[(size_t)f * NB + lb],
-                                to_fixed(v[F::j(f)], s_qs[F::j(f)]));
+                      red_pair(&s_ylo[(size_t)f * NB + lb], &s_yhi[(size_t)f * NB + lb],
+                                to_fixed(v[F::j(f)], s_qs[F::j(f)]), odd_lane);
                 }
               }
               }
