@@ -46,55 +46,70 @@ constexpr int kBatch = kThreads;              // candidates staged per batch
 constexpr int kMaxSeg = 512;
 constexpr int kMaxCols = 1024;
 
+// Per corel: the main fields m(k), k < FM, the jackknife fields j(g), g < FJ, and
+// jm(g), the main slot holding jackknife field g (m(jm(g)) == j(g)).
 template <int C> struct FieldMap;
 template <> struct FieldMap<COREL_DD> {
   static constexpr int FM = 1, FJ = 1;
-  __device__ static constexpr int m(int) { return 0; }
-  __device__ static constexpr int j(int) { return 0; }
+  __host__ __device__ static constexpr int m(int) { return 0; }
+  __host__ __device__ static constexpr int j(int) { return 0; }
+  __host__ __device__ static constexpr int jm(int) { return 0; }
 };
 template <> struct FieldMap<COREL_SD> {
   static constexpr int FM = 7, FJ = 4;
-  __device__ static constexpr int m(int k) {
+  __host__ __device__ static constexpr int m(int k) {
     return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 2 : k == 3 ? 3 : k == 4 ? 4 : k == 5 ? 11 : 12;
   }
-  __device__ static constexpr int j(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 3 : 11; }
+  __host__ __device__ static constexpr int j(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 3 : 11; }
+  __host__ __device__ static constexpr int jm(int g) { return g == 0 ? 0 : g == 1 ? 1 : g == 2 ? 3 : 5; }
 };
 template <> struct FieldMap<COREL_SS> {
   static constexpr int FM = 11, FJ = 6;
-  __device__ static constexpr int m(int k) { return k < 2 ? k : k == 2 ? 2 : k + 2; }
-  __device__ static constexpr int j(int k) { return k == 0 ? 0 : 2 * k - 1 + (k >= 2 ? 2 : 0); }
+  __host__ __device__ static constexpr int m(int k) { return k < 2 ? k : k == 2 ? 2 : k + 2; }
+  __host__ __device__ static constexpr int j(int k) { return k == 0 ? 0 : 2 * k - 1 + (k >= 2 ? 2 : 0); }
+  __host__ __device__ static constexpr int jm(int g) { return g == 0 ? 0 : 2 * g - 1; }
 };
 template <> struct FieldMap<COREL_SSA> {
   static constexpr int FM = 13, FJ = 7;
-  __device__ static constexpr int m(int k) { return k; }
-  __device__ static constexpr int j(int k) { return k == 0 ? 0 : 2 * k - 1; }
+  __host__ __device__ static constexpr int m(int k) { return k; }
+  __host__ __device__ static constexpr int j(int k) { return k == 0 ? 0 : 2 * k - 1; }
+  __host__ __device__ static constexpr int jm(int g) { return g == 0 ? 0 : 2 * g - 1; }
 };
 // density_convergence: wt, data[1].val
 template <> struct FieldMap<COREL_DK> {
   static constexpr int FM = 2, FJ = 2;
-  __device__ static constexpr int m(int k) { return k; }
-  __device__ static constexpr int j(int k) { return k; }
+  __host__ __device__ static constexpr int m(int k) { return k; }
+  __host__ __device__ static constexpr int j(int k) { return k; }
+  __host__ __device__ static constexpr int jm(int g) { return g; }
 };
 // shape_convergence: wt, data[1].val, data[3].val, data[5].val
 template <> struct FieldMap<COREL_SK> {
   static constexpr int FM = 4, FJ = 4;
-  __device__ static constexpr int m(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 5 : 9; }
-  __device__ static constexpr int j(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 5 : 9; }
+  __host__ __device__ static constexpr int m(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 5 : 9; }
+  __host__ __device__ static constexpr int j(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 5 : 9; }
+  __host__ __device__ static constexpr int jm(int g) { return g; }
 };
 // ED: wt, data[6].val, data[6].err (regions: wt, data[6].val)
 template <> struct FieldMap<COREL_ED> {
   static constexpr int FM = 3, FJ = 2;
-  __device__ static constexpr int m(int k) { return k == 0 ? 0 : k == 1 ? 11 : 12; }
-  __device__ static constexpr int j(int k) { return k == 0 ? 0 : 11; }
+  __host__ __device__ static constexpr int m(int k) { return k == 0 ? 0 : k == 1 ? 11 : 12; }
+  __host__ __device__ static constexpr int j(int k) { return k == 0 ? 0 : 11; }
+  __host__ __device__ static constexpr int jm(int g) { return g; }
 };
 
-// main-histogram slot of jackknife field g (FM::j(g) is one of the FM::m fields)
-template <class FM>
-__device__ constexpr int jk_in_main(int g) {
-  int k = 0;
-  while (FM::m(k) != FM::j(g)) k++;
-  return k;
+template <class FM, int G = 0>
+constexpr bool jm_consistent() {
+  if constexpr (G >= FM::FJ) {
+    return true;
+  } else {
+    return FM::m(FM::jm(G)) == FM::j(G) && jm_consistent<FM, G + 1>();
+  }
 }
+static_assert(jm_consistent<FieldMap<COREL_DD>>() && jm_consistent<FieldMap<COREL_SD>>() &&
+                  jm_consistent<FieldMap<COREL_SS>>() && jm_consistent<FieldMap<COREL_SSA>>() &&
+                  jm_consistent<FieldMap<COREL_DK>>() && jm_consistent<FieldMap<COREL_SK>>() &&
+                  jm_consistent<FieldMap<COREL_ED>>(),
+              "jackknife fields must map onto main slots");
 
 // Padding that puts the high-word array (FW * NB words after the low words)
 // 16 banks away from the low-word array.
@@ -133,10 +148,11 @@ __device__ __forceinline__ int to_fixed(float v, float scale) {
 // lanes the high word first: lanes of one instruction that hit the same bin then
 // split over two addresses 16 banks apart (same-address shared reductions are
 // serialised), halving those collisions.
-__device__ __forceinline__ void red_pair(unsigned *lo, unsigned *hi, int u, bool odd) {
-  const unsigned a = (unsigned)u & 0x3FFFu, b = (unsigned)(u >> 14);
-  atomicAdd(odd ? hi : lo, odd ? b : a);
-  atomicAdd(odd ? lo : hi, odd ? a : b);
+// wa, wb: the lane's two words in that order (low, high for even lanes).
+__device__ __forceinline__ void red_pair(unsigned *lo, unsigned *hi, unsigned wa, unsigned wb,
+                                         bool odd) {
+  atomicAdd(odd ? hi : lo, wa);
+  atomicAdd(odd ? lo : hi, wb);
 }
 __device__ __forceinline__ double fixed_total(unsigned lw, unsigned hw, double inv_scale) {
   const long long tot = (long long)(int)hw * 16384ll + (long long)lw;
@@ -254,7 +270,7 @@ __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsi
       const long long tn = (long long)(int)nhi[o] * 16384ll + (long long)nlo[o];
       nlo[o] = 0u;
       nhi[o] = 0u;
-      const long long tx = tm[jk_in_main<FMAP>(g)] - tn;
+      const long long tx = tm[FMAP::jm(g)] - tn;
       const int fld = FMAP::j(g);
       if (g >= f0 && tx != 0) atomicAdd(&J.acc_sums[xc * kNF + fld], (double)tx * s_iqs[fld]);
     }
@@ -760,13 +776,24 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                   v[10] = xa * xa + xb * xb;
                 }
               }
+              // fixed-point words of the main fields, in this lane's order (even
+              // lanes low word first, odd lanes high word first: red_pair); the
+              // region histograms reuse them
               const bool odd_lane = (lane & 1) != 0;
+              unsigned wa[F::FM], wb[F::FM];
+#pragma unroll
+              for (int f = 0; f < F::FM; f++) {
+                const int u = to_fixed(v[F::m(f)], s_qs[F::m(f)]);
+                const unsigned a = (unsigned)u & 0x3FFFu, b = (unsigned)(u >> 14);
+                wa[f] = odd_lane ? b : a;
+                wb[f] = odd_lane ? a : b;
+              }
               atomicAdd(&s_mnum[lb], 1u);
 #pragma unroll
               for (int f = 0; f < F::FM; f++)
                 if (f >= f0)
-                  red_pair(&s_mlo[(size_t)f * NB + lb], &s_mhi[(size_t)f * NB + lb],
-                            to_fixed(v[F::m(f)], s_qs[F::m(f)]), odd_lane);
+                  red_pair(&s_mlo[(size_t)f * NB + lb], &s_mhi[(size_t)f * NB + lb], wa[f],
+                           wb[f], odd_lane);
               if (JK) {
                 // jk_check_PB (jk.cpp:64-71): the tile's region takes a same-region
                 // pair and a cross-region pair whose row is kept (main - NX); the
@@ -776,18 +803,18 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                 if (nxc) {
                   atomicAdd(&s_xnum[lb], 1u);
 #pragma unroll
-                  for (int f = 0; f < F::FJ; f++)
-                    if (f >= f0)
-                      red_pair(&s_xlo[(size_t)f * NB + lb], &s_xhi[(size_t)f * NB + lb],
-                                to_fixed(v[F::j(f)], s_qs[F::j(f)]), odd_lane);
+                  for (int g = 0; g < F::FJ; g++)
+                    if (g >= f0)
+                      red_pair(&s_xlo[(size_t)g * NB + lb], &s_xhi[(size_t)g * NB + lb],
+                               wa[F::jm(g)], wb[F::jm(g)], odd_lane);
                 }
                 if (yc) {
                   atomicAdd(&s_ynum[lb], 1u);
 #pragma unroll
-                  for (int f = 0; f < F::FJ; f++)
-                    if (f >= f0)
-                      red_pair(&s_ylo[(size_t)f * NB + lb], &s_yhi[(size_t)f * NB + lb],
-                                to_fixed(v[F::j(f)], s_qs[F::j(f)]), odd_lane);
+                  for (int g = 0; g < F::FJ; g++)
+                    if (g >= f0)
+                      red_pair(&s_ylo[(size_t)g * NB + lb], &s_yhi[(size_t)g * NB + lb],
+                               wa[F::jm(g)], wb[F::jm(g)], odd_lane);
                 }
               }
               }
