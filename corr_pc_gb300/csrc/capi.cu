@@ -351,12 +351,22 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   // coordinates 7 the mu bins have no locality in z: a block holds every mu bin
   // when they fit (else the units are repeated over slices of wpi mu bins)
   const bool rmu = p.coordinates == 7;
+  // Automatic window: the largest that fits 4 blocks per SM when it holds at
+  // least 12 Pi bins (or all of them), else the largest for 3 blocks.
   const size_t static_b = fast_static_smem_bytes();
-  const size_t budget = (size_t)(228 * 1024) / kFastBlocksPerSM - static_b - 1024;
+  auto fit = [&](int blocks) {
+    const size_t budget = (size_t)(228 * 1024) / blocks - static_b - 1024;
+    int w = npi;
+    while (w > (rmu ? 1 : 8) && fast_smem_bytes(jp.rule.corel, jk, nrp * w) > budget) w--;
+    return w;
+  };
   int wpi = npi;
-  if (c->tune_wpi > 0 && !rmu) wpi = std::min(npi, c->tune_wpi);
-  else
-    while (wpi > (rmu ? 1 : 8) && fast_smem_bytes(jp.rule.corel, jk, nrp * wpi) > budget) wpi--;
+  if (c->tune_wpi > 0 && !rmu) {
+    wpi = std::min(npi, c->tune_wpi);
+  } else {
+    wpi = fit(kFastBlocksPerSM);
+    if (wpi < npi && wpi < 12) wpi = std::max(wpi, fit(kFastBlocksPerSM - 1));
+  }
   if (!rmu && wpi < npi && wpi < 8) wpi = std::min(npi, 8);
   jp.wpi = wpi;
   jp.tile = kTileThreads;
@@ -747,7 +757,7 @@ cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt = 0) {
       for (UnitDesc d : u) {
         d.job = k;
         const int64_t ncol = (int64_t)(d.cx_hi - d.cx_lo + 1) * (d.cy_hi - d.cy_lo + 1);
-        if (ncol < 1 || ncol > 1024 || d.g1_count < 1 || d.g1_count > kTileThreads)
+        if (ncol < 1 || ncol > kFastMaxCols || d.g1_count < 1 || d.g1_count > kTileThreads)
           return fail(c, CPC_ERR_INVALID, "work unit outside kernel limits (too many neighbour columns)");
         all.push_back(d);
       }
@@ -773,12 +783,13 @@ cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt = 0) {
       wmax = std::max(wmax, jp.wpi * jp.jd.nrp);
     }
     const size_t smem = fast_smem_bytes(corel, jk, wmax);
-    int bps = fast_blocks_per_sm(corel, jk, smem);
+    int bps = 0;
+    const int minb = fast_variant(corel, jk, smem, &bps);
     if (bps <= 0) return fail(c, CPC_ERR_INVALID, "fast kernel does not fit on an SM with these bins");
     const int n_units = (int)(ranges[g].second - ranges[g].first);
     const int grid = (int)std::min<int64_t>((int64_t)c0->sm_count * bps, n_units);
     CK(cudaMemsetAsync(c0->d_unit_ctr.p, 0, sizeof(unsigned int), st), "memset");
-    CK(launch_fast(corel, jk, c0->d_jobs.p, c0->d_units.p + ranges[g].first, n_units,
+    CK(launch_fast(corel, jk, minb, c0->d_jobs.p, c0->d_units.p + ranges[g].first, n_units,
                    c0->d_unit_ctr.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, smem, grid, st),
        "fast kernel");
     c0->launches += 1;
@@ -1417,7 +1428,8 @@ cpc_status cpc_accum_shape(const cpc_ctx *c, int *n_hist, int *n_bins, int *n_p_
 
 cpc_status cpc_set_tuning(cpc_ctx *c, int cells_per_rmax, int pi_window, int tile) {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
-  if (cells_per_rmax < 0 || cells_per_rmax > 16 || pi_window < 0 || (tile != 0 && tile != kTileThreads))
+  if (cells_per_rmax < 0 || cells_per_rmax > kMaxCellsPerRmax || pi_window < 0 ||
+      (tile != 0 && tile != kTileThreads))
     return fail(c, CPC_ERR_INVALID, "tuning values out of range");
   c->tune_k = cells_per_rmax;
   c->tune_wpi = pi_window;
@@ -1556,7 +1568,28 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
   acc.num = num.data();
   acc.sums = sums.data();
   const int ks[3] = {2, 3, 4};
-  const int ws[4] = {0, 16, 24, 32};
+  // Pi windows: for 4, 3 and 2 blocks per SM the largest window whose
+  // histograms fit, and three quarters of it (more, narrower units)
+  std::vector<int> ws;
+  {
+    JobRule rule;
+    if (job_rule(p, kind, c->slots[slot_g1].n, c->slots[slot_g2].n, rule) != 0)
+      return fail(c, CPC_ERR_INVALID, "bad pair kind");
+    const int jk = p.do_jk ? 1 : 0, nrp = p.n_bins, npi = p.n_p_bin;
+    const size_t static_b = fast_static_smem_bytes();
+    for (int b = 4; b >= 2; b--) {
+      const size_t budget = (size_t)(228 * 1024) / b - static_b - 1024;
+      int w = npi;
+      while (w > 1 && fast_smem_bytes(rule.corel, jk, nrp * w) > budget) w--;
+      if (fast_smem_bytes(rule.corel, jk, nrp * w) > budget) continue;
+      for (int cand : {w, (3 * w + 3) / 4}) {
+        if (cand < std::min(npi, 8)) continue;
+        if (std::find(ws.begin(), ws.end(), cand) == ws.end()) ws.push_back(cand);
+      }
+      if (w == npi) break;  // every Pi bin fits: fewer blocks gain nothing
+    }
+    if (ws.empty()) ws.push_back(0);
+  }
   const int64_t stride = std::max<int64_t>(1, sample_stride);
   double best = INFINITY;
   int bk = c->slots[slot_g1].kcells, bw = c->tune_wpi;
@@ -1568,7 +1601,6 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
         (s = rebuild_cells(c, c->slots[slot_g2], k)) != CPC_OK)
       return s;
     for (int w : ws) {
-      if (w > p.n_p_bin) continue;
       c->tune_wpi = w;
       // first run builds the work units, the second is timed
       if (cpc_count(c, kind, slot_g1, slot_g2, CPC_ENGINE_FAST, stride, 0, &acc) != CPC_OK) continue;

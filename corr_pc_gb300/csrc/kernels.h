@@ -68,13 +68,20 @@ double from_orderable_key(unsigned long long k);
 
 // pair_fast.cu
 constexpr int kTileThreads = 128;  // g1 rows per tile (the block has 2 warp groups over them)
-constexpr int kFastBlocksPerSM = 3;  // occupancy target: registers and shared memory sized for it
+constexpr int kFastBlocksPerSM = 4;  // occupancy target: registers and shared memory sized for it
+// Per work unit: at most kFastMaxCols neighbour columns (the host rejects units
+// with more; (2k + 3)^2 columns for cells r_max / k wide, so k <= 9) and
+// candidate slots taken kFastMaxSeg at a time.
+constexpr int kFastMaxCols = 512;
+constexpr int kFastMaxSeg = 256;
+constexpr int kMaxCellsPerRmax = 9;
 size_t fast_smem_bytes(int corel, int do_jk, int NB);
 size_t fast_static_smem_bytes();
-int fast_blocks_per_sm(int corel, int jk, size_t smem);
-cudaError_t launch_fast(int corel, int jk, const JobDev *jobs, const UnitDesc *units, int n_units,
-                        unsigned int *unit_ctr, QEntry *q, unsigned long long *qcount,
-                        unsigned long long qcap, size_t smem, int grid, cudaStream_t st);
+int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm);
+cudaError_t launch_fast(int corel, int jk, int minb, const JobDev *jobs, const UnitDesc *units,
+                        int n_units, unsigned int *unit_ctr, QEntry *q,
+                        unsigned long long *qcount, unsigned long long qcap, size_t smem,
+                        int grid, cudaStream_t st);
 cudaError_t launch_recheck(const JobDev *jobs, const QEntry *q, const unsigned long long *qcount,
                            unsigned long long qcap, int grid, cudaStream_t st);
 

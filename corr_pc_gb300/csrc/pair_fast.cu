@@ -43,8 +43,8 @@ constexpr int kTile = kTileThreads;          // g1 rows per tile
 constexpr int kGroups = 2;                    // warp groups sharing the rows
 constexpr int kThreads = kTile * kGroups;     // block size
 constexpr int kBatch = kThreads;              // candidates staged per batch
-constexpr int kMaxSeg = 512;
-constexpr int kMaxCols = 1024;
+constexpr int kMaxSeg = kFastMaxSeg;
+constexpr int kMaxCols = kFastMaxCols;
 
 // Per corel: the main fields m(k), k < FM, the jackknife fields j(g), g < FJ, and
 // jm(g), the main slot holding jackknife field g (m(jm(g)) == j(g)).
@@ -280,8 +280,10 @@ __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsi
 constexpr int kQCap = 64;  // per-warp ring of binned pairs awaiting the heavy step
 constexpr unsigned kEdgeFlag = 0x8000u;  // queue entry: near the window edge
 
-template <int C, bool JK>
-__global__ void __launch_bounds__(kThreads, kFastBlocksPerSM)
+// MINB: blocks per SM the registers are bounded for (4 when the job's
+// histograms fit a quarter of shared memory, else 3)
+template <int C, bool JK, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
 fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ units,
                   int n_units, unsigned int *__restrict__ unit_ctr, QEntry *__restrict__ queue,
                   unsigned long long *__restrict__ qcount, unsigned long long qcap,
@@ -877,28 +879,13 @@ __global__ void recheck_kernel(const JobDev *__restrict__ jobs, const QEntry *__
 }
 
 // ---- host-side launchers (called from capi.cu) ----
-template <int C, bool JK>
-static cudaError_t launch_fast_t(const JobDev *jobs, const UnitDesc *units, int n_units,
-                                 unsigned int *unit_ctr, QEntry *q, unsigned long long *qcount,
-                                 unsigned long long qcap, size_t smem, int grid,
-                                 cudaStream_t st) {
-  auto kern = fast_pairs_kernel<C, JK>;
-  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
-  const int zero_words = (int)((smem - sizeof(float4) * 2 * kBatch) / 4);
-  kern<<<grid, kThreads, smem, st>>>(jobs, units, n_units, unit_ctr, q, qcount, qcap, zero_words);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_fast(int corel, int jk, const JobDev *jobs, const UnitDesc *units, int n_units,
-                        unsigned int *unit_ctr, QEntry *q, unsigned long long *qcount,
-                        unsigned long long qcap, size_t smem, int grid, cudaStream_t st) {
-#define CPC_CASE(CC)                                                                         \
-  if (corel == CC) {                                                                         \
-    return jk ? launch_fast_t<CC, true>(jobs, units, n_units, unit_ctr, q, qcount, qcap, smem, \
-                                        grid, st)                                            \
-              : launch_fast_t<CC, false>(jobs, units, n_units, unit_ctr, q, qcount, qcap,    \
-                                         smem, grid, st);                                    \
+// Calls fn.run<C, JK, MINB>() for the runtime corel, jackknife flag and bound.
+template <class Fn>
+static auto dispatch(int corel, int jk, int minb, const Fn &fn) -> decltype(fn.template run<0, false, 3>()) {
+#define CPC_CASE(CC)                                                                  \
+  if (corel == CC) {                                                                  \
+    if (jk) return minb == 4 ? fn.template run<CC, true, 4>() : fn.template run<CC, true, 3>(); \
+    return minb == 4 ? fn.template run<CC, false, 4>() : fn.template run<CC, false, 3>();       \
   }
   CPC_CASE(COREL_DD)
   CPC_CASE(COREL_SD)
@@ -908,31 +895,62 @@ cudaError_t launch_fast(int corel, int jk, const JobDev *jobs, const UnitDesc *u
   CPC_CASE(COREL_SK)
   CPC_CASE(COREL_ED)
 #undef CPC_CASE
-  return cudaErrorInvalidValue;
+  return fn.template run<COREL_DD, false, 3>();  // unreachable for valid corels
 }
 
-int fast_blocks_per_sm(int corel, int jk, size_t smem) {
-  int nb = 0;
-  cudaError_t e = cudaErrorInvalidValue;
-#define CPC_OCC(CC)                                                                             \
-  if (corel == CC) {                                                                            \
-    if (jk) {                                                                                   \
-      cudaFuncSetAttribute(fast_pairs_kernel<CC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fast_pairs_kernel<CC, true>, kThreads, smem); \
-    } else {                                                                                    \
-      cudaFuncSetAttribute(fast_pairs_kernel<CC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fast_pairs_kernel<CC, false>, kThreads, smem); \
-    }                                                                                           \
+struct LaunchFast {
+  const JobDev *jobs;
+  const UnitDesc *units;
+  int n_units;
+  unsigned int *unit_ctr;
+  QEntry *q;
+  unsigned long long *qcount, qcap;
+  size_t smem;
+  int grid;
+  cudaStream_t st;
+  template <int C, bool JK, int MINB>
+  cudaError_t run() const {
+    auto kern = fast_pairs_kernel<C, JK, MINB>;
+    cudaError_t err =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return err;
+    const int zero_words = (int)((smem - sizeof(float4) * 2 * kBatch) / 4);
+    kern<<<grid, kThreads, smem, st>>>(jobs, units, n_units, unit_ctr, q, qcount, qcap, zero_words);
+    return cudaGetLastError();
   }
-  CPC_OCC(COREL_DD)
-  CPC_OCC(COREL_SD)
-  CPC_OCC(COREL_SS)
-  CPC_OCC(COREL_SSA)
-  CPC_OCC(COREL_DK)
-  CPC_OCC(COREL_SK)
-  CPC_OCC(COREL_ED)
-#undef CPC_OCC
-  return e == cudaSuccess ? nb : 0;
+};
+
+struct Occupancy {
+  size_t smem;
+  template <int C, bool JK, int MINB>
+  int run() const {
+    auto kern = fast_pairs_kernel<C, JK, MINB>;
+    int nb = 0;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kThreads, smem) != cudaSuccess)
+      return 0;
+    return nb;
+  }
+};
+
+cudaError_t launch_fast(int corel, int jk, int minb, const JobDev *jobs, const UnitDesc *units,
+                        int n_units, unsigned int *unit_ctr, QEntry *q,
+                        unsigned long long *qcount, unsigned long long qcap, size_t smem,
+                        int grid, cudaStream_t st) {
+  if (corel < COREL_DD || corel > COREL_ED) return cudaErrorInvalidValue;
+  return dispatch(corel, jk, minb,
+                  LaunchFast{jobs, units, n_units, unit_ctr, q, qcount, qcap, smem, grid, st});
+}
+
+// The register-bound variant for this shared-memory size and its blocks per SM:
+// the 4-block variant when 4 blocks fit, else the 3-block one.
+int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm) {
+  if (corel < COREL_DD || corel > COREL_ED) { *blocks_per_sm = 0; return 3; }
+  const int b4 = dispatch(corel, jk, 4, Occupancy{smem});
+  if (b4 >= 4) { *blocks_per_sm = b4; return 4; }
+  *blocks_per_sm = dispatch(corel, jk, 3, Occupancy{smem});
+  return 3;
 }
 
 cudaError_t launch_recheck(const JobDev *jobs, const QEntry *q, const unsigned long long *qcount,
@@ -946,7 +964,7 @@ cudaError_t launch_recheck(const JobDev *jobs, const QEntry *q, const unsigned l
 namespace cpc {
 size_t fast_static_smem_bytes() {
   cudaFuncAttributes a;
-  if (cudaFuncGetAttributes(&a, fast_pairs_kernel<COREL_SS, true>) != cudaSuccess) return 24 * 1024;
+  if (cudaFuncGetAttributes(&a, fast_pairs_kernel<COREL_SS, true, 4>) != cudaSuccess) return 24 * 1024;
   return a.sharedSizeBytes;
 }
 }  // namespace cpc

@@ -180,16 +180,16 @@ cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind
                            const int *slots_g1, const int *slots_g2, cpc_accum *outs);
 
 /* Tuning knobs of the fast kernel (0 = automatic).  cells_per_rmax: column
- * width = r_max / k; pi_window: Pi bins held per block; tile: g1 rows per
- * block (64 or 128). */
+ * width = r_max / k, k <= 9; pi_window: Pi bins held per block; tile: g1 rows
+ * per block (0 or 128). */
 cpc_status cpc_set_tuning(cpc_ctx *ctx, int cells_per_rmax, int pi_window, int tile);
 
 /* Autotuner: times the fast kernel on every `sample_stride`-th outer row of
  * this pair type for cell widths r_max / k (k = 2, 3, 4; the cell lists are
- * rebuilt on the device) and block-local Pi windows (automatic, 16, 24, 32
- * bins), keeps the fastest for this context (as cpc_set_tuning would) and
- * returns it.  Results never depend on the choice.  Box runs only (sky runs
- * return zeros). */
+ * rebuilt on the device) and block-local Pi windows (for 4, 3 and 2 blocks per
+ * SM, the largest window that fits and three quarters of it), keeps the
+ * fastest for this context (as cpc_set_tuning would) and returns it.  Results
+ * never depend on the choice.  Box runs only (sky runs return zeros). */
 cpc_status cpc_autotune(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_g2,
                         int64_t sample_stride, int *cells_per_rmax, int *pi_window);
 
