@@ -29,7 +29,8 @@
 // one other region ("Y", the partner's region for cross-region pairs) -- with
 // 32-bit counts and fixed-point sums split over two 32-bit words per field
 // (exact integer addition, order independent), flushed to the FP64 global
-// histogram block every kFlushCands staged candidates and at the end of the unit.
+// histogram block when the pairs added since the last flush could overflow a
+// word (below) and at the end of the unit.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <climits>
@@ -135,12 +136,12 @@ size_t fast_smem_bytes(int corel, int do_jk, int NB) {
 // into its low 14 bits (0..16383) and the arithmetic shift u >> 14
 // (-2^12..2^12), each added to its own 32-bit word with a plain reduction (no
 // return value: no scoreboard wait; lanes of one instruction that hit the same
-// word are serialised, which red_pair halves).  A block flushes its histograms after every
-// kFlushCands staged candidates, so a bin takes at most kTile * kFlushCands =
-// 2^18 terms between flushes: the low word stays below 2^32 and the high word,
-// read as a signed integer, within +-2^30.
-constexpr int kFlushCands = 2048;
-static_assert((long long)kTileThreads * kFlushCands <= (1ll << 18), "fixed-point word headroom");
+// word are serialised, which red_pair halves).  A block counts the pairs its
+// warps queued since the last flush and flushes before a batch that could take
+// the count past 2^18 (a batch adds at most kTile * kBatch pairs), so a bin takes
+// at most 2^18 terms between flushes: the low word stays below 2^32 and the high
+// word, read as a signed integer, within +-2^30.
+constexpr unsigned kFlushTerms = 1u << 18;
 __device__ __forceinline__ int to_fixed(float v, float scale) {
   return __float2int_rn(v * scale);
 }
@@ -305,6 +306,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   __shared__ unsigned char s_keep[kBatch];
   __shared__ float2 s_lo[kBatch];
   __shared__ unsigned long long s_red[kThreads / 32];
+  __shared__ unsigned s_nbin;  // pairs queued by the block's warps since the last flush
   __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
   __shared__ float s_qs[kNF];
   __shared__ double s_iqs[kNF];
@@ -320,6 +322,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   {
     unsigned int *z = reinterpret_cast<unsigned int *>(hist_base);
     for (int k = t; k < zero_words; k += kThreads) z[k] = 0u;
+    if (t == 0) s_nbin = 0u;
   }
   __syncthreads();
 
@@ -438,7 +441,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     __syncthreads();
     const int total_slots = s_cnt[ncol];
     int cur_y = -1;        // region held in the Y histogram
-    int since_flush = 0;   // candidates staged since the last flush
+    unsigned wbin = 0;     // pairs this warp queued in the current batch
 
     for (int chunk0 = 0; chunk0 < total_slots; chunk0 += kMaxSeg) {
       const int nslot = min(kMaxSeg, total_slots - chunk0);
@@ -536,16 +539,16 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
 
         for (int base = 0; base < gN; base += kBatch) {
           const int nb = min(kBatch, gN - base);
-          if (since_flush + nb > kFlushCands) {  // keep every word below 2^32
+          // s_nbin is read after a barrier and changed only after the next one
+          if (s_nbin + (unsigned)(kTile * nb) > kFlushTerms) {  // keep every word below 2^32
             __syncthreads();
             flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_xnum, s_xlo, s_xhi, NB, wpi,
                                           npi, nrp, n2_base, 1 + U.region, JK, f0, s_iqs, J);
             if (JK && cur_y >= 0)
               flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
                                          1 + cur_y, f0, s_iqs, J);
-            since_flush = 0;
+            if (t == 0) s_nbin = 0u;
           }
-          since_flush += nb;
           if (t < nb) {
             const int p = s_pre[k] + (int)(((long long)(base + t) * ks) % gN);
             int lo = k, hi = g;  // segment s_order[lo] with s_pre[lo] <= p < s_pre[lo+1]
@@ -822,9 +825,12 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               }
             }
             qhead += take;
+            wbin += (unsigned)take;
             __syncwarp();
             if (step >= nk && qtail == qhead) break;
           }
+          if (lane == 0 && wbin) atomicAdd(&s_nbin, wbin);
+          wbin = 0;
           __syncthreads();
         }
         k = g;
@@ -839,6 +845,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     if (JK && cur_y >= 0)
       flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y, f0,
                                  s_iqs, J);
+    if (t == 0) s_nbin = 0u;
     // window-pair counter (once per pair: mu slices other than the first skip it)
     {
       unsigned long long v = (rmu && n2_base != 0) ? 0ull : (unsigned long long)nwin;
