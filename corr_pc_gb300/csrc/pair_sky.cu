@@ -26,7 +26,8 @@
 //    window pair through the FP64 path, global atomics (CPC_ENGINE_FP64).
 //  * sky_warp_kernel -- the fast kernel (CPC_ENGINE_FAST): one warp per g1 row
 //    (dynamic row queue), lanes take consecutive candidates of the row's
-//    redshift range (coalesced float4 loads); FP32 definite-in/definite-out
+//    redshift range, their float views prefetched into per-warp shared stages
+//    with asynchronous copies one 32-candidate stage ahead; FP32 definite-in/definite-out
 //    window tests (ambiguous ones re-tested in double); FP32 prefilters that
 //    reject pairs certainly outside the Pi range or certainly outside
 //    [thr_0, thr_nrp) in r_p (the chord |u1 - u2| of float unit vectors with a
@@ -137,6 +138,7 @@ sky_fp64_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, int2 *hq,
 constexpr int kSkyThreads = 256;
 constexpr int kSkyWarps = kSkyThreads / 32;
 constexpr int kSkyQ = 64;
+constexpr int kSkyAhead = 1;  // candidate stages copied ahead of the tested one
 
 struct SkyRow {
   int64_t i;
@@ -386,6 +388,20 @@ __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r,
   }
 }
 
+// 16-byte asynchronous copy global -> shared (the candidate prefetch below)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// all but the newest kSkyAhead groups complete: the current stage has landed
+__device__ __forceinline__ void cp_async_wait_prev() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(kSkyAhead) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
 // window membership of x in [lo, hi] from the float value: 1 in, 0 out,
 // -1 undecided (x within a float ulp of a bound, or a NaN bound)
 __device__ __forceinline__ int fwin(float x, float lo_ru, float hi_rd, float lo_rd, float hi_ru) {
@@ -402,6 +418,9 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
                 int zero_bin) {
   extern __shared__ __align__(16) unsigned char sky_smem[];
   __shared__ int s_q[kSkyWarps][kSkyQ];
+  // per warp, kSkyAhead + 1 stages of 32 candidates' sw and su views: the next
+  // kSkyAhead stages are copied asynchronously while the current one is tested
+  __shared__ float4 s_pw[kSkyWarps][kSkyAhead + 1][32], s_pu[kSkyWarps][kSkyAhead + 1][32];
   __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
   const JobDev &J = *jobp;
   const int ncell = J.nrp * J.npi;
@@ -463,11 +482,30 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
       if (b.d.z[mid] > z_max) end = mid; else l2 = mid + 1;
     }
     int count = 0;
-    for (int64_t base = lo; base < end; base += 32) {
+    // each lane prefetches its own candidate slot (no cross-lane reads of the
+    // stage buffers): stage 0 now, stage k+1 while stage k is tested
+    for (int a0 = 0; a0 < kSkyAhead; a0++) {
+      const int64_t jp = lo + 32 * a0 + lane;
+      if (jp < end) {
+        cp_async16(&s_pw[warp][a0][lane], fb.sw + jp);
+        cp_async16(&s_pu[warp][a0][lane], fb.su + jp);
+      }
+      cp_async_commit();
+    }
+    int stage = 0;
+    for (int64_t base = lo; base < end; base += 32, stage = (stage + 1) % (kSkyAhead + 1)) {
       const int64_t j = base + lane;
+      const int64_t jn = j + 32 * kSkyAhead;
+      const int sn = (stage + kSkyAhead) % (kSkyAhead + 1);
+      if (jn < end) {
+        cp_async16(&s_pw[warp][sn][lane], fb.sw + jn);
+        cp_async16(&s_pu[warp][sn][lane], fb.su + jn);
+      }
+      cp_async_commit();
+      cp_async_wait_prev();  // this lane's copies of the current stage are done
       bool need = false;
       if (j < end && (!J.auto_mode || b.d.orig[j] > oi)) {  // corels1: partners after i
-        const float4 w2 = fb.sw[j];
+        const float4 w2 = s_pw[warp][stage][lane];
         int in = fwin(w2.y, de_lru, de_hrd, de_lrd, de_hru);
         if (in < 0) {
           const double d2 = b.d.y[j];
@@ -489,7 +527,7 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
           const bool pi_out = (pf < pmin_f - pe) || (pf > pmax_f + pe);
           if (!pi_out) {
             // r_p bounds from the chord of float unit vectors
-            const float4 u2 = fb.su[j];
+            const float4 u2 = s_pu[warp][stage][lane];
             const float dx = u1.x - u2.x, dy = u1.y - u2.y, dz = u1.z - u2.z;
             const float c2 = dx * dx + dy * dy + dz * dz;
             const float ch = sqrtf(c2);
@@ -518,6 +556,7 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
         __syncwarp();
       }
     }
+    cp_async_wait_all();  // no copy in flight into the stage buffers of the next row
     if (lane < count)
       sky_pair_mixed<SMEM>(J, r, rf, b, fb, q[lane], s_num, s_fix, s_qs, hq, hq_n, hq_cap, esum, s_A,
                            s_B, s_PA, s_PB);
