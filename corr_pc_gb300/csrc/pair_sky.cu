@@ -421,6 +421,7 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
   // per warp, kSkyAhead + 1 stages of 32 candidates' sw and su views: the next
   // kSkyAhead stages are copied asynchronously while the current one is tested
   __shared__ float4 s_pw[kSkyWarps][kSkyAhead + 1][32], s_pu[kSkyWarps][kSkyAhead + 1][32];
+  __shared__ SkyRowF s_rowf[kSkyWarps];
   __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
   const JobDev &J = *jobp;
   const int ncell = J.nrp * J.npi;
@@ -449,27 +450,33 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
     if (J.row_stride > 1 && ((a.d.orig[i] - J.row_offset) % J.row_stride) != 0) continue;
     if (J.auto_mode == 2 && !(a.d.aflag[i] & kAutoStart0)) continue;  // corels1, sorted
     const int64_t oi = a.d.orig[i];
+    // the mixed path reads the row's index, region and keep flag; the FP64 path
+    // reloads the rest by index
     SkyRow r;
     r.i = i;
-    r.ra = a.d.x[i]; r.dec = a.d.y[i]; r.dc = a.dc[i]; r.da = a.da[i];
-    r.sd = a.sd[i]; r.cd = a.cd[i]; r.rar = a.rar[i]; r.decr = a.decr[i];
-    r.w = a.d.w[i]; r.e1 = a.d.e1[i]; r.e2 = a.d.e2[i]; r.phi = a.d.phi[i];
-    r.jk = a.d.jk[i]; r.keep = a.d.keep[i];
+    r.jk = a.d.jk[i];
+    r.keep = a.d.keep[i];
     const double z_min = a.win[i], z_max = a.win[n1 + i];
-    const double ra_min = a.win[2 * n1 + i], ra_max = a.win[3 * n1 + i];
-    const double dec_min = a.win[4 * n1 + i], dec_max = a.win[5 * n1 + i];
-    const float ra_lru = __double2float_ru(ra_min), ra_hrd = __double2float_rd(ra_max);
-    const float ra_lrd = __double2float_rd(ra_min), ra_hru = __double2float_ru(ra_max);
-    const float de_lru = __double2float_ru(dec_min), de_hrd = __double2float_rd(dec_max);
-    const float de_lrd = __double2float_rd(dec_min), de_hru = __double2float_ru(dec_max);
+    // RA / Dec windows: float bounds rounded both ways here; the exact double
+    // bounds are reloaded in the rare undecided case (fewer live registers)
+    const double *w_ra_min = a.win + 2 * n1 + i, *w_ra_max = a.win + 3 * n1 + i;
+    const double *w_de_min = a.win + 4 * n1 + i, *w_de_max = a.win + 5 * n1 + i;
+    const float ra_lru = __double2float_ru(*w_ra_min), ra_hrd = __double2float_rd(*w_ra_max);
+    const float ra_lrd = __double2float_rd(*w_ra_min), ra_hru = __double2float_ru(*w_ra_max);
+    const float de_lru = __double2float_ru(*w_de_min), de_hrd = __double2float_rd(*w_de_max);
+    const float de_lrd = __double2float_rd(*w_de_min), de_hru = __double2float_ru(*w_de_max);
     const float4 u1 = fa.su[i];
     const float dc1f = fa.sw[i].w;
-    SkyRowF rf;
-    rf.u = u1;
-    rf.ul = fa.sl[i];
-    rf.w = fa.sw[i];
-    rf.x = fa.sx[i];
-    rf.sh = fa.ss[i];
+    // the row's float views for the heavy step, in this warp's shared slot
+    SkyRowF &rf = s_rowf[warp];
+    if (lane == 0) {
+      rf.u = u1;
+      rf.ul = fa.sl[i];
+      rf.w = fa.sw[i];
+      rf.x = fa.sx[i];
+      rf.sh = fa.ss[i];
+    }
+    __syncwarp();
     // redshift range [lo, hi): z_min <= z <= z_max
     int64_t lo = 0, hi = n2;
     while (lo < hi) {
@@ -509,13 +516,13 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
         int in = fwin(w2.y, de_lru, de_hrd, de_lrd, de_hru);
         if (in < 0) {
           const double d2 = b.d.y[j];
-          in = !(d2 > dec_max || d2 < dec_min);
+          in = !(d2 > *w_de_max || d2 < *w_de_min);
         }
         if (in) {
           int ir = fwin(w2.x, ra_lru, ra_hrd, ra_lrd, ra_hru);
           if (ir < 0) {
             const double a2 = b.d.x[j];
-            ir = !(a2 < ra_min || a2 > ra_max);
+            ir = !(a2 < *w_ra_min || a2 > *w_ra_max);
           }
           in = ir;
         }
