@@ -135,6 +135,15 @@ def cases():
     p.coordinates = 7
     p.lin_bin = 1
     out.append(("box_wpp_rmu_linear", p, c, c, True))
+
+    # integer lattice in r-mu: mu = 0 (Pi = 0) sits on a bin edge and mu = +-1
+    # (dx = dy = 0) on the range ends; linear r bins put integer r on edges
+    c = lattice(700, 40.0, 43, 2)
+    p = synth._box_params(which_corr=0, L=40.0, rmin=0.0, rmax=12.0, nrp=6, npi=4, pmax=1.0,
+                          njk=8, n=c.n)
+    p.coordinates = 7
+    p.lin_bin = 1
+    out.append(("box_lattice_rmu", p, c, c, True))
     return out
 
 
