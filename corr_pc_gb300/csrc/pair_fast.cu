@@ -207,12 +207,12 @@ __device__ __forceinline__ float ephi_f(float phi, float theta) {
   return t > 1.5707963267948966f ? 3.14159265358979f - t : t;
 }
 
-// Flush one block histogram (count, low and high words of each field) into
-// the global FP64 block at histogram index h, and zero it.
-template <int NF, bool JKMAP, class FM>
-__device__ __forceinline__ void flush_hist(unsigned *cnt, unsigned *lo, unsigned *hi, int NB,
-                                           int wpi, int npi, int nrp, int n2_base, int h, int f0,
-                                           const double *s_iqs, const JobDev &J) {
+// Flush the partner-region histogram (jackknife fields) into the global FP64
+// block at histogram index h, and zero it.
+template <class FMAP>
+__device__ __forceinline__ void flush_region(unsigned *cnt, unsigned *lo, unsigned *hi, int NB,
+                                             int wpi, int npi, int nrp, int n2_base, int h, int f0,
+                                             const double *s_iqs, const JobDev &J) {
   const int64_t hb = (int64_t)h * nrp * npi;
   for (int lb = threadIdx.x; lb < NB; lb += kThreads) {
     const unsigned n = cnt[lb];
@@ -221,10 +221,10 @@ __device__ __forceinline__ void flush_hist(unsigned *cnt, unsigned *lo, unsigned
     atomicAdd(&J.acc_num[cell], (unsigned long long)n);
     cnt[lb] = 0u;
 #pragma unroll
-    for (int f = 0; f < NF; f++) {
-      const size_t o = (size_t)f * NB + lb;
-      const int fld = JKMAP ? FM::j(f) : FM::m(f);
-      if (f >= f0) {
+    for (int g = 0; g < FMAP::FJ; g++) {
+      const size_t o = (size_t)g * NB + lb;
+      const int fld = FMAP::j(g);
+      if (g >= f0) {
         const double v = fixed_total(lo[o], hi[o], s_iqs[fld]);
         if (v != 0.0) atomicAdd(&J.acc_sums[cell * kNF + fld], v);
       }
@@ -525,7 +525,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         if (JK && !same_region && cur_y != region2) {
           if (cur_y >= 0) {
             __syncthreads();
-            flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
+            flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
                                        1 + cur_y, f0, s_iqs, J);
             __syncthreads();
           }
@@ -545,7 +545,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_xnum, s_xlo, s_xhi, NB, wpi,
                                           npi, nrp, n2_base, 1 + U.region, JK, f0, s_iqs, J);
             if (JK && cur_y >= 0)
-              flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
+              flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
                                          1 + cur_y, f0, s_iqs, J);
             if (t == 0) s_nbin = 0u;
           }
@@ -843,7 +843,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_xnum, s_xlo, s_xhi, NB, wpi, npi, nrp,
                                   n2_base, 1 + U.region, JK, f0, s_iqs, J);
     if (JK && cur_y >= 0)
-      flush_hist<F::FJ, true, F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y, f0,
+      flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y, f0,
                                  s_iqs, J);
     if (t == 0) s_nbin = 0u;
     // window-pair counter (once per pair: mu slices other than the first skip it)
