@@ -84,6 +84,8 @@ def load() -> ctypes.CDLL:
     lib.cpc_upload.argtypes = [V, I, P(cpc_catalog)]
     lib.cpc_count.argtypes = [V, I, I, I, I, I64, I64, P(cpc_accum)]
     lib.cpc_count_auto.argtypes = [V, I, I, I, I64, I64, P(cpc_accum)]
+    lib.cpc_count_async.argtypes = [V, I, I, I, I, I64, I64, V]
+    lib.cpc_count_finish.argtypes = [V, P(cpc_accum)]
     lib.cpc_accum_shape.argtypes = [V, P(I), P(I), P(I)]
     lib.cpc_count_batch.argtypes = [I, P(V), P(I), P(I), P(I), P(cpc_accum)]
     lib.cpc_set_tuning.argtypes = [V, I, I, I]
@@ -239,6 +241,22 @@ class Context:
                 "n_rechecked": acc.n_rechecked, "kernel_ms": acc.kernel_ms,
                 "pair_kernel_ms": acc.pair_kernel_ms}
 
+
+    def count_async(self, kind: str, slot_g1: int, slot_g2: int, engine: str = "fast",
+                    stream: int = 0, row_stride: int = 1, row_offset: int = 0) -> None:
+        """Enqueue a count after the work on CUDA stream `stream` (a raw
+        cudaStream_t handle, 0 = default stream); collect it with finish()."""
+        check(self.lib.cpc_count_async(self.h, PAIR[kind], slot_g1, slot_g2, ENGINE[engine],
+                                       row_stride, row_offset, ctypes.c_void_p(stream or None)),
+              self.h)
+
+    def finish(self) -> dict:
+        """Wait for the count enqueued by count_async and return it like count()."""
+        acc, num, sums = self.new_accum()
+        check(self.lib.cpc_count_finish(self.h, ctypes.byref(acc)), self.h)
+        return {"num": num, "sums": sums, "n_window": acc.n_window, "n_binned": acc.n_binned,
+                "n_rechecked": acc.n_rechecked, "kernel_ms": acc.kernel_ms,
+                "pair_kernel_ms": acc.pair_kernel_ms}
 
     def count_auto(self, kind: str, slot: int, engine: str = "fast", row_stride: int = 1,
                    row_offset: int = 0) -> dict:

@@ -108,6 +108,10 @@ struct UnitCache {
 
 }  // namespace
 
+namespace {
+struct JobPlan;  // one planned count (below)
+}  // namespace
+
 struct cpc_ctx {
   cpc_params p{};
   std::vector<double> H, dA;
@@ -121,6 +125,7 @@ struct cpc_ctx {
   int device = 0, sm_count = 152;
   cudaStream_t st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  cudaEvent_t e_in = nullptr, e_done = nullptr;  // cpc_count_async ordering
   // scratch
   DevBuf<JobDev> d_jobs;
   DevBuf<UnitDesc> d_units;
@@ -147,6 +152,9 @@ struct cpc_ctx {
   DevBuf<int2> d_hq;
   DevBuf<unsigned long long> d_hq_n;
   std::vector<UnitCache> unit_cache;
+  // a count enqueued by cpc_count_async, collected by cpc_count_finish
+  int pending = 0;  // 0 none, 1 fast engine, 2 FP64 engine
+  std::vector<JobPlan> pending_jobs;
   int64_t launches = 0;  // kernels launched by this context (all entry points)
 };
 
@@ -700,12 +708,17 @@ DCat zview(Slot &s) {
   return d;
 }
 
-cpc_status run_plain(JobPlan &jp) {
+// the plain FP64 kernel: enqueue on the context's stream, then fetch
+cpc_status enqueue_plain(JobPlan &jp) {
   cpc_ctx *c = jp.c;
   cpc_status s;
   if ((s = alloc_accum(c)) != CPC_OK) return s;
   if ((s = zero_accum(c, c->st)) != CPC_OK) return s;
-  if (jp.empty) return fetch_accum(c, jp.out, c->st, 0);
+  CK(cudaEventRecord(c->e0, c->st), "event");
+  if (jp.empty) {
+    CK(cudaEventRecord(c->e1, c->st), "event");
+    return CPC_OK;
+  }
   Slot &g1 = c->slots[jp.s1], &g2 = c->slots[jp.s2];
   if ((s = build_zorder(c, g1)) != CPC_OK) return s;
   if ((s = build_zorder(c, g2)) != CPC_OK) return s;
@@ -717,10 +730,15 @@ cpc_status run_plain(JobPlan &jp) {
   jp.jd.d1 = a;
   jp.jd.d2 = b;
   CK(cudaMemcpyAsync(c->d_jobs.p, &jp.jd, sizeof(JobDev), cudaMemcpyHostToDevice, c->st), "H2D job");
-  CK(cudaEventRecord(c->e0, c->st), "event");
   CK(launch_plain_fp64(c->d_jobs.p, a, b, c->st), "plain fp64 kernel");
   c->launches += 1;
   CK(cudaEventRecord(c->e1, c->st), "event");
+  return CPC_OK;
+}
+
+cpc_status finish_plain(JobPlan &jp) {
+  cpc_ctx *c = jp.c;
+  cpc_status s;
   if ((s = fetch_accum(c, jp.out, c->st, 0)) != CPC_OK) return s;
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, c->e0, c->e1), "event time");
@@ -729,8 +747,17 @@ cpc_status run_plain(JobPlan &jp) {
   return CPC_OK;
 }
 
-// fast engine over one or more jobs (one persistent launch per corel group)
-cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt = 0) {
+cpc_status run_plain(JobPlan &jp) {
+  const cpc_status s = enqueue_plain(jp);
+  return s != CPC_OK ? s : finish_plain(jp);
+}
+
+// fast engine over one or more jobs (one persistent launch per corel group):
+// enqueue on the first context's stream, then wait, check the edge queue and
+// fetch
+cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt = 0);
+
+cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
   cpc_ctx *c0 = jobs[0].c;
   cpc_ctx *c = c0;
   cudaStream_t st = c0->st;
@@ -799,6 +826,14 @@ cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt = 0) {
      "recheck kernel");
   c0->launches += 1;
   CK(cudaEventRecord(c0->e1, st), "event");
+  return CPC_OK;
+}
+
+cpc_status finish_fast(std::vector<JobPlan> &jobs, int grow_attempt) {
+  cpc_ctx *c0 = jobs[0].c;
+  cpc_ctx *c = c0;
+  cudaStream_t st = c0->st;
+  cpc_status s;
   CK(cudaStreamSynchronize(st), "fast kernels");
   float ms = 0, pms = 0;
   CK(cudaEventElapsedTime(&ms, c0->e0, c0->e1), "event time");
@@ -822,6 +857,11 @@ cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt = 0) {
     jobs[k].out->pair_kernel_ms = pms;
   }
   return CPC_OK;
+}
+
+cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt) {
+  const cpc_status s = enqueue_fast(jobs);
+  return s != CPC_OK ? s : finish_fast(jobs, grow_attempt);
 }
 
 // Cell list of slot s from a catalogue held in the context's upload buffers
@@ -1402,6 +1442,8 @@ cpc_status cpc_create(cpc_ctx **out, const cpc_params *params) {
   e = cudaEventCreate(&c->e0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->e1);
   if (e == cudaSuccess) e = cudaEventCreate(&c->e2);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->e_in, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->e_done, cudaEventDisableTiming);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "event");
   *out = c.release();
   return CPC_OK;
@@ -1413,6 +1455,8 @@ cpc_status cpc_destroy(cpc_ctx *c) {
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
   if (c->e2) cudaEventDestroy(c->e2);
+  if (c->e_in) cudaEventDestroy(c->e_in);
+  if (c->e_done) cudaEventDestroy(c->e_done);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return CPC_OK;
@@ -1426,8 +1470,16 @@ cpc_status cpc_accum_shape(const cpc_ctx *c, int *n_hist, int *n_bins, int *n_p_
   return CPC_OK;
 }
 
+// a count enqueued by cpc_count_async must be collected first
+static bool busy(cpc_ctx *c) {
+  if (!c || !c->pending) return false;
+  fail(c, CPC_ERR_STATE, "a count is pending: call cpc_count_finish first");
+  return true;
+}
+
 cpc_status cpc_set_tuning(cpc_ctx *c, int cells_per_rmax, int pi_window, int tile) {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (busy(c)) return CPC_ERR_STATE;
   if (cells_per_rmax < 0 || cells_per_rmax > kMaxCellsPerRmax || pi_window < 0 ||
       (tile != 0 && tile != kTileThreads))
     return fail(c, CPC_ERR_INVALID, "tuning values out of range");
@@ -1439,6 +1491,7 @@ cpc_status cpc_set_tuning(cpc_ctx *c, int cells_per_rmax, int pi_window, int til
 
 cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   if (!c || !cat) return fail(c, CPC_ERR_INVALID, "null argument");
+  if (busy(c)) return CPC_ERR_STATE;
   if (slot < 0 || slot >= kMaxSlots) return fail(c, CPC_ERR_INVALID, "slot out of range");
   const cpc_params &p = c->p;
   const int64_t n = cat->n;
@@ -1512,6 +1565,7 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
 cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, cpc_engine engine,
                      int64_t row_stride, int64_t row_offset, cpc_accum *out) {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (busy(c)) return CPC_ERR_STATE;
   if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
     return fail(c, CPC_ERR_INVALID, "unknown engine");
   if (kind == CPC_PAIR_SS)
@@ -1528,9 +1582,57 @@ cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, c
   return run_fast(jobs);
 }
 
+cpc_status cpc_count_async(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2,
+                           cpc_engine engine, int64_t row_stride, int64_t row_offset,
+                           void *stream) {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (busy(c)) return CPC_ERR_STATE;
+  if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
+    return fail(c, CPC_ERR_INVALID, "unknown engine");
+  if (kind == CPC_PAIR_SS)
+    return fail(c, CPC_ERR_INVALID, "CPC_PAIR_SS pairs one catalogue: use cpc_count_auto");
+  if (c->p.coordinates == 0)
+    return fail(c, CPC_ERR_INVALID,
+                "sky counts finish on the host (edge tier): use cpc_count for coordinates 0");
+  cudaStream_t user = reinterpret_cast<cudaStream_t>(stream);
+  std::vector<JobPlan> jobs(1);
+  cpc_accum placeholder{};  // plan_job checks the output arrays; the real ones come at finish
+  int64_t dummy_num = 0;
+  double dummy_sums = 0;
+  placeholder.num = &dummy_num;
+  placeholder.sums = &dummy_sums;
+  cpc_status s = plan_job(c, kind, slot_g1, slot_g2, row_stride, row_offset, &placeholder, jobs[0]);
+  if (s != CPC_OK) return s;
+  jobs[0].out = nullptr;
+  // the count follows the caller's earlier work on `stream`
+  CK(cudaEventRecord(c->e_in, user), "event");
+  CK(cudaStreamWaitEvent(c->st, c->e_in, 0), "stream wait");
+  s = engine == CPC_ENGINE_FP64 ? enqueue_plain(jobs[0]) : enqueue_fast(jobs);
+  if (s != CPC_OK) return s;
+  // and the caller's later work on `stream` follows the count
+  CK(cudaEventRecord(c->e_done, c->st), "event");
+  CK(cudaStreamWaitEvent(user, c->e_done, 0), "stream wait");
+  c->pending = engine == CPC_ENGINE_FP64 ? 2 : 1;
+  c->pending_jobs = std::move(jobs);
+  return CPC_OK;
+}
+
+cpc_status cpc_count_finish(cpc_ctx *c, cpc_accum *out) {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (!c->pending) return fail(c, CPC_ERR_STATE, "no count is pending");
+  if (!out || !out->num || !out->sums) return fail(c, CPC_ERR_INVALID, "null output arrays");
+  std::vector<JobPlan> jobs = std::move(c->pending_jobs);
+  const int mode = c->pending;
+  c->pending = 0;
+  c->pending_jobs.clear();
+  jobs[0].out = out;
+  return mode == 2 ? finish_plain(jobs[0]) : finish_fast(jobs, 0);
+}
+
 cpc_status cpc_count_auto(cpc_ctx *c, cpc_pair_kind kind, int slot, cpc_engine engine,
                           int64_t row_stride, int64_t row_offset, cpc_accum *out) {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (busy(c)) return CPC_ERR_STATE;
   if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
     return fail(c, CPC_ERR_INVALID, "unknown engine");
   if (kind != CPC_PAIR_SS && kind != CPC_PAIR_RSRS)
@@ -1550,6 +1652,7 @@ cpc_status cpc_count_auto(cpc_ctx *c, cpc_pair_kind kind, int slot, cpc_engine e
 cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2,
                         int64_t sample_stride, int *cells_per_rmax, int *pi_window) {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (busy(c)) return CPC_ERR_STATE;
   const cpc_params &p = c->p;
   if (slot_g1 < 0 || slot_g1 >= kMaxSlots || slot_g2 < 0 || slot_g2 >= kMaxSlots)
     return fail(c, CPC_ERR_INVALID, "slot out of range");
@@ -1631,6 +1734,8 @@ cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind
                            const int *slots_g1, const int *slots_g2, cpc_accum *outs) {
   if (n_jobs <= 0 || !ctxs || !kinds || !slots_g1 || !slots_g2 || !outs)
     return fail(nullptr, CPC_ERR_INVALID, "bad batch arguments");
+  for (int k = 0; k < n_jobs; k++)
+    if (busy(ctxs[k])) return CPC_ERR_STATE;
   for (int k = 0; k < n_jobs; k++)
     if (!ctxs[k]) return fail(nullptr, CPC_ERR_INVALID, "null context in batch");
   for (int k = 0; k < n_jobs; k++)

@@ -156,6 +156,20 @@ cpc_status cpc_count(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_g2,
                      cpc_engine engine, int64_t row_stride, int64_t row_offset,
                      cpc_accum *out);
 
+/* Asynchronous form of cpc_count for box runs (coordinates 6 and 7): plans the
+ * count and enqueues its kernels after the work already queued on `stream` (a
+ * cudaStream_t; NULL is the legacy default stream), makes later work on
+ * `stream` wait for it, and returns without waiting.  cpc_count_finish then
+ * waits, writes the histogram block into *out and returns the status; no other
+ * call on ctx may come in between (they return CPC_ERR_STATE).  Sky counts
+ * (coordinates 0) finish on the host and are only available through cpc_count.
+ * Extends the reference's synchronous corels2 for callers that overlap the
+ * count with their own GPU work. */
+cpc_status cpc_count_async(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_g2,
+                           cpc_engine engine, int64_t row_stride, int64_t row_offset,
+                           void *stream);
+cpc_status cpc_count_finish(cpc_ctx *ctx, cpc_accum *out);
+
 /* Auto pairs of one catalogue: the reference's
  *     long corels1(gal g1[], bin_jk &bjk, data_info &data_inf)
  *     (corr.cpp:103-216; do_corr.cpp:63 with do_SS, :76 with do_RsRs)

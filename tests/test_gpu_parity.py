@@ -152,3 +152,32 @@ def test_autotune_keeps_results_identical():
     r2 = ctx.count("SD", 0, 1)
     assert np.array_equal(r2["num"], g.raw_num)
     ctx.close()
+
+
+@pytest.mark.parametrize("engine", ["fast", "fp64"])
+def test_async_count_on_a_caller_stream(engine):
+    """cpc_count_async after work queued on a caller stream equals cpc_count;
+    other calls are refused until cpc_count_finish."""
+    import torch
+    g = Golden("box_wgp_clustered")
+    p = g.params
+    cats = host.prepare(p, [("S", g.S), ("D", g.D)])
+    ctx = _lib.Context(p)
+    ctx.upload(0, cats["D"])
+    ctx.upload(1, cats["S"])
+    ref = ctx.count("SD", 0, 1, engine=engine)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        junk = torch.ones(1 << 20, device="cuda")
+        junk = junk * 2.0  # work queued before the count
+    ctx.count_async("SD", 0, 1, engine=engine, stream=s.cuda_stream)
+    with pytest.raises(_lib.CpcError):
+        ctx.count("SD", 0, 1)
+    r = ctx.finish()
+    s.synchronize()
+    assert r["n_binned"] == ref["n_binned"] == g.n_in and r["n_window"] == ref["n_window"]
+    assert np.array_equal(r["num"], ref["num"])
+    check_sums(r["sums"], g.raw_sums)
+    with pytest.raises(_lib.CpcError):
+        ctx.finish()  # nothing pending
+    ctx.close()
