@@ -340,10 +340,10 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     // words, so the low and high word of one bin are 16 banks apart (red_pair)
     unsigned *s_mlo = s_mnum + NB;
     unsigned *s_mhi = s_mlo + (size_t)F::FM * NB + hi_pad(F::FM * NB);
-    unsigned *s_xnum = s_mhi + (size_t)F::FM * NB;
-    unsigned *s_xlo = s_xnum + NB;
-    unsigned *s_xhi = s_xlo + (size_t)F::FJ * NB + hi_pad(F::FJ * NB);
-    unsigned *s_ynum = s_xhi + (size_t)F::FJ * NB;
+    unsigned *s_nxnum = s_mhi + (size_t)F::FM * NB;
+    unsigned *s_nxlo = s_nxnum + NB;
+    unsigned *s_nxhi = s_nxlo + (size_t)F::FJ * NB + hi_pad(F::FJ * NB);
+    unsigned *s_ynum = s_nxhi + (size_t)F::FJ * NB;
     unsigned *s_ylo = s_ynum + NB;
     unsigned *s_yhi = s_ylo + (size_t)F::FJ * NB + hi_pad(F::FJ * NB);
     const int f0 = J.unit_w ? 1 : 0;  // unit weights: wt_num = count, not accumulated
@@ -542,7 +542,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
           // s_nbin is read after a barrier and changed only after the next one
           if (s_nbin + (unsigned)(kTile * nb) > kFlushTerms) {  // keep every word below 2^32
             __syncthreads();
-            flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_xnum, s_xlo, s_xhi, NB, wpi,
+            flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_nxnum, s_nxlo, s_nxhi, NB, wpi,
                                           npi, nrp, n2_base, 1 + U.region, JK, f0, s_iqs, J);
             if (JK && cur_y >= 0)
               flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
@@ -806,11 +806,11 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                 const bool nxc = !same_region && !s_rkeep[er];
                 const bool yc = !same_region && s_keep[ec];
                 if (nxc) {
-                  atomicAdd(&s_xnum[lb], 1u);
+                  atomicAdd(&s_nxnum[lb], 1u);
 #pragma unroll
                   for (int g = 0; g < F::FJ; g++)
                     if (g >= f0)
-                      red_pair(&s_xlo[(size_t)g * NB + lb], &s_xhi[(size_t)g * NB + lb],
+                      red_pair(&s_nxlo[(size_t)g * NB + lb], &s_nxhi[(size_t)g * NB + lb],
                                wa[F::jm(g)], wb[F::jm(g)], odd_lane);
                 }
                 if (yc) {
@@ -840,7 +840,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
 
     // ---- flush main, X and the last Y ----
     __syncthreads();
-    flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_xnum, s_xlo, s_xhi, NB, wpi, npi, nrp,
+    flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_nxnum, s_nxlo, s_nxhi, NB, wpi, npi, nrp,
                                   n2_base, 1 + U.region, JK, f0, s_iqs, J);
     if (JK && cur_y >= 0)
       flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y, f0,
