@@ -148,13 +148,15 @@ def _hbm_peak():
 
 
 def _peaks() -> dict:
-    """Live FP32 FFMA and shared-memory 32-bit atomic peaks (this GPU)."""
+    """Live FP32 FFMA and shared-memory 32-bit atomic peaks (this GPU): the
+    conflict-free reduction without a returned value, the kind the pair kernels
+    issue."""
     from corr_pc_gb300 import build as b
     lib = ctypes.CDLL(b.PEAKS)
     lib.cpc_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                              ctypes.POINTER(ctypes.c_double)]
     out = {}
-    for k, nm in ((0, "ffma_flops"), (5, "smem_atomic_u32_ops")):
+    for k, nm in ((0, "ffma_flops"), (1, "smem_atomic_u32_ops")):
         v = ctypes.c_double()
         rc = lib.cpc_peak(k, ctypes.byref(v), None)
         out[nm] = v.value if rc == 0 else None

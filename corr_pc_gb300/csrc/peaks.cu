@@ -37,7 +37,7 @@ __global__ void smem_atomic_ret_kernel(T *out, int iters, int conflict) {
   for (int i = 0; i < iters; i++) {
     const int a = (base + (i & 3) * blockDim.x) % n;
     const T old = atomicAdd(&h[a], T(1));
-    if (old + T(1) < old) acc += T(1);  // the carry test the pair kernel does
+    if (old + T(1) < old) acc += T(1);  // consume the returned value
   }
   __syncthreads();
   if (threadIdx.x == 0 && h[0] == T(-1)) out[0] = h[1] + acc;
