@@ -312,7 +312,9 @@ __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r,
     // unit vectors (3e-16 / c), and the reference's own sum = cos(theta)
     // rounding through acos (< 1.2e-15 / theta^2), each with margin
     const float rp = asinf(0.5f * c) * (rf.u.w + u2.w);
-    const float tol = rp * (1.5e-6f + 3e-14f / c + 4e-15f / c2);
+    // (approximate reciprocal: the factor 1.001 covers its few-ulp error)
+    const float rc = __fdividef(1.0f, c);
+    const float tol = rp * fmaf(4e-15f * rc, rc, fmaf(3e-14f, rc, 1.5e-6f)) * 1.001f;
     const int est = J.lin_bin ? (int)floorf((rp - J.rmin_f) * J.inv_rsize_f)
                               : (int)floorf((__log2f(rp * rp) - J.l2rmin2) * J.inv_lw);
     k1 = band_bin(rp, tol, est, J.nrp, s_A, s_B, J.rej_lo, J.rej_hi);
@@ -336,9 +338,9 @@ __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r,
     const float ddec = (w2.y - rf.w.y) + (x2.y - rf.x.y);
     const float xx = dra * __cosf(0.5f * (rf.x.z + x2.z)), yy = ddec;
     const float a = xx * xx, bb = yy * yy;
-    const float inv = 1.0f / (a + bb);
+    const float inv = __fdividef(1.0f, a + bb);
     const float cs = (a - bb) * inv, sn = 2.0f * xx * yy * inv;
-    const float theta = atanf(yy / xx);
+    const float theta = atanf(__fdividef(yy, xx));
     float v[kNF];
     for (int q = 0; q < kNF; q++) v[q] = 0.0f;
     v[0] = wt;
