@@ -173,12 +173,13 @@ def _cpu_sample(p, cats, budget_s: float, n_binned_full: int, threads: int, offs
     rate_guess = 4e6 * threads  # binned pairs/s on one ARM/x86 core, rough
     stride = max(1, int(n_binned_full / (rate_guess * budget_s)))
     t = time.perf_counter()
-    _, _, ntot, nin = oracle.port_corels2(p, "SD", ocats["D"], ocats["S"], n_threads=threads,
-                                          row_stride=stride, row_offset=offset % stride)
+    num, sums, ntot, nin = oracle.port_corels2(p, "SD", ocats["D"], ocats["S"],
+                                               n_threads=threads, row_stride=stride,
+                                               row_offset=offset % stride)
     dt = time.perf_counter() - t
     return {"value": nin / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"every {stride}-th outer row (offset {offset % stride}): "
-                      f"{nin} binned pairs in {dt:.2f} s"}, stride, nin, dt
+                      f"{nin} binned pairs in {dt:.2f} s"}, stride, nin, dt, (num, sums)
 
 
 def run_reference(args) -> None:
@@ -192,11 +193,12 @@ def run_reference(args) -> None:
     cats = host.prepare(p, [("S", wl.shape), ("D", wl.density)])
     threads = os.cpu_count() or 1
     # estimate the full binned count cheaply from a tiny sample
-    probe, stride0, nin0, _ = _cpu_sample(p, cats, 0.5, 10 ** 10, threads)
+    probe, stride0, nin0, _, _ = _cpu_sample(p, cats, 0.5, 10 ** 10, threads)
     n_full = nin0 * stride0
     tot_pairs, tot_t, last = 0, 0.0, None
     for s in range(args.warmup + args.steps):
-        res, stride, nin, dt = _cpu_sample(p, cats, args.ref_budget, n_full, threads, offset=s)
+        res, stride, nin, dt, _ = _cpu_sample(p, cats, args.ref_budget, n_full, threads,
+                                              offset=s)
         if s >= args.warmup:
             tot_pairs += nin
             tot_t += dt
@@ -266,17 +268,19 @@ def _sky_oracle_sample(wl, cats, budget_s, rows_hint, threads, offset=0):
     zsep = synth.derived_z_sep(p, wl.table)[0]
     strides = _sky_strides(cats, rows_hint)
     tot, dt = 0, 0.0
+    hists = {}
     for (t, a, b), st in zip(SKY_TERMS, strides):
         t0 = time.perf_counter()
-        _, _, _, nin = oracle.port_corels2(p, t, ocats[a], ocats[b], n_threads=threads,
-                                           row_stride=st, row_offset=offset % st,
-                                           H_z=wl.table.H, dA_z=wl.table.transverse,
-                                           z_sep_max=zsep)
+        num, sums, _, nin = oracle.port_corels2(p, t, ocats[a], ocats[b], n_threads=threads,
+                                                row_stride=st, row_offset=offset % st,
+                                                H_z=wl.table.H, dA_z=wl.table.transverse,
+                                                z_sep_max=zsep)
         dt += time.perf_counter() - t0
         tot += nin
+        hists[t] = (num, sums, st, offset % st)
         if dt > budget_s:
             break
-    return tot, dt, strides
+    return tot, dt, hists
 
 
 def run_sky(args) -> None:
@@ -363,11 +367,22 @@ def run_sky(args) -> None:
             "sample": f"8x sparser row sample: {nb64} binned pairs in {ms64:.1f} ms"}
     fp64["speedup_of_fast"] = value / fp64["value"]
     cpu = None
+    accuracy = None
     if not args.no_cpu:
-        n, dt, _ = _sky_oracle_sample(wl, cats, args.cpu_budget, args.sky_cpu_rows, threads)
+        n, dt, hists = _sky_oracle_sample(wl, cats, args.cpu_budget, args.sky_cpu_rows, threads)
         cpu = {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"about {args.sky_cpu_rows} outer rows per pair type: {n} binned "
                          f"pairs in {dt:.2f} s"}
+        # the fast kernel on the same rows of every term, against the oracle
+        accuracy = {"against": "oracle (FP64 restatement of corels2) on the CPU-baseline rows",
+                    "rows": cpu["sample"], "terms": {}}
+        for (t, a, bb) in SKY_TERMS:
+            if t not in hists:
+                continue
+            onum, osums, st, off = hists[t]
+            rf = ctx.count(t, SKY_SLOTS[a], SKY_SLOTS[bb], row_stride=st, row_offset=off)
+            accuracy["terms"][t] = metrics.accuracy_report(rf["num"], rf["sums"], onum, osums)
+        accuracy["ok"] = all(v["ok"] for v in accuracy["terms"].values())
     peaks = _peaks()
     F = metrics.flops_per_pair(p.which_corr, p.coordinates)
     A = metrics.smem_updates_per_pair(p.which_corr, bool(p.do_jk))
@@ -384,7 +399,7 @@ def run_sky(args) -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded generator, in memory)", "config": _sky_describe(wl, rows),
             "n_binned_per_step": n_bin / args.steps, "n_window_per_step": n_win / args.steps,
-            "roofline": roofline, "cpu_baseline": cpu, "fp64_gpu": fp64,
+            "roofline": roofline, "cpu_baseline": cpu, "fp64_gpu": fp64, "accuracy": accuracy,
             "e2e": {"value": nb_e / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_t},
             "gpu_launches": launches, "clocks": clk.summary()}
@@ -477,6 +492,7 @@ def main() -> None:
             tot_pair_ms += pms
     torch.cuda.synchronize()
     launches = sum(c.launches() for c in ctxs) - l0
+    g_cap, g_rep = ctxs[0].graph_stats()
     t_step = tot_ms / args.steps
     if dist:
         tt = torch.tensor([t_step], device="cuda")
@@ -555,19 +571,33 @@ def main() -> None:
                           f"{r64['kernel_ms']:.1f} ms"}
         fp64["speedup_of_fast"] = value / fp64["value"]
     cpu = None
+    accuracy = None
     if not args.no_cpu and len(wls) == 1:
-        cpu, _, _, _ = _cpu_sample(p, preps[0], args.cpu_budget, n_per_step,
-                                   os.cpu_count() or 1)
+        cpu, cstride, _, _, (onum, osums) = _cpu_sample(p, preps[0], args.cpu_budget,
+                                                        n_per_step, os.cpu_count() or 1)
+        # the fast kernel on the same rows, checked against the oracle's FP64 histograms
+        rf = ctxs[0].count("SD", 0, 1, row_stride=cstride)
+        accuracy = dict(metrics.accuracy_report(rf["num"], rf["sums"], onum, osums),
+                        against="oracle (FP64 restatement of corels2) on the CPU-baseline rows",
+                        rows=cpu["sample"])
+    elif fp64 is not None:
+        rf = ctxs[0].count("SD", 0, 1, row_stride=stride)
+        accuracy = dict(metrics.accuracy_report(rf["num"], rf["sums"], r64["num"], r64["sums"]),
+                        against="plain FP64 GPU kernel on its rows", rows=fp64["sample"])
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64", "data": "synthetic (seeded generator, in memory)",
             "config": dict(_describe(wls), tuning=tuning), "n_binned_per_step": n_per_step,
             "n_window_per_step": n_win / args.steps,
-            "roofline": roofline, "cpu_baseline": cpu, "fp64_gpu": fp64,
+            "roofline": roofline, "cpu_baseline": cpu, "fp64_gpu": fp64, "accuracy": accuracy,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_t},
-            "gpu_launches": launches, "clocks": clk.summary()}
+            "gpu_launches": launches,
+            "cuda_graph": {"captures": g_cap, "replays": g_rep,
+                           "note": "each step replays the captured zeroing + pair kernel + "
+                                   "recheck; captures include the autotuner's trial counts"},
+            "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

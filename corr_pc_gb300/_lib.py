@@ -96,6 +96,8 @@ def load() -> ctypes.CDLL:
     lib.cpc_host_rp_thresholds.argtypes = [P(cpc_params), V]
     lib.cpc_host_pi_thresholds.argtypes = [P(cpc_params), V]
     lib.cpc_launch_count.argtypes = [V, P(I64)]
+    lib.cpc_set_graph_replay.argtypes = [V, I]
+    lib.cpc_graph_stats.argtypes = [V, P(I64), P(I64)]
     lib.cpc_host_finalize_cross.argtypes = [ctypes.c_char_p] + [V] * 9
     lib.cpc_host_finalize_auto.argtypes = [ctypes.c_char_p] + [V] * 7
     lib.cpc_host_finalize_auto.restype = I
@@ -107,7 +109,8 @@ def load() -> ctypes.CDLL:
                "cpc_accum_shape",
                "cpc_count_batch", "cpc_set_tuning", "cpc_host_rand_uniform",
                "cpc_host_elip_angle", "cpc_host_rp_thresholds", "cpc_host_pi_thresholds",
-               "cpc_launch_count", "cpc_host_finalize_cross"):
+               "cpc_launch_count", "cpc_host_finalize_cross", "cpc_set_graph_replay",
+               "cpc_graph_stats"):
         getattr(lib, fn).restype = I
     _lib = lib
     return lib
@@ -222,6 +225,17 @@ class Context:
         v = ctypes.c_int64()
         check(self.lib.cpc_launch_count(self.h, ctypes.byref(v)), self.h)
         return v.value
+
+    def set_graph_replay(self, enable: bool) -> None:
+        """Replay fast counts from a captured CUDA graph (default) or launch
+        their kernels directly."""
+        check(self.lib.cpc_set_graph_replay(self.h, 1 if enable else 0), self.h)
+
+    def graph_stats(self) -> tuple:
+        """(captures, replays) of this context's fast-count graph."""
+        c, r = ctypes.c_int64(), ctypes.c_int64()
+        check(self.lib.cpc_graph_stats(self.h, ctypes.byref(c), ctypes.byref(r)), self.h)
+        return c.value, r.value
 
     def new_accum(self):
         nh, nb, npb = self.shape

@@ -156,6 +156,12 @@ struct cpc_ctx {
   int pending = 0;  // 0 none, 1 fast engine, 2 FP64 engine
   std::vector<JobPlan> pending_jobs;
   int64_t launches = 0;  // kernels launched by this context (all entry points)
+  // CUDA graph of the fast engine's device work (zeroing, pair kernels,
+  // recheck), replayed while every value baked into it stays the same
+  int graph_on = 1;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<uint64_t> gkey;
+  int64_t graph_captures = 0, graph_replays = 0;
 };
 
 namespace {
@@ -757,6 +763,127 @@ cpc_status run_plain(JobPlan &jp) {
 // fetch
 cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt = 0);
 
+// one persistent launch of the fast kernel over a range of the unit list
+struct FastGroup {
+  int corel, jk, minb, grid;
+  size_t first, n_units, smem;
+};
+
+size_t accum_cells(const cpc_ctx *c) {
+  const cpc_params &p = c->p;
+  return (size_t)(1 + (p.do_jk ? p.n_jk : 0)) * p.n_bins * p.n_p_bin;
+}
+
+// The device work of one fast count, in stream order on st: zero every job's
+// histogram block and counters, the edge-queue counter, then per group the
+// unit counter and the persistent kernel, then the FP64 recheck.  `rec`
+// records the timing events (cudaEventRecordExternal inside a capture, so
+// that they become event nodes of the graph).
+cpc_status fast_body(cpc_ctx *c0, std::vector<JobPlan> &jobs, const std::vector<FastGroup> &gs,
+                     cudaStream_t st, unsigned rec_flags) {
+  cpc_ctx *c = c0;
+  for (size_t k = 0; k < jobs.size(); k++) {
+    const cpc_status s = zero_accum(jobs[k].c, st);
+    if (s != CPC_OK) return s;
+  }
+  CK(cudaMemsetAsync(c0->d_qcount.p, 0, sizeof(unsigned long long), st), "memset");
+  CK(cudaEventRecordWithFlags(c0->e0, st, rec_flags), "event");
+  for (const FastGroup &g : gs) {
+    CK(cudaMemsetAsync(c0->d_unit_ctr.p, 0, sizeof(unsigned int), st), "memset");
+    CK(launch_fast(g.corel, g.jk, g.minb, c0->d_jobs.p, c0->d_units.p + g.first, (int)g.n_units,
+                   c0->d_unit_ctr.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, g.smem, g.grid, st),
+       "fast kernel");
+  }
+  CK(cudaEventRecordWithFlags(c0->e2, st, rec_flags), "event");
+  CK(launch_recheck(c0->d_jobs.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, c0->sm_count * 8, st),
+     "recheck kernel");
+  CK(cudaEventRecordWithFlags(c0->e1, st, rec_flags), "event");
+  return CPC_OK;
+}
+
+// Everything fast_body bakes into its launches: buffer addresses and sizes,
+// queue capacity, and each group's kernel, unit range, grid and shared memory.
+std::vector<uint64_t> fast_graph_key(cpc_ctx *c0, const std::vector<JobPlan> &jobs,
+                                     const std::vector<FastGroup> &gs) {
+  std::vector<uint64_t> k;
+  auto put = [&](uint64_t v) { k.push_back(v); };
+  put((uint64_t)(uintptr_t)c0->st);
+  put((uint64_t)(uintptr_t)c0->d_jobs.p);
+  put((uint64_t)(uintptr_t)c0->d_units.p);
+  put((uint64_t)(uintptr_t)c0->d_unit_ctr.p);
+  put((uint64_t)(uintptr_t)c0->d_queue.p);
+  put((uint64_t)(uintptr_t)c0->d_qcount.p);
+  put(c0->qcap);
+  put((uint64_t)c0->sm_count);
+  put(jobs.size());
+  for (const JobPlan &jp : jobs) {
+    put((uint64_t)(uintptr_t)jp.c->d_num.p);
+    put((uint64_t)(uintptr_t)jp.c->d_sums.p);
+    put((uint64_t)(uintptr_t)jp.c->d_counters.p);
+    put(accum_cells(jp.c));
+  }
+  put(gs.size());
+  for (const FastGroup &g : gs) {
+    put((uint64_t)g.corel);
+    put((uint64_t)g.jk);
+    put((uint64_t)g.minb);
+    put((uint64_t)g.grid);
+    put(g.first);
+    put(g.n_units);
+    put(g.smem);
+  }
+  return k;
+}
+
+void drop_graph(cpc_ctx *c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  c->gexec = nullptr;
+  c->gkey.clear();
+}
+
+// Launch the fast count's device work: replay the context's graph when it was
+// captured for the same key, else capture it anew (or launch directly when
+// graphs are off or the capture fails, which turns graphs off for the context).
+cpc_status launch_fast_body(cpc_ctx *c0, std::vector<JobPlan> &jobs,
+                            const std::vector<FastGroup> &gs) {
+  cpc_ctx *c = c0;
+  cudaStream_t st = c0->st;
+  const int64_t n_launch = (int64_t)gs.size() + 1;
+  if (!c0->graph_on) {
+    const cpc_status s = fast_body(c0, jobs, gs, st, cudaEventRecordDefault);
+    if (s == CPC_OK) c0->launches += n_launch;
+    return s;
+  }
+  std::vector<uint64_t> key = fast_graph_key(c0, jobs, gs);
+  if (!c0->gexec || key != c0->gkey) {
+    drop_graph(c0);
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const cpc_status s = fast_body(c0, jobs, gs, st, cudaEventRecordExternal);
+    const cudaError_t e_end = cudaStreamEndCapture(st, &g);
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e_inst = cudaErrorUnknown;
+    if (s == CPC_OK && e_end == cudaSuccess && g) e_inst = cudaGraphInstantiate(&ex, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (s != CPC_OK || e_end != cudaSuccess || e_inst != cudaSuccess) {
+      // capture unavailable here: direct launches from now on
+      cudaGetLastError();
+      if (ex) cudaGraphExecDestroy(ex);
+      c0->graph_on = 0;
+      const cpc_status s2 = fast_body(c0, jobs, gs, st, cudaEventRecordDefault);
+      if (s2 == CPC_OK) c0->launches += n_launch;
+      return s2;
+    }
+    c0->gexec = ex;
+    c0->gkey = std::move(key);
+    c0->graph_captures++;
+  }
+  CK(cudaGraphLaunch(c0->gexec, st), "graph launch");
+  c0->graph_replays++;
+  c0->launches += n_launch;
+  return CPC_OK;
+}
+
 cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
   cpc_ctx *c0 = jobs[0].c;
   cpc_ctx *c = c0;
@@ -765,7 +892,6 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
   for (size_t k = 0; k < jobs.size(); k++) {
     cpc_status s;
     if ((s = alloc_accum(jobs[k].c)) != CPC_OK) return s;
-    if ((s = zero_accum(jobs[k].c, st)) != CPC_OK) return s;
     jobs[k].jd.acc_num = jobs[k].c->d_num.p;
     jobs[k].jd.acc_sums = jobs[k].c->d_sums.p;
     jobs[k].jd.counters = jobs[k].c->d_counters.p;
@@ -800,8 +926,7 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
   CK(cudaMemcpyAsync(c0->d_jobs.p, jds.data(), sizeof(JobDev) * jds.size(), cudaMemcpyHostToDevice, st), "H2D jobs");
   if (total_units)
     CK(cudaMemcpyAsync(c0->d_units.p, all.data(), sizeof(UnitDesc) * total_units, cudaMemcpyHostToDevice, st), "H2D units");
-  CK(cudaMemsetAsync(c0->d_qcount.p, 0, sizeof(unsigned long long), st), "memset");
-  CK(cudaEventRecord(c0->e0, st), "event");
+  std::vector<FastGroup> gs;
   for (size_t g = 0; g < ranges.size(); g++) {
     const int corel = gkeys[g].first, jk = gkeys[g].second;
     int wmax = 0;
@@ -813,20 +938,12 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
     int bps = 0;
     const int minb = fast_variant(corel, jk, smem, &bps);
     if (bps <= 0) return fail(c, CPC_ERR_INVALID, "fast kernel does not fit on an SM with these bins");
-    const int n_units = (int)(ranges[g].second - ranges[g].first);
-    const int grid = (int)std::min<int64_t>((int64_t)c0->sm_count * bps, n_units);
-    CK(cudaMemsetAsync(c0->d_unit_ctr.p, 0, sizeof(unsigned int), st), "memset");
-    CK(launch_fast(corel, jk, minb, c0->d_jobs.p, c0->d_units.p + ranges[g].first, n_units,
-                   c0->d_unit_ctr.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, smem, grid, st),
-       "fast kernel");
-    c0->launches += 1;
+    const size_t n_units = ranges[g].second - ranges[g].first;
+    if (n_units == 0) continue;
+    const int grid = (int)std::min<int64_t>((int64_t)c0->sm_count * bps, (int64_t)n_units);
+    gs.push_back(FastGroup{corel, jk, minb, grid, ranges[g].first, n_units, smem});
   }
-  CK(cudaEventRecord(c0->e2, st), "event");
-  CK(launch_recheck(c0->d_jobs.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, c0->sm_count * 8, st),
-     "recheck kernel");
-  c0->launches += 1;
-  CK(cudaEventRecord(c0->e1, st), "event");
-  return CPC_OK;
+  return launch_fast_body(c0, jobs, gs);
 }
 
 cpc_status finish_fast(std::vector<JobPlan> &jobs, int grow_attempt) {
@@ -1452,6 +1569,7 @@ cpc_status cpc_create(cpc_ctx **out, const cpc_params *params) {
 cpc_status cpc_destroy(cpc_ctx *c) {
   if (!c) return CPC_OK;
   cudaStreamSynchronize(c->st);
+  drop_graph(c);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
   if (c->e2) cudaEventDestroy(c->e2);
@@ -1775,6 +1893,22 @@ cpc_status cpc_host_rp_thresholds(const cpc_params *p, double *thr) {
   if (p->n_bins <= 0 || p->n_bins > kMaxRp) return fail(nullptr, CPC_ERR_INVALID, "n_bins out of range");
   const int rc = rp_thresholds(p->lin_bin, p->n_bins, p->bin_r_min, p->bin_r_max, thr);
   return rc == 0 ? CPC_OK : fail(nullptr, CPC_ERR_INVALID, "threshold derivation failed");
+}
+
+cpc_status cpc_set_graph_replay(cpc_ctx *c, int enable) {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (busy(c)) return CPC_ERR_STATE;
+  cudaStreamSynchronize(c->st);
+  drop_graph(c);
+  c->graph_on = enable ? 1 : 0;
+  return CPC_OK;
+}
+
+cpc_status cpc_graph_stats(const cpc_ctx *c, int64_t *captures, int64_t *replays) {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (captures) *captures = c->graph_captures;
+  if (replays) *replays = c->graph_replays;
+  return CPC_OK;
 }
 
 cpc_status cpc_launch_count(const cpc_ctx *c, int64_t *launches) {

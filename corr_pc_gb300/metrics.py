@@ -34,3 +34,56 @@ def flops_per_pair(which_corr: int, coordinates: int = 6) -> int:
 
 def smem_updates_per_pair(which_corr: int, do_jk: bool, attributions: float = 1.0) -> float:
     return SMEM_MAIN[which_corr] + (attributions * SMEM_JK[which_corr] if do_jk else 0.0)
+
+
+# histogram fields (cpc_accum layout): p_bin.wt_num, then data[1..6].val/.err
+FIELD_NAMES = ["wt_num"] + [f"data{j}.{v}" for j in range(1, 7) for v in ("val", "err")]
+# fields whose per-pair terms cannot cancel (weights, squares, the theta term)
+NONCANCEL = (0, 2, 4, 6, 8, 10, 11, 12)
+
+
+def accuracy_report(num, sums, ref_num, ref_sums, rtol: float = 1e-6, big_frac: float = 1e-2):
+    """Per-bin error of a histogram block against a double-precision one of the
+    same rows: whether every integer count (full sample and every jackknife
+    region) is identical, and per field the largest |error| over all bins as a
+    fraction of the field's largest |value| (the absolute floor of the accuracy
+    bar), the largest relative error over the bins holding at least `big_frac`
+    of that value, and the largest relative error of the Pi-integrated r_p
+    profile (sum over Pi bins, full sample: the numerator of w(r_p)).  `ok`
+    applies the bar: counts identical, every field within rtol of its largest
+    value, and -- for the fields whose terms cannot cancel (weights, squares,
+    theta term) -- bins and profiles holding >= big_frac of it within rtol
+    relative (a cancelling sum near zero is held to the absolute floor)."""
+    import numpy as np
+    num, ref_num = np.asarray(num), np.asarray(ref_num)
+    sums, ref_sums = np.asarray(sums, dtype=np.float64), np.asarray(ref_sums, dtype=np.float64)
+    out = {"counts_bit_exact": bool(np.array_equal(num, ref_num)),
+           "n_bins_compared": int(ref_num.size), "fields": {}}
+    ok = out["counts_bit_exact"]
+    for f in range(ref_sums.shape[-1]):
+        r, g = ref_sums[..., f], sums[..., f]
+        fmax = float(np.abs(r).max()) if r.size else 0.0
+        if fmax == 0.0:
+            if r.size and float(np.abs(g).max()) != 0.0:
+                ok = False
+            continue
+        err = np.abs(g - r)
+        big = np.abs(r) >= big_frac * fmax
+        rel_big = float((err[big] / np.abs(r[big])).max())
+        pr, pg = r[0].sum(axis=-1), g[0].sum(axis=-1)  # full sample, summed over Pi
+        pmax = float(np.abs(pr).max())
+        pbig = np.abs(pr) >= big_frac * pmax
+        prof = float((np.abs(pg - pr)[pbig] / np.abs(pr[pbig])).max()) if pmax > 0 else 0.0
+        e_floor = float(err.max()) / fmax
+        out["fields"][FIELD_NAMES[f]] = {"max_err_over_field_max": e_floor,
+                                         "max_rel_err_bins_ge_1pct": rel_big,
+                                         "max_rel_err_rp_profile": prof,
+                                         "cancelling": f not in NONCANCEL}
+        ok = ok and e_floor <= rtol
+        if f in NONCANCEL:
+            ok = ok and rel_big <= rtol and prof <= rtol
+    out["ok"] = bool(ok)
+    out["bar"] = (f"counts identical; |error| <= {rtol:g} x field max in every bin; "
+                  f"non-cancelling fields <= {rtol:g} relative in bins and r_p profiles "
+                  f"holding >= {big_frac:g} of it")
+    return out

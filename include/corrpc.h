@@ -211,6 +211,22 @@ cpc_status cpc_autotune(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_
  * for a batch, counted on the first job's context). */
 cpc_status cpc_launch_count(const cpc_ctx *ctx, int64_t *launches);
 
+/* CUDA graphs of the fast box engine (no counterpart in the reference, whose
+ * pair loop is an OpenMP loop on the host).  A fast count -- cpc_count,
+ * cpc_count_async, cpc_count_auto, cpc_count_batch (on the first job's
+ * context) -- zeroes its histogram blocks, runs one persistent pair-kernel
+ * launch per corel group and the FP64 recheck.  The context captures that
+ * device work once into a CUDA graph and replays it on later counts whose
+ * launches are the same (same buffers, queue capacity, unit ranges, grids and
+ * shared memory; the job descriptors and work units are copied in before each
+ * replay), capturing again when any of them changes.  Results do not depend on
+ * it.  Enabled by default; cpc_set_graph_replay(ctx, 0) launches directly.  If
+ * a capture fails the context falls back to direct launches. */
+cpc_status cpc_set_graph_replay(cpc_ctx *ctx, int enable);
+
+/* Graph captures and replays of this context's fast counts so far. */
+cpc_status cpc_graph_stats(const cpc_ctx *ctx, int64_t *captures, int64_t *replays);
+
 /* ---- host helpers of the reference's read path (no GPU needed) ---- */
 
 /* glibc rand() stream after srand(seed): out[i] = rand_{skip+i}() /

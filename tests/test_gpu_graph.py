@@ -1,0 +1,82 @@
+"""CUDA-graph replay of the fast box engine: a count captured once and
+replayed gives the reference's results on every replay, a change of the launch
+shape captures again, and direct launches give the same results."""
+import numpy as np
+import pytest
+
+import oracle
+from corr_pc_gb300 import _lib, host, synth
+from helpers import Golden, check_sums
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx_for(p, S, D):
+    cats = host.prepare(p, [("S", S), ("D", D)])
+    ctx = _lib.Context(p)
+    ctx.upload(0, cats["D"])
+    ctx.upload(1, cats["S"])
+    return ctx
+
+
+def _check(r, g, label):
+    assert r["n_binned"] == g.n_in and r["n_window"] == g.n_total
+    assert np.array_equal(r["num"], g.raw_num)
+    check_sums(r["sums"], g.raw_sums, label=label)
+
+
+@pytest.mark.parametrize("name", ["box_wgp_clustered", "box_wpp_weighted_distinct"])
+def test_replayed_counts_match_reference(name):
+    g = Golden(name)
+    ctx = _ctx_for(g.params, g.S, g.D)
+    for k in range(3):
+        _check(ctx.count("SD", 0, 1), g, f"{name} replay {k}")
+    captures, replays = ctx.graph_stats()
+    assert captures == 1 and replays == 3
+    # direct launches: the same results
+    ctx.set_graph_replay(False)
+    _check(ctx.count("SD", 0, 1), g, f"{name} direct")
+    assert ctx.graph_stats() == (1, 3)
+
+
+def test_changed_launch_shape_captures_again():
+    g = Golden("box_wpp_uniform")
+    ctx = _ctx_for(g.params, g.S, g.D)
+    _check(ctx.count("SD", 0, 1), g, "first")
+    ctx.set_tuning(0, 9, 0)  # another Pi window: other units, grid, shared memory
+    _check(ctx.count("SD", 0, 1), g, "window 9")
+    _check(ctx.count("SD", 0, 1), g, "window 9 replay")
+    assert ctx.graph_stats() == (2, 3)
+    # a row sample differs only in the job descriptor (copied in before each
+    # replay): the same graph serves it and the full count after it
+    r = ctx.count("SD", 0, 1, row_stride=5, row_offset=2)
+    assert 0 < r["n_binned"] < g.n_in
+    _check(ctx.count("SD", 0, 1), g, "full again")
+    assert ctx.graph_stats() == (2, 5)
+
+
+def test_async_count_replays_on_a_caller_stream():
+    import torch
+    g = Golden("box_wgp_clustered")
+    ctx = _ctx_for(g.params, g.S, g.D)
+    s = torch.cuda.Stream()
+    for _ in range(2):
+        ctx.count_async("SD", 0, 1, stream=s.cuda_stream)
+        _check(ctx.finish(), g, "async")
+    assert ctx.graph_stats() == (1, 2)
+
+
+def test_batch_replays_match_oracle():
+    wls = synth.box_batch_wpp(n_boxes=5, seed=11, scale=0.02)
+    ctxs = [_ctx_for(w.params, w.shape, w.density) for w in wls]
+    ref = []
+    for w in wls:
+        oc = oracle.read_like_reference(w.params, [("S", w.shape), ("D", w.density)])
+        ref.append(oracle.port_corels2(w.params, "SD", oc["D"], oc["S"]))
+    for rep in range(2):
+        rs = _lib.count_batch([(c, "SD", 0, 1) for c in ctxs])
+        for r, (num, sums, n_total, n_in) in zip(rs, ref):
+            assert r["n_binned"] == n_in and r["n_window"] == n_total
+            assert np.array_equal(r["num"], num)
+            check_sums(r["sums"], sums, label=f"batch replay {rep}")
+    assert ctxs[0].graph_stats() == (1, 2)
