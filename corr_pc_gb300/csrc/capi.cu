@@ -371,7 +371,7 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   auto fit = [&](int blocks) {
     const size_t budget = (size_t)(228 * 1024) / blocks - static_b - 1024;
     int w = npi;
-    while (w > (rmu ? 1 : 8) && fast_smem_bytes(jp.rule.corel, jk, nrp * w) > budget) w--;
+    while (w > (rmu ? 1 : 8) && fast_smem_bytes(jp.rule.corel, jk, nrp, w) > budget) w--;
     return w;
   };
   int wpi = npi;
@@ -929,12 +929,11 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
   std::vector<FastGroup> gs;
   for (size_t g = 0; g < ranges.size(); g++) {
     const int corel = gkeys[g].first, jk = gkeys[g].second;
-    int wmax = 0;
+    size_t smem = 0;  // the largest any job of the group needs
     for (size_t k = ranges[g].first; k < ranges[g].second; k++) {
       const JobPlan &jp = jobs[all[k].job];
-      wmax = std::max(wmax, jp.wpi * jp.jd.nrp);
+      smem = std::max(smem, fast_smem_bytes(corel, jk, jp.jd.nrp, jp.wpi));
     }
-    const size_t smem = fast_smem_bytes(corel, jk, wmax);
     int bps = 0;
     const int minb = fast_variant(corel, jk, smem, &bps);
     if (bps <= 0) return fail(c, CPC_ERR_INVALID, "fast kernel does not fit on an SM with these bins");
@@ -1801,8 +1800,8 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
     for (int b = 4; b >= 2; b--) {
       const size_t budget = (size_t)(228 * 1024) / b - static_b - 1024;
       int w = npi;
-      while (w > 1 && fast_smem_bytes(rule.corel, jk, nrp * w) > budget) w--;
-      if (fast_smem_bytes(rule.corel, jk, nrp * w) > budget) continue;
+      while (w > 1 && fast_smem_bytes(rule.corel, jk, nrp, w) > budget) w--;
+      if (fast_smem_bytes(rule.corel, jk, nrp, w) > budget) continue;
       for (int cand : {w, (3 * w + 3) / 4}) {
         if (cand < std::min(npi, 8)) continue;
         if (std::find(ws.begin(), ws.end(), cand) == ws.end()) ws.push_back(cand);

@@ -75,7 +75,7 @@ constexpr int kFastBlocksPerSM = 4;  // occupancy target: registers and shared m
 constexpr int kFastMaxCols = 512;
 constexpr int kFastMaxSeg = 256;
 constexpr int kMaxCellsPerRmax = 9;
-size_t fast_smem_bytes(int corel, int do_jk, int NB);
+size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi);
 size_t fast_static_smem_bytes();
 int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm);
 cudaError_t launch_fast(int corel, int jk, int minb, const JobDev *jobs, const UnitDesc *units,

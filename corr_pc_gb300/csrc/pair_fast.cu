@@ -46,6 +46,9 @@ constexpr int kThreads = kTile * kGroups;     // block size
 constexpr int kBatch = kThreads;              // candidates staged per batch
 constexpr int kMaxSeg = kFastMaxSeg;
 constexpr int kMaxCols = kFastMaxCols;
+// candidates of a group per block barrier: a chunk adds at most kTile * kChunk
+// = 2^17 terms to any word, so the flush test below runs once per chunk
+constexpr int kChunk = 4 * kThreads;
 
 // Per corel: the main fields m(k), k < FM, the jackknife fields j(g), g < FJ, and
 // jm(g), the main slot holding jackknife field g (m(jm(g)) == j(g)).
@@ -116,8 +119,36 @@ static_assert(jm_consistent<FieldMap<COREL_DD>>() && jm_consistent<FieldMap<CORE
 // 16 banks away from the low-word array.
 __host__ __device__ constexpr int hi_pad(int words) { return (16 - (words & 31) + 32) & 31; }
 
-// Shared-memory bytes a block needs for a job with NB = nrp * wpi local bins.
-size_t fast_smem_bytes(int corel, int do_jk, int NB) {
+// Replicas of the hot r_p bins.  Most pairs fall in the few largest r_p bins
+// (their count grows as r_p^2), so the lanes of one heavy-step instruction
+// often add into the same main-histogram bins, and same-address shared
+// reductions are serialised.  The top kHotBins r_p bins of the main histogram
+// therefore get kHotRep copies each, the copy picked by lane bits 1-2 (bit 0
+// already splits lanes over the low and high words); the flush adds the copies
+// together in exact integer arithmetic.
+#ifndef CPC_HOT_REP
+#define CPC_HOT_REP 1
+#endif
+#ifndef CPC_HOT_BINS
+#define CPC_HOT_BINS 4
+#endif
+constexpr int kHotRep = CPC_HOT_REP, kHotBins = CPC_HOT_BINS;
+static_assert(kHotRep == 1 || kHotRep == 2 || kHotRep == 4 || kHotRep == 8, "replicas: 1, 2, 4 or 8");
+// main-histogram bins of a block: nrp * wpi, plus the hot bins' extra copies
+__host__ __device__ __forceinline__ int hot_rows(int nrp) { return nrp < kHotBins ? nrp : kHotBins; }
+__host__ __device__ __forceinline__ int main_bins(int nrp, int wpi) {
+  return nrp * wpi + (kHotRep - 1) * hot_rows(nrp) * wpi;
+}
+// bin of copy r (1 <= r < kHotRep) of hot bin (n1, elk), n1 >= nrp - hot_rows(nrp)
+__host__ __device__ __forceinline__ int rep_bin(int r, int n1, int elk, int nrp, int wpi) {
+  const int h = hot_rows(nrp);
+  return nrp * wpi + ((r - 1) * h + (n1 - (nrp - h))) * wpi + elk;
+}
+
+// Shared-memory bytes a block needs for a job with nrp r_p bins and a wpi-bin
+// Pi window.
+size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi) {
+  const int NB = nrp * wpi, NBm = main_bins(nrp, wpi);
   int FM = 1, FJ = 1;
   if (corel == COREL_SD) { FM = 7; FJ = 4; }
   if (corel == COREL_SS) { FM = 11; FJ = 6; }
@@ -126,7 +157,7 @@ size_t fast_smem_bytes(int corel, int do_jk, int NB) {
   if (corel == COREL_SK) { FM = 4; FJ = 4; }
   if (corel == COREL_ED) { FM = 3; FJ = 2; }
   size_t b = sizeof(float4) * 2 * kBatch;                // staging
-  b += 8ull * FM * NB + 4ull * NB + 4ull * hi_pad(FM * NB);
+  b += 8ull * FM * NBm + 4ull * NBm + 4ull * hi_pad(FM * NBm);
   if (do_jk) b += 2 * (8ull * FJ * NB + 4ull * NB + 4ull * hi_pad(FJ * NB));
   return b;
 }
@@ -236,29 +267,39 @@ __device__ __forceinline__ void flush_region(unsigned *cnt, unsigned *lo, unsign
 
 // Flush the main histogram (into h = 0) and the tile's region (into hx): the
 // region takes main minus NX, in exact integer arithmetic; zero both.
+// Main bins are strided by NBm (main_bins: the hot bins' copies after the NB
+// plain bins); the copies of a hot bin are summed into it.
 template <int FM, int FJ, class FMAP>
 __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsigned *mhi,
                                              unsigned *ncnt, unsigned *nlo, unsigned *nhi, int NB,
-                                             int wpi, int npi, int nrp, int n2_base, int hx,
-                                             bool jk, int f0, const double *s_iqs,
+                                             int NBm, int wpi, int npi, int nrp, int n2_base,
+                                             int hx, bool jk, int f0, const double *s_iqs,
                                              const JobDev &J) {
   const int64_t hsz = (int64_t)nrp * npi;
+  const int hot0 = nrp - hot_rows(nrp);
   for (int lb = threadIdx.x; lb < NB; lb += kThreads) {
-    const unsigned n = mcnt[lb];
+    const int n1 = lb / wpi, elk = lb - n1 * wpi;
+    const int nrep = (kHotRep > 1 && n1 >= hot0) ? kHotRep : 1;
+    unsigned n = mcnt[lb];
+    for (int r = 1; r < nrep; r++) n += mcnt[rep_bin(r, n1, elk, nrp, wpi)];
     if (!n) continue;  // no pair in this bin since the last flush: every word is 0
-    const int64_t cell = (int64_t)(lb / wpi) * npi + n2_base + lb % wpi;
+    const int64_t cell = (int64_t)n1 * npi + n2_base + elk;
     atomicAdd(&J.acc_num[cell], (unsigned long long)n);
     mcnt[lb] = 0u;
+    for (int r = 1; r < nrep; r++) mcnt[rep_bin(r, n1, elk, nrp, wpi)] = 0u;
     long long tm[FM];
 #pragma unroll
     for (int f = 0; f < FM; f++) {
-      const size_t o = (size_t)f * NB + lb;
-      tm[f] = (long long)(int)mhi[o] * 16384ll + (long long)mlo[o];
+      tm[f] = 0;
+      for (int r = 0; r < nrep; r++) {
+        const size_t o = (size_t)f * NBm + (r == 0 ? lb : rep_bin(r, n1, elk, nrp, wpi));
+        tm[f] += (long long)(int)mhi[o] * 16384ll + (long long)mlo[o];
+        mlo[o] = 0u;
+        mhi[o] = 0u;
+      }
       const int fld = FMAP::m(f);
       if (f >= f0 && tm[f] != 0)
         atomicAdd(&J.acc_sums[cell * kNF + fld], (double)tm[f] * s_iqs[fld]);
-      mlo[o] = 0u;
-      mhi[o] = 0u;
     }
     if (!jk) continue;
     const int64_t xc = (int64_t)hx * hsz + cell;
@@ -294,11 +335,14 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   float4 *s_pos = reinterpret_cast<float4 *>(smem);
   float4 *s_shp = s_pos + kBatch;
   unsigned char *hist_base = smem + sizeof(float4) * 2 * kBatch;
+  // the candidate slots of a unit, used only while the staging buffer is idle
+  // (between the unit's slot set-up barriers, before any candidate is staged)
+  int *s_slot_b = reinterpret_cast<int *>(s_pos);
+  int *s_slot_info = s_slot_b + kMaxSeg;
+  static_assert(2 * kMaxSeg * sizeof(int) <= kBatch * sizeof(float4), "slot tables fit the staging buffer");
 
   __shared__ int s_unit;
   __shared__ int s_cnt[kMaxCols + 1];
-  __shared__ int s_slot_b[kMaxSeg];
-  __shared__ int s_slot_info[kMaxSeg];
   __shared__ int s_seg_a[kMaxSeg], s_seg_len[kMaxSeg], s_seg_key[kMaxSeg];
   __shared__ int s_order[kMaxSeg], s_pre[kMaxSeg + 1];
   __shared__ int s_jidx[kBatch];
@@ -315,6 +359,10 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   __shared__ float2 s_rlo[kTile];
   __shared__ float s_rzlo[kTile], s_zlo[kBatch];  // z lo parts (ED separations)
   __shared__ unsigned char s_rkeep[kTile];
+  // corels1 rule of each row for each z image sz (index sz + 1), as a threshold
+  // on the partner's input index: -1 every partner (and every pair outside
+  // corels1), the row's own index: partners after it, INT_MAX: none
+  __shared__ int s_rothr[3][kTile];
   __shared__ unsigned s_wq[kThreads / 32][kQCap];
 
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
@@ -334,13 +382,15 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     const UnitDesc U = units[u];
     const JobDev &J = jobs[U.job];
     const int nrp = J.nrp, wpi = J.wpi, npi = J.npi, NB = nrp * wpi;
-    // per histogram: count[NB], low words [F][NB], high words [F][NB]
+    const int NBm = main_bins(nrp, wpi), hot0 = nrp - hot_rows(nrp);
+    // per histogram: count[NB], low words [F][NB], high words [F][NB] (main:
+    // NBm bins, the hot bins' copies included)
     unsigned *s_mnum = reinterpret_cast<unsigned *>(hist_base);
     // the high words sit hi_pad words after a 32-word-aligned offset from the low
     // words, so the low and high word of one bin are 16 banks apart (red_pair)
-    unsigned *s_mlo = s_mnum + NB;
-    unsigned *s_mhi = s_mlo + (size_t)F::FM * NB + hi_pad(F::FM * NB);
-    unsigned *s_nxnum = s_mhi + (size_t)F::FM * NB;
+    unsigned *s_mlo = s_mnum + NBm;
+    unsigned *s_mhi = s_mlo + (size_t)F::FM * NBm + hi_pad(F::FM * NBm);
+    unsigned *s_nxnum = s_mhi + (size_t)F::FM * NBm;
     unsigned *s_nxlo = s_nxnum + NB;
     unsigned *s_nxhi = s_nxlo + (size_t)F::FJ * NB + hi_pad(F::FJ * NB);
     unsigned *s_ynum = s_nxhi + (size_t)F::FJ * NB;
@@ -348,24 +398,12 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     unsigned *s_yhi = s_ylo + (size_t)F::FJ * NB + hi_pad(F::FJ * NB);
     const int f0 = J.unit_w ? 1 : 0;  // unit weights: wt_num = count, not accumulated
 
-    // ---- this thread's g1 row.  The lanes of a warp are spread over the whole
-    // tile (tile row q = lane * W + warp) so that simultaneous pairs of a warp
-    // fall in different Pi bins; both warp groups hold the same rows and split
-    // the candidates. ----
-    // W warps hold the tile's rows (row q = lane * W + warp-in-group); the
-    // block's 8 warps form G = 8 / W such groups, each taking a share of every
-    // staged batch, so small tiles still keep every warp busy
+    // ---- the tile's g1 rows, in shared memory.  Row slot tr = s * 32 + l holds
+    // tile row q = l * W + s (s < W): a warp holds slots s * 32 .. s * 32 + 31 in
+    // its pass s, so its lanes are spread over the whole tile and simultaneous
+    // pairs of a warp fall in different Pi bins.  Every warp tests its own
+    // candidates against every row, one pass of 32 rows at a time. ----
     const int W = (U.g1_count + 31) >> 5;
-    const int G = (kThreads / 32) / W;
-    const int grp = wid / W;
-    const int tr = (wid - grp * W) * 32 + lane;  // row slot in the tile (< 32 W)
-    const int q = lane * W + (wid - grp * W);
-    const bool has1 = grp < G && q < U.g1_count;
-    const int64_t i1 = (int64_t)U.g1_start + (int64_t)q * U.g1_stride;
-    float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool valid = false;
-    int oi = 0;       // input index of the row (corels1)
-    uint8_t af = 0;   // its corels1 scan-start flags
     // hi + lo positions for the orientation angle (raw separations) and the ED
     // separation
     constexpr bool kTheta = C == COREL_SD || C == COREL_SS || C == COREL_SSA || C == COREL_SK;
@@ -375,24 +413,34 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     // jobs only)
     const int gws = J.gws, lin_bin = J.lin_bin;
     const float rmin_f = J.rmin_f, inv_rsize_f = J.inv_rsize_f;
-    if (has1) {
-      p1 = J.f1.pos[i1];
-      valid = true;
-      if (J.auto_mode) {
-        oi = (int)J.d1.orig[i1];
-        af = J.f1.aflag[i1];
-      }
-      if (J.row_stride > 1) {
-        const int64_t o = J.d1.orig[i1] - J.row_offset;
-        valid = (o % J.row_stride) == 0;
-      }
-      if (grp == 0) {
-        s_rpos[tr] = p1;
+    for (int tr = t; tr < 32 * W; tr += kThreads) {
+      const int q = (tr & 31) * W + (tr >> 5);
+      float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+      unsigned char ok = 0, af = 0;
+      int oi = 0;
+      if (q < U.g1_count) {
+        const int64_t i1 = (int64_t)U.g1_start + (int64_t)q * U.g1_stride;
+        p = J.f1.pos[i1];
+        ok = 1;
+        if (J.auto_mode) {
+          oi = (int)J.d1.orig[i1];  // input index (corels1)
+          af = J.f1.aflag[i1];      // corels1 scan-start flags
+        }
+        if (J.row_stride > 1) {
+          const int64_t o = J.d1.orig[i1] - J.row_offset;
+          ok = (o % J.row_stride) == 0;
+        }
         if (C != COREL_DD) s_rshp[tr] = J.f1.shp[i1];
         if (has_lo) s_rlo[tr] = J.f1.lo[i1];
         if (C == COREL_ED && has_lo) s_rzlo[tr] = J.f1.zlo[i1];
         if (JK) s_rkeep[tr] = J.f1.keep[i1];
       }
+      // a row that is not counted gets z = NaN: every window test fails
+      if (!ok) p.z = __int_as_float(0x7fc00000);
+      s_rpos[tr] = p;
+      for (int z = -1; z <= 1; z++)
+        s_rothr[z + 1][tr] = auto_image_all(J.auto_mode, z, af) ? -1
+                             : auto_image_gt(J.auto_mode, z, af) ? oi : INT_MAX;
     }
     const float Lf = J.Lf;
     const float xy_in = J.xy_in, xy_out = J.xy_out;
@@ -509,10 +557,6 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         int sx, sy, sz;
         shift_decode(code, sx, sy, sz);
         const bool same_region = region2 == U.region;
-        // corels1: this image counts every partner, or only partners after the
-        // row in input order, or none
-        const bool a_all = auto_image_all(J.auto_mode, sz, af);
-        const bool a_gt = !a_all && auto_image_gt(J.auto_mode, sz, af);
         // staging order: position (i * ks) mod N over the group's N candidates,
         // ks coprime with N and ~0.618 N, so a batch is a spread-out sample of
         // the group's columns and z range (decorrelated bins, fewer collisions)
@@ -531,26 +575,38 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
           }
           cur_y = region2;
         }
-        // g1-side shift for +1 images (x1 - L exact for x1 >= L/2), g2-side for -1
-        const float x1s = sx == 1 ? p1.x - Lf : p1.x;
-        const float y1s = sy == 1 ? p1.y - Lf : p1.y;
-        const float z1s = sz == 1 ? p1.z - Lf : p1.z;
+        // g2-side shift for -1 images (x2 - L exact for the candidates that can
+        // reach the window); the g1-side shift for +1 images (x1 - L exact for
+        // x1 >= L/2) is applied per row below
         const float g2sx = sx == -1 ? Lf : 0.f, g2sy = sy == -1 ? Lf : 0.f, g2sz = sz == -1 ? Lf : 0.f;
 
-        for (int base = 0; base < gN; base += kBatch) {
-          const int nb = min(kBatch, gN - base);
+        for (int base = 0; base < gN; base += kChunk) {
+          const int nc = min(kChunk, gN - base);
           // s_nbin is read after a barrier and changed only after the next one
-          if (s_nbin + (unsigned)(kTile * nb) > kFlushTerms) {  // keep every word below 2^32
+          if (s_nbin + (unsigned)(kTile * nc) > kFlushTerms) {  // keep every word below 2^32
             __syncthreads();
-            flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_nxnum, s_nxlo, s_nxhi, NB, wpi,
-                                          npi, nrp, n2_base, 1 + U.region, JK, f0, s_iqs, J);
+            flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_nxnum, s_nxlo, s_nxhi, NB, NBm,
+                                          wpi, npi, nrp, n2_base, 1 + U.region, JK, f0, s_iqs,
+                                          J);
             if (JK && cur_y >= 0)
               flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
                                          1 + cur_y, f0, s_iqs, J);
             if (t == 0) s_nbin = 0u;
+            __syncthreads();
           }
-          if (t < nb) {
-            const int p = s_pre[k] + (int)(((long long)(base + t) * ks) % gN);
+          // this warp's share of the chunk, positions [wlo, wlo + wlen) (an
+          // eighth of it), in nbw batches of at most 32 candidates of even size,
+          // staged in the warp's own slots c0 .. c0 + 31 (read by this warp
+          // only: no block barrier)
+          const int c0 = wid * 32;
+          const int wlo = (wid * nc) / (kThreads / 32);
+          const int wlen = ((wid + 1) * nc) / (kThreads / 32) - wlo;
+          const int nbw = (wlen + 31) >> 5;
+          for (int bw = 0; bw < nbw; bw++) {
+          const int s0 = wlo + (bw * wlen) / nbw;
+          const int nk = wlo + ((bw + 1) * wlen) / nbw - s0;  // 1 .. 32
+          if (lane < nk) {
+            const int p = s_pre[k] + (int)(((long long)(base + s0 + lane) * ks) % gN);
             int lo = k, hi = g;  // segment s_order[lo] with s_pre[lo] <= p < s_pre[lo+1]
             while (hi - lo > 1) {
               const int mid = (lo + hi) >> 1;
@@ -570,21 +626,32 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             if (J.auto_mode) s_orig[t] = (int)J.d2.orig[j2];
             if (JK) s_keep[t] = J.f2.keep[j2];
           }
-          __syncthreads();
+          __syncwarp();
 
-          // ---- light pass over the batch, binned pairs queued per warp; the
-          // heavy step runs whenever 32 are queued (all lanes busy) ----
-          // lane l at step s takes slot c0 + (s + l) mod nk, so a warp works on
-          // 32 different candidates;
-          // group g takes batch slots [c0, c0 + nk); warps outside every group
-          // (8 % W of them) skip the pass
-          const int c0 = grp < G ? (grp * nb) / G : 0;
-          const int nk = grp < G ? ((grp + 1) * nb) / G - c0 : 0;
+          // ---- light pass over the warp's candidates, row pass by row pass;
+          // binned pairs are queued per warp and the heavy step runs whenever
+          // 32 are queued (all lanes busy).  Lane l at step s takes slot
+          // c0 + (s + l) mod nk, so a warp works on 32 different candidates. ----
+          // row registers of pass `pass` (row slot pass * 32 + lane): the
+          // shifted position and othr, the row's corels1 threshold for this image
+          int pass = 0;
+          float x1s, y1s, z1s;
+          int othr;
+#define CPC_SET_ROW()                                                         \
+  {                                                                           \
+    const int tr_ = pass * 32 + lane;                                         \
+    const float4 p1 = s_rpos[tr_];                                            \
+    x1s = sx == 1 ? p1.x - Lf : p1.x;                                         \
+    y1s = sy == 1 ? p1.y - Lf : p1.y;                                         \
+    z1s = sz == 1 ? p1.z - Lf : p1.z;                                         \
+    othr = s_rothr[sz + 1][tr_];                                              \
+  }
+          CPC_SET_ROW();
           int step = 0;
           int qhead = 0, qtail = 0;
-          int cr = nk > 0 ? lane % nk : 0;  // (step + lane) mod nk, kept incrementally
+          int cr = lane % nk;  // (step + lane) mod nk, kept incrementally
           for (;;) {
-            while (step < nk && (qtail - qhead) < 32) {
+            while (pass < W && (qtail - qhead) < 32) {
               const int c = c0 + cr;
               const float4 p2 = s_pos[c];
               const float dz = p2.z - z1s;
@@ -592,7 +659,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               const float dy = y1s - p2.y;
               const float m = fmaxf(fabsf(dx), fabsf(dy));
               bool binned = false, edge = false;
-              if (valid && (a_all || (a_gt && s_orig[c] > oi)) && dz >= pi_out_lo &&
+              if ((othr < 0 || s_orig[c] > othr) && dz >= pi_out_lo &&
                   dz <= pi_out_hi && m <= xy_out) {
                 if (!(dz >= pi_in_lo && dz <= pi_in_hi && m <= xy_in)) {
                   // near the window edge: queued with a flag, the heavy step hands
@@ -610,10 +677,15 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               const unsigned bm = __ballot_sync(0xffffffffu, push);
               if (push)
                 s_wq[wid][(qtail + __popc(bm & lt_mask)) & (kQCap - 1)] =
-                    (unsigned)tr | ((unsigned)c << 7) | (edge ? kEdgeFlag : 0u);
+                    (unsigned)(pass * 32 + lane) | ((unsigned)c << 7) | (edge ? kEdgeFlag : 0u);
               qtail += __popc(bm);
-              step++;
-              cr = (cr + 1 == nk) ? 0 : cr + 1;
+              if (++step == nk) {  // next row pass
+                step = 0;
+                cr = lane % nk;
+                if (++pass < W) CPC_SET_ROW();
+              } else {
+                cr = (cr + 1 == nk) ? 0 : cr + 1;
+              }
             }
             const int avail = qtail - qhead;
             if (avail == 0) break;
@@ -793,11 +865,15 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                 wa[f] = odd_lane ? b : a;
                 wb[f] = odd_lane ? a : b;
               }
-              atomicAdd(&s_mnum[lb], 1u);
+              // the main bin, or one of its copies for a hot r_p bin
+              const int rep = (lane >> 1) & (kHotRep - 1);
+              const int lbm = (kHotRep > 1 && n1 >= hot0 && rep != 0)
+                                  ? rep_bin(rep, n1, elk, nrp, wpi) : lb;
+              atomicAdd(&s_mnum[lbm], 1u);
 #pragma unroll
               for (int f = 0; f < F::FM; f++)
                 if (f >= f0)
-                  red_pair(&s_mlo[(size_t)f * NB + lb], &s_mhi[(size_t)f * NB + lb], wa[f],
+                  red_pair(&s_mlo[(size_t)f * NBm + lbm], &s_mhi[(size_t)f * NBm + lbm], wa[f],
                            wb[f], odd_lane);
               if (JK) {
                 // jk_check_PB (jk.cpp:64-71): the tile's region takes a same-region
@@ -827,10 +903,14 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             qhead += take;
             wbin += (unsigned)take;
             __syncwarp();
-            if (step >= nk && qtail == qhead) break;
+            if (pass >= W && qtail == qhead) break;
           }
           if (lane == 0 && wbin) atomicAdd(&s_nbin, wbin);
           wbin = 0;
+          __syncwarp();  // every lane is done with the staged slots before restaging
+          }
+#undef CPC_SET_ROW
+          // s_nbin complete before the next chunk's flush test
           __syncthreads();
         }
         k = g;
@@ -840,8 +920,8 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
 
     // ---- flush main, X and the last Y ----
     __syncthreads();
-    flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_nxnum, s_nxlo, s_nxhi, NB, wpi, npi, nrp,
-                                  n2_base, 1 + U.region, JK, f0, s_iqs, J);
+    flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_nxnum, s_nxlo, s_nxhi, NB, NBm, wpi, npi,
+                                  nrp, n2_base, 1 + U.region, JK, f0, s_iqs, J);
     if (JK && cur_y >= 0)
       flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y, f0,
                                  s_iqs, J);
