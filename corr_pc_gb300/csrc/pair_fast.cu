@@ -119,13 +119,16 @@ static_assert(jm_consistent<FieldMap<COREL_DD>>() && jm_consistent<FieldMap<CORE
 // 16 banks away from the low-word array.
 __host__ __device__ constexpr int hi_pad(int words) { return (16 - (words & 31) + 32) & 31; }
 
-// Replicas of the hot r_p bins.  Most pairs fall in the few largest r_p bins
-// (their count grows as r_p^2), so the lanes of one heavy-step instruction
-// often add into the same main-histogram bins, and same-address shared
-// reductions are serialised.  The top kHotBins r_p bins of the main histogram
-// therefore get kHotRep copies each, the copy picked by lane bits 1-2 (bit 0
-// already splits lanes over the low and high words); the flush adds the copies
-// together in exact integer arithmetic.
+// Replicas of the hot r_p bins (a build option, off by default).  Most pairs
+// fall in the few largest r_p bins (their count grows as r_p^2), so the lanes of
+// one heavy-step instruction often add into the same main-histogram bins, and
+// same-address shared reductions are serialised.  With CPC_HOT_REP > 1 the top
+// kHotBins r_p bins of the main histogram get kHotRep copies each, the copy
+// picked by lane bits 1-2 (bit 0 already splits lanes over the low and high
+// words), and the flush adds the copies together in exact integer arithmetic.
+// Measured on GB300: 4 copies of the top 4 bins gain 2% on the 200k wg+ box and
+// lose 3-4% on the kappa and ED workloads (the copies take shared memory from
+// the Pi window), so the default is one copy.
 #ifndef CPC_HOT_REP
 #define CPC_HOT_REP 1
 #endif
