@@ -767,6 +767,7 @@ cpc_status run_fast(std::vector<JobPlan> &jobs, int grow_attempt = 0);
 struct FastGroup {
   int corel, jk, minb, grid;
   size_t first, n_units, smem;
+  FastScales sc;
 };
 
 size_t accum_cells(const cpc_ctx *c) {
@@ -791,7 +792,8 @@ cpc_status fast_body(cpc_ctx *c0, std::vector<JobPlan> &jobs, const std::vector<
   for (const FastGroup &g : gs) {
     CK(cudaMemsetAsync(c0->d_unit_ctr.p, 0, sizeof(unsigned int), st), "memset");
     CK(launch_fast(g.corel, g.jk, g.minb, c0->d_jobs.p, c0->d_units.p + g.first, (int)g.n_units,
-                   c0->d_unit_ctr.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, g.smem, g.grid, st),
+                   c0->d_unit_ctr.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, g.sc, g.smem,
+                   g.grid, st),
        "fast kernel");
   }
   CK(cudaEventRecordWithFlags(c0->e2, st, rec_flags), "event");
@@ -831,6 +833,11 @@ std::vector<uint64_t> fast_graph_key(cpc_ctx *c0, const std::vector<JobPlan> &jo
     put(g.first);
     put(g.n_units);
     put(g.smem);
+    for (int f = 0; f < kNF; f++) {  // the scales are kernel parameters too
+      uint32_t b;
+      std::memcpy(&b, &g.sc.qs[f], sizeof b);
+      put(b);
+    }
   }
   return k;
 }
@@ -930,9 +937,19 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
   for (size_t g = 0; g < ranges.size(); g++) {
     const int corel = gkeys[g].first, jk = gkeys[g].second;
     size_t smem = 0;  // the largest any job of the group needs
+    FastScales sc;    // per field the smallest scale of the group's jobs
+    for (int f = 0; f < kNF; f++) {
+      sc.qs[f] = INFINITY;
+      sc.iqs[f] = 0.0;
+    }
     for (size_t k = ranges[g].first; k < ranges[g].second; k++) {
       const JobPlan &jp = jobs[all[k].job];
       smem = std::max(smem, fast_smem_bytes(corel, jk, jp.jd.nrp, jp.wpi));
+      for (int f = 0; f < kNF; f++)
+        if (jp.jd.qscale[f] < sc.qs[f]) {
+          sc.qs[f] = jp.jd.qscale[f];
+          sc.iqs[f] = jp.jd.inv_qscale[f];
+        }
     }
     int bps = 0;
     const int minb = fast_variant(corel, jk, smem, &bps);
@@ -940,7 +957,7 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
     const size_t n_units = ranges[g].second - ranges[g].first;
     if (n_units == 0) continue;
     const int grid = (int)std::min<int64_t>((int64_t)c0->sm_count * bps, (int64_t)n_units);
-    gs.push_back(FastGroup{corel, jk, minb, grid, ranges[g].first, n_units, smem});
+    gs.push_back(FastGroup{corel, jk, minb, grid, ranges[g].first, n_units, smem, sc});
   }
   return launch_fast_body(c0, jobs, gs);
 }

@@ -78,10 +78,19 @@ constexpr int kMaxCellsPerRmax = 9;
 size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi);
 size_t fast_static_smem_bytes();
 int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm);
+// Fixed-point scales of one fast-kernel launch (kernel parameters, read from
+// the constant bank): field f's terms are rint(v qs[f]), summed back with
+// iqs[f] = 1 / qs[f].  A launch over several jobs takes, per field, the smallest
+// of the jobs' scales (all powers of two), which keeps every job's terms within
+// their bound.
+struct FastScales {
+  float qs[kNF];
+  double iqs[kNF];
+};
 cudaError_t launch_fast(int corel, int jk, int minb, const JobDev *jobs, const UnitDesc *units,
                         int n_units, unsigned int *unit_ctr, QEntry *q,
-                        unsigned long long *qcount, unsigned long long qcap, size_t smem,
-                        int grid, cudaStream_t st);
+                        unsigned long long *qcount, unsigned long long qcap,
+                        const FastScales &sc, size_t smem, int grid, cudaStream_t st);
 cudaError_t launch_recheck(const JobDev *jobs, const QEntry *q, const unsigned long long *qcount,
                            unsigned long long qcap, int grid, cudaStream_t st);
 

@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(kThreads, MINB)
 fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ units,
                   int n_units, unsigned int *__restrict__ unit_ctr, QEntry *__restrict__ queue,
                   unsigned long long *__restrict__ qcount, unsigned long long qcap,
-                  int zero_words) {
+                  const __grid_constant__ FastScales sc, int zero_words) {
   using F = FieldMap<C>;
   extern __shared__ __align__(16) unsigned char smem[];
   float4 *s_pos = reinterpret_cast<float4 *>(smem);
@@ -355,8 +355,6 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   __shared__ unsigned long long s_red[kThreads / 32];
   __shared__ unsigned s_nbin;  // pairs queued by the block's warps since the last flush
   __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
-  __shared__ float s_qs[kNF];
-  __shared__ double s_iqs[kNF];
   // the tile's g1 rows, for the heavy step (any lane may process any row)
   __shared__ float4 s_rpos[kTile], s_rshp[kTile];
   __shared__ float2 s_rlo[kTile];
@@ -453,7 +451,6 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     const float mu_rel = J.mu_rel, mu_abs = J.mu_abs;
     for (int k = t; k < nrp; k += kThreads) { s_A[k] = J.A[k]; s_B[k] = J.B[k]; }
     for (int k = t; k < npi; k += kThreads) { s_PA[k] = J.PA[k]; s_PB[k] = J.PB[k]; }
-    if (t < kNF) { s_qs[t] = J.qscale[t]; s_iqs[t] = J.inv_qscale[t]; }
     const float l2rmin2 = J.l2rmin2, inv_lw = J.inv_lw, rej_lo = J.rej_lo, rej_hi = J.rej_hi;
     const int n2_base = U.n2_base;
     unsigned nwin = 0;  // window pairs of this thread's row in this unit
@@ -573,7 +570,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
           if (cur_y >= 0) {
             __syncthreads();
             flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
-                                       1 + cur_y, f0, s_iqs, J);
+                                       1 + cur_y, f0, sc.iqs, J);
             __syncthreads();
           }
           cur_y = region2;
@@ -589,11 +586,11 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
           if (s_nbin + (unsigned)(kTile * nc) > kFlushTerms) {  // keep every word below 2^32
             __syncthreads();
             flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_nxnum, s_nxlo, s_nxhi, NB, NBm,
-                                          wpi, npi, nrp, n2_base, 1 + U.region, JK, f0, s_iqs,
+                                          wpi, npi, nrp, n2_base, 1 + U.region, JK, f0, sc.iqs,
                                           J);
             if (JK && cur_y >= 0)
               flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
-                                         1 + cur_y, f0, s_iqs, J);
+                                         1 + cur_y, f0, sc.iqs, J);
             if (t == 0) s_nbin = 0u;
             __syncthreads();
           }
@@ -799,8 +796,10 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                 v[11] = __fdividef(dot * dot, see);
                 v[12] = v[11] * v[11];
               } else if (C != COREL_DD) {
-                const float4 e1v = s_rshp[er];
-                const float4 s2 = s_shp[ec];
+                // wg+ reads only the shape holder's (e1, e2) and the row's phi
+                // (8 + 4 bytes of shared memory); the other corels both rows'
+                const float4 e1v = C == COREL_SD ? make_float4(0.f, 0.f, 0.f, 0.f) : s_rshp[er];
+                const float4 s2 = C == COREL_SD ? make_float4(0.f, 0.f, 0.f, 0.f) : s_shp[ec];
                 const float a = dxr * dxr, b = dyr * dyr;
                 const float inv = __fdividef(1.0f, a + b);
                 const float c2 = (a - b) * inv, s2v = 2.0f * dxr * dyr * inv;
@@ -819,13 +818,16 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                     v[1] = v[5] = v[9] = 0.0f;
                   }
                 } else if (C == COREL_SD) {
-                  const float es0 = gws == 2 ? s2.x : e1v.x, es1 = gws == 2 ? s2.y : e1v.y;
+                  const float2 *eh = gws == 2 ? reinterpret_cast<const float2 *>(&s_shp[ec])
+                                              : reinterpret_cast<const float2 *>(&s_rshp[er]);
+                  const float2 e = *eh;
+                  const float es0 = e.x, es1 = e.y;
                   const float ep = c2 * es0 - s2v * es1, ex = s2v * es0 + c2 * es1;
                   v[1] = w * ep;
                   v[2] = v[1] * v[1];
                   v[3] = w * ex;
                   v[4] = v[3] * v[3];
-                  v[11] = ephi_f(e1v.z, theta);
+                  v[11] = ephi_f(s_rshp[er].z, theta);
                   v[12] = v[11] * v[11];
                 } else {
                   const float ei0 = c2 * e1v.x - s2v * e1v.y, ei1 = s2v * e1v.x + c2 * e1v.y;
@@ -863,7 +865,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               unsigned wa[F::FM], wb[F::FM];
 #pragma unroll
               for (int f = 0; f < F::FM; f++) {
-                const int u = to_fixed(v[F::m(f)], s_qs[F::m(f)]);
+                const int u = to_fixed(v[F::m(f)], sc.qs[F::m(f)]);
                 const unsigned a = (unsigned)u & 0x3FFFu, b = (unsigned)(u >> 14);
                 wa[f] = odd_lane ? b : a;
                 wb[f] = odd_lane ? a : b;
@@ -924,10 +926,10 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     // ---- flush main, X and the last Y ----
     __syncthreads();
     flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_nxnum, s_nxlo, s_nxhi, NB, NBm, wpi, npi,
-                                  nrp, n2_base, 1 + U.region, JK, f0, s_iqs, J);
+                                  nrp, n2_base, 1 + U.region, JK, f0, sc.iqs, J);
     if (JK && cur_y >= 0)
       flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y, f0,
-                                 s_iqs, J);
+                                 sc.iqs, J);
     if (t == 0) s_nbin = 0u;
     // window-pair counter (once per pair: mu slices other than the first skip it)
     {
@@ -995,6 +997,7 @@ struct LaunchFast {
   unsigned int *unit_ctr;
   QEntry *q;
   unsigned long long *qcount, qcap;
+  const FastScales *sc;
   size_t smem;
   int grid;
   cudaStream_t st;
@@ -1005,7 +1008,8 @@ struct LaunchFast {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
     const int zero_words = (int)((smem - sizeof(float4) * 2 * kBatch) / 4);
-    kern<<<grid, kThreads, smem, st>>>(jobs, units, n_units, unit_ctr, q, qcount, qcap, zero_words);
+    kern<<<grid, kThreads, smem, st>>>(jobs, units, n_units, unit_ctr, q, qcount, qcap, *sc,
+                                       zero_words);
     return cudaGetLastError();
   }
 };
@@ -1026,11 +1030,11 @@ struct Occupancy {
 
 cudaError_t launch_fast(int corel, int jk, int minb, const JobDev *jobs, const UnitDesc *units,
                         int n_units, unsigned int *unit_ctr, QEntry *q,
-                        unsigned long long *qcount, unsigned long long qcap, size_t smem,
-                        int grid, cudaStream_t st) {
+                        unsigned long long *qcount, unsigned long long qcap,
+                        const FastScales &sc, size_t smem, int grid, cudaStream_t st) {
   if (corel < COREL_DD || corel > COREL_ED) return cudaErrorInvalidValue;
   return dispatch(corel, jk, minb,
-                  LaunchFast{jobs, units, n_units, unit_ctr, q, qcount, qcap, smem, grid, st});
+                  LaunchFast{jobs, units, n_units, unit_ctr, q, qcount, qcap, &sc, smem, grid, st});
 }
 
 // The register-bound variant for this shared-memory size and its blocks per SM:
