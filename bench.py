@@ -127,17 +127,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _profile_traffic(workload: str):
-    """DRAM bytes per launch of the fast kernel (dram__bytes_read.sum +
-    dram__bytes_write.sum) from the committed ncu summary of this workload."""
+def _profile_value(workload: str, key: str):
+    """A figure of the committed ncu summary of the fast kernel on this workload
+    (a table row "| key | value |")."""
     path = os.path.join(ROOT, "profiles", f"fast_pairs_kernel_{workload}.md")
     try:
         for line in open(path):
-            if line.startswith("| traffic_bytes_per_launch |"):
+            if line.startswith(f"| {key} |"):
                 return float(line.split("|")[2])
-    except OSError:
+    except (OSError, ValueError):
         pass
     return None
+
+
+def _profile_traffic(workload: str):
+    """DRAM bytes per launch of the fast kernel (dram__bytes_read.sum +
+    dram__bytes_write.sum) from the committed ncu summary of this workload."""
+    return _profile_value(workload, "traffic_bytes_per_launch")
 
 
 def _hbm_peak():
@@ -560,6 +566,18 @@ def main() -> None:
                                  "frac": achieved_atom / peaks["smem_atomic_u32_ops"]
                                  if peaks["smem_atomic_u32_ops"] else None},
                 "hbm": hbm}
+    wl_name = _describe(wls)["workload"]
+    pipe = _profile_value(wl_name, "shared_pipe_wavefronts_pct_of_peak")
+    if pipe is not None:
+        # the resource that binds the kernel, measured by ncu on this workload:
+        # shared-memory wavefronts (histogram reductions scattered over the 32
+        # banks, plus the staged-candidate and row loads) and instruction issue
+        roofline["binding"] = {
+            "resource": "shared-memory pipe (wavefronts) and instruction issue",
+            "shared_pipe_frac": pipe / 100.0,
+            "issue_active_frac": (_profile_value(wl_name, "issue_active_pct") or float("nan")) / 100.0,
+            "wavefronts_per_binned_pair": _profile_value(wl_name, "shared_wavefronts_per_binned_pair"),
+            "source": f"ncu --set full, profiles/fast_pairs_kernel_{wl_name}.md"}
     # plain FP64 GPU kernel on a bounded row sample of the same workload
     fp64 = None
     if len(ctxs) == 1:

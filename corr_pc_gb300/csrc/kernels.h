@@ -67,7 +67,7 @@ unsigned long long orderable_key(double v);
 double from_orderable_key(unsigned long long k);
 
 // pair_fast.cu
-constexpr int kTileThreads = 128;  // g1 rows per tile (the block has 2 warp groups over them)
+constexpr int kTileThreads = 128;  // g1 rows per tile (a warp tests them in passes of 32)
 constexpr int kFastBlocksPerSM = 4;  // occupancy target: registers and shared memory sized for it
 // Per work unit: at most kFastMaxCols neighbour columns (the host rejects units
 // with more; (2k + 3)^2 columns for cells r_max / k wide, so k <= 9) and

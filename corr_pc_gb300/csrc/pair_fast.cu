@@ -3,12 +3,13 @@
 // One persistent launch drains a device work queue of "units".  A unit is a
 // tile of up to kTile g1 rows from one (column, jackknife region) bucket and
 // z-chunk, paired with every g2 candidate of the neighbouring columns inside
-// the unit's shifted-z range.  A block of 256 threads holds the tile's rows
-// in several warp groups (one row per lane; the lanes of a warp are spread over
-// the tile) and the groups split each staged batch of 256 candidates; a tile
-// of up to 32 W rows is held by 8 / W groups of W warps.  Batches
-// are drawn as a coprime-stride permutation of the (partner region, image
-// shift) group, so simultaneous pairs of a warp fall in different bins.
+// the unit's shifted-z range.  A block of 8 warps keeps the tile's rows in
+// shared memory; each warp stages its own batches of up to 32 candidates and
+// tests them against every row, in W passes of 32 rows for a tile of up to
+// 32 W rows (one row per lane; the lanes of a warp are spread over the tile).
+// Candidates are drawn in chunks of a coprime-stride permutation of the
+// (partner region, image shift) group, so simultaneous pairs of a warp fall in
+// different bins; the block meets at a barrier once per chunk.
 //
 // Light pass (every candidate): FP32 separations with the image shift applied
 // exactly, definite in / definite out tests of the reference's window, r^2
@@ -41,9 +42,8 @@
 namespace cpc {
 
 constexpr int kTile = kTileThreads;          // g1 rows per tile
-constexpr int kGroups = 2;                    // warp groups sharing the rows
-constexpr int kThreads = kTile * kGroups;     // block size
-constexpr int kBatch = kThreads;              // candidates staged per batch
+constexpr int kThreads = 256;                 // block size: 8 warps
+constexpr int kBatch = kThreads;              // staging slots: 32 per warp
 constexpr int kMaxSeg = kFastMaxSeg;
 constexpr int kMaxCols = kFastMaxCols;
 // candidates of a group per block barrier: a chunk adds at most kTile * kChunk
@@ -171,8 +171,8 @@ size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi) {
 // (-2^12..2^12), each added to its own 32-bit word with a plain reduction (no
 // return value: no scoreboard wait; lanes of one instruction that hit the same
 // word are serialised, which red_pair halves).  A block counts the pairs its
-// warps queued since the last flush and flushes before a batch that could take
-// the count past 2^18 (a batch adds at most kTile * kBatch pairs), so a bin takes
+// warps queued since the last flush and flushes before a chunk that could take
+// the count past 2^18 (a chunk adds at most kTile * kChunk pairs), so a bin takes
 // at most 2^18 terms between flushes: the low word stays below 2^32 and the high
 // word, read as a signed integer, within +-2^30.
 constexpr unsigned kFlushTerms = 1u << 18;
@@ -489,7 +489,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     __syncthreads();
     const int total_slots = s_cnt[ncol];
     int cur_y = -1;        // region held in the Y histogram
-    unsigned wbin = 0;     // pairs this warp queued in the current batch
+    unsigned wbin = 0;     // pairs this warp queued in its current batch
 
     for (int chunk0 = 0; chunk0 < total_slots; chunk0 += kMaxSeg) {
       const int nslot = min(kMaxSeg, total_slots - chunk0);
