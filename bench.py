@@ -174,7 +174,8 @@ def _cpu_sample(p, cats, budget_s: float, n_binned_full: int, threads: int, offs
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # the CPU baseline (test infrastructure)
     ocats = {r: oracle.OracleCatalog(c.x, c.y, c.z, w=c.w, e1=c.e1, e2=c.e2, phi=c.phi,
-                                      jk=c.jk, jk_prob=c.jk_prob, include_prob=c.include_prob)
+                                      jk=c.jk, jk_prob=c.jk_prob, include_prob=c.include_prob,
+                                      e3=getattr(c, "e3", None))
              for r, c in cats.items()}
     rate_guess = 4e6 * threads  # binned pairs/s on one ARM/x86 core, rough
     stride = max(1, int(n_binned_full / (rate_guess * budget_s)))
