@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -623,6 +624,13 @@ cpc_status ensure_scratch(cpc_ctx *c, size_t n_units, size_t n_jobs) {
   CK(c->d_qcount.alloc(1), "alloc queue counter");
   if (!c->d_queue.p) {
     c->qcap = CPC_EDGE_QUEUE_INIT;
+    // CPC_EDGE_QUEUE_INIT in the environment (a positive entry count) starts the
+    // context with another capacity: tests use a small one to drive the overflow
+    // path (grow, count again)
+    if (const char *ev = std::getenv("CPC_EDGE_QUEUE_INIT")) {
+      const long long v = std::atoll(ev);
+      if (v > 0) c->qcap = (unsigned long long)v;
+    }
     cudaError_t e = c->d_queue.alloc(c->qcap);
     if (e != cudaSuccess) {
       cudaGetLastError();

@@ -80,3 +80,37 @@ def test_batch_replays_match_oracle():
             assert np.array_equal(r["num"], num)
             check_sums(r["sums"], sums, label=f"batch replay {rep}")
     assert ctxs[0].graph_stats() == (1, 2)
+
+
+def test_new_scales_capture_again():
+    """The fixed-point scales are kernel parameters: catalogues with other
+    ellipticity bounds must not replay a graph made for the old ones."""
+    g = Golden("box_wgp_clustered")
+    ctx = _ctx_for(g.params, g.S, g.D)
+    _check(ctx.count("SD", 0, 1), g, "first")
+    half = lambda c: synth.Catalog(c.x, c.y, c.z, c.w,
+                                   None if c.e1 is None else 0.37 * np.asarray(c.e1),
+                                   None if c.e2 is None else 0.37 * np.asarray(c.e2), c.jk, c.e3)
+    S2, D2 = half(g.S), half(g.D)
+    cats = host.prepare(g.params, [("S", S2), ("D", D2)])
+    ctx.upload(0, cats["D"])
+    ctx.upload(1, cats["S"])
+    r = ctx.count("SD", 0, 1)
+    assert ctx.graph_stats()[0] == 2
+    oc = oracle.read_like_reference(g.params, [("S", S2), ("D", D2)])
+    num, sums, n_total, n_in = oracle.port_corels2(g.params, "SD", oc["D"], oc["S"])
+    assert r["n_binned"] == n_in and r["n_window"] == n_total
+    assert np.array_equal(r["num"], num)
+    check_sums(r["sums"], sums, label="scaled shapes")
+
+
+def test_edge_queue_growth_counts_again(monkeypatch):
+    """A context that starts with a 16-entry edge queue overflows it, grows it,
+    counts again (a new graph) and still gives the reference's results."""
+    g = Golden("box_lattice_edges")
+    monkeypatch.setenv("CPC_EDGE_QUEUE_INIT", "16")
+    ctx = _ctx_for(g.params, g.S, g.D)
+    r = ctx.count("SD", 0, 1)
+    assert r["n_rechecked"] > 16
+    _check(r, g, "grown queue")
+    _check(ctx.count("SD", 0, 1), g, "grown queue, replay")
