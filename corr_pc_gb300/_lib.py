@@ -97,6 +97,7 @@ def load() -> ctypes.CDLL:
     lib.cpc_host_pi_thresholds.argtypes = [P(cpc_params), V]
     lib.cpc_launch_count.argtypes = [V, P(I64)]
     lib.cpc_set_graph_replay.argtypes = [V, I]
+    lib.cpc_set_shard.argtypes = [V, I, I]
     lib.cpc_graph_stats.argtypes = [V, P(I64), P(I64)]
     lib.cpc_host_finalize_cross.argtypes = [ctypes.c_char_p] + [V] * 9
     lib.cpc_host_finalize_auto.argtypes = [ctypes.c_char_p] + [V] * 7
@@ -110,7 +111,7 @@ def load() -> ctypes.CDLL:
                "cpc_count_batch", "cpc_set_tuning", "cpc_host_rand_uniform",
                "cpc_host_elip_angle", "cpc_host_rp_thresholds", "cpc_host_pi_thresholds",
                "cpc_launch_count", "cpc_host_finalize_cross", "cpc_set_graph_replay",
-               "cpc_graph_stats"):
+               "cpc_graph_stats", "cpc_set_shard"):
         getattr(lib, fn).restype = I
     _lib = lib
     return lib
@@ -225,6 +226,11 @@ class Context:
         v = ctypes.c_int64()
         check(self.lib.cpc_launch_count(self.h, ctypes.byref(v)), self.h)
         return v.value
+
+    def set_shard(self, shard: int, n_shards: int) -> None:
+        """Count only the work units i with i % n_shards == shard (fast box
+        engine); the shards' raw blocks sum to the whole count."""
+        check(self.lib.cpc_set_shard(self.h, shard, n_shards), self.h)
 
     def set_graph_replay(self, enable: bool) -> None:
         """Replay fast counts from a captured CUDA graph (default) or launch

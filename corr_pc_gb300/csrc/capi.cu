@@ -159,6 +159,8 @@ struct cpc_ctx {
   int64_t launches = 0;  // kernels launched by this context (all entry points)
   // CUDA graph of the fast engine's device work (zeroing, pair kernels,
   // recheck), replayed while every value baked into it stays the same
+  // work-unit shard of the fast box engine (cpc_set_shard)
+  int shard = 0, n_shards = 1;
   int graph_on = 1;
   cudaGraphExec_t gexec = nullptr;
   std::vector<uint64_t> gkey;
@@ -922,7 +924,12 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
     const size_t b = all.size();
     for (int k : g.second) {
       const std::vector<UnitDesc> &u = build_units(jobs[k]);
-      for (UnitDesc d : u) {
+      // this context's shard of the units (cpc_set_shard): every n_shards-th
+      // unit from `shard`; the units partition the pairs, so the shards' blocks
+      // sum to the whole count
+      const int nsh = jobs[k].c->n_shards, sh = jobs[k].c->shard;
+      for (size_t ui = (size_t)sh; ui < u.size(); ui += (size_t)nsh) {
+        UnitDesc d = u[ui];
         d.job = k;
         const int64_t ncol = (int64_t)(d.cx_hi - d.cx_lo + 1) * (d.cy_hi - d.cy_lo + 1);
         if (ncol < 1 || ncol > kFastMaxCols || d.g1_count < 1 || d.g1_count > kTileThreads)
@@ -1917,6 +1924,16 @@ cpc_status cpc_host_rp_thresholds(const cpc_params *p, double *thr) {
   if (p->n_bins <= 0 || p->n_bins > kMaxRp) return fail(nullptr, CPC_ERR_INVALID, "n_bins out of range");
   const int rc = rp_thresholds(p->lin_bin, p->n_bins, p->bin_r_min, p->bin_r_max, thr);
   return rc == 0 ? CPC_OK : fail(nullptr, CPC_ERR_INVALID, "threshold derivation failed");
+}
+
+cpc_status cpc_set_shard(cpc_ctx *c, int shard, int n_shards) {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (busy(c)) return CPC_ERR_STATE;
+  if (n_shards < 1 || shard < 0 || shard >= n_shards)
+    return fail(c, CPC_ERR_INVALID, "shard must satisfy 0 <= shard < n_shards");
+  c->shard = shard;
+  c->n_shards = n_shards;
+  return CPC_OK;
 }
 
 cpc_status cpc_set_graph_replay(cpc_ctx *c, int enable) {

@@ -207,6 +207,19 @@ cpc_status cpc_set_tuning(cpc_ctx *ctx, int cells_per_rmax, int pi_window, int t
 cpc_status cpc_autotune(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_g2,
                         int64_t sample_stride, int *cells_per_rmax, int *pi_window);
 
+/* Work sharding over GPUs (replaces the reference's division of the outer
+ * rows over OpenMP threads, corr.cpp:299-302 and 329-424): later
+ * fast-engine box counts on ctx (cpc_count, cpc_count_async, cpc_count_auto,
+ * cpc_count_batch) process only the work units i with i % n_shards == shard.
+ * A unit is a tile of outer rows against one slice of its candidates, and the
+ * units partition the pairs, so the RAW blocks of shards 0 .. n_shards-1 (one
+ * per GPU, each on its own context with the same catalogues) sum to the whole
+ * count: counts exactly, sums up to the order of FP64 additions.  Unlike
+ * row_stride, whose skipped rows still pass through every unit, each shard does
+ * about 1/n_shards of the work.  Sky counts and the FP64 engine shard by rows
+ * (row_stride / row_offset), which they skip cheaply.  Default: shard 0 of 1. */
+cpc_status cpc_set_shard(cpc_ctx *ctx, int shard, int n_shards);
+
 /* Number of GPU kernels this context has launched so far (all entry points;
  * for a batch, counted on the first job's context). */
 cpc_status cpc_launch_count(const cpc_ctx *ctx, int64_t *launches);

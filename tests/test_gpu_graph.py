@@ -114,3 +114,30 @@ def test_edge_queue_growth_counts_again(monkeypatch):
     assert r["n_rechecked"] > 16
     _check(r, g, "grown queue")
     _check(ctx.count("SD", 0, 1), g, "grown queue, replay")
+
+
+@pytest.mark.parametrize("name", ["box_wgp_clustered", "box_wpp_weighted_distinct"])
+def test_unit_shards_sum_to_the_whole_count(name):
+    """Three contexts, each counting one shard of the work units (as three GPUs
+    would): the raw blocks add up to the reference's."""
+    g = Golden(name)
+    parts = []
+    for sh in range(3):
+        ctx = _ctx_for(g.params, g.S, g.D)
+        ctx.set_shard(sh, 3)
+        parts.append(ctx.count("SD", 0, 1))
+        ctx.close()
+    assert all(0 < p["n_binned"] < g.n_in for p in parts)
+    assert sum(p["n_binned"] for p in parts) == g.n_in
+    assert sum(p["n_window"] for p in parts) == g.n_total
+    assert np.array_equal(sum(p["num"] for p in parts), g.raw_num)
+    check_sums(sum(p["sums"] for p in parts), g.raw_sums, label=f"{name} shards")
+
+
+def test_bad_shard_is_rejected():
+    g = Golden("box_wgp_clustered")
+    ctx = _ctx_for(g.params, g.S, g.D)
+    with pytest.raises(_lib.CpcError):
+        ctx.set_shard(3, 3)
+    with pytest.raises(_lib.CpcError):
+        ctx.set_shard(0, 0)

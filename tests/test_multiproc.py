@@ -1,7 +1,10 @@
 """Two processes (gloo, CPU) each count half of the outer rows and reduce the
 raw blocks: the sum equals the single-process count.  The per-rank counter
-here is the oracle, so the test runs without a GPU; on GPUs each rank calls
-cpc_count with the same (row_stride, row_offset)."""
+here is the oracle, so the test runs without a GPU; on GPUs each rank counts
+its shard of the fast engine's work units (cpc_set_shard) or, for the sky and
+FP64 engines, the same (row_stride, row_offset) of rows -- the GPU test
+test_gpu_graph.py::test_unit_shards_sum_to_the_whole_count covers the unit
+shards on one GPU."""
 import os
 import sys
 
