@@ -201,3 +201,37 @@ def test_auto_finalisation_matches_reference_files(name, tmp_path):
         if fname.endswith(".info"):
             continue
         compare_files(open(p.out_file + fname).read(), ref, label=f"{name}:{fname}")
+
+
+def test_integration_binding_links_into_the_reference():
+    """The corels2/corels1 binding of INTEGRATION.md compiles against the
+    reference's own headers and links, with the reference's objects (its pair
+    loops renamed away) and main.cpp, into a corr_pc executable that calls this
+    library (built here, not run: it needs a GPU)."""
+    import shutil
+    import subprocess
+    if not os.path.isdir("/root/reference") or shutil.which("g++") is None:
+        pytest.skip("reference sources not present on this host")
+    from corr_pc_gb300 import build as b
+    if not os.path.exists(b.LIB):
+        pytest.skip("library not built")
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    start = text.index("```cpp\n") + len("```cpp\n")
+    code = text[start:text.index("```", start)]
+    odir = os.path.join(ROOT, "oracle", "_ref")
+    os.makedirs(odir, exist_ok=True)
+    src = os.path.join(odir, "corr_gpu.cpp")
+    with open(src, "w") as f:
+        f.write(code)
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "drop_in",
+                        f"BINDING={src}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    exe = os.path.join(odir, "corr_pc_gpu")
+    syms = subprocess.run(["nm", "-C", exe], capture_output=True, text=True).stdout
+    # the binding's corels2/corels1 are the ones do_corr calls; the reference's
+    # CPU loops are still there under their new names
+    for name in ("corels2(gal*, gal*, bin_jk&, data_info&)", "corels1(gal*, bin_jk&, data_info&)",
+                 "corels2_cpu", "corels1_cpu"):
+        assert name in syms, name
+    needed = subprocess.run(["readelf", "-d", exe], capture_output=True, text=True).stdout
+    assert "libcorrpc_gb300.so" in needed
