@@ -12,6 +12,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -190,6 +191,24 @@ cpc_status cuda_fail(cpc_ctx *c, cudaError_t e, const char *where) {
   } while (0)
 
 // float ULP at magnitude v (v > 0)
+// Run f(begin, end, part) over [0, n) in contiguous chunks on the host's cores
+// (one chunk per thread, at least 16384 rows each; in the calling thread when
+// n is small).  f must not throw.
+template <class F>
+void host_parallel(int64_t n, F &&f) {
+  const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const int T = (int)std::max<int64_t>(1, std::min<int64_t>({hw, 64, n / 16384}));
+  if (T <= 1) {
+    f((int64_t)0, n, 0);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(T);
+  for (int t = 0; t < T; t++)
+    th.emplace_back([&f, n, t, T] { f(n * t / T, n * (t + 1) / T, t); });
+  for (auto &x : th) x.join();
+}
+
 double ulpf(double v) {
   if (!(v > 0)) return std::ldexp(1.0, -149);
   int ex;
@@ -1204,50 +1223,86 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   std::vector<int32_t> jk(n, 0);
   std::vector<uint8_t> keep(n, 0);
   s.has_e = cat->e1 && cat->e2;
+  // per row, on the host's cores: the read-path checks (the first failing row
+  // in input order is reported), the statistics that size the fixed-point
+  // scales, the angles and the lim_calc_sky window with the C library
+  struct Part {
+    int64_t bad = -1;
+    std::string msg;
+    double wmax = 0, wmin = 1e300, emax = 0, phimax = 0;
+  };
+  const int kMaxParts = 64;
+  std::vector<Part> parts(kMaxParts);
+  host_parallel(n, [&](int64_t b0, int64_t b1, int part) {
+    Part &P = parts[part];
+    for (int64_t i = b0; i < b1; i++) {
+      auto bad = [&](const std::string &m) {
+        P.bad = i;
+        P.msg = m;
+      };
+      const double ra = cat->x[i], dec = cat->y[i], z = cat->z[i];
+      if (!std::isfinite(ra) || !std::isfinite(dec) || !std::isfinite(z) ||
+          !std::isfinite(cat->dc[i]) || !std::isfinite(cat->da[i])) {
+        bad("non-finite position or distance at row " + std::to_string(i));
+        return;
+      }
+      if (z < 0 || z > p.z_max) {  // read_dat.cpp:228-234
+        bad("redshift outside [0, z_max] at row " + std::to_string(i));
+        return;
+      }
+      if (cat->w) {
+        if (!std::isfinite(cat->w[i])) { bad("non-finite weight"); return; }
+        w[i] = cat->w[i];
+      }
+      if (s.has_e) {
+        if (!std::isfinite(cat->e1[i]) || !std::isfinite(cat->e2[i])) {
+          bad("non-finite ellipticity");
+          return;
+        }
+        e1[i] = cat->e1[i];
+        e2[i] = cat->e2[i];
+      }
+      if (cat->phi) {
+        if (!std::isfinite(cat->phi[i])) { bad("non-finite phi"); return; }
+        phi[i] = cat->phi[i];
+      }
+      if (p.do_jk) {
+        const int r = cat->jk[i];
+        if (r < 0 || r >= p.n_jk) {
+          bad("jackknife label out of range at row " + std::to_string(i));
+          return;
+        }
+        jk[i] = r;
+      }
+      if (cat->jk_prob) keep[i] = cat->jk_prob[i] >= 0.5 ? 1 : 0;
+      P.wmax = std::max(P.wmax, std::fabs(w[i]));
+      P.wmin = std::min(P.wmin, w[i]);
+      P.emax = std::max(P.emax, std::max(std::fabs(e1[i]), std::fabs(e2[i])));
+      P.phimax = std::max(P.phimax, std::fabs(phi[i]));
+      sky_angles(ra, dec, &rar[i], &decr[i], &sd[i], &cd[i]);
+      double wv[6];
+      const int rc = sky_window(sp, ra, dec, z, wv);
+      if (rc == 1) {  // lim_calc_ra_dec exits the program here (sky_calcs.cpp:109-113)
+        bad("window z_min above z_max at row " + std::to_string(i));
+        return;
+      }
+      if (rc == 2) {
+        bad("distance table too short for the window of row " + std::to_string(i));
+        return;
+      }
+      for (int q = 0; q < 6; q++) win[(size_t)q * n + i] = wv[q];
+    }
+  });
   s.wmax = 0;
   s.wmin = n > 0 ? 1e300 : 1.0;
   s.emax = 0;
   s.phimax = 0;
-  for (int64_t i = 0; i < n; i++) {
-    const double ra = cat->x[i], dec = cat->y[i], z = cat->z[i];
-    if (!std::isfinite(ra) || !std::isfinite(dec) || !std::isfinite(z) ||
-        !std::isfinite(cat->dc[i]) || !std::isfinite(cat->da[i]))
-      return fail(c, CPC_ERR_RANGE, "non-finite position or distance at row " + std::to_string(i));
-    if (z < 0 || z > p.z_max)  // read_dat.cpp:228-234
-      return fail(c, CPC_ERR_RANGE, "redshift outside [0, z_max] at row " + std::to_string(i));
-    if (cat->w) {
-      if (!std::isfinite(cat->w[i])) return fail(c, CPC_ERR_RANGE, "non-finite weight");
-      w[i] = cat->w[i];
-    }
-    if (s.has_e) {
-      if (!std::isfinite(cat->e1[i]) || !std::isfinite(cat->e2[i]))
-        return fail(c, CPC_ERR_RANGE, "non-finite ellipticity");
-      e1[i] = cat->e1[i];
-      e2[i] = cat->e2[i];
-    }
-    if (cat->phi) {
-      if (!std::isfinite(cat->phi[i])) return fail(c, CPC_ERR_RANGE, "non-finite phi");
-      phi[i] = cat->phi[i];
-    }
-    if (p.do_jk) {
-      const int r = cat->jk[i];
-      if (r < 0 || r >= p.n_jk)
-        return fail(c, CPC_ERR_RANGE, "jackknife label out of range at row " + std::to_string(i));
-      jk[i] = r;
-    }
-    if (cat->jk_prob) keep[i] = cat->jk_prob[i] >= 0.5 ? 1 : 0;
-    s.wmax = std::max(s.wmax, std::fabs(w[i]));
-    s.wmin = std::min(s.wmin, w[i]);
-    s.emax = std::max(s.emax, std::max(std::fabs(e1[i]), std::fabs(e2[i])));
-    s.phimax = std::max(s.phimax, std::fabs(phi[i]));
-    sky_angles(ra, dec, &rar[i], &decr[i], &sd[i], &cd[i]);
-    double wv[6];
-    const int rc = sky_window(sp, ra, dec, z, wv);
-    if (rc == 1)  // lim_calc_ra_dec exits the program here (sky_calcs.cpp:109-113)
-      return fail(c, CPC_ERR_RANGE, "window z_min above z_max at row " + std::to_string(i));
-    if (rc == 2)
-      return fail(c, CPC_ERR_RANGE, "distance table too short for the window of row " + std::to_string(i));
-    for (int q = 0; q < 6; q++) win[(size_t)q * n + i] = wv[q];
+  for (const Part &P : parts) {  // chunks are in input order: the first bad row
+    if (P.bad >= 0) return fail(c, CPC_ERR_RANGE, P.msg);
+    s.wmax = std::max(s.wmax, P.wmax);
+    s.wmin = std::min(s.wmin, P.wmin);
+    s.emax = std::max(s.emax, P.emax);
+    s.phimax = std::max(s.phimax, P.phimax);
   }
   // redshift order (stable: ties keep the input order)
   cudaStream_t st = c->st;
@@ -1272,7 +1327,9 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   }
   auto take = [&](const double *src, std::vector<double> &dst) {
     dst.resize(n);
-    for (int64_t k = 0; k < n; k++) dst[k] = src[perm[k]];
+    host_parallel(n, [&](int64_t b0, int64_t b1, int) {
+      for (int64_t k = b0; k < b1; k++) dst[k] = src[perm[k]];
+    });
   };
   std::vector<double> zs, sds, cds, rars, decrs;
   take(cat->x, s.hs_ra);
@@ -1293,15 +1350,17 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   std::vector<int64_t> orig(n);
   std::vector<double> wins(6 * (size_t)n);
   std::vector<uint8_t> aflag(n);
-  for (int64_t k = 0; k < n; k++) {
-    const uint32_t o = perm[k];
-    s.hs_jk[k] = jk[o];
-    s.hs_keep[k] = keep[o];
-    orig[k] = o;
-    for (int q = 0; q < 6; q++) wins[(size_t)q * n + k] = win[(size_t)q * n + o];
-    // corels1 scan start: row o + 1 (input order) against z_min of row o
-    aflag[k] = (o + 1 < (uint32_t)n && !(cat->z[o + 1] < win[o])) ? kAutoStart0 : 0;
-  }
+  host_parallel(n, [&](int64_t b0, int64_t b1, int) {
+    for (int64_t k = b0; k < b1; k++) {
+      const uint32_t o = perm[k];
+      s.hs_jk[k] = jk[o];
+      s.hs_keep[k] = keep[o];
+      orig[k] = o;
+      for (int q = 0; q < 6; q++) wins[(size_t)q * n + k] = win[(size_t)q * n + o];
+      // corels1 scan start: row o + 1 (input order) against z_min of row o
+      aflag[k] = (o + 1 < (uint32_t)n && !(cat->z[o + 1] < win[o])) ? kAutoStart0 : 0;
+    }
+  });
   auto put = [&](DevBuf<double> &d, const std::vector<double> &h, size_t cnt) -> cudaError_t {
     cudaError_t e = d.alloc(std::max<size_t>(cnt, 1));
     if (e != cudaSuccess || cnt == 0) return e;
@@ -1318,17 +1377,21 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   std::vector<float4> su(n), sl(n), sw(n), sx(n), ss(n);
   auto hi = [](double v) { return (float)v; };
   auto lo = [](double v) { return (float)(v - (double)(float)v); };
+  std::vector<double> dcm(kMaxParts, 0.0);
+  host_parallel(n, [&](int64_t b0, int64_t b1, int part) {
+    for (int64_t k = b0; k < b1; k++) {
+      const double ux = cds[k] * std::cos(rars[k]), uy = cds[k] * std::sin(rars[k]), uz = sds[k];
+      const double dcv = s.hs_dc[k];
+      dcm[part] = std::max(dcm[part], std::fabs(dcv));
+      su[k] = make_float4(hi(ux), hi(uy), hi(uz), (float)s.hs_da[k]);
+      sl[k] = make_float4(lo(ux), lo(uy), lo(uz), lo(dcv));
+      sw[k] = make_float4(hi(s.hs_ra[k]), hi(s.hs_dec[k]), (float)zs[k], hi(dcv));
+      sx[k] = make_float4(lo(s.hs_ra[k]), lo(s.hs_dec[k]), (float)decrs[k], (float)s.hs_w[k]);
+      ss[k] = make_float4((float)s.hs_e1[k], (float)s.hs_e2[k], (float)s.hs_phi[k], 0.f);
+    }
+  });
   s.dcmax = 0;
-  for (int64_t k = 0; k < n; k++) {
-    const double ux = cds[k] * std::cos(rars[k]), uy = cds[k] * std::sin(rars[k]), uz = sds[k];
-    const double dcv = s.hs_dc[k];
-    s.dcmax = std::max(s.dcmax, std::fabs(dcv));
-    su[k] = make_float4(hi(ux), hi(uy), hi(uz), (float)s.hs_da[k]);
-    sl[k] = make_float4(lo(ux), lo(uy), lo(uz), lo(dcv));
-    sw[k] = make_float4(hi(s.hs_ra[k]), hi(s.hs_dec[k]), (float)zs[k], hi(dcv));
-    sx[k] = make_float4(lo(s.hs_ra[k]), lo(s.hs_dec[k]), (float)decrs[k], (float)s.hs_w[k]);
-    ss[k] = make_float4((float)s.hs_e1[k], (float)s.hs_e2[k], (float)s.hs_phi[k], 0.f);
-  }
+  for (double v : dcm) s.dcmax = std::max(s.dcmax, v);
   DevBuf<float4> *fbufs[5] = {&s.sky_su, &s.sky_sl, &s.sky_sw, &s.sky_sx, &s.sky_ss};
   const std::vector<float4> *fsrc[5] = {&su, &sl, &sw, &sx, &ss};
   for (int q = 0; q < 5; q++) {
