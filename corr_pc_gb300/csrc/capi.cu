@@ -192,12 +192,12 @@ cpc_status cuda_fail(cpc_ctx *c, cudaError_t e, const char *where) {
 
 // float ULP at magnitude v (v > 0)
 // Run f(begin, end, part) over [0, n) in contiguous chunks on the host's cores
-// (one chunk per thread, at least 16384 rows each; in the calling thread when
-// n is small).  f must not throw.
+// (one chunk per thread, part < 64, at least min_chunk items each; in the
+// calling thread when n is small).  f must not throw.
 template <class F>
-void host_parallel(int64_t n, F &&f) {
+void host_parallel(int64_t n, F &&f, int64_t min_chunk = 16384) {
   const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
-  const int T = (int)std::max<int64_t>(1, std::min<int64_t>({hw, 64, n / 16384}));
+  const int T = (int)std::max<int64_t>(1, std::min<int64_t>({hw, 64, n / min_chunk}));
   if (T <= 1) {
     f((int64_t)0, n, 0);
     return;
@@ -571,70 +571,80 @@ const std::vector<UnitDesc> &build_units(JobPlan &jp) {
   std::vector<UnitDesc> &units = uc.units;
   units.clear();
   const int nb = (int)g1.h_bk_start.size();
-  for (int b = 0; b < nb; b++) {
-    const int s = g1.h_bk_start[b], e = g1.h_bk_end[b];
-    int i = s;
-    while (i < e) {
-      // z-chunk of extent <= Emax, dealt round-robin into tiles of <= tile rows
-      const float z0 = g1.h_pos[i].z;
-      int j = i;
-      float bx0 = INFINITY, bx1 = -INFINITY, by0 = INFINITY, by1 = -INFINITY;
-      while (j < e && (double)g1.h_pos[j].z - z0 <= Emax) {
-        bx0 = std::min(bx0, g1.h_pos[j].x);
-        bx1 = std::max(bx1, g1.h_pos[j].x);
-        by0 = std::min(by0, g1.h_pos[j].y);
-        by1 = std::max(by1, g1.h_pos[j].y);
-        j++;
-      }
-      const int m = j - i;
-      const int nt = (m + jp.tile - 1) / jp.tile;
-      const double zt0 = g1.h_pos[i].z, zt1 = g1.h_pos[j - 1].z;
-      const double rg = p.bin_r_max + guard;
-      int cx0 = (int)std::floor((bx0 - rg) * inv_cwx), cx1 = (int)std::floor((bx1 + rg) * inv_cwx);
-      int cy0 = (int)std::floor((by0 - rg) * inv_cwy), cy1 = (int)std::floor((by1 + rg) * inv_cwy);
-      if (p.periodic_box) {
-        cx0 = std::max(cx0, -ncx); cx1 = std::min(cx1, 2 * ncx - 1);
-        cy0 = std::max(cy0, -ncy); cy1 = std::min(cy1, 2 * ncy - 1);
-      } else {
-        cx0 = std::max(cx0, 0); cx1 = std::min(cx1, ncx - 1);
-        cy0 = std::max(cy0, 0); cy1 = std::min(cy1, ncy - 1);
-      }
-      const double Zlo = zt0 + zw0 - guard, Zhi = zt1 + zw1 + guard;
-      for (int k = 0; k < nt; k++) {
-        UnitDesc u;
-        std::memset(&u, 0, sizeof u);
-        u.g1_start = i + k;
-        u.g1_stride = nt;
-        u.g1_count = (m - k + nt - 1) / nt;
-        u.region = g1.h_bk_region[b];
-        u.cx_lo = cx0; u.cx_hi = cx1; u.cy_lo = cy0; u.cy_hi = cy1;
-        if (wpi >= npi || rmu) {
-          // coordinates 7: one unit per slice of wpi mu bins; each pair is
-          // taken by the slice holding its estimated bin (pair_fast.cu)
-          u.zlo = Zlo;
-          u.zhi = Zhi;
-          for (int base = 0; base < npi; base += wpi) {
-            u.n2_base = base;
-            units.push_back(u);
-          }
+  // buckets are independent: contiguous bucket ranges on the host's cores, each
+  // into its own list, concatenated in bucket order (the serial order)
+  std::vector<std::vector<UnitDesc>> part_units(64);
+  host_parallel(nb, [&](int64_t b_lo, int64_t b_hi, int part) {
+    std::vector<UnitDesc> &units = part_units[part];
+    for (int b = (int)b_lo; b < (int)b_hi; b++) {
+      const int s = g1.h_bk_start[b], e = g1.h_bk_end[b];
+      int i = s;
+      while (i < e) {
+        // z-chunk of extent <= Emax, dealt round-robin into tiles of <= tile rows
+        const float z0 = g1.h_pos[i].z;
+        int j = i;
+        float bx0 = INFINITY, bx1 = -INFINITY, by0 = INFINITY, by1 = -INFINITY;
+        while (j < e && (double)g1.h_pos[j].z - z0 <= Emax) {
+          bx0 = std::min(bx0, g1.h_pos[j].x);
+          bx1 = std::max(bx1, g1.h_pos[j].x);
+          by0 = std::min(by0, g1.h_pos[j].y);
+          by1 = std::max(by1, g1.h_pos[j].y);
+          j++;
+        }
+        const int m = j - i;
+        const int nt = (m + jp.tile - 1) / jp.tile;
+        const double zt0 = g1.h_pos[i].z, zt1 = g1.h_pos[j - 1].z;
+        const double rg = p.bin_r_max + guard;
+        int cx0 = (int)std::floor((bx0 - rg) * inv_cwx), cx1 = (int)std::floor((bx1 + rg) * inv_cwx);
+        int cy0 = (int)std::floor((by0 - rg) * inv_cwy), cy1 = (int)std::floor((by1 + rg) * inv_cwy);
+        if (p.periodic_box) {
+          cx0 = std::max(cx0, -ncx); cx1 = std::min(cx1, 2 * ncx - 1);
+          cy0 = std::max(cy0, -ncy); cy1 = std::min(cy1, 2 * ncy - 1);
         } else {
-          const double span = std::max(ps, (wpi - 4) * ps - (zt1 - zt0));
-          const int U = std::max(1, (int)std::ceil((Zhi - Zlo) / span));
-          for (int q = 0; q < U; q++) {
-            const double a = (q == 0) ? Zlo : Zlo + (Zhi - Zlo) * q / U;
-            const double bnd = (q == U - 1) ? Zhi : Zlo + (Zhi - Zlo) * (q + 1) / U;
-            int base = (int)std::floor((a - zt1 - p.p_min) / ps) - 1;
-            base = std::max(0, std::min(base, npi - wpi));
-            u.n2_base = base;
-            u.zlo = a;
-            u.zhi = bnd;
-            units.push_back(u);
+          cx0 = std::max(cx0, 0); cx1 = std::min(cx1, ncx - 1);
+          cy0 = std::max(cy0, 0); cy1 = std::min(cy1, ncy - 1);
+        }
+        const double Zlo = zt0 + zw0 - guard, Zhi = zt1 + zw1 + guard;
+        for (int k = 0; k < nt; k++) {
+          UnitDesc u;
+          std::memset(&u, 0, sizeof u);
+          u.g1_start = i + k;
+          u.g1_stride = nt;
+          u.g1_count = (m - k + nt - 1) / nt;
+          u.region = g1.h_bk_region[b];
+          u.cx_lo = cx0; u.cx_hi = cx1; u.cy_lo = cy0; u.cy_hi = cy1;
+          if (wpi >= npi || rmu) {
+            // coordinates 7: one unit per slice of wpi mu bins; each pair is
+            // taken by the slice holding its estimated bin (pair_fast.cu)
+            u.zlo = Zlo;
+            u.zhi = Zhi;
+            for (int base = 0; base < npi; base += wpi) {
+              u.n2_base = base;
+              units.push_back(u);
+            }
+          } else {
+            const double span = std::max(ps, (wpi - 4) * ps - (zt1 - zt0));
+            const int U = std::max(1, (int)std::ceil((Zhi - Zlo) / span));
+            for (int q = 0; q < U; q++) {
+              const double a = (q == 0) ? Zlo : Zlo + (Zhi - Zlo) * q / U;
+              const double bnd = (q == U - 1) ? Zhi : Zlo + (Zhi - Zlo) * (q + 1) / U;
+              int base = (int)std::floor((a - zt1 - p.p_min) / ps) - 1;
+              base = std::max(0, std::min(base, npi - wpi));
+              u.n2_base = base;
+              u.zlo = a;
+              u.zhi = bnd;
+              units.push_back(u);
+            }
           }
         }
+        i = j;
       }
-      i = j;
     }
-  }
+  }, 512);  // a bucket's units take microseconds: threads pay for large catalogues
+  size_t total = 0;
+  for (const auto &v : part_units) total += v.size();
+  units.reserve(total);
+  for (const auto &v : part_units) units.insert(units.end(), v.begin(), v.end());
   return units;
 }
 
@@ -1113,9 +1123,17 @@ cpc_status build_cells(cpc_ctx *c, Slot &s, int64_t n, int k, const int64_t *ori
   std::vector<float> bz0, bz1;
   const int ncol = s.ncx * s.ncy;
   std::vector<int> cb(ncol, 0), ce(ncol, 0);
-  for (int64_t i = 0; i < n;) {
-    int64_t j = i + 1;
-    while (j < n && hb[j] == hb[i]) j++;
+  // bucket starts (rows whose key differs from the previous row's), found in
+  // chunks on the host's cores and concatenated in row order
+  std::vector<std::vector<int64_t>> part_starts(64);
+  host_parallel(n, [&](int64_t b0, int64_t b1, int part) {
+    for (int64_t i = b0; i < b1; i++)
+      if (i == 0 || hb[i] != hb[i - 1]) part_starts[part].push_back(i);
+  }, 1 << 20);  // a cheap pass: threads only pay for millions of rows
+  std::vector<int64_t> starts;
+  for (const auto &v : part_starts) starts.insert(starts.end(), v.begin(), v.end());
+  for (size_t q = 0; q < starts.size(); q++) {
+    const int64_t i = starts[q], j = q + 1 < starts.size() ? starts[q + 1] : n;
     const int b = (int)s.h_bk_start.size();
     const int col = (int)(hb[i] / s.n_reg), reg = (int)(hb[i] % s.n_reg);
     if (ce[col] == 0 && cb[col] == 0) cb[col] = b;
@@ -1125,7 +1143,6 @@ cpc_status build_cells(cpc_ctx *c, Slot &s, int64_t n, int k, const int64_t *ori
     s.h_bk_region.push_back(reg);
     bz0.push_back(s.h_pos[i].z);
     bz1.push_back(s.h_pos[j - 1].z);
-    i = j;
   }
   // columns with no bucket: empty range
   for (int q = 0; q < ncol; q++)
