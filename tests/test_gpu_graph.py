@@ -141,3 +141,46 @@ def test_bad_shard_is_rejected():
         ctx.set_shard(3, 3)
     with pytest.raises(_lib.CpcError):
         ctx.set_shard(0, 0)
+
+
+@pytest.mark.parametrize("name", ["auto_box_wpp_rebin", "auto_box_wgp_unsorted"])
+def test_unit_shards_of_auto_pairs_sum_to_the_reference(name):
+    """corels1 (cpc_count_auto) on two work-unit shards adds up to the
+    reference's auto-correlation block."""
+    from helpers import AutoGolden
+    g = AutoGolden(name)
+    rnum, rsums, rin, rtot = g.term("SS")
+    cats = host.prepare(g.params, g.read_order(), table=g.table)
+    parts = []
+    for sh in range(2):
+        ctx = _lib.Context(g.params, table=g.table)
+        ctx.upload(0, cats["S"])
+        ctx.set_shard(sh, 2)
+        parts.append(ctx.count_auto("SS", 0))
+        ctx.close()
+    assert sum(p["n_binned"] for p in parts) == rin
+    assert sum(p["n_window"] for p in parts) == rtot
+    assert np.array_equal(sum(p["num"] for p in parts), rnum)
+    check_sums(sum(p["sums"] for p in parts), rsums, label=f"{name} auto shards")
+
+
+def test_unit_shards_of_a_batch_sum_to_the_whole_batch():
+    """Every context of a batch on the same shard of its units, then the other
+    shard: the two batches add up to the oracle's counts of every box."""
+    wls = synth.box_batch_wpp(n_boxes=4, seed=5, scale=0.02)
+    ref = []
+    for w in wls:
+        oc = oracle.read_like_reference(w.params, [("S", w.shape), ("D", w.density)])
+        ref.append(oracle.port_corels2(w.params, "SD", oc["D"], oc["S"]))
+    ctxs = [_ctx_for(w.params, w.shape, w.density) for w in wls]
+    halves = []
+    for sh in range(2):
+        for c in ctxs:
+            c.set_shard(sh, 2)
+        halves.append(_lib.count_batch([(c, "SD", 0, 1) for c in ctxs]))
+    for k, (num, sums, n_total, n_in) in enumerate(ref):
+        a, b = halves[0][k], halves[1][k]
+        assert a["n_binned"] + b["n_binned"] == n_in
+        assert a["n_window"] + b["n_window"] == n_total
+        assert np.array_equal(a["num"] + b["num"], num)
+        check_sums(a["sums"] + b["sums"], sums, label=f"batch box {k} shards")
