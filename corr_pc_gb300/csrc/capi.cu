@@ -158,10 +158,10 @@ struct cpc_ctx {
   int pending = 0;  // 0 none, 1 fast engine, 2 FP64 engine
   std::vector<JobPlan> pending_jobs;
   int64_t launches = 0;  // kernels launched by this context (all entry points)
-  // CUDA graph of the fast engine's device work (zeroing, pair kernels,
-  // recheck), replayed while every value baked into it stays the same
   // work-unit shard of the fast box engine (cpc_set_shard)
   int shard = 0, n_shards = 1;
+  // CUDA graph of the fast engine's device work (zeroing, pair kernels,
+  // recheck), replayed while every value baked into it stays the same
   int graph_on = 1;
   cudaGraphExec_t gexec = nullptr;
   std::vector<uint64_t> gkey;
@@ -190,7 +190,6 @@ cpc_status cuda_fail(cpc_ctx *c, cudaError_t e, const char *where) {
     if (_e != cudaSuccess) return cuda_fail(c, _e, where); \
   } while (0)
 
-// float ULP at magnitude v (v > 0)
 // Run f(begin, end, part) over [0, n) in contiguous chunks on the host's cores
 // (one chunk per thread, part < 64, at least min_chunk items each; in the
 // calling thread when n is small).  f must not throw.
@@ -209,6 +208,7 @@ void host_parallel(int64_t n, F &&f, int64_t min_chunk = 16384) {
   for (auto &x : th) x.join();
 }
 
+// float ULP at magnitude v (v > 0)
 double ulpf(double v) {
   if (!(v > 0)) return std::ldexp(1.0, -149);
   int ex;
@@ -816,7 +816,7 @@ size_t accum_cells(const cpc_ctx *c) {
 
 // The device work of one fast count, in stream order on st: zero every job's
 // histogram block and counters, the edge-queue counter, then per group the
-// unit counter and the persistent kernel, then the FP64 recheck.  `rec`
+// unit counter and the persistent kernel, then the FP64 recheck.  rec_flags
 // records the timing events (cudaEventRecordExternal inside a capture, so
 // that they become event nodes of the graph).
 cpc_status fast_body(cpc_ctx *c0, std::vector<JobPlan> &jobs, const std::vector<FastGroup> &gs,
