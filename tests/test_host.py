@@ -235,3 +235,31 @@ def test_integration_binding_links_into_the_reference():
         assert name in syms, name
     needed = subprocess.run(["readelf", "-d", exe], capture_output=True, text=True).stdout
     assert "libcorrpc_gb300.so" in needed
+
+
+def test_accuracy_report_applies_the_bar():
+    """bench.py's per-field accuracy report: identical blocks pass, a changed
+    count or a non-cancelling field off by 1e-5 fails, a cancelling field is
+    held only to the absolute floor."""
+    from corr_pc_gb300 import metrics
+    rng = np.random.default_rng(3)
+    num = rng.integers(1, 1000, size=(3, 4, 5))
+    sums = np.zeros((3, 4, 5, 13))
+    sums[..., 0] = num
+    sums[..., 1] = rng.normal(size=num.shape) * 10.0     # e+ sum: cancelling
+    sums[..., 2] = rng.uniform(1.0, 2.0, num.shape) * num  # its square: non-cancelling
+    rep = metrics.accuracy_report(num, sums, num, sums)
+    assert rep["ok"] and rep["counts_bit_exact"]
+    assert set(rep["fields"]) == {"wt_num", "data1.val", "data1.err"}
+    bad_num = num.copy()
+    bad_num[1, 2, 3] += 1
+    assert not metrics.accuracy_report(bad_num, sums, num, sums)["ok"]
+    worse = sums.copy()
+    worse[..., 2] *= 1 + 1e-5
+    assert not metrics.accuracy_report(num, worse, num, sums)["ok"]
+    # a cancelling field: a small bin may be off relatively, within the floor
+    canc = sums.copy()
+    i = np.unravel_index(np.argmin(np.abs(sums[..., 1])), num.shape)
+    canc[i + (1,)] += 1e-7 * np.abs(sums[..., 1]).max()
+    rep = metrics.accuracy_report(num, canc, num, sums)
+    assert rep["ok"] and rep["fields"]["data1.val"]["cancelling"]
