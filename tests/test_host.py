@@ -263,3 +263,58 @@ def test_accuracy_report_applies_the_bar():
     canc[i + (1,)] += 1e-7 * np.abs(sums[..., 1]).max()
     rep = metrics.accuracy_report(num, canc, num, sums)
     assert rep["ok"] and rep["fields"]["data1.val"]["cancelling"]
+
+
+@pytest.fixture(scope="module")
+def asan_driver(tmp_path_factory):
+    """tests/host_asan_driver.cpp and the C++ host sources, built with
+    AddressSanitizer and UndefinedBehaviorSanitizer (once per module)."""
+    import shutil
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    csrc = os.path.join(ROOT, "corr_pc_gb300", "csrc")
+    exe = str(tmp_path_factory.mktemp("asan") / "host_asan_driver")
+    srcs = [os.path.join(ROOT, "tests", "host_asan_driver.cpp")] + [
+        os.path.join(csrc, s) for s in ("host/inp.cpp", "host/reader.cpp", "host/finalize.cpp",
+                                        "host/outp.cpp", "host_helpers.cpp")]
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined",
+                        "-fno-sanitize-recover=all", "-fno-omit-frame-pointer",
+                        "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-I" + csrc,
+                        *srcs, "-o", exe], capture_output=True, text=True)
+    if r.returncode != 0 and "asan" in (r.stderr or "").lower():
+        pytest.skip("sanitizer runtime not available: " + r.stderr[-300:])
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+@pytest.mark.parametrize("name", ["box_wgp_clustered", "box_wpp_weighted_distinct",
+                                  "box_kappa_unsorted", "box_ed_rmu"])
+def test_host_pipeline_under_address_and_ub_sanitizers(name, asan_driver, tmp_path):
+    """The C++ host side of the command line (positional .inp, the catalogue
+    readers with their rand() draws, the delete-one step, the finalisation and
+    the output writers), built with AddressSanitizer and
+    UndefinedBehaviorSanitizer and fed the reference's own raw SD block: it runs
+    clean and writes the reference's output files."""
+    g = Golden(name)
+    wl = synth.Workload(name, g.params, g.S, g.D)
+    inp = synth.write_box_run(str(tmp_path), wl, same_files=g.meta["same_files"], n_threads=1)
+    nfile, sfile = str(tmp_path / "num.bin"), str(tmp_path / "sums.bin")
+    np.ascontiguousarray(g.raw_num, dtype=np.int64).tofile(nfile)
+    np.ascontiguousarray(g.raw_sums, dtype=np.float64).tofile(sfile)
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:exitcode=23",
+               UBSAN_OPTIONS="print_stacktrace=1")
+    r = subprocess.run([asan_driver, inp, nfile, sfile], capture_output=True, text=True,
+                       env=env, timeout=300)
+    if "LeakSanitizer has encountered a fatal error" in r.stderr:  # no ptrace here
+        env["ASAN_OPTIONS"] = "detect_leaks=0:exitcode=23"
+        r = subprocess.run([asan_driver, inp, nfile, sfile], capture_output=True, text=True,
+                           env=env, timeout=300)
+    assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-4000:])
+    assert "runtime error" not in r.stderr, r.stderr[-4000:]
+    # synth.write_box_run names the output prefix <dir>/out/run_
+    for fname, ref in g.files.items():
+        if fname.endswith(".info"):
+            continue
+        path = tmp_path / "out" / ("run_" + fname)
+        assert path.exists(), fname
+        compare_files(path.read_text(), ref, label=f"{name}:{fname} (sanitized host)")
