@@ -22,7 +22,8 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-PORT_SO = os.path.join(HERE, "_build", "libcpc_oracle.so")
+# CPC_ORACLE_SO: another build of the restatement (the sanitizer test's)
+PORT_SO = os.environ.get("CPC_ORACLE_SO") or os.path.join(HERE, "_build", "libcpc_oracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
 NF = 13  # wt, d1v, d1e, ..., d6v, d6e
 KIND = {"SD": 0, "SRd": 1, "DRs": 2, "RsRd": 3, "RsRs": 4, "SRs": 5, "SS": 6}

@@ -107,3 +107,34 @@ def test_port_corels1_matches_reference(name):
         assert np.array_equal(num, rnum), t
         scale = np.abs(rsums).max(axis=(0, 1, 2)) + 1e-300
         assert (np.abs(sums - rsums) / scale).max() < 1e-12, t
+
+
+def test_port_under_address_and_ub_sanitizers(tmp_path):
+    """The C restatement built with AddressSanitizer and UndefinedBehaviorSanitizer
+    passes every other test of this file (box, sky and auto golden runs, thread
+    counts, row samples) with no report."""
+    import os
+    import shutil
+    import subprocess
+    import sys
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    here = os.path.dirname(os.path.abspath(__file__))
+    src = os.path.join(os.path.dirname(here), "oracle", "cpc_oracle.c")
+    so = str(tmp_path / "libcpc_oracle_asan.so")
+    r = subprocess.run(["gcc", "-O1", "-g", "-fsanitize=address,undefined",
+                        "-fno-sanitize-recover=all", "-fno-omit-frame-pointer", "-fopenmp",
+                        "-ffp-contract=off", "-fPIC", "-shared", "-std=c11", "-D_GNU_SOURCE", src,
+                        "-o", so, "-lm"], capture_output=True, text=True)
+    libasan = subprocess.run(["gcc", "-print-file-name=libasan.so"], capture_output=True,
+                             text=True).stdout.strip()
+    if r.returncode != 0 or not os.path.isabs(libasan):
+        pytest.skip("sanitizer runtime not available")
+    env = dict(os.environ, LD_PRELOAD=libasan, ASAN_OPTIONS="detect_leaks=0",
+               UBSAN_OPTIONS="print_stacktrace=1", CPC_ORACLE_SO=so)
+    r = subprocess.run([sys.executable, "-m", "pytest", os.path.join(here, "test_oracle.py"),
+                        "-q", "-p", "no:cacheprovider", "-k", "not sanitizers"],
+                       capture_output=True, text=True, env=env, timeout=900, cwd=here)
+    assert r.returncode == 0, (r.stdout[-3000:], r.stderr[-3000:])
+    assert "runtime error" not in r.stdout + r.stderr
+    assert "ERROR: AddressSanitizer" not in r.stdout + r.stderr
