@@ -12,6 +12,7 @@
 #include <cstring>
 #include <iostream>
 #include <string>
+#include <vector>
 
 #include "host.h"
 
@@ -23,6 +24,41 @@ struct Ctx {
   cpc_ctx *c = nullptr;
   ~Ctx() { cpc_destroy(c); }
 };
+
+// one counted pair type, for the run record
+struct TermRecord {
+  std::string name;
+  int64_t n_window, n_binned, n_rechecked;
+  double wall_s, kernel_ms;
+};
+std::vector<TermRecord> g_terms;
+
+const char *term_name(cpc_pair_kind k) {
+  static const char *names[] = {"SD", "SRd", "DRs", "RsRd", "RsRs", "SRs", "SS"};
+  return (k >= CPC_PAIR_SD && k <= CPC_PAIR_SS) ? names[k] : "?";
+}
+
+// <out_file>run.json: the engine and, per pair type, the window and binned
+// pairs, the pairs resolved by the FP64 recheck, the wall time of the call, the
+// device time of the count and the binned pairs per second of device time
+void write_run_record(const Info &d, cpc_engine eng) {
+  FILE *f = std::fopen((d.out_file + "run.json").c_str(), "w");
+  if (!f) return;
+  std::fprintf(f, "{\"library\": \"%s\", \"engine\": \"%s\", \"terms\": [", cpc_version(),
+               eng == CPC_ENGINE_FP64 ? "fp64" : "fast");
+  for (size_t k = 0; k < g_terms.size(); k++) {
+    const TermRecord &t = g_terms[k];
+    std::fprintf(f,
+                 "%s\n  {\"pair_type\": \"%s\", \"n_window\": %lld, \"n_binned\": %lld, "
+                 "\"n_rechecked\": %lld, \"wall_s\": %.6g, \"kernel_ms\": %.6g, "
+                 "\"binned_pairs_per_s\": %.6g}",
+                 k ? "," : "", t.name.c_str(), (long long)t.n_window, (long long)t.n_binned,
+                 (long long)t.n_rechecked, t.wall_s, t.kernel_ms,
+                 t.kernel_ms > 0 ? t.n_binned / (t.kernel_ms * 1e-3) : 0.0);
+  }
+  std::fprintf(f, "\n]}\n");
+  std::fclose(f);
+}
 
 int count_term(Ctx &ctx, Info &d, cpc_pair_kind kind, int s1, int s2, Bins &out, cpc_engine eng,
                bool auto_pairs = false) {
@@ -42,6 +78,8 @@ int count_term(Ctx &ctx, Info &d, cpc_pair_kind kind, int s1, int s2, Bins &out,
     return 1;
   }
   add_count(out, d, num.data(), sums.data());
+  g_terms.push_back(TermRecord{term_name(kind), acc.n_window, acc.n_binned, acc.n_rechecked, dt,
+                               acc.kernel_ms});
   std::cout << (auto_pairs ? "corel 1 ends: time:" : "corel2 ends::time: ") << dt
             << "  total pair= " << acc.n_window
             << "\tpairs out= " << acc.n_window - acc.n_binned << "   pairs in=" << acc.n_binned
@@ -142,5 +180,6 @@ int main(int argc, char **argv) {
   }
   std::cout << "Binning done" << std::endl;
   outp_data_info(d, d.out_file + "inp2.info");
+  write_run_record(d, eng);
   return 0;
 }

@@ -1,5 +1,6 @@
 """The corr_pc_gb300 command line (the reference's argv, .inp and files) on
 the golden cases: every output file equals the reference's."""
+import json
 import os
 import subprocess
 
@@ -26,6 +27,12 @@ def test_cli_output_files_match_reference(name, tmp_path):
         if fname.endswith(".info"):
             continue
         compare_files(open(out + fname).read(), ref, label=f"{name}:{fname}")
+    # the run record: one entry per counted pair type
+    rec = json.load(open(out + "run.json"))
+    sd = [t for t in rec["terms"] if t["pair_type"] == "SD"]
+    assert rec["engine"] == "fast" and len(sd) == 1
+    assert sd[0]["n_binned"] == g.n_in and sd[0]["n_window"] == g.n_total
+    assert sd[0]["kernel_ms"] > 0 and sd[0]["binned_pairs_per_s"] > 0
 
 
 @pytest.mark.parametrize("name", ["sky_wgp_jk", "sky_wgg_distinct_wrap", "nbox_wgp_ls"])
@@ -43,6 +50,9 @@ def test_cli_sky_output_files_match_reference(name, tmp_path):
     for t in g.terms:
         assert f"pairs in={g.term(t)[2]}" in r.stdout, t
     out = os.path.join(str(tmp_path), "out", "run_")
+    rec = {t["pair_type"]: t for t in json.load(open(out + "run.json"))["terms"]}
+    for t in g.terms:
+        assert rec[t]["n_binned"] == g.term(t)[2], t
     for fname, ref in g.files.items():
         if fname.endswith(".info"):
             continue
@@ -70,6 +80,9 @@ def test_cli_auto_output_files_match_reference(name, tmp_path):
     for t in g.terms:
         assert f"pairs in={g.term(t)[2]}" in r.stdout, t
     out = os.path.join(str(tmp_path), "out", "run_")
+    rec = {t["pair_type"]: t for t in json.load(open(out + "run.json"))["terms"]}
+    for t in g.terms:
+        assert rec[t]["n_binned"] == g.term(t)[2], t
     for fname, ref in g.files.items():
         if fname.endswith(".info"):
             continue
