@@ -87,3 +87,40 @@ def test_cli_auto_output_files_match_reference(name, tmp_path):
         if fname.endswith(".info"):
             continue
         compare_files(open(out + fname).read(), ref, label=f"{name}:{fname}")
+
+
+def test_cli_batch_of_box_runs_matches_reference(tmp_path):
+    """Three periodic-box runs (their own .inp, catalogues and output prefix)
+    through one `--batch` call: their SD terms are counted in one launch and
+    every run writes the reference's files."""
+    names = ["box_wgg_uniform", "box_wgp_clustered", "box_wpp_weighted_distinct"]
+    inps, outs, goldens = [], [], []
+    for k, name in enumerate(names):
+        g = Golden(name)
+        d = tmp_path / f"run{k}"
+        d.mkdir()
+        wl = synth.Workload(name, g.params, g.S, g.D)
+        inps.append(synth.write_box_run(str(d), wl, same_files=g.meta["same_files"]))
+        outs.append(os.path.join(str(d), "out", "run_"))
+        goldens.append(g)
+    r = subprocess.run([build.CLI, "--batch", *inps], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for name, g, out in zip(names, goldens, outs):
+        assert f"pairs in={g.n_in}" in r.stdout, name
+        for fname, ref in g.files.items():
+            if fname.endswith(".info"):
+                continue
+            compare_files(open(out + fname).read(), ref, label=f"batch {name}:{fname}")
+        sd = [t for t in json.load(open(out + "run.json"))["terms"] if t["pair_type"] == "SD"]
+        assert sd[0]["n_binned"] == g.n_in and sd[0]["n_window"] == g.n_total
+
+
+def test_cli_batch_rejects_a_sky_run(tmp_path):
+    from helpers import SkyGolden
+    g = SkyGolden("sky_wgp_jk")
+    c = g.cats
+    wl = synth.SkyWorkload("sky_wgp_jk", g.params, g.table, c["S"], c["D"], c["Rs"], c["Rd"])
+    inp = synth.write_sky_run(str(tmp_path), wl, same_files=g.meta["same_files"])
+    r = subprocess.run([build.CLI, "--batch", inp], capture_output=True, text=True, timeout=600)
+    assert r.returncode != 0 and "--batch takes periodic-box cross runs" in r.stdout
