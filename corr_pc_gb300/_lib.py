@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(PKG, "_build", "libcorrpc_gb300.so")
 CPC_OK = 0
 STATUS_NAMES = {0: "CPC_OK", 1: "CPC_ERR_INVALID", 2: "CPC_ERR_CUDA", 3: "CPC_ERR_NOMEM",
                 4: "CPC_ERR_TIMEOUT", 5: "CPC_ERR_STATE", 6: "CPC_ERR_RANGE",
-                7: "CPC_ERR_NODEVICE"}
+                7: "CPC_ERR_NODEVICE", 8: "CPC_ERR_HOST"}
 # cpc_pair_kind (the data_info.do_* flag of each corels2 call)
 PAIR = {"SD": 0, "SRd": 1, "DRs": 2, "RsRd": 3, "RsRs": 4, "SRs": 5, "SS": 6}
 ENGINE = {"fast": 0, "fp64": 1}

@@ -8,10 +8,13 @@
 #include <cstdio>
 #include <cstring>
 #include <cstdlib>
+#include <exception>
 #include <map>
 #include <memory>
 #include <mutex>
+#include <stdexcept>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <tuple>
 #include <vector>
@@ -170,11 +173,42 @@ struct cpc_ctx {
 
 namespace {
 
-cpc_status fail(cpc_ctx *c, cpc_status s, const std::string &msg) {
-  if (c) c->err = msg;
-  std::lock_guard<std::mutex> lk(g_err_mu);
-  g_err = msg;
+// Record msg as the context's (and the library's) last error and return s.  A
+// message that cannot be stored (out of host memory) leaves the old one.
+cpc_status fail(cpc_ctx *c, cpc_status s, const std::string &msg) noexcept {
+  try {
+    if (c) c->err = msg;
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_err = msg;
+  } catch (...) {
+  }
   return s;
+}
+
+// The status of a C++ exception that reached an entry point (called from its
+// catch block): no exception crosses the C ABI.  A stream capture left open
+// by the interrupted call is closed so that the context stays usable.
+cpc_status host_exception(cpc_ctx *c) noexcept {
+  if (c && c->st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(c->st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(c->st, &g);
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+    }
+  }
+  try {
+    throw;
+  } catch (const std::bad_alloc &) {
+    return fail(c, CPC_ERR_NOMEM, "host allocation failed");
+  } catch (const std::length_error &) {
+    return fail(c, CPC_ERR_NOMEM, "host allocation too large");
+  } catch (const std::exception &e) {
+    return fail(c, CPC_ERR_HOST, std::string("host error: ") + e.what());
+  } catch (...) {
+    return fail(c, CPC_ERR_HOST, "host error");
+  }
 }
 
 cpc_status cuda_fail(cpc_ctx *c, cudaError_t e, const char *where) {
@@ -192,7 +226,9 @@ cpc_status cuda_fail(cpc_ctx *c, cudaError_t e, const char *where) {
 
 // Run f(begin, end, part) over [0, n) in contiguous chunks on the host's cores
 // (one chunk per thread, part < 64, at least min_chunk items each; in the
-// calling thread when n is small).  f must not throw.
+// calling thread when n is small).  Parts whose thread cannot be started run in
+// the calling thread; the first exception thrown by a part is rethrown here
+// after every part has finished.
 template <class F>
 void host_parallel(int64_t n, F &&f, int64_t min_chunk = 16384) {
   const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
@@ -201,11 +237,28 @@ void host_parallel(int64_t n, F &&f, int64_t min_chunk = 16384) {
     f((int64_t)0, n, 0);
     return;
   }
+  std::exception_ptr errs[64];
+  auto part = [&f, &errs, n, T](int t) {
+    try {
+      f(n * t / T, n * (t + 1) / T, t);
+    } catch (...) {
+      errs[t] = std::current_exception();
+    }
+  };
   std::vector<std::thread> th;
   th.reserve(T);
-  for (int t = 0; t < T; t++)
-    th.emplace_back([&f, n, t, T] { f(n * t / T, n * (t + 1) / T, t); });
+  int t = 0;
+  for (; t < T; t++) {
+    try {
+      th.emplace_back(part, t);
+    } catch (const std::system_error &) {
+      break;
+    }
+  }
+  for (; t < T; t++) part(t);
   for (auto &x : th) x.join();
+  for (int k = 0; k < T; k++)
+    if (errs[k]) std::rethrow_exception(errs[k]);
 }
 
 // float ULP at magnitude v (v > 0)
@@ -1637,7 +1690,7 @@ const char *cpc_last_error(const cpc_ctx *ctx) {
   return g_err.c_str();
 }
 
-cpc_status cpc_create(cpc_ctx **out, const cpc_params *params) {
+cpc_status cpc_create(cpc_ctx **out, const cpc_params *params) try {
   if (!out || !params) return fail(nullptr, CPC_ERR_INVALID, "null argument");
   *out = nullptr;
   cpc_status s = validate_params(nullptr, *params);
@@ -1675,9 +1728,11 @@ cpc_status cpc_create(cpc_ctx **out, const cpc_params *params) {
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "event");
   *out = c.release();
   return CPC_OK;
+} catch (...) {
+  return host_exception(nullptr);
 }
 
-cpc_status cpc_destroy(cpc_ctx *c) {
+cpc_status cpc_destroy(cpc_ctx *c) try {
   if (!c) return CPC_OK;
   cudaStreamSynchronize(c->st);
   drop_graph(c);
@@ -1689,6 +1744,8 @@ cpc_status cpc_destroy(cpc_ctx *c) {
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return CPC_OK;
+} catch (...) {
+  return host_exception(c);
 }
 
 cpc_status cpc_accum_shape(const cpc_ctx *c, int *n_hist, int *n_bins, int *n_p_bin) {
@@ -1718,7 +1775,7 @@ cpc_status cpc_set_tuning(cpc_ctx *c, int cells_per_rmax, int pi_window, int til
   return CPC_OK;
 }
 
-cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
+cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) try {
   if (!c || !cat) return fail(c, CPC_ERR_INVALID, "null argument");
   if (busy(c)) return CPC_ERR_STATE;
   if (slot < 0 || slot >= kMaxSlots) return fail(c, CPC_ERR_INVALID, "slot out of range");
@@ -1789,10 +1846,12 @@ cpc_status cpc_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
                        st), "D2H");
   }
   return build_cells(c, s, n, c->tune_k > 0 ? c->tune_k : 2, nullptr, true);
+} catch (...) {
+  return host_exception(c);
 }
 
 cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, cpc_engine engine,
-                     int64_t row_stride, int64_t row_offset, cpc_accum *out) {
+                     int64_t row_stride, int64_t row_offset, cpc_accum *out) try {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
   if (busy(c)) return CPC_ERR_STATE;
   if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
@@ -1809,11 +1868,13 @@ cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, c
   if (engine == CPC_ENGINE_FP64) return run_plain(jobs[0]);
   if (engine != CPC_ENGINE_FAST) return fail(c, CPC_ERR_INVALID, "unknown engine");
   return run_fast(jobs);
+} catch (...) {
+  return host_exception(c);
 }
 
 cpc_status cpc_count_async(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2,
                            cpc_engine engine, int64_t row_stride, int64_t row_offset,
-                           void *stream) {
+                           void *stream) try {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
   if (busy(c)) return CPC_ERR_STATE;
   if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
@@ -1844,9 +1905,11 @@ cpc_status cpc_count_async(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot
   c->pending = engine == CPC_ENGINE_FP64 ? 2 : 1;
   c->pending_jobs = std::move(jobs);
   return CPC_OK;
+} catch (...) {
+  return host_exception(c);
 }
 
-cpc_status cpc_count_finish(cpc_ctx *c, cpc_accum *out) {
+cpc_status cpc_count_finish(cpc_ctx *c, cpc_accum *out) try {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
   if (!c->pending) return fail(c, CPC_ERR_STATE, "no count is pending");
   if (!out || !out->num || !out->sums) return fail(c, CPC_ERR_INVALID, "null output arrays");
@@ -1856,10 +1919,12 @@ cpc_status cpc_count_finish(cpc_ctx *c, cpc_accum *out) {
   c->pending_jobs.clear();
   jobs[0].out = out;
   return mode == 2 ? finish_plain(jobs[0]) : finish_fast(jobs, 0);
+} catch (...) {
+  return host_exception(c);
 }
 
 cpc_status cpc_count_auto(cpc_ctx *c, cpc_pair_kind kind, int slot, cpc_engine engine,
-                          int64_t row_stride, int64_t row_offset, cpc_accum *out) {
+                          int64_t row_stride, int64_t row_offset, cpc_accum *out) try {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
   if (busy(c)) return CPC_ERR_STATE;
   if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
@@ -1876,10 +1941,12 @@ cpc_status cpc_count_auto(cpc_ctx *c, cpc_pair_kind kind, int slot, cpc_engine e
   if (s != CPC_OK) return s;
   if (engine == CPC_ENGINE_FP64) return run_plain(jobs[0]);
   return run_fast(jobs);
+} catch (...) {
+  return host_exception(c);
 }
 
 cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2,
-                        int64_t sample_stride, int *cells_per_rmax, int *pi_window) {
+                        int64_t sample_stride, int *cells_per_rmax, int *pi_window) try {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
   if (busy(c)) return CPC_ERR_STATE;
   const cpc_params &p = c->p;
@@ -1957,10 +2024,12 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
   if (cells_per_rmax) *cells_per_rmax = bk;
   if (pi_window) *pi_window = bw;
   return CPC_OK;
+} catch (...) {
+  return host_exception(c);
 }
 
 cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind *kinds,
-                           const int *slots_g1, const int *slots_g2, cpc_accum *outs) {
+                           const int *slots_g1, const int *slots_g2, cpc_accum *outs) try {
   if (n_jobs <= 0 || !ctxs || !kinds || !slots_g1 || !slots_g2 || !outs)
     return fail(nullptr, CPC_ERR_INVALID, "bad batch arguments");
   for (int k = 0; k < n_jobs; k++)
@@ -1983,27 +2052,35 @@ cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind
     if (s != CPC_OK) return s;
   }
   return run_fast(jobs);
+} catch (...) {
+  return host_exception(n_jobs > 0 && ctxs ? ctxs[0] : nullptr);
 }
 
-cpc_status cpc_host_rand_uniform(uint32_t seed, int64_t skip, int64_t n, double *out) {
+cpc_status cpc_host_rand_uniform(uint32_t seed, int64_t skip, int64_t n, double *out) try {
   if (n < 0 || skip < 0 || (n > 0 && !out)) return fail(nullptr, CPC_ERR_INVALID, "bad arguments");
   std::vector<int32_t> r(n);
   glibc_rand_stream(seed, skip, n, r.data());
   for (int64_t i = 0; i < n; i++) out[i] = r[i] / (2147483647 + 1.);
   return CPC_OK;
+} catch (...) {
+  return host_exception(nullptr);
 }
 
-cpc_status cpc_host_elip_angle(int64_t n, const double *e1, const double *e2, double *phi) {
+cpc_status cpc_host_elip_angle(int64_t n, const double *e1, const double *e2, double *phi) try {
   if (n < 0 || (n > 0 && (!e1 || !e2 || !phi))) return fail(nullptr, CPC_ERR_INVALID, "bad arguments");
   for (int64_t i = 0; i < n; i++) phi[i] = elip_angle(e1[i], e2[i]);
   return CPC_OK;
+} catch (...) {
+  return host_exception(nullptr);
 }
 
-cpc_status cpc_host_rp_thresholds(const cpc_params *p, double *thr) {
+cpc_status cpc_host_rp_thresholds(const cpc_params *p, double *thr) try {
   if (!p || !thr) return fail(nullptr, CPC_ERR_INVALID, "null argument");
   if (p->n_bins <= 0 || p->n_bins > kMaxRp) return fail(nullptr, CPC_ERR_INVALID, "n_bins out of range");
   const int rc = rp_thresholds(p->lin_bin, p->n_bins, p->bin_r_min, p->bin_r_max, thr);
   return rc == 0 ? CPC_OK : fail(nullptr, CPC_ERR_INVALID, "threshold derivation failed");
+} catch (...) {
+  return host_exception(nullptr);
 }
 
 cpc_status cpc_set_shard(cpc_ctx *c, int shard, int n_shards) {
@@ -2016,13 +2093,15 @@ cpc_status cpc_set_shard(cpc_ctx *c, int shard, int n_shards) {
   return CPC_OK;
 }
 
-cpc_status cpc_set_graph_replay(cpc_ctx *c, int enable) {
+cpc_status cpc_set_graph_replay(cpc_ctx *c, int enable) try {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
   if (busy(c)) return CPC_ERR_STATE;
   cudaStreamSynchronize(c->st);
   drop_graph(c);
   c->graph_on = enable ? 1 : 0;
   return CPC_OK;
+} catch (...) {
+  return host_exception(c);
 }
 
 cpc_status cpc_graph_stats(const cpc_ctx *c, int64_t *captures, int64_t *replays) {
@@ -2038,11 +2117,13 @@ cpc_status cpc_launch_count(const cpc_ctx *c, int64_t *launches) {
   return CPC_OK;
 }
 
-cpc_status cpc_host_pi_thresholds(const cpc_params *p, double *thr) {
+cpc_status cpc_host_pi_thresholds(const cpc_params *p, double *thr) try {
   if (!p || !thr) return fail(nullptr, CPC_ERR_INVALID, "null argument");
   if (p->n_p_bin <= 0 || p->n_p_bin > kMaxPi) return fail(nullptr, CPC_ERR_INVALID, "n_p_bin out of range");
   const int rc = pi_thresholds(p->n_p_bin, p->p_min, p->p_max, thr);
   return rc == 0 ? CPC_OK : fail(nullptr, CPC_ERR_INVALID, "threshold derivation failed");
+} catch (...) {
+  return host_exception(nullptr);
 }
 
 }  // extern "C"

@@ -5,6 +5,7 @@
 // (initialization.cpp:357-444), because they are printed in the outputs.
 #include <cmath>
 #include <cstdio>
+#include <new>
 #include <sstream>
 
 #include "host.h"
@@ -440,7 +441,7 @@ extern "C" cpc_status cpc_host_finalize_cross(const char *inp_path, const int64_
                                               const double *sd_sums, const int64_t *srd_num,
                                               const double *srd_sums, const int64_t *drs_num,
                                               const double *drs_sums, const int64_t *rsrd_num,
-                                              const double *rsrd_sums, const double *weights) {
+                                              const double *rsrd_sums, const double *weights) try {
   using namespace cpch;
   if (!inp_path || !weights) return CPC_ERR_INVALID;
   Info d;
@@ -466,6 +467,10 @@ extern "C" cpc_status cpc_host_finalize_cross(const char *inp_path, const int64_
   if (do_bining(d, SS, SRs, RsRs, SD, SRd, DRs, RsRd, err)) return CPC_ERR_INVALID;
   outp_data_info(d, d.out_file + "inp2.info");
   return CPC_OK;
+} catch (const std::bad_alloc &) {
+  return CPC_ERR_NOMEM;
+} catch (...) {
+  return CPC_ERR_HOST;
 }
 
 // C ABI: finalisation and output files of an auto-correlation run (the auto
@@ -474,7 +479,7 @@ extern "C" cpc_status cpc_host_finalize_cross(const char *inp_path, const int64_
 extern "C" cpc_status cpc_host_finalize_auto(const char *inp_path, const int64_t *ss_num,
                                              const double *ss_sums, const int64_t *srs_num,
                                              const double *srs_sums, const int64_t *rsrs_num,
-                                             const double *rsrs_sums, const double *weights) {
+                                             const double *rsrs_sums, const double *weights) try {
   using namespace cpch;
   if (!inp_path || !weights) return CPC_ERR_INVALID;
   Info d;
@@ -492,4 +497,8 @@ extern "C" cpc_status cpc_host_finalize_auto(const char *inp_path, const int64_t
   if (do_bining_auto(d, SS, SRs, RsRs, err)) return CPC_ERR_INVALID;
   outp_data_info(d, d.out_file + "inp2.info");
   return CPC_OK;
+} catch (const std::bad_alloc &) {
+  return CPC_ERR_NOMEM;
+} catch (...) {
+  return CPC_ERR_HOST;
 }

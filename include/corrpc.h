@@ -37,7 +37,8 @@ typedef enum {
   CPC_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
   CPC_ERR_STATE = 5,       /* call order (e.g. count before upload) */
   CPC_ERR_RANGE = 6,       /* data out of range (jackknife label, NaN position) */
-  CPC_ERR_NODEVICE = 7     /* no CUDA device */
+  CPC_ERR_NODEVICE = 7,    /* no CUDA device */
+  CPC_ERR_HOST = 8         /* other host-side failure (e.g. a thread could not start) */
 } cpc_status;
 
 /* pair type: the data_info.do_* flag set around each corels2 call

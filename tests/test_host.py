@@ -39,6 +39,26 @@ def test_rand_stream_matches_oracle_and_glibc():
     assert np.array_equal(_lib.rand_uniform(124693517, 1234, 10), o[1234:1244])
 
 
+def test_host_exception_becomes_a_status():
+    """A C++ exception inside an entry point (here the length_error of a host
+    vector longer than its max_size, thrown before anything is allocated) comes
+    back as a status and a message instead of ending the process."""
+    lib = _lib.load()
+    out = np.empty(1)
+    st = lib.cpc_host_rand_uniform(1, 0, 1 << 62, out.ctypes.data)
+    assert _lib.STATUS_NAMES[st] == "CPC_ERR_NOMEM"
+    assert b"host allocation too large" in lib.cpc_last_error(None)
+    # the library keeps working afterwards
+    assert np.array_equal(_lib.rand_uniform(7, 0, 3), oracle.glibc_rand(7, 0, 3) / 2147483648.0)
+
+
+def test_status_codes_match_header():
+    text = open(os.path.join(os.path.dirname(__file__), "..", "include", "corrpc.h")).read()
+    enum = text[text.index("typedef enum {"):text.index("} cpc_status;")]
+    codes = {int(v): k for k, v in re.findall(r"(CPC_\w+) = (\d+)", enum)}
+    assert codes == _lib.STATUS_NAMES
+
+
 def test_elip_angle_matches_reference_formula():
     rng = np.random.default_rng(3)
     e1, e2 = rng.normal(0, 0.5, 4000), rng.normal(0, 0.5, 4000)
