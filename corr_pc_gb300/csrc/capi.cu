@@ -11,7 +11,6 @@
 #include <exception>
 #include <map>
 #include <memory>
-#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <system_error>
@@ -34,8 +33,8 @@ using namespace cpc;
 
 namespace {
 
-std::mutex g_err_mu;
-std::string g_err;
+// message of the calling thread's last failing call (entry points without a context)
+thread_local std::string g_err;
 
 template <class T>
 struct DevBuf {
@@ -178,7 +177,6 @@ namespace {
 cpc_status fail(cpc_ctx *c, cpc_status s, const std::string &msg) noexcept {
   try {
     if (c) c->err = msg;
-    std::lock_guard<std::mutex> lk(g_err_mu);
     g_err = msg;
   } catch (...) {
   }
@@ -1686,7 +1684,6 @@ const char *cpc_version(void) { return "corr_pc_gb300 0.1 (sm_103a)"; }
 
 const char *cpc_last_error(const cpc_ctx *ctx) {
   if (ctx) return ctx->err.c_str();
-  std::lock_guard<std::mutex> lk(g_err_mu);
   return g_err.c_str();
 }
 

@@ -138,8 +138,9 @@ cpc_status cpc_create(cpc_ctx **ctx, const cpc_params *params);
 /* Destroy a context and free its device memory (NULL is a no-op). */
 cpc_status cpc_destroy(cpc_ctx *ctx);
 
-/* Message for the last failing call on ctx (or a global message if ctx is
- * NULL).  The pointer stays valid until the next call on ctx. */
+/* Message for the last failing call on ctx, or, for ctx NULL, of the calling
+ * thread's last failing call (any entry point).  The pointer stays valid until
+ * the next call on ctx (for NULL: the thread's next failing call). */
 const char *cpc_last_error(const cpc_ctx *ctx);
 
 /* Copy a catalogue into slot `slot` (0..7) and build its on-device cell list

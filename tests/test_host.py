@@ -52,6 +52,24 @@ def test_host_exception_becomes_a_status():
     assert np.array_equal(_lib.rand_uniform(7, 0, 3), oracle.glibc_rand(7, 0, 3) / 2147483648.0)
 
 
+def test_context_free_messages_are_per_thread():
+    """cpc_last_error(NULL) reports the calling thread's own last failure."""
+    import threading
+    lib = _lib.load()
+    assert lib.cpc_host_rand_uniform(1, 0, -1, None) != 0
+    seen = []
+
+    def other():
+        assert lib.cpc_host_rp_thresholds(None, None) != 0
+        seen.append(lib.cpc_last_error(None))
+
+    t = threading.Thread(target=other)
+    t.start()
+    t.join()
+    assert seen == [b"null argument"]
+    assert lib.cpc_last_error(None) == b"bad arguments"
+
+
 def test_status_codes_match_header():
     text = open(os.path.join(os.path.dirname(__file__), "..", "include", "corrpc.h")).read()
     enum = text[text.index("typedef enum {"):text.index("} cpc_status;")]
