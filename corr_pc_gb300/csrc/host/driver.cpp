@@ -145,6 +145,7 @@ int run_prepare(Run &r, const char *inp, cpc_engine eng, bool defer_sd) {
   for (Bins *b : {&r.SS, &r.SRs, &r.RsRs, &r.SD, &r.SRd, &r.DRs, &r.RsRd}) b->init(d, nh);
   // do_corr.cpp:40-52: S, then the shape randoms; slots S 0, Rs 1, D 2, Rd 3
   int64_t draws = 0;
+  TextCache files;  // S and D (Rs and Rd) naming the same files parse them once
   auto upload = [&](int slot, const Catalog &c) {
     cpc_catalog v = c.view();
     if (cpc_upload(ctx.c, slot, &v) != CPC_OK) {
@@ -153,10 +154,10 @@ int run_prepare(Run &r, const char *inp, cpc_engine eng, bool defer_sd) {
     }
     return 0;
   };
-  if (read_catalog(d, ROLE_S, r.S, draws, err)) { std::cout << err << std::endl; return 1; }
+  if (read_catalog(d, ROLE_S, r.S, draws, err, &files)) { std::cout << err << std::endl; return 1; }
   if (upload(0, r.S)) return 1;
   if (read_rs) {
-    if (read_catalog(d, ROLE_RS, r.Rs, draws, err)) { std::cout << err << std::endl; return 1; }
+    if (read_catalog(d, ROLE_RS, r.Rs, draws, err, &files)) { std::cout << err << std::endl; return 1; }
     if (upload(1, r.Rs)) return 1;
   }
   // do_corr.cpp:56-81: auto pair types
@@ -172,10 +173,10 @@ int run_prepare(Run &r, const char *inp, cpc_engine eng, bool defer_sd) {
   }
   // do_corr.cpp:83-133: cross pair types
   if (d.do_cross_corr) {
-    if (read_catalog(d, ROLE_D, r.D, draws, err)) { std::cout << err << std::endl; return 1; }
+    if (read_catalog(d, ROLE_D, r.D, draws, err, &files)) { std::cout << err << std::endl; return 1; }
     if (upload(2, r.D)) return 1;
     if (!d.RsRd_same) {
-      if (read_catalog(d, ROLE_RD, r.Rd, draws, err)) { std::cout << err << std::endl; return 1; }
+      if (read_catalog(d, ROLE_RD, r.Rd, draws, err, &files)) { std::cout << err << std::endl; return 1; }
       if (upload(3, r.Rd)) return 1;
       if (count_term(ctx, d, CPC_PAIR_SRD, 3, 0, r.SRd, eng, r.terms)) return 1;
       if (count_term(ctx, d, CPC_PAIR_RSRD, 3, 1, r.RsRd, eng, r.terms)) return 1;

@@ -3,6 +3,7 @@
 // analytic periodic-box RR of PB_calcs.cpp:63-85).  Bin edges are formed in
 // single precision exactly as the reference's initialisers do
 // (initialization.cpp:357-444), because they are printed in the outputs.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <new>
@@ -301,29 +302,49 @@ void final_calc_auto(Info &d, Bins &ss, Bins &sr, Bins &rr, Bins &fin, int h) {
   integrate(fin, h, d);
 }
 
+// One output table: sample h of a bin tree, as outp_bins (1-D) or outp_2Dbins.
+struct OutTable {
+  const Bins *b;
+  int h;
+  bool two_d;
+  std::string path;
+};
+
+// Write the tables on the host's cores (each file depends only on its own
+// sample, which is final once queued); nonzero if any could not be written.
+int write_tables(const std::vector<OutTable> &ts) {
+  std::atomic<int> bad{0};
+  run_parallel((int64_t)ts.size(), [&](int64_t i) {
+    const OutTable &t = ts[i];
+    if ((t.two_d ? outp_2Dbins(*t.b, t.h, t.path) : outp_bins(*t.b, t.h, t.path)) != 0) bad = 1;
+  });
+  return bad.load();
+}
+
 }  // namespace
 
 // do_bining's auto part (do_corr.cpp:220-324)
 int do_bining_auto(Info &d, Bins &SS, Bins &SRs, Bins &RsRs, std::string &err) {
   const std::string &o = d.out_file;
   int bad = 0;
+  std::vector<OutTable> out;
   if (d.do_auto_rebin) {
     re_bin(SS, 0, d);
     re_bin(SRs, 0, d);
     re_bin(RsRs, 0, d);
     bad |= outp_2Dbins(SRs, 0, o + "bins_auto_SR2.temp");
   }
-  Bins fin;
+  Bins fin, jk;
   fin.init(d, SS.nh);
   final_calc_auto(d, SS, SRs, RsRs, fin, 0);
-  bad |= outp_bins(fin, 0, o + "bins_auto_final.dat");
-  bad |= outp_bins(SS, 0, o + "bins_auto_SS.dat");
-  bad |= outp_bins(SRs, 0, o + "bins_auto_SR.dat");
-  bad |= outp_bins(RsRs, 0, o + "bins_auto_RR.dat");
-  bad |= outp_2Dbins(fin, 0, o + "bins2D_auto_final.dat");
-  bad |= outp_2Dbins(SS, 0, o + "bins2D_auto_SS.dat");
-  bad |= outp_2Dbins(SRs, 0, o + "bins2D_auto_SR.dat");
-  bad |= outp_2Dbins(RsRs, 0, o + "bins2D_auto_RR.dat");
+  out.push_back({&fin, 0, false, o + "bins_auto_final.dat"});
+  out.push_back({&SS, 0, false, o + "bins_auto_SS.dat"});
+  out.push_back({&SRs, 0, false, o + "bins_auto_SR.dat"});
+  out.push_back({&RsRs, 0, false, o + "bins_auto_RR.dat"});
+  out.push_back({&fin, 0, true, o + "bins2D_auto_final.dat"});
+  out.push_back({&SS, 0, true, o + "bins2D_auto_SS.dat"});
+  out.push_back({&SRs, 0, true, o + "bins2D_auto_SR.dat"});
+  out.push_back({&RsRs, 0, true, o + "bins2D_auto_RR.dat"});
   if (d.do_jk) {
     for (int r = 0; r < d.n_jk; r++) {
       const int h = r + 1;
@@ -335,23 +356,23 @@ int do_bining_auto(Info &d, Bins &SS, Bins &SRs, Bins &RsRs, std::string &err) {
       final_calc_auto(d, SS, SRs, RsRs, fin, h);
       const std::string s = o + "bins_auto_jk" + std::to_string(r);
       const std::string s2 = o + "bins2D_auto_jk" + std::to_string(r);
-      bad |= outp_bins(SS, h, s + "_SS.dat");
-      bad |= outp_bins(RsRs, h, s + "_RR.dat");
-      bad |= outp_bins(SRs, h, s + "_SR.dat");
-      bad |= outp_bins(fin, h, s + "_final.dat");
-      bad |= outp_2Dbins(fin, h, s2 + "_final.dat");
-      bad |= outp_2Dbins(SS, h, s2 + "_SS.dat");
-      bad |= outp_2Dbins(RsRs, h, s2 + "_RR.dat");
-      bad |= outp_2Dbins(SRs, h, s2 + "_SR.dat");
+      out.push_back({&SS, h, false, s + "_SS.dat"});
+      out.push_back({&RsRs, h, false, s + "_RR.dat"});
+      out.push_back({&SRs, h, false, s + "_SR.dat"});
+      out.push_back({&fin, h, false, s + "_final.dat"});
+      out.push_back({&fin, h, true, s2 + "_final.dat"});
+      out.push_back({&SS, h, true, s2 + "_SS.dat"});
+      out.push_back({&RsRs, h, true, s2 + "_RR.dat"});
+      out.push_back({&SRs, h, true, s2 + "_SR.dat"});
     }
     if (d.do_jk == 1) {
-      Bins jk;
       jk.init(d, 1);
       jk_final(jk, fin, d);
-      bad |= outp_bins(jk, 0, o + "bins_auto_jk_final.dat");
-      bad |= outp_2Dbins(jk, 0, o + "bins2D_auto_jk_final.dat");
+      out.push_back({&jk, 0, false, o + "bins_auto_jk_final.dat"});
+      out.push_back({&jk, 0, true, o + "bins2D_auto_jk_final.dat"});
     }
   }
+  bad |= write_tables(out);
   if (bad) {
     err = "could not write output files with prefix " + o;
     return 1;
@@ -389,42 +410,43 @@ int do_bining(Info &d, Bins &SS, Bins &SRs, Bins &RsRs, Bins &SD, Bins &SRd, Bin
 int do_bining_cross(Info &d, Bins &SD, Bins &SRd, Bins &DRs, Bins &RsRd, std::string &err) {
   const std::string &o = d.out_file;
   int bad = 0;
-  Bins fin;
+  std::vector<OutTable> out;
+  Bins fin, jk;
   fin.init(d, SD.nh);
   final_calc(d, SD, SRd, DRs, RsRd, fin, 0);
-  bad |= outp_bins(fin, 0, o + "bins_cross_final.dat");
-  bad |= outp_2Dbins(fin, 0, o + "bins2D_cross_final.dat");
-  bad |= outp_bins(SD, 0, o + "bins_cross_SD.dat");
-  bad |= outp_2Dbins(SD, 0, o + "bins2D_cross_SD.dat");
-  bad |= outp_bins(SRd, 0, o + "bins_cross_SR.dat");
-  bad |= outp_2Dbins(SRd, 0, o + "bins2D_cross_SR.dat");
-  bad |= outp_bins(DRs, 0, o + "bins_cross_DR.dat");
-  bad |= outp_2Dbins(DRs, 0, o + "bins2D_cross_DR.dat");
-  bad |= outp_bins(RsRd, 0, o + "bins_cross_RR.dat");
-  bad |= outp_2Dbins(RsRd, 0, o + "bins2D_cross_RR.dat");
+  out.push_back({&fin, 0, false, o + "bins_cross_final.dat"});
+  out.push_back({&fin, 0, true, o + "bins2D_cross_final.dat"});
+  out.push_back({&SD, 0, false, o + "bins_cross_SD.dat"});
+  out.push_back({&SD, 0, true, o + "bins2D_cross_SD.dat"});
+  out.push_back({&SRd, 0, false, o + "bins_cross_SR.dat"});
+  out.push_back({&SRd, 0, true, o + "bins2D_cross_SR.dat"});
+  out.push_back({&DRs, 0, false, o + "bins_cross_DR.dat"});
+  out.push_back({&DRs, 0, true, o + "bins2D_cross_DR.dat"});
+  out.push_back({&RsRd, 0, false, o + "bins_cross_RR.dat"});
+  out.push_back({&RsRd, 0, true, o + "bins2D_cross_RR.dat"});
   if (d.do_jk) {
     for (int r = 0; r < d.n_jk; r++) {
       const int h = r + 1;
       final_calc(d, SD, SRd, DRs, RsRd, fin, h);
       const std::string s = o + "bins_cross_jk" + std::to_string(r);
       const std::string s2 = o + "bins2D_cross_jk" + std::to_string(r);
-      bad |= outp_bins(SD, h, s + "_SD.dat");
-      bad |= outp_bins(RsRd, h, s + "_RR.dat");
-      bad |= outp_bins(DRs, h, s + "_DR.dat");
-      bad |= outp_bins(SRd, h, s + "_SR.dat");
-      bad |= outp_bins(fin, h, s + "_final.dat");
-      bad |= outp_2Dbins(fin, h, s2 + "_final.dat");
-      bad |= outp_2Dbins(SD, h, s2 + "_SD.dat");
-      bad |= outp_2Dbins(RsRd, h, s2 + "_RR.dat");
-      bad |= outp_2Dbins(DRs, h, s2 + "_DR.dat");
-      bad |= outp_2Dbins(SRd, h, s2 + "_SR.dat");
+      out.push_back({&SD, h, false, s + "_SD.dat"});
+      out.push_back({&RsRd, h, false, s + "_RR.dat"});
+      out.push_back({&DRs, h, false, s + "_DR.dat"});
+      out.push_back({&SRd, h, false, s + "_SR.dat"});
+      out.push_back({&fin, h, false, s + "_final.dat"});
+      out.push_back({&fin, h, true, s2 + "_final.dat"});
+      out.push_back({&SD, h, true, s2 + "_SD.dat"});
+      out.push_back({&RsRd, h, true, s2 + "_RR.dat"});
+      out.push_back({&DRs, h, true, s2 + "_DR.dat"});
+      out.push_back({&SRd, h, true, s2 + "_SR.dat"});
     }
-    Bins jk;
     jk.init(d, 1);
     jk_final(jk, fin, d);
-    bad |= outp_bins(jk, 0, o + "bins_cross_jk_final.dat");
-    bad |= outp_2Dbins(jk, 0, o + "bins2D_cross_jk_final.dat");
+    out.push_back({&jk, 0, false, o + "bins_cross_jk_final.dat"});
+    out.push_back({&jk, 0, true, o + "bins2D_cross_jk_final.dat"});
   }
+  bad |= write_tables(out);
   if (bad) {
     err = "could not write output files with prefix " + o;
     return 1;

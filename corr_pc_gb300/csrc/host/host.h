@@ -9,13 +9,57 @@
 //   outp.cpp     outp_bins / outp_2Dbins / outp_data_info (outp.cpp:45-162)
 //   driver.cpp   corr_pc command line: main + do_corr    (main.cpp, do_corr.cpp)
 #pragma once
+#include <algorithm>
+#include <atomic>
 #include <cstdint>
+#include <exception>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "../../../include/corrpc.h"
 
 namespace cpch {
+
+// Run task(i) for every i in [0, n) on the host's cores: the calling thread and
+// up to 63 workers take indices from a shared counter.  When a worker cannot
+// be started the others do its share; the first exception a task throws is
+// rethrown here once every thread has stopped.
+template <class F>
+void run_parallel(int64_t n, F &&task) {
+  if (n <= 0) return;
+  const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const int64_t nt = std::min<int64_t>({hw, n, 64});
+  std::atomic<int64_t> next{0};
+  std::exception_ptr first;
+  std::mutex mu;
+  auto work = [&] {
+    for (int64_t i; (i = next.fetch_add(1)) < n;) {
+      try {
+        task(i);
+      } catch (...) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!first) first = std::current_exception();
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int64_t t = 1; t < nt; t++) {
+    try {
+      th.emplace_back(work);
+    } catch (const std::system_error &) {
+      break;
+    }
+  }
+  work();
+  for (auto &x : th) x.join();
+  if (first) std::rethrow_exception(first);
+}
 
 // data_info (data_def.h:46-96): the fields read from the .inp plus the values
 // data_ini derives.
@@ -62,9 +106,17 @@ struct Catalog {
   cpc_catalog view() const;
 };
 enum Role { ROLE_S = 0, ROLE_D = 1, ROLE_RS = 2, ROLE_RD = 3 };
+// The number files of one run, each parsed once: samples that name the same
+// file (S and D from one catalogue, as the notebooks write them) share it.
+struct TextCache {
+  std::map<std::string, std::shared_ptr<const std::vector<double>>> reals;
+  std::map<std::string, std::shared_ptr<const std::vector<int32_t>>> ints;
+};
 // read one sample like read_data; `draws` is the running index into the glibc
-// rand() stream (advanced by the draws this sample consumes).
-int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &err);
+// rand() stream (advanced by the draws this sample consumes).  Files already
+// in `cache` are not read again; files read are added to it.
+int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &err,
+                 TextCache *cache = nullptr);
 
 // bin tree of one term (bin_jk: full sample + n_jk jackknife samples)
 struct Bins {

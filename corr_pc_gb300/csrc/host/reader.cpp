@@ -7,12 +7,11 @@
 // jackknife), phi (elip_angle, or -10 without shapes), include_prob (a second
 // draw for random catalogues), the table distances D_C and D_A of a non-periodic
 // run, and the weight totals.  Numbers are parsed with
-// std::from_chars, which rounds exactly as the reference's istream >> double.
+// std::from_chars, which rounds exactly as the reference's istream >> double,
+// in chunks on the host's cores.
 #include <charconv>
 #include <cmath>
 #include <cstdio>
-#include <fstream>
-#include <sstream>
 
 #include "../host_helpers.h"
 #include "host.h"
@@ -21,41 +20,125 @@ namespace cpch {
 
 namespace {
 
+inline bool is_ws(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r'; }
+
+// The whole file in one buffer; false if it cannot be opened.
+bool slurp(const std::string &path, std::string &buf) {
+  FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  buf.clear();
+  if (std::fseek(f, 0, SEEK_END) == 0) {
+    const long sz = std::ftell(f);
+    if (sz > 0) buf.reserve((size_t)sz);
+    std::rewind(f);
+  }
+  char tmp[1 << 16];
+  size_t k;
+  while ((k = std::fread(tmp, 1, sizeof tmp, f)) > 0) buf.append(tmp, k);
+  std::fclose(f);
+  return true;
+}
+
+// Numbers of [b, e) in order, as istream >> reads them one after another:
+// whitespace skipped, one leading '+' allowed, each number the longest prefix
+// from_chars accepts.  Returns true when it stopped at something that is not a
+// number (the numbers after it are never read).
+template <class T>
+bool parse_span(const char *b, const char *e, std::vector<T> &out) {
+  const char *p = b;
+  for (;;) {
+    while (p < e && is_ws(*p)) p++;
+    if (p >= e) return false;
+    const char *q = *p == '+' ? p + 1 : p;
+    T v;
+    const auto r = std::from_chars(q, e, v);
+    if (r.ec != std::errc()) return true;
+    out.push_back(v);
+    p = r.ptr;
+  }
+}
+
+// parse_span over a whole file, in chunks of >= 1 MiB on the host's cores.
+// Chunks start at whitespace, where the sequential reader always starts a new
+// number (no number contains whitespace), so the numbers are the same; the
+// list ends at the first chunk that stopped early.
+template <class T>
+std::vector<T> parse_numbers(const std::string &buf) {
+  const size_t n = buf.size();
+  const char *b = buf.data();
+  const int64_t parts = (int64_t)std::min<size_t>(256, std::max<size_t>(1, n >> 20));
+  std::vector<T> out;
+  if (parts == 1) {
+    parse_span(b, b + n, out);
+    return out;
+  }
+  std::vector<size_t> cut(parts + 1);
+  cut[0] = 0;
+  cut[parts] = n;
+  for (int64_t t = 1; t < parts; t++) {
+    size_t c = std::max(cut[t - 1], n * (size_t)t / (size_t)parts);
+    while (c < n && !is_ws(b[c])) c++;
+    cut[t] = c;
+  }
+  std::vector<std::vector<T>> piece(parts);
+  std::vector<char> stopped(parts, 0);
+  run_parallel(parts, [&](int64_t t) {
+    piece[t].reserve((cut[t + 1] - cut[t]) / 8);
+    stopped[t] = parse_span(b + cut[t], b + cut[t + 1], piece[t]);
+  });
+  size_t total = 0;
+  int64_t last = parts - 1;
+  for (int64_t t = 0; t < parts; t++) {
+    total += piece[t].size();
+    if (stopped[t]) { last = t; break; }
+  }
+  out.resize(total);
+  size_t at = 0;
+  for (int64_t t = 0; t <= last; t++) {
+    std::copy(piece[t].begin(), piece[t].end(), out.begin() + at);
+    at += piece[t].size();
+    std::vector<T>().swap(piece[t]);
+  }
+  return out;
+}
+
+// One number file of a sample, read in order by get().
 struct TextCols {
-  std::string buf;
+  std::shared_ptr<const std::vector<double>> reals;
+  std::shared_ptr<const std::vector<int32_t>> ints;
   size_t pos = 0;
-  bool open(const std::string &path) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f.is_open()) return false;
-    std::ostringstream ss;
-    ss << f.rdbuf();
-    buf = ss.str();
-    pos = 0;
+  template <class T, class M>
+  static bool load(const std::string &path, TextCache *cache, M &map,
+                   std::shared_ptr<const std::vector<T>> &dst) {
+    if (cache) {
+      auto it = map.find(path);
+      if (it != map.end()) {
+        dst = it->second;
+        return true;
+      }
+    }
+    std::string buf;
+    if (!slurp(path, buf)) return false;
+    dst = std::make_shared<const std::vector<T>>(parse_numbers<T>(buf));
+    if (cache) map[path] = dst;
     return true;
   }
-  void skip_ws() {
-    while (pos < buf.size() && (buf[pos] == ' ' || buf[pos] == '\t' || buf[pos] == '\n' ||
-                                buf[pos] == '\r'))
-      pos++;
+  bool open(const std::string &path, TextCache *cache) {
+    TextCache local;
+    return load(path, cache, cache ? cache->reals : local.reals, reals);
+  }
+  bool open_ints(const std::string &path, TextCache *cache) {
+    TextCache local;
+    return load(path, cache, cache ? cache->ints : local.ints, ints);
   }
   bool get(double &v) {
-    skip_ws();
-    if (pos >= buf.size()) return false;
-    const char *b = buf.data() + pos, *e = buf.data() + buf.size();
-    if (*b == '+') b++;
-    auto r = std::from_chars(b, e, v);
-    if (r.ec != std::errc()) return false;
-    pos = r.ptr - buf.data();
+    if (!reals || pos >= reals->size()) return false;
+    v = (*reals)[pos++];
     return true;
   }
   bool get(int32_t &v) {
-    skip_ws();
-    if (pos >= buf.size()) return false;
-    const char *b = buf.data() + pos, *e = buf.data() + buf.size();
-    if (*b == '+') b++;
-    auto r = std::from_chars(b, e, v);
-    if (r.ec != std::errc()) return false;
-    pos = r.ptr - buf.data();
+    if (!ints || pos >= ints->size()) return false;
+    v = (*ints)[pos++];
     return true;
   }
 };
@@ -127,7 +210,8 @@ cpc_catalog Catalog::view() const {
   return c;
 }
 
-int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &err) {
+int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &err,
+                 TextCache *cache) {
   const EFlags ef = e_flags(d, role);
   std::string p_f, z_f, w_f, jk_f;
   const std::string &e_f = ef.file;
@@ -151,11 +235,11 @@ int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &er
   const bool randoms = role == ROLE_RS || role == ROLE_RD;
   const bool read_jk = jk_f != "0" && d.do_jk;
   TextCols fp, fz, fe, fw, fj;
-  if (!fp.open(p_f)) { err = "pos file not open: " + p_f; return 1; }
-  if (!fz.open(z_f)) { err = "z file not open: " + z_f; return 1; }
-  if (w_f != "0" && !fw.open(w_f)) { err = "wt file not open: " + w_f; return 1; }
-  if (read_jk && !fj.open(jk_f)) { err = "jk file not open: " + jk_f; return 1; }
-  if (ef.any() && !fe.open(e_f)) { err = "e file not open: " + e_f; return 1; }
+  if (!fp.open(p_f, cache)) { err = "pos file not open: " + p_f; return 1; }
+  if (!fz.open(z_f, cache)) { err = "z file not open: " + z_f; return 1; }
+  if (w_f != "0" && !fw.open(w_f, cache)) { err = "wt file not open: " + w_f; return 1; }
+  if (read_jk && !fj.open_ints(jk_f, cache)) { err = "jk file not open: " + jk_f; return 1; }
+  if (ef.any() && !fe.open(e_f, cache)) { err = "e file not open: " + e_f; return 1; }
   const uint32_t seed = d.periodic_box ? 124693517u : 1u;  // srand only in a box
   cpc::GlibcRand rng(seed);
   for (int64_t s = 0; s < draws; s++) rng.next();

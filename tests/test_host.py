@@ -315,7 +315,7 @@ def asan_driver(tmp_path_factory):
     srcs = [os.path.join(ROOT, "tests", "host_asan_driver.cpp")] + [
         os.path.join(csrc, s) for s in ("host/inp.cpp", "host/reader.cpp", "host/finalize.cpp",
                                         "host/outp.cpp", "host_helpers.cpp")]
-    r = subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined",
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-pthread", "-fsanitize=address,undefined",
                         "-fno-sanitize-recover=all", "-fno-omit-frame-pointer",
                         "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-I" + csrc,
                         *srcs, "-o", exe], capture_output=True, text=True)
@@ -356,3 +356,54 @@ def test_host_pipeline_under_address_and_ub_sanitizers(name, asan_driver, tmp_pa
         path = tmp_path / "out" / ("run_" + fname)
         assert path.exists(), fname
         compare_files(path.read_text(), ref, label=f"{name}:{fname} (sanitized host)")
+
+
+def _run_sanitized(args):
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0:exitcode=23",
+               UBSAN_OPTIONS="print_stacktrace=1")
+    return subprocess.run(args, capture_output=True, text=True, env=env, timeout=600)
+
+
+def test_chunked_reader_under_sanitizers(asan_driver, tmp_path):
+    """The C++ catalogue reader parses each file in ~1 MiB chunks on several
+    threads and parses a file that S and D share once: on a 300k-galaxy box
+    (files of 7-16 MB) it returns exactly the written values, the oracle's
+    rand() draws and angles, and on a file with a bad value the row at which
+    the sequential reader stops."""
+    cat = synth.uniform_box(300000, 500.0, 11, nside_jk=4, with_shapes=True)
+    p = synth._box_params(which_corr=1, L=500.0, rmin=0.1, rmax=60.0, nrp=20, npi=40,
+                          pmax=100.0, njk=64, n=cat.n)
+    inp = synth.write_box_run(str(tmp_path), synth.Workload("chunked", p, cat, cat))
+    assert os.path.getsize(str(tmp_path / "S_pos.dat")) > 8 << 20
+    out = str(tmp_path / "dump.bin")
+    r = _run_sanitized([asan_driver, "--dump", inp, out])
+    assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-4000:])
+    assert "runtime error" not in r.stderr, r.stderr[-4000:]
+    raw = open(out, "rb").read()
+    ref = oracle.read_like_reference(p, [("S", cat), ("D", cat)])
+    at = 0
+    for role in ("S", "D"):
+        n = int(np.frombuffer(raw, np.int64, 1, at)[0])
+        at += 8
+        assert n == cat.n
+        cols = np.frombuffer(raw, np.float64, 8 * n, at).reshape(8, n)
+        at += 64 * n
+        jk = np.frombuffer(raw, np.int32, n, at)
+        at += 4 * n
+        e1, e2 = (np.zeros(n) if e is None else e for e in (ref[role].e1, ref[role].e2))
+        assert (role == "S") == (ref[role].e1 is not None)  # D carries no shapes in wg+
+        for k, want in enumerate((cat.x, cat.y, cat.z, np.ones(n), ref[role].phi,
+                                  ref[role].jk_prob, e1, e2)):
+            assert np.array_equal(cols[k], want), (role, k)
+        assert np.array_equal(jk, cat.jk)
+    # a value that is not a number in the middle of the z file: reading stops
+    # at that row, as the sequential reader does
+    zf = str(tmp_path / "S_z.dat")
+    lines = open(zf).read().split("\n")
+    bad_row = 171234
+    lines[bad_row] = "x" + lines[bad_row]
+    open(zf, "w").write("\n".join(lines))
+    r = _run_sanitized([asan_driver, "--dump", inp, out])
+    assert r.returncode == 1
+    assert f"gal data reading ended unexpectedly at row {bad_row} " in r.stdout, r.stdout
+    assert "runtime error" not in r.stderr
