@@ -407,3 +407,56 @@ def test_chunked_reader_under_sanitizers(asan_driver, tmp_path):
     assert r.returncode == 1
     assert f"gal data reading ended unexpectedly at row {bad_row} " in r.stdout, r.stdout
     assert "runtime error" not in r.stderr
+
+
+def test_host_threads_under_thread_sanitizer(tmp_path):
+    """The host side's threads (chunked parsing of the catalogue files, the
+    output tables written in parallel) under ThreadSanitizer: no data race
+    reported, and the reference's output files."""
+    import shutil
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    csrc = os.path.join(ROOT, "corr_pc_gb300", "csrc")
+    exe = str(tmp_path / "host_tsan_driver")
+    srcs = [os.path.join(ROOT, "tests", "host_asan_driver.cpp")] + [
+        os.path.join(csrc, s) for s in ("host/inp.cpp", "host/reader.cpp", "host/finalize.cpp",
+                                        "host/outp.cpp", "host_helpers.cpp")]
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-pthread", "-fsanitize=thread",
+                        "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-I" + csrc,
+                        *srcs, "-o", exe], capture_output=True, text=True)
+    if r.returncode != 0 and "tsan" in (r.stderr or "").lower():
+        pytest.skip("thread sanitizer runtime not available: " + r.stderr[-300:])
+    assert r.returncode == 0, r.stderr
+    env = dict(os.environ, TSAN_OPTIONS="halt_on_error=1:exitcode=66")
+    # a 300k-galaxy box: files of several MiB, parsed in chunks
+    cat = synth.uniform_box(300000, 500.0, 5, nside_jk=3, with_shapes=True)
+    p = synth._box_params(which_corr=2, L=500.0, rmin=0.1, rmax=60.0, nrp=20, npi=40,
+                          pmax=100.0, njk=27, n=cat.n)
+    big = tmp_path / "big"
+    inp = synth.write_box_run(str(big), synth.Workload("tsan", p, cat, cat))
+    r = subprocess.run([exe, "--dump", inp, str(big / "dump.bin")], capture_output=True,
+                       text=True, env=env, timeout=600)
+    if "FATAL: ThreadSanitizer" in r.stderr:
+        pytest.skip("thread sanitizer cannot run here: " + r.stderr[-300:])
+    assert r.returncode == 0 and "WARNING: ThreadSanitizer" not in r.stderr, r.stderr[-4000:]
+    # a golden run with jackknife regions: every output table written in parallel
+    g = Golden("box_wgp_clustered")
+    run = tmp_path / "golden"
+    inp = synth.write_box_run(str(run), synth.Workload("g", g.params, g.S, g.D),
+                              same_files=g.meta["same_files"], n_threads=1)
+    nfile, sfile = str(run / "num.bin"), str(run / "sums.bin")
+    np.ascontiguousarray(g.raw_num, dtype=np.int64).tofile(nfile)
+    np.ascontiguousarray(g.raw_sums, dtype=np.float64).tofile(sfile)
+    r = subprocess.run([exe, inp, nfile, sfile], capture_output=True, text=True, env=env,
+                       timeout=600)
+    assert r.returncode == 0 and "WARNING: ThreadSanitizer" not in r.stderr, r.stderr[-4000:]
+    n_files = 0
+    for fname, ref in g.files.items():
+        if fname.endswith(".info"):
+            continue
+        compare_files((run / "out" / ("run_" + fname)).read_text(), ref,
+                      label=f"{fname} (thread sanitizer)")
+        n_files += 1
+    assert n_files > 0
+    # 27 regions x 10 tables, the full-sample and jackknife-final tables, temporaries
+    assert len(os.listdir(run / "out")) > 27 * 10
