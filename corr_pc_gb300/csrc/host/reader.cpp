@@ -282,7 +282,6 @@ int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &er
     if (read_jk && !fj.get(c.jk[i])) { err = "jk file ended early"; return 1; }
     if (two) {
       if (!fe.get(c.e1[i]) || !fe.get(c.e2[i])) { err = "e file ended early"; return 1; }
-      c.phi[i] = cpc::elip_angle(c.e1[i], c.e2[i]);
     }
     if (ef.e3) {  // read_dat.cpp:282-293: normalised to unit length when non-zero
       if (!fe.get(c.e1[i]) || !fe.get(c.e2[i]) || !fe.get(c.e3[i])) {
@@ -305,6 +304,11 @@ int read_catalog(Info &d, Role role, Catalog &c, int64_t &draws, std::string &er
     wt[0] += c.w[i];
     wt[1] += c.w[i] * c.w[i];
   }
+  if (two)  // phi = elip_angle(e1, e2) per galaxy (read_dat.cpp:279), in blocks on the host's cores
+    run_parallel((n_gal + 65535) / 65536, [&](int64_t b) {
+      const int64_t lo = b * 65536, hi = std::min<int64_t>(n_gal, lo + 65536);
+      for (int64_t i = lo; i < hi; i++) c.phi[i] = cpc::elip_angle(c.e1[i], c.e2[i]);
+    });
   if (!read_jk && d.do_jk) c.jk.assign(n_gal, -1);
   return 0;
 }
