@@ -175,8 +175,10 @@ int run_prepare(Run &r, const char *inp, cpc_engine eng, bool defer_sd) {
   if (d.do_cross_corr) {
     if (read_catalog(d, ROLE_D, r.D, draws, err, &files)) { std::cout << err << std::endl; return 1; }
     if (upload(2, r.D)) return 1;
+    if (d.RsRd_same) files = TextCache();  // D was the last sample read
     if (!d.RsRd_same) {
       if (read_catalog(d, ROLE_RD, r.Rd, draws, err, &files)) { std::cout << err << std::endl; return 1; }
+      files = TextCache();
       if (upload(3, r.Rd)) return 1;
       if (count_term(ctx, d, CPC_PAIR_SRD, 3, 0, r.SRd, eng, r.terms)) return 1;
       if (count_term(ctx, d, CPC_PAIR_RSRD, 3, 1, r.RsRd, eng, r.terms)) return 1;
