@@ -460,3 +460,21 @@ def test_host_threads_under_thread_sanitizer(tmp_path):
     assert n_files > 0
     # 27 regions x 10 tables, the full-sample and jackknife-final tables, temporaries
     assert len(os.listdir(run / "out")) > 27 * 10
+
+
+def test_unwritable_output_prefix_is_an_error(asan_driver, tmp_path):
+    """Output tables written in parallel: one that cannot be opened still makes
+    the finalisation fail with the writer's message."""
+    g = Golden("box_wgp_clustered")
+    wl = synth.Workload("g", g.params, g.S, g.D)
+    inp = synth.write_box_run(str(tmp_path), wl, same_files=g.meta["same_files"], n_threads=1)
+    p = synth.InpParams.read(inp)
+    p.out_file = str(tmp_path / "missing_dir" / "run_")
+    p.write(inp)
+    nfile, sfile = str(tmp_path / "num.bin"), str(tmp_path / "sums.bin")
+    np.ascontiguousarray(g.raw_num, dtype=np.int64).tofile(nfile)
+    np.ascontiguousarray(g.raw_sums, dtype=np.float64).tofile(sfile)
+    r = _run_sanitized([asan_driver, inp, nfile, sfile])
+    assert r.returncode == 1, (r.stdout, r.stderr[-2000:])
+    assert "could not write output files with prefix" in r.stdout
+    assert "runtime error" not in r.stderr
