@@ -1,25 +1,32 @@
 #!/usr/bin/env python3
 """Benchmark of the pair-counting hot path: binned pairs/s.
 
-Default workload: the 200,000-galaxy Neyman-Scott periodic box with shapes
-(wg+ and wgg, 64 jackknife cubes, 20 log r_p x 40 Pi bins) -- the workload the
-headline metric "binned pairs/s (wgg+wg+ w/ jackknife)" is quoted on.  Other
-workloads: --workload box_uniform_wgg_20k | box_ns_wpp_20M | box_batch_wpp_64 |
-box_ns_ed_rmu_200k | box_ns_kappa_200k (the same box with the ED and kappa
-variants) | sky_wgp_500k_5M | sky_wgp_50k_500k (sky survey: SRd, RsRd, SD, DRs
-on a row sample).
+Default workload: the 20,000,000-point Neyman-Scott periodic box with shapes
+(wgg + wg+ + w++ from one which_corr 2 count, 125 jackknife cubes, 25 log r_p
+x 50 Pi bins, float32 positions) -- the configuration the headline target is
+stated on.  Other workloads: --workload box_ns_wgp_200k | box_uniform_wgg_20k |
+box_ns_wpp_2M (the 20M box's geometry at a tenth of the points: the profiling
+case) | box_batch_wpp_64 | box_ns_ed_rmu_200k | box_ns_kappa_200k (the 200k
+box with the ED and kappa variants) | sky_wgp_500k_5M | sky_wgp_50k_500k (sky
+survey: SRd, RsRd, SD, DRs on a row sample).
 
-One step = one corels2 call (the SD pair type these runs use) over the whole
-catalogue.  `value` times the device work with the catalogues resident in HBM
-(CUDA events on the library's stream around the zeroing, the pair kernel and
-the FP64 edge recheck); L2 is flushed (256 MB write) between timed steps.
-`e2e` times the same through the C ABI from host buffers: both uploads (copy +
-on-device cell list) + count + histogram readback, wall clock.
+One step = one corels2 call (the SD pair type these runs use).  On the 20M box
+a step counts one of 20 shards of the work queue (the units i with
+i % 20 == k % 20: every g2 candidate, a twentieth of the outer tiles), so 20
+steps are one full count and the timed region stays near a minute; on the
+other box workloads a step is the whole count.  `value` times the device work
+with the catalogues resident in HBM (CUDA events on the library's stream around
+the zeroing, the pair kernel and the FP64 edge recheck; the on-device cell-list
+build is reported beside it as `cell_list`); the 20M box's inputs (2.3 GB per
+catalogue) exceed L2, the smaller boxes flush L2 (256 MB write) between timed
+steps.  `e2e` times the public C ABI from host buffers, wall clock: both
+uploads (copy + on-device cell list) + the count + the histogram readback (one
+full count on the 20M box).
 
 `--impl reference` times the CPU implementation of the path on this host's
-cores (the oracle restatement of corels2; the reference binary itself is
-built from its sources only where they exist and cannot travel to this host)
-on a bounded row sample per step.
+cores (the oracle restatement of corels2, fed as the reference's read path
+feeds it; the reference binary itself is built from its sources only where
+they exist and cannot travel to this host) on a bounded row sample per step.
 """
 from __future__ import annotations
 
@@ -33,11 +40,16 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "binned pairs/s (wgg+wg+ w/ jackknife) vs plain FP64 GPU & host CPU; % roofline"
 UNIT = "pairs/s"
+DEFAULT_WORKLOAD = "box_ns_wpp_20M"
+# work-queue shards of one full count (one shard per step)
+SHARDS = {"box_ns_wpp_20M": 20}
 
 
 def _workload(name: str):
@@ -48,6 +60,12 @@ def _workload(name: str):
         return [synth.box_uniform_wgg()]
     if name == "box_ns_wpp_20M":
         return [synth.box_ns_large_wpp()]
+    if name == "box_ns_wpp_2M":
+        # the 20M box's geometry and binning at a tenth of the parents: the
+        # profiling case of the w++ kernel (one count about half a second)
+        wl = synth.box_ns_large_wpp(n_parents=20000)
+        wl.name = "box_ns_wpp_2M"
+        return [wl]
     if name == "box_batch_wpp_64":
         return synth.box_batch_wpp()
     if name == "box_ns_ed_rmu_200k":
@@ -59,14 +77,28 @@ def _workload(name: str):
 
 def _describe(wls) -> dict:
     p = wls[0].params
-    d = {"workload": wls[0].name if len(wls) == 1 else "box_batch_wpp_64",
+    name = wls[0].name if len(wls) == 1 else "box_batch_wpp_64"
+    n_pts = int(sum(w.shape.n for w in wls))
+    d = {"workload": name,
          "which_corr": p.which_corr, "coordinates": p.coordinates, "n_jk": p.n_jk_regions,
          "rp_bins": p.n_bins, "pi_bins": p.n_p_bin, "rp_range": [p.bin_r_min, p.bin_r_max],
          "pi_range": [p.p_min, p.p_max], "box": p.periodic_box_size,
-         "n_points": int(sum(w.shape.n for w in wls)), "n_catalogs": len(wls),
+         "n_points": n_pts, "n_catalogs": len(wls),
          "pair_type": "SD (shape x density, S and D the same points)",
-         "l2": "flushed between timed steps (256 MB write)"}
+         "l2": ("inputs larger than L2 (about 2.3 GB per uploaded catalogue)"
+                if n_pts >= 10_000_000 else "flushed between timed steps (256 MB write)")}
     return d
+
+
+def _step_definition(name: str, impl: str) -> str:
+    if impl == "reference":
+        return ("every k-th outer row of the corels2 call (offset changes every step), k sized "
+                "for a bounded sample")
+    k = SHARDS.get(name, 1)
+    if k > 1:
+        return (f"one corels2 call over one of {k} shards of the work queue (units i with "
+                f"i % {k} == step % {k}); {k} steps = one full count")
+    return "one corels2 call over the whole workload"
 
 
 class ClockSampler:
@@ -169,14 +201,20 @@ def _peaks() -> dict:
     return out
 
 
-def _cpu_sample(p, cats, budget_s: float, n_binned_full: int, threads: int, offset: int = 0):
+def _oracle_cats(p, wl):
+    """The oracle's inputs, derived from the synthetic catalogue the way the
+    reference's read path derives them (glibc rand() jackknife draws in read
+    order, elip_angle) by the oracle itself -- independent of the product
+    library."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the CPU baseline and checker (test infrastructure)
+    return oracle.read_like_reference(p, [("S", wl.shape), ("D", wl.density)])
+
+
+def _cpu_sample(p, ocats, budget_s: float, n_binned_full: int, threads: int, offset: int = 0):
     """Time the oracle restatement of corels2 on every k-th outer row."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # the CPU baseline (test infrastructure)
-    ocats = {r: oracle.OracleCatalog(c.x, c.y, c.z, w=c.w, e1=c.e1, e2=c.e2, phi=c.phi,
-                                      jk=c.jk, jk_prob=c.jk_prob, include_prob=c.include_prob,
-                                      e3=getattr(c, "e3", None))
-             for r, c in cats.items()}
     rate_guess = 4e6 * threads  # binned pairs/s on one ARM/x86 core, rough
     stride = max(1, int(n_binned_full / (rate_guess * budget_s)))
     t = time.perf_counter()
@@ -193,18 +231,17 @@ def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from corr_pc_gb300 import host
     wls = _workload(args.workload)
     wl = wls[0]
     p = wl.params
-    cats = host.prepare(p, [("S", wl.shape), ("D", wl.density)])
+    ocats = _oracle_cats(p, wl)
     threads = os.cpu_count() or 1
     # estimate the full binned count cheaply from a tiny sample
-    probe, stride0, nin0, _, _ = _cpu_sample(p, cats, 0.5, 10 ** 10, threads)
+    probe, stride0, nin0, _, _ = _cpu_sample(p, ocats, 0.5, 10 ** 12, threads)
     n_full = nin0 * stride0
     tot_pairs, tot_t, last = 0, 0.0, None
     for s in range(args.warmup + args.steps):
-        res, stride, nin, dt, _ = _cpu_sample(p, cats, args.ref_budget, n_full, threads,
+        res, stride, nin, dt, _ = _cpu_sample(p, ocats, args.ref_budget, n_full, threads,
                                               offset=s)
         if s >= args.warmup:
             tot_pairs += nin
@@ -215,6 +252,7 @@ def run_reference(args) -> None:
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded, in memory)", "config": _describe(wls),
+            "step_definition": _step_definition(_describe(wls)["workload"], "reference"),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": last["sample"] if last else ""},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -226,6 +264,8 @@ def run_reference(args) -> None:
 # ---------------------------------------------------------------------------
 
 SKY_TERMS = (("SRd", "Rd", "S"), ("RsRd", "Rd", "Rs"), ("SD", "D", "S"), ("DRs", "Rs", "D"))
+# row shards of one full pass over the four terms (one shard per step)
+SKY_SHARDS = {"sky_wgp_500k_5M": 40, "sky_wgp_50k_500k": 4}
 SKY_SLOTS = {"S": 0, "Rs": 1, "D": 2, "Rd": 3}
 
 
@@ -248,8 +288,6 @@ def _sky_describe(wl, rows):
             "pi_range": [p.p_min, p.p_max], "n_data": wl.shape.n, "n_randoms": wl.shape_rand.n,
             "patch_deg": [10, 10], "chi_range": [500, 1500],
             "pair_types": [t for t, _, _ in SKY_TERMS],
-            "row_sample": f"about {rows} outer rows per pair type per step (row stride, offset "
-                          "changes every step)",
             "l2": "inputs larger than L2 (about 1.2 GB per random catalogue); L2 flushed "
                   "between steps"}
 
@@ -327,9 +365,21 @@ def run_sky(args) -> None:
         ctx.upload(SKY_SLOTS[r], c)
     rows = args.sky_rows
     strides = _sky_strides(cats, rows)
+    K = SKY_SHARDS.get(wl.name, 1)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    jobs = [(ctx, t, SKY_SLOTS[a], SKY_SLOTS[bb]) for t, a, bb in SKY_TERMS]
 
-    def step(k, engine="fast", mult=1):
+    def step(k):
+        """Shard k % K of the four terms, in one launch of the fast kernel."""
+        ctx.set_shard(k % K, K)
+        rs = _lib.count_batch(jobs)
+        return (sum(r["n_binned"] for r in rs), sum(r["n_window"] for r in rs),
+                rs[0]["kernel_ms"])
+
+    def step_rows(k, engine, mult=1):
+        """Every st-th outer row of each term (the FP64 kernel's sample), one
+        launch per term."""
+        ctx.set_shard(0, 1)
         nb = nw = 0
         ms = 0.0
         for (t, a, bb), st in zip(SKY_TERMS, strides):
@@ -358,18 +408,21 @@ def run_sky(args) -> None:
             n_win += nw
             tot_ms += ms
     launches = ctx.launches() - l0
+    ctx.set_shard(0, 1)
     value = n_bin / (tot_ms * 1e-3)
-    # end to end: the four uploads (host windows, device sort) + one step
+    # end to end: the four uploads (host windows, device sort) + the four terms
+    # over every outer row in one launch
     h2d = sum(8 * 9 * c.n + 4 * c.n + c.n for c in cats.values())
     t0 = time.perf_counter()
     for r, c in cats.items():
         ctx.upload(SKY_SLOTS[r], c)
-    nb_e, _, _ = step(0)
+    rs_e = _lib.count_batch(jobs)
     e2e_t = time.perf_counter() - t0
+    nb_e = sum(r["n_binned"] for r in rs_e)
     nh, nbins, npb = ctx.shape
     d2h = 4 * nh * nbins * npb * (8 + 8 * _lib.NF)
     # plain FP64 sky kernel on an 8x sparser row sample
-    nb64, _, ms64 = step(0, engine="fp64", mult=8)
+    nb64, _, ms64 = step_rows(0, "fp64", mult=8)
     fp64 = {"value": nb64 / (ms64 * 1e-3), "unit": UNIT,
             "sample": f"8x sparser row sample: {nb64} binned pairs in {ms64:.1f} ms"}
     fp64["speedup_of_fast"] = value / fp64["value"]
@@ -398,13 +451,16 @@ def run_sky(args) -> None:
                 "peak": (peaks["ffma_flops"] or float("nan")) / 1e12, "unit": "TFLOP/s",
                 "frac": achieved_flops / peaks["ffma_flops"] if peaks["ffma_flops"] else None,
                 "traffic": None, "kernel": "sky_warp_kernel",
-                "kernel_ms_per_launch": tot_ms / (args.steps * len(SKY_TERMS)),
+                "kernel_ms_per_launch": tot_ms / args.steps,
                 "work_per_pair": {"fp32_flops": F, "smem_atomic_updates": A},
                 "peak_source": "measured live in this run (FFMA microbenchmark)"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded generator, in memory)", "config": _sky_describe(wl, rows),
+            "step_definition": f"the four terms in one launch over one of {K} row shards "
+                               f"(redshift-ordered positions k % {K} == step % {K}); {K} steps "
+                               "= one full count of every term",
             "n_binned_per_step": n_bin / args.steps, "n_window_per_step": n_win / args.steps,
             "roofline": roofline, "cpu_baseline": cpu, "fp64_gpu": fp64, "accuracy": accuracy,
             "e2e": {"value": nb_e / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -419,10 +475,12 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="box_ns_wgp_200k")
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline")
-    ap.add_argument("--ref-budget", type=float, default=8.0, help="seconds per reference step")
+    ap.add_argument("--ref-budget", type=float, default=5.0, help="seconds per reference step")
     ap.add_argument("--fp64-budget", type=float, default=3.0, help="seconds of FP64 kernel")
+    ap.add_argument("--cell-fp64-pairs", type=float, default=1e8,
+                    help="binned pairs of the cell-list FP64 comparison (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")
     ap.add_argument("--tune", default=None,
@@ -453,6 +511,9 @@ def main() -> None:
     from corr_pc_gb300 import _lib, host, metrics
 
     wls = _workload(args.workload)
+    wl_name = _describe(wls)["workload"]
+    n_shards = SHARDS.get(wl_name, 1)
+    big = sum(w.shape.n for w in wls) >= 10_000_000  # inputs far larger than L2
     preps = [host.prepare(w.params, [("S", w.shape), ("D", w.density)]) for w in wls]
     ctxs = [_lib.Context(w.params) for w in wls]
     tuning = None
@@ -461,27 +522,43 @@ def main() -> None:
         for c in ctxs:
             c.set_tuning(tk, tw)
         tuning = {"cells_per_rmax": tk, "pi_window": tw, "by": "--tune"}
+    t_up = time.perf_counter()
     for c, cat in zip(ctxs, preps):
         c.upload(0, cat["D"])
         c.upload(1, cat["S"])
+    torch.cuda.synchronize()
+    upload_s = time.perf_counter() - t_up
     if len(ctxs) == 1 and not args.no_tune and not args.tune:  # outside the timed region
         n_rows = wls[0].density.n
         k, w = ctxs[0].autotune("SD", 0, 1, sample_stride=max(1, n_rows // 25000))
         tuning = {"cells_per_rmax": k, "pi_window": w, "by": "cpc_autotune on a row sample"}
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    elif len(ctxs) > 1 and not args.no_tune and not args.tune:
+        k, w = _lib.autotune_batch([(c, "SD", 0, 1) for c in ctxs])
+        tuning = {"cells_per_rmax": k, "pi_window": w,
+                  "by": "cpc_autotune_batch on row samples of every box"}
+    # the uploads (copy, device checks, radix sort into the cell list, gather of
+    # the SoA streams, host bucket tables), wall clock, outside the timed steps
+    cell_list = {"upload_wall_ms_per_catalog": 1e3 * upload_s / (2 * len(ctxs)),
+                 "catalogs": 2 * len(ctxs),
+                 "note": "cpc_upload from host buffers: H2D copy, on-device checks, radix sort "
+                         "by (column, region, z), gather of the SoA streams, bucket tables"}
+    flush = None if big else torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
-    def step():
+    def step(k=0):
         if len(ctxs) == 1:
+            if n_shards > 1:
+                ctxs[0].set_shard(k % n_shards, n_shards)
             r = ctxs[0].count("SD", 0, 1)
             return r["n_binned"], r["kernel_ms"], r["pair_kernel_ms"], r["n_window"]
         rs = _lib.count_batch([(c, "SD", 0, 1) for c in ctxs])
         return (sum(r["n_binned"] for r in rs), rs[0]["kernel_ms"], rs[0]["pair_kernel_ms"],
                 sum(r["n_window"] for r in rs))
 
-    for _ in range(args.warmup):
-        flush.zero_()
+    for k in range(args.warmup):
+        if flush is not None:
+            flush.zero_()
         torch.cuda.synchronize()
-        step()
+        step(k)
     l0 = sum(c.launches() for c in ctxs)
     tot_ms = tot_pair_ms = 0.0
     n_bin = n_win = 0
@@ -489,16 +566,19 @@ def main() -> None:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.zero_()
+        for k in range(args.steps):
+            if flush is not None:
+                flush.zero_()
             torch.cuda.synchronize()
-            nb, ms, pms, nw = step()
+            nb, ms, pms, nw = step(args.warmup + k)
             n_bin += nb
             n_win += nw
             tot_ms += ms
             tot_pair_ms += pms
     torch.cuda.synchronize()
     launches = sum(c.launches() for c in ctxs) - l0
+    if n_shards > 1:
+        ctxs[0].set_shard(0, 1)
     g_cap, g_rep = ctxs[0].graph_stats()
     t_step = tot_ms / args.steps
     if dist:
@@ -520,16 +600,22 @@ def main() -> None:
             h2d += g.n
     d2h_hist = sum(c.shape[0] * c.shape[1] * c.shape[2] * (8 + 8 * _lib.NF) for c in ctxs)
     d2h = d2h_hist + sum(20 * (cat["D"].n + cat["S"].n) for cat in preps)
-    e2e_steps = max(1, min(args.steps, 5))
+    # the 20M box: one full count (all shards); the others: up to 5 repeats
+    e2e_steps = 1 if n_shards > 1 else max(1, min(args.steps, 5))
     torch.cuda.synchronize()
+    e2e_bin = 0
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         for c, cat in zip(ctxs, preps):
             c.upload(0, cat["D"])
             c.upload(1, cat["S"])
-        step()
+        e2e_bin += step()[0]
     e2e_t = (time.perf_counter() - t0) / e2e_steps
-    e2e_value = n_bin / args.steps / e2e_t
+    e2e_value = e2e_bin / e2e_steps / e2e_t
+    if n_shards > 1:  # one full count: the value's timed steps together count it once
+        full_pairs = e2e_bin / e2e_steps
+    else:
+        full_pairs = n_bin / args.steps
 
     if rank != 0:
         if dist:
@@ -582,18 +668,41 @@ def main() -> None:
     # plain FP64 GPU kernel on a bounded row sample of the same workload
     fp64 = None
     if len(ctxs) == 1:
-        est_rate = 1.5e8
-        stride = max(1, int(n_per_step / (est_rate * args.fp64_budget)))
+        est_rate = 1.5e8 if not big else 2e7
+        stride = max(1, int(full_pairs / (est_rate * args.fp64_budget)))
         r64 = ctxs[0].count("SD", 0, 1, engine="fp64", row_stride=stride)
         fp64 = {"value": r64["n_binned"] / (r64["kernel_ms"] * 1e-3), "unit": UNIT,
                 "sample": f"every {stride}-th outer row: {r64['n_binned']} binned pairs in "
                           f"{r64['kernel_ms']:.1f} ms"}
         fp64["speedup_of_fast"] = value / fp64["value"]
+    # the same cell list and work units with every window candidate evaluated by
+    # the FP64 path (the edge queue and its recheck kernel): the precision
+    # comparison at equal algorithm, on one shard of the work queue sized for
+    # about args.cell_fp64_pairs binned pairs, against the fast engine on the
+    # same shard
+    cell64 = None
+    if len(ctxs) == 1 and args.cell_fp64_pairs > 0:
+        K = max(1, int(full_pairs / args.cell_fp64_pairs))
+        ctxs[0].set_shard(0, K)
+        ctxs[0].count("SD", 0, 1, engine="cell_fp64")  # sizes the edge queue
+        rc = ctxs[0].count("SD", 0, 1, engine="cell_fp64")
+        rfs = ctxs[0].count("SD", 0, 1)
+        ctxs[0].set_shard(0, 1)
+        v64 = rc["n_binned"] / (rc["kernel_ms"] * 1e-3)
+        vf = rfs["n_binned"] / (rfs["kernel_ms"] * 1e-3)
+        cell64 = {"value": v64, "unit": UNIT,
+                  "sample": f"shard 0 of {K} of the work queue: {rc['n_binned']} binned pairs in "
+                            f"{rc['kernel_ms']:.1f} ms",
+                  "fast_on_same_shard": vf, "speedup_of_fast": vf / v64,
+                  "counts_equal_fast": bool(np.array_equal(rc["num"], rfs["num"])),
+                  "accuracy_fast_vs_cell_fp64": metrics.accuracy_report(
+                      rfs["num"], rfs["sums"], rc["num"], rc["sums"])["ok"]}
     cpu = None
     accuracy = None
     if not args.no_cpu and len(wls) == 1:
-        cpu, cstride, _, _, (onum, osums) = _cpu_sample(p, preps[0], args.cpu_budget,
-                                                        n_per_step, os.cpu_count() or 1)
+        ocats = _oracle_cats(p, wls[0])
+        cpu, cstride, _, _, (onum, osums) = _cpu_sample(p, ocats, args.cpu_budget,
+                                                        full_pairs, os.cpu_count() or 1)
         # the fast kernel on the same rows, checked against the oracle's FP64 histograms
         rf = ctxs[0].count("SD", 0, 1, row_stride=cstride)
         accuracy = dict(metrics.accuracy_report(rf["num"], rf["sums"], onum, osums),
@@ -607,9 +716,15 @@ def main() -> None:
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64", "data": "synthetic (seeded generator, in memory)",
-            "config": dict(_describe(wls), tuning=tuning), "n_binned_per_step": n_per_step,
-            "n_window_per_step": n_win / args.steps,
-            "roofline": roofline, "cpu_baseline": cpu, "fp64_gpu": fp64, "accuracy": accuracy,
+            "config": dict(_describe(wls), tuning=tuning),
+            "step_definition": _step_definition(wl_name, "gb300"),
+            "value_scope": "device time of the count (zeroing, pair kernel, FP64 edge recheck) "
+                           "with both catalogues' cell lists resident; the cell-list build is "
+                           "`cell_list`, everything from host buffers is `e2e`",
+            "n_binned_per_step": n_per_step, "n_binned_full_count": full_pairs,
+            "n_window_per_step": n_win / args.steps, "cell_list": cell_list,
+            "roofline": roofline, "cpu_baseline": cpu, "fp64_gpu": fp64,
+            "cell_list_fp64_gpu": cell64, "accuracy": accuracy,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_t},
             "gpu_launches": launches,

@@ -20,7 +20,7 @@ STATUS_NAMES = {0: "CPC_OK", 1: "CPC_ERR_INVALID", 2: "CPC_ERR_CUDA", 3: "CPC_ER
                 7: "CPC_ERR_NODEVICE", 8: "CPC_ERR_HOST"}
 # cpc_pair_kind (the data_info.do_* flag of each corels2 call)
 PAIR = {"SD": 0, "SRd": 1, "DRs": 2, "RsRd": 3, "RsRs": 4, "SRs": 5, "SS": 6}
-ENGINE = {"fast": 0, "fp64": 1}
+ENGINE = {"fast": 0, "fp64": 1, "cell_fp64": 2}
 NF = 13
 
 EXPORTED = ["cpc_version", "cpc_create", "cpc_destroy", "cpc_last_error", "cpc_upload",
@@ -90,6 +90,7 @@ def load() -> ctypes.CDLL:
     lib.cpc_count_batch.argtypes = [I, P(V), P(I), P(I), P(I), P(cpc_accum)]
     lib.cpc_set_tuning.argtypes = [V, I, I, I]
     lib.cpc_autotune.argtypes = [V, I, I, I, I64, P(I), P(I)]
+    lib.cpc_autotune_batch.argtypes = [I, P(V), P(I), P(I), P(I), I64, P(I), P(I)]
     lib.cpc_autotune.restype = I
     lib.cpc_host_rand_uniform.argtypes = [ctypes.c_uint32, I64, I64, V]
     lib.cpc_host_elip_angle.argtypes = [I64, V, V, V]
@@ -288,6 +289,27 @@ class Context:
         return {"num": num, "sums": sums, "n_window": acc.n_window, "n_binned": acc.n_binned,
                 "n_rechecked": acc.n_rechecked, "kernel_ms": acc.kernel_ms,
                 "pair_kernel_ms": acc.pair_kernel_ms}
+
+
+def autotune_batch(jobs, sample_stride: int = 0) -> tuple:
+    """jobs: list of (Context, kind, slot_g1, slot_g2) as for count_batch.
+    Times batched launches on a row sample of every job for the cell widths
+    and Pi windows the single-job autotuner tries, keeps the fastest on every
+    context and returns (cells_per_rmax, pi_window).  sample_stride 0: about
+    a 25,000-row sample of the largest job's g1 catalogue."""
+    lib = load()
+    n = len(jobs)
+    if sample_stride <= 0:
+        rows = max(j[0].sizes.get(j[2], 1) for j in jobs)
+        sample_stride = max(1, rows // 25000)
+    ctxs = (ctypes.c_void_p * n)(*[j[0].h.value for j in jobs])
+    kinds = (ctypes.c_int * n)(*[PAIR[j[1]] for j in jobs])
+    s1 = (ctypes.c_int * n)(*[j[2] for j in jobs])
+    s2 = (ctypes.c_int * n)(*[j[3] for j in jobs])
+    k, w = ctypes.c_int(), ctypes.c_int()
+    check(lib.cpc_autotune_batch(n, ctxs, kinds, s1, s2, sample_stride, ctypes.byref(k),
+                                 ctypes.byref(w)))
+    return k.value, w.value
 
 
 def count_batch(jobs) -> list:

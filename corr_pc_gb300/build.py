@@ -27,7 +27,8 @@ CU_SOURCES = ["cell_list.cu", "pair_fast.cu", "pair_fp64.cu", "pair_sky.cu", "ca
 CPP_SOURCES = ["host_helpers.cpp"]
 HOST_SOURCES = ["host/inp.cpp", "host/reader.cpp", "host/finalize.cpp", "host/outp.cpp",
                 "host/driver.cpp"]
-HEADERS = ["cpc_device.cuh", "kernels.h", "host_helpers.h", "pair_values.h", "host/host.h"]
+HEADERS = ["cpc_device.cuh", "kernels.h", "host_helpers.h", "pair_values.h", "host/host.h",
+           "df32.cuh", "pair_df.cuh", "param_check.h"]
 
 
 def nvcc() -> str:

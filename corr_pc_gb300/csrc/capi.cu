@@ -21,6 +21,7 @@
 #include "../../include/corrpc.h"
 #include "cpc_device.cuh"
 #include "host_helpers.h"
+#include "param_check.h"
 #include "kernels.h"
 
 using namespace cpc;
@@ -73,8 +74,7 @@ struct Slot {
   int ncx = 0, ncy = 0, n_reg = 1, kcells = 0;
   double cw_x = 0, cw_y = 0;
   // device, cell order
-  DevBuf<float4> pos, shp;
-  DevBuf<float2> lo;
+  DevBuf<float4> pos, shp, ewt, aux;
   DevBuf<float> zlo, zf;
   DevBuf<double> x, y, z, w, e1, e2, phi, e3;
   DevBuf<int32_t> jk;
@@ -96,12 +96,23 @@ struct Slot {
   // redshift-ordered catalogue; these the sky-only per-galaxy quantities
   bool sky = false;
   DevBuf<double> dc, da, sd, cd, rar, decr, win;
-  DevBuf<float4> sky_su, sky_sl, sky_sw, sky_sx, sky_ss;  // float views (SkyFast)
+  DevBuf<float4> sky_su, sky_sl, sky_sw, sky_sx, sky_ss, sky_sh;  // float views (SkyFast)
+  DevBuf<float2> sky_sp;
   double dcmax = 0;  // largest |D_C| (error bound of the float Pi)
   // host copies in the same order for the host edge tier
   std::vector<double> hs_ra, hs_dec, hs_dc, hs_da, hs_w, hs_e1, hs_e2, hs_phi;
   std::vector<int32_t> hs_jk;
   std::vector<uint8_t> hs_keep;
+  std::vector<int64_t> hs_orig;  // input row of each redshift-ordered row (row samples)
+};
+
+// device buffers of one job of a sky launch: its histogram block, fixed-point
+// sums, counters, host-tier queue and row sample
+struct SkyJobBufs {
+  DevBuf<unsigned long long> num, fix, counters, hq_n;
+  DevBuf<double> sums;
+  DevBuf<int2> hq;
+  DevBuf<int> rows;
 };
 
 struct UnitCache {
@@ -140,6 +151,10 @@ struct cpc_ctx {
   DevBuf<unsigned long long> d_num;
   DevBuf<double> d_sums;
   DevBuf<unsigned long long> d_counters;
+  // sky launches: one buffer set per job of the launch, the chunk table
+  std::vector<std::unique_ptr<SkyJobBufs>> sky_bufs;
+  DevBuf<long long> d_chunk0;
+  DevBuf<unsigned long long> d_chunk_ctr;
   // sort scratch
   DevBuf<uint64_t> d_keys, d_ktmp;
   DevBuf<uint32_t> d_vals, d_vtmp, d_hist, d_bucket;
@@ -162,6 +177,10 @@ struct cpc_ctx {
   int64_t launches = 0;  // kernels launched by this context (all entry points)
   // work-unit shard of the fast box engine (cpc_set_shard)
   int shard = 0, n_shards = 1;
+  // register bound of the fast sky kernel: 2 or 3 blocks of 256 threads per SM
+  // (CPC_SKY_BLOCKS_PER_SM in the environment; the autotuner of a sky context
+  // would set it)
+  int sky_blocks_per_sm = 2;
   // CUDA graph of the fast engine's device work (zeroing, pair kernels,
   // recheck), replayed while every value baked into it stays the same
   int graph_on = 1;
@@ -278,42 +297,7 @@ float f_down(double v) {
 }
 
 cpc_status validate_params(cpc_ctx *c, const cpc_params &p) {
-  if (p.coordinates != 6 && p.coordinates != 7 && p.coordinates != 0)
-    return fail(c, CPC_ERR_INVALID,
-                "coordinates: 6 (x,y,z with r_p, Pi), 7 (x,y,z with r, mu) and 0 (sky, r_p and "
-                "Pi) are supported");
-  if (p.which_corr < 0 || p.which_corr > 5)
-    return fail(c, CPC_ERR_INVALID, "which_corr must be in 0..5");
-  // coordinates 7 outside a periodic box takes the sky window (lim_calc_sky,
-  // corr.cpp:311-324) in the reference: not a box computation
-  if (p.coordinates == 7 && !p.periodic_box)
-    return fail(c, CPC_ERR_INVALID, "coordinates 7 (r, mu) needs a periodic box");
-  if (p.sig_crit != 0) return fail(c, CPC_ERR_INVALID, "sig_crit weights are not supported");
-  if (p.rand_subsample != 0) return fail(c, CPC_ERR_INVALID, "rand_subsample is not supported");
-  if (p.do_jk != 0 && p.do_jk != 1) return fail(c, CPC_ERR_INVALID, "do_jk must be 0 or 1");
-  if (p.do_jk && (p.n_jk <= 0 || p.n_jk > 100000)) return fail(c, CPC_ERR_INVALID, "n_jk out of range");
-  if (p.n_bins <= 0 || p.n_bins > kMaxRp) return fail(c, CPC_ERR_INVALID, "n_bins must be in 1..64");
-  if (p.n_p_bin <= 0 || p.n_p_bin > kMaxPi) return fail(c, CPC_ERR_INVALID, "n_p_bin must be in 1..128");
-  if (!(p.bin_r_max > p.bin_r_min) || !(p.bin_r_min >= 0) || (!p.lin_bin && !(p.bin_r_min > 0)))
-    return fail(c, CPC_ERR_INVALID, "bad r_p bin limits");
-  if (!(p.p_max > p.p_min)) return fail(c, CPC_ERR_INVALID, "bad Pi bin limits");
-  if (p.coordinates == 0) {
-    if (p.periodic_box) return fail(c, CPC_ERR_INVALID, "coordinates 0 (sky) cannot be periodic");
-    if (p.which_corr > 2)
-      return fail(c, CPC_ERR_INVALID, "which_corr 3-5 (kappa, ED) run in x,y,z (coordinates 6, 7)");
-    if (!p.H_z || !p.dA_z || p.n_table < 2)
-      return fail(c, CPC_ERR_INVALID, "sky runs need the distance table (H_z, dA_z, n_table)");
-    if (!(p.dz > 0) || !(p.z_max > 0) || !std::isfinite(p.z_sep_max))
-      return fail(c, CPC_ERR_INVALID, "sky runs need dz > 0, z_max > 0 and a finite z_sep_max");
-    return CPC_OK;
-  }
-  if (!(p.periodic_box_size > 0)) return fail(c, CPC_ERR_INVALID, "box size must be > 0");
-  if (p.periodic_box) {
-    const double L = p.periodic_box_size;
-    const bool rmu = p.coordinates == 7;  // p_min, p_max bound mu there
-    if (p.bin_r_max > L || (!rmu && (p.p_max > L || -p.p_min > L)))
-      return fail(c, CPC_ERR_INVALID, "bin limits larger than the periodic box");
-  }
+  if (const char *m = param_error(p)) return fail(c, CPC_ERR_INVALID, m);
   return CPC_OK;
 }
 
@@ -364,7 +348,8 @@ void fill_views(Slot &s, FCat &f, DCat &d) {
   f.n = s.n;
   f.pos = s.pos.p;
   f.shp = s.shp.p;
-  f.lo = s.lo.p;
+  f.ewt = s.ewt.p;
+  f.aux = s.aux.p;
   f.zlo = s.zlo.p;
   f.zf = s.zf.p;
   f.keep = s.keep.p;
@@ -551,7 +536,8 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
     J.inv_lw = (float)(1.0 / (2.0 * std::log2(p.bin_r_max / p.bin_r_min) / nrp));
   }
   // fixed-point scales: field f's terms are rint(v 2^S_f) with
-  // |v_f| 2^S_f <= 2^26 (see pair_fast.cu); S_f from a bound on |v_f|
+  // |v_f| 2^S_f <= 2^29 / (1 + 2^-12) < 2^29 - 2^17 (see pair_fast.cu); S_f
+  // from a bound on |v_f| (emax bounds |e|, so every rotated ellipticity)
   {
     const double wm = std::max(g1.wmax, 1e-30) * std::max(g2.wmax, 1e-30);
     const double em = std::max({g1.emax, g2.emax, 1e-30});
@@ -572,14 +558,14 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
       vb[12] = vb[11] * vb[11];
     }
     for (int f = 0; f < kNF; f++) {
-      const double v = std::max(vb[f] * 1.0001, 1e-30);
-      int S = 26 - (int)std::ceil(std::log2(v));
+      const double v = std::max(vb[f] * (1.0 + 1.0 / 4096.0), 1e-30);
+      int S = 29 - (int)std::ceil(std::log2(v));
       S = std::min(60, std::max(-60, S));
       J.qscale[f] = (float)std::ldexp(1.0, S);
       J.inv_qscale[f] = std::ldexp(1.0, -S);
     }
   }
-  J.qbias = 1 << 26;
+  J.qbias = 1 << 29;
   J.unit_w = (g1.wmax == 1.0 && g1.wmin == 1.0 && g2.wmax == 1.0 && g2.wmin == 1.0) ? 1 : 0;
   return CPC_OK;
 }
@@ -743,14 +729,17 @@ cpc_status zero_accum(cpc_ctx *c, cudaStream_t st) {
   return CPC_OK;
 }
 
-cpc_status fetch_accum(cpc_ctx *c, cpc_accum *out, cudaStream_t st, int unit_w) {
+// the histogram block and counters in device buffers num / sums / counters
+cpc_status fetch_accum_from(cpc_ctx *c, const unsigned long long *num, const double *sums,
+                            const unsigned long long *counters, cpc_accum *out, cudaStream_t st,
+                            int unit_w) {
   const cpc_params &p = c->p;
   const size_t n_hist = 1 + (p.do_jk ? p.n_jk : 0);
   const size_t cells = n_hist * p.n_bins * p.n_p_bin;
   unsigned long long cnt[4];
-  CK(cudaMemcpyAsync(out->num, c->d_num.p, sizeof(int64_t) * cells, cudaMemcpyDeviceToHost, st), "D2H");
-  CK(cudaMemcpyAsync(out->sums, c->d_sums.p, sizeof(double) * cells * kNF, cudaMemcpyDeviceToHost, st), "D2H");
-  CK(cudaMemcpyAsync(cnt, c->d_counters.p, sizeof cnt, cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaMemcpyAsync(out->num, num, sizeof(int64_t) * cells, cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaMemcpyAsync(out->sums, sums, sizeof(double) * cells * kNF, cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, st), "D2H");
   CK(cudaStreamSynchronize(st), "sync");
   if (unit_w)
     for (size_t k = 0; k < cells; k++) out->sums[k * kNF] = (double)out->num[k];
@@ -761,6 +750,10 @@ cpc_status fetch_accum(cpc_ctx *c, cpc_accum *out, cudaStream_t st, int unit_w) 
   for (size_t k = 0; k < c0; k++) nb += out->num[k];
   out->n_binned = nb;
   return CPC_OK;
+}
+
+cpc_status fetch_accum(cpc_ctx *c, cpc_accum *out, cudaStream_t st, int unit_w) {
+  return fetch_accum_from(c, c->d_num.p, c->d_sums.p, c->d_counters.p, out, st, unit_w);
 }
 
 cpc_status build_zorder(cpc_ctx *c, Slot &s) {
@@ -1120,7 +1113,7 @@ cpc_status build_cells(cpc_ctx *c, Slot &s, int64_t n, int k, const int64_t *ori
   CK(c->d_census.alloc(8 * 256), "alloc");
   CK(c->d_bucket.alloc(nn), "alloc");
   CK(s.pos.alloc(nn), "alloc"); CK(s.shp.alloc(nn), "alloc"); CK(s.zf.alloc(nn), "alloc");
-  CK(s.lo.alloc(nn), "alloc"); CK(s.zlo.alloc(nn), "alloc"); CK(s.e3.alloc(nn), "alloc");
+  CK(s.ewt.alloc(nn), "alloc"); CK(s.aux.alloc(nn), "alloc"); CK(s.zlo.alloc(nn), "alloc"); CK(s.e3.alloc(nn), "alloc");
   CK(s.x.alloc(nn), "alloc"); CK(s.y.alloc(nn), "alloc"); CK(s.z.alloc(nn), "alloc");
   CK(s.w.alloc(nn), "alloc"); CK(s.e1.alloc(nn), "alloc"); CK(s.e2.alloc(nn), "alloc");
   CK(s.phi.alloc(nn), "alloc"); CK(s.jk.alloc(nn), "alloc"); CK(s.keep.alloc(nn), "alloc");
@@ -1132,7 +1125,7 @@ cpc_status build_cells(cpc_ctx *c, Slot &s, int64_t n, int k, const int64_t *ori
   if (n > 0) c->launches += 2;  // cell keys + gather
   GatherIn in{ox.p, oy.p, oz.p, ow.p, oe1.p, oe2.p, ophi.p, ojk.p, okeep.p, oe3.p};
   GatherOut go{};
-  go.pos = s.pos.p; go.shp = s.shp.p; go.lo = s.lo.p; go.zlo = s.zlo.p; go.zf = s.zf.p;
+  go.pos = s.pos.p; go.shp = s.shp.p; go.ewt = s.ewt.p; go.aux = s.aux.p; go.zlo = s.zlo.p; go.zf = s.zf.p;
   go.bucket = c->d_bucket.p;
   go.x = s.x.p; go.y = s.y.p; go.z = s.z.p; go.w = s.w.p; go.e1 = s.e1.p; go.e2 = s.e2.p;
   go.e3 = s.e3.p;
@@ -1345,7 +1338,7 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
       if (cat->jk_prob) keep[i] = cat->jk_prob[i] >= 0.5 ? 1 : 0;
       P.wmax = std::max(P.wmax, std::fabs(w[i]));
       P.wmin = std::min(P.wmin, w[i]);
-      P.emax = std::max(P.emax, std::max(std::fabs(e1[i]), std::fabs(e2[i])));
+      P.emax = std::max(P.emax, std::sqrt(e1[i] * e1[i] + e2[i] * e2[i]) * (1.0 + 1e-15));
       P.phimax = std::max(P.phimax, std::fabs(phi[i]));
       sky_angles(ra, dec, &rar[i], &decr[i], &sd[i], &cd[i]);
       double wv[6];
@@ -1415,7 +1408,8 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   take(decr.data(), decrs);
   s.hs_jk.resize(n);
   s.hs_keep.resize(n);
-  std::vector<int64_t> orig(n);
+  std::vector<int64_t> &orig = s.hs_orig;
+  orig.assign(n, 0);
   std::vector<double> wins(6 * (size_t)n);
   std::vector<uint8_t> aflag(n);
   host_parallel(n, [&](int64_t b0, int64_t b1, int) {
@@ -1442,7 +1436,8 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   CK(put(s.cd, cds, n), "sky upload"); CK(put(s.rar, rars, n), "sky upload");
   CK(put(s.decr, decrs, n), "sky upload"); CK(put(s.win, wins, 6 * (size_t)n), "sky upload");
   // float views for the fast kernel: hi parts and the remainders
-  std::vector<float4> su(n), sl(n), sw(n), sx(n), ss(n);
+  std::vector<float4> su(n), sl(n), sw(n), sx(n), ss(n), sh(n);
+  std::vector<float2> sph(n);
   auto hi = [](double v) { return (float)v; };
   auto lo = [](double v) { return (float)(v - (double)(float)v); };
   std::vector<double> dcm(kMaxParts, 0.0);
@@ -1455,19 +1450,30 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
       sl[k] = make_float4(lo(ux), lo(uy), lo(uz), lo(dcv));
       sw[k] = make_float4(hi(s.hs_ra[k]), hi(s.hs_dec[k]), (float)zs[k], hi(dcv));
       sx[k] = make_float4(lo(s.hs_ra[k]), lo(s.hs_dec[k]), (float)decrs[k], (float)s.hs_w[k]);
-      ss[k] = make_float4((float)s.hs_e1[k], (float)s.hs_e2[k], (float)s.hs_phi[k], 0.f);
+      // weighted ellipticity and the half Dec angle's cosine and sine as hi +
+      // lo parts (the compensated shape terms: cos of the pair's mean Dec is
+      // cos(d1/2) cos(d2/2) - sin(d1/2) sin(d2/2))
+      const double we1 = s.hs_w[k] * s.hs_e1[k], we2 = s.hs_w[k] * s.hs_e2[k];
+      ss[k] = make_float4(hi(we1), hi(we2), lo(we1), lo(we2));
+      const double ch = std::cos(decrs[k] / 2.0), sh2 = std::sin(decrs[k] / 2.0);
+      sh[k] = make_float4(hi(ch), lo(ch), hi(sh2), lo(sh2));
+      sph[k] = make_float2((float)s.hs_phi[k], lo(s.hs_w[k]));
     }
   });
   s.dcmax = 0;
   for (double v : dcm) s.dcmax = std::max(s.dcmax, v);
-  DevBuf<float4> *fbufs[5] = {&s.sky_su, &s.sky_sl, &s.sky_sw, &s.sky_sx, &s.sky_ss};
-  const std::vector<float4> *fsrc[5] = {&su, &sl, &sw, &sx, &ss};
-  for (int q = 0; q < 5; q++) {
+  DevBuf<float4> *fbufs[6] = {&s.sky_su, &s.sky_sl, &s.sky_sw, &s.sky_sx, &s.sky_ss, &s.sky_sh};
+  const std::vector<float4> *fsrc[6] = {&su, &sl, &sw, &sx, &ss, &sh};
+  for (int q = 0; q < 6; q++) {
     CK(fbufs[q]->alloc(nn), "alloc");
     if (n > 0)
       CK(cudaMemcpyAsync(fbufs[q]->p, fsrc[q]->data(), sizeof(float4) * n, cudaMemcpyHostToDevice,
                          st), "H2D");
   }
+  CK(s.sky_sp.alloc(nn), "alloc");
+  if (n > 0)
+    CK(cudaMemcpyAsync(s.sky_sp.p, sph.data(), sizeof(float2) * n, cudaMemcpyHostToDevice, st),
+       "H2D");
   CK(s.jk.alloc(nn), "alloc"); CK(s.keep.alloc(nn), "alloc"); CK(s.orig.alloc(nn), "alloc");
   CK(s.aflag.alloc(nn), "alloc");
   if (n > 0) {
@@ -1481,6 +1487,18 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
   return CPC_OK;
 }
 
+// One sky corels2 call of a launch (several pair types may share one launch of
+// the fast kernel): its job descriptor, device buffers and output.
+struct SkyPlan {
+  cpc_pair_kind kind;
+  int s1, s2;  // slots after the swap rule
+  JobRule rule;
+  cpc_accum *out;
+  JobDev J;
+  bool empty;
+  size_t cells, n_fix;
+};
+
 SkyView sky_view(Slot &s) {
   SkyView v;
   v.d.n = s.n;
@@ -1492,9 +1510,17 @@ SkyView sky_view(Slot &s) {
   return v;
 }
 
-// one sky corels2 call: GPU FP64 kernel, then the host edge tier
-cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, int64_t rs,
-                     int64_t ro, cpc_engine engine, cpc_accum *out, int auto_mode = 0) {
+SkyFast sky_fast(Slot &s) {
+  return SkyFast{s.sky_su.p, s.sky_sl.p, s.sky_sw.p, s.sky_sx.p, s.sky_ss.p, s.sky_sh.p,
+                 s.sky_sp.p};
+}
+
+// Plan job k of a sky launch: the corels2 rules, the bands and fixed-point
+// scales of the mixed-precision path, zeroed device buffers (set k), the row
+// sample as a list of g1 rows.
+cpc_status sky_plan(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, int64_t rs,
+                    int64_t ro, cpc_engine engine, cpc_accum *out, int auto_mode, size_t k,
+                    SkyPlan &P) {
   if (slot_g1 < 0 || slot_g1 >= kMaxSlots || slot_g2 < 0 || slot_g2 >= kMaxSlots)
     return fail(c, CPC_ERR_INVALID, "slot out of range");
   Slot &A = c->slots[slot_g1], &B = c->slots[slot_g2];
@@ -1506,13 +1532,30 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
     return fail(c, CPC_ERR_INVALID, "bad pair kind");
   const int s1 = rule.swapped ? slot_g2 : slot_g1, s2 = rule.swapped ? slot_g1 : slot_g2;
   Slot &g1 = c->slots[s1], &g2 = c->slots[s2];
-  cpc_status st_;
-  if ((st_ = alloc_accum(c)) != CPC_OK) return st_;
-  if ((st_ = zero_accum(c, c->st)) != CPC_OK) return st_;
+  P.kind = kind;
+  P.s1 = s1;
+  P.s2 = s2;
+  P.rule = rule;
+  P.out = out;
+  P.empty = A.n == 0 || B.n == 0;  // corr.cpp:273-277
+  P.cells = (size_t)(1 + (p.do_jk ? p.n_jk : 0)) * p.n_bins * p.n_p_bin;
+  P.n_fix = P.cells * kNF;
   out->kernel_ms = out->pair_kernel_ms = 0;
-  if (A.n == 0 || B.n == 0) return fetch_accum(c, out, c->st, 0);  // corr.cpp:273-277
-  JobDev J;
+  while (c->sky_bufs.size() <= k) c->sky_bufs.emplace_back(new SkyJobBufs());
+  SkyJobBufs &Bf = *c->sky_bufs[k];
+  cudaStream_t st = c->st;
+  CK(Bf.num.alloc(P.cells), "alloc histograms");
+  CK(Bf.sums.alloc(P.cells * kNF), "alloc histograms");
+  CK(Bf.counters.alloc(4), "alloc counters");
+  CK(cudaMemsetAsync(Bf.num.p, 0, sizeof(unsigned long long) * P.cells, st), "memset");
+  CK(cudaMemsetAsync(Bf.sums.p, 0, sizeof(double) * P.cells * kNF, st), "memset");
+  CK(cudaMemsetAsync(Bf.counters.p, 0, sizeof(unsigned long long) * 4, st), "memset");
+  JobDev &J = P.J;
   std::memset(&J, 0, sizeof J);
+  J.acc_num = Bf.num.p;
+  J.acc_sums = Bf.sums.p;
+  J.counters = Bf.counters.p;
+  if (P.empty) return CPC_OK;
   J.corel = rule.corel;
   J.gws = rule.gws;
   J.which_corr = p.which_corr;
@@ -1533,10 +1576,7 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
   J.pmax = p.p_max;
   J.ps = c->ps;
   J.rsize = c->rsize;
-  for (int k = 0; k <= p.n_bins; k++) J.thr[k] = c->thr_rp[k];
-  J.acc_num = c->d_num.p;
-  J.acc_sums = c->d_sums.p;
-  J.counters = c->d_counters.p;
+  for (int q = 0; q <= p.n_bins; q++) J.thr[q] = c->thr_rp[q];
   // float bands of the mixed-precision path.  r_p bin k is certain when
   // [rp - tol, rp + tol] lies inside [A_k, B_k) (the exact thresholds rounded
   // inwards; tol is per pair).  The float Pi differs from the reference's by at
@@ -1567,8 +1607,9 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
       J.inv_lw = (float)(1.0 / (2.0 * std::log2(p.bin_r_max / p.bin_r_min) / nrp));
     }
   }
-  // fixed-point scales of the fast kernel: terms rint(v 2^S_f), |v| 2^S_f <= 2^28
-  // (64-bit integer sums; 2^35 terms per bin before any overflow)
+  // fixed-point scales of the fast kernel: terms rint(v 2^S_f),
+  // |v| 2^S_f <= 2^30 / (1 + 2^-12) (64-bit integer sums: 2^33 terms per bin
+  // before any overflow, checked after the count)
   {
     const double wm = std::max(g1.wmax, 1e-30) * std::max(g2.wmax, 1e-30);
     const double em = std::max({g1.emax, g2.emax, 1e-30});
@@ -1583,8 +1624,8 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
     vb[11] = tm2;
     vb[12] = 2 * tm * tm;
     for (int f = 0; f < kNF; f++) {
-      const double v = std::max(vb[f] * 1.0001, 1e-30);
-      int S = 28 - (int)std::ceil(std::log2(v));
+      const double v = std::max(vb[f] * (1.0 + 1.0 / 4096.0), 1e-30);
+      int S = 30 - (int)std::ceil(std::log2(v));
       S = std::min(60, std::max(-60, S));
       J.qscale[f] = (float)std::ldexp(1.0, S);
       J.inv_qscale[f] = std::ldexp(1.0, -S);
@@ -1592,48 +1633,69 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
     J.unit_w = (engine == CPC_ENGINE_FAST && g1.wmax == 1.0 && g1.wmin == 1.0 &&
                 g2.wmax == 1.0 && g2.wmin == 1.0) ? 1 : 0;
   }
-  const size_t n_fix = (size_t)(1 + (p.do_jk ? p.n_jk : 0)) * p.n_bins * p.n_p_bin * kNF;
-  CK(c->d_fix.alloc(n_fix), "alloc fixed-point sums");
-  CK(cudaMemsetAsync(c->d_fix.p, 0, sizeof(unsigned long long) * n_fix, c->st), "memset");
-  J.acc_fix = c->d_fix.p;
+  CK(Bf.fix.alloc(P.n_fix), "alloc fixed-point sums");
+  CK(cudaMemsetAsync(Bf.fix.p, 0, sizeof(unsigned long long) * P.n_fix, st), "memset");
+  J.acc_fix = Bf.fix.p;
   J.sky1 = sky_view(g1);
   J.sky2 = sky_view(g2);
-  if ((st_ = ensure_scratch(c, 1, 1)) != CPC_OK) return st_;
-  CK(c->d_hq.alloc(kSkyHostQueue), "alloc host queue");
-  CK(c->d_hq_n.alloc(1), "alloc");
-  CK(cudaMemsetAsync(c->d_hq_n.p, 0, sizeof(unsigned long long), c->st), "memset");
-  CK(cudaMemcpyAsync(c->d_jobs.p, &J, sizeof J, cudaMemcpyHostToDevice, c->st), "H2D job");
-  // bound on |sum_gpu - sum_libm|: cos differs by <= 3 ulp (CUDA 2 + C library
-  // 1), one more ulp from each of the product and the sum, doubled
-  const double esum = 8.0 * std::ldexp(1.0, -52);
-  CK(cudaMemsetAsync(c->d_unit_ctr.p, 0, sizeof(unsigned int), c->st), "memset");
-  CK(cudaEventRecord(c->e0, c->st), "event");
-  if (engine == CPC_ENGINE_FP64) {
-    CK(launch_sky_fp64(c->d_jobs.p, sky_view(g1), sky_view(g2), c->d_hq.p, c->d_hq_n.p,
-                       kSkyHostQueue, esum, c->st), "sky kernel");
-  } else {
-    const SkyFast fa{g1.sky_su.p, g1.sky_sl.p, g1.sky_sw.p, g1.sky_sx.p, g1.sky_ss.p};
-    const SkyFast fb{g2.sky_su.p, g2.sky_sl.p, g2.sky_sw.p, g2.sky_sx.p, g2.sky_ss.p};
-    const float rp_lo_f = f_down(c->thr_rp[0]), rp_hi_f = f_up(c->thr_rp[p.n_bins]);
-    CK(launch_sky_warp(c->d_jobs.p, sky_view(g1), sky_view(g2), fa, fb, c->d_unit_ctr.p,
-                       c->d_hq.p, c->d_hq_n.p, kSkyHostQueue, esum, rp_lo_f, rp_hi_f,
-                       c->thr_rp[0] <= 0.0 ? 1 : 0, p.n_bins, p.n_p_bin, c->sm_count, c->st),
-       "sky kernel");
-    CK(launch_fix_to_sums((int64_t)n_fix, c->d_fix.p, c->d_sums.p, c->d_jobs.p, c->st),
-       "fixed-point sums");
-    c->launches += 1;
+  J.sf1 = sky_fast(g1);
+  J.sf2 = sky_fast(g2);
+  CK(Bf.hq.alloc(kSkyHostQueue), "alloc host queue");
+  CK(Bf.hq_n.alloc(1), "alloc");
+  CK(cudaMemsetAsync(Bf.hq_n.p, 0, sizeof(unsigned long long), st), "memset");
+  J.hq = Bf.hq.p;
+  J.hq_n = Bf.hq_n.p;
+  // a row sample: the redshift-ordered positions of the g1 rows whose input
+  // index i satisfies i % rs == ro (the outer rows corels2 would count); a
+  // work shard of the fast engine (cpc_set_shard): the positions k with
+  // k % n_shards == shard
+  J.row_list = nullptr;
+  J.n_rows = g1.n;
+  const int W = engine == CPC_ENGINE_FAST ? c->n_shards : 1;
+  if (rs > 1 || W > 1) {
+    std::vector<int> rows;
+    rows.reserve((size_t)(g1.n / std::max<int64_t>(1, rs) / W + 1));
+    for (int64_t i = W > 1 ? c->shard : 0; i < g1.n; i += W)
+      if (rs <= 1 || ((g1.hs_orig[i] - ro) % rs) == 0) rows.push_back((int)i);
+    CK(Bf.rows.alloc(std::max<size_t>(rows.size(), 1)), "alloc row sample");
+    if (!rows.empty())
+      CK(cudaMemcpyAsync(Bf.rows.p, rows.data(), sizeof(int) * rows.size(),
+                         cudaMemcpyHostToDevice, st), "H2D");
+    CK(cudaStreamSynchronize(st), "sync");  // rows is a host temporary
+    J.row_list = Bf.rows.p;
+    J.n_rows = (int64_t)rows.size();
   }
-  c->launches += 1;
-  CK(cudaEventRecord(c->e1, c->st), "event");
-  if ((st_ = fetch_accum(c, out, c->st, J.unit_w)) != CPC_OK) return st_;
+  return CPC_OK;
+}
+
+// The host edge tier of a finished job: the pairs the GPU queued are binned with
+// the C library in the reference's operation order and added to the output.
+cpc_status sky_finish(cpc_ctx *c, SkyPlan &P, size_t k, cpc_engine engine, float ms) {
+  const cpc_params &p = c->p;
+  cpc_accum *out = P.out;
+  SkyJobBufs &Bf = *c->sky_bufs[k];
+  cpc_status st_;
+  if ((st_ = fetch_accum_from(c, Bf.num.p, Bf.sums.p, Bf.counters.p, out, c->st,
+                              P.empty ? 0 : P.J.unit_w)) != CPC_OK)
+    return st_;
+  out->kernel_ms = out->pair_kernel_ms = ms;
+  if (P.empty) return CPC_OK;
+  if (engine != CPC_ENGINE_FP64) {
+    // the 64-bit fixed-point words hold 2^33 terms of |u| < 2^30 per bin
+    for (size_t q = 0; q < P.cells; q++)
+      if ((unsigned long long)out->num[q] >= (1ull << 33))
+        return fail(c, CPC_ERR_RANGE,
+                    "a sky bin holds 2^33 pairs or more: its fixed-point sums may overflow; "
+                    "count the term in row samples (row_stride)");
+  }
   unsigned long long nq = 0;
-  CK(cudaMemcpy(&nq, c->d_hq_n.p, sizeof nq, cudaMemcpyDeviceToHost), "D2H");
+  CK(cudaMemcpy(&nq, Bf.hq_n.p, sizeof nq, cudaMemcpyDeviceToHost), "D2H");
   if (nq > kSkyHostQueue)
     return fail(c, CPC_ERR_RANGE, "too many pairs within the trigonometry error bound of a bin edge");
   std::vector<int2> q(nq);
-  if (nq) CK(cudaMemcpy(q.data(), c->d_hq.p, sizeof(int2) * nq, cudaMemcpyDeviceToHost), "D2H");
-  float ms = 0;
-  CK(cudaEventElapsedTime(&ms, c->e0, c->e1), "event time");
+  if (nq) CK(cudaMemcpy(q.data(), Bf.hq.p, sizeof(int2) * nq, cudaMemcpyDeviceToHost), "D2H");
+  const JobRule &rule = P.rule;
+  Slot &g1 = c->slots[P.s1], &g2 = c->slots[P.s2];
   // host edge tier: the reference's own arithmetic with the C library
   const SkyParams sp = sky_params(c);
   const int nb = p.n_bins, npb = p.n_p_bin;
@@ -1668,12 +1730,82 @@ cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, i
     }
   }
   int64_t nbin = 0;
-  for (size_t k = 0; k < hstride; k++) nbin += out->num[k];
+  for (size_t q2 = 0; q2 < hstride; q2++) nbin += out->num[q2];
   out->n_binned = nbin;
   out->n_rechecked = (int64_t)nq;
-  out->kernel_ms = ms;
-  out->pair_kernel_ms = ms;
   return CPC_OK;
+}
+
+// Sky counts (coordinates 0) of one context: the fast engine runs every job in
+// one launch of the chunked warp kernel, then the fixed-point blocks are
+// converted and each job's host edge tier runs; the FP64 engine runs the plain
+// kernel per job.
+constexpr int kSkyRowsPerChunk = 64;
+cpc_status sky_run(cpc_ctx *c, std::vector<SkyPlan> &plans, cpc_engine engine) {
+  const cpc_params &p = c->p;
+  cudaStream_t st = c->st;
+  cpc_status st_;
+  if ((st_ = ensure_scratch(c, 1, plans.size())) != CPC_OK) return st_;
+  std::vector<JobDev> jd;
+  std::vector<long long> chunk0(1, 0);
+  std::vector<size_t> idx;  // plan of each launched job
+  for (size_t k = 0; k < plans.size(); k++) {
+    if (plans[k].empty) continue;
+    jd.push_back(plans[k].J);
+    idx.push_back(k);
+    const long long nr = plans[k].J.n_rows;
+    chunk0.push_back(chunk0.back() + (nr + kSkyRowsPerChunk - 1) / kSkyRowsPerChunk);
+  }
+  // bound on |sum_gpu - sum_libm|: cos differs by <= 3 ulp (CUDA 2 + C library
+  // 1), one more ulp from each of the product and the sum, doubled
+  const double esum = 8.0 * std::ldexp(1.0, -52);
+  CK(cudaEventRecord(c->e0, st), "event");
+  if (!jd.empty()) {
+    CK(cudaMemcpyAsync(c->d_jobs.p, jd.data(), sizeof(JobDev) * jd.size(), cudaMemcpyHostToDevice,
+                       st), "H2D jobs");
+    if (engine == CPC_ENGINE_FP64) {
+      for (size_t m = 0; m < jd.size(); m++) {
+        Slot &g1 = c->slots[plans[idx[m]].s1], &g2 = c->slots[plans[idx[m]].s2];
+        CK(launch_sky_fp64(c->d_jobs.p + m, sky_view(g1), sky_view(g2), jd[m].hq, jd[m].hq_n,
+                           kSkyHostQueue, esum, st), "sky kernel");
+        c->launches += 1;
+      }
+    } else {
+      CK(c->d_chunk0.alloc(chunk0.size()), "alloc chunk table");
+      CK(c->d_chunk_ctr.alloc(1), "alloc");
+      CK(cudaMemcpyAsync(c->d_chunk0.p, chunk0.data(), sizeof(long long) * chunk0.size(),
+                         cudaMemcpyHostToDevice, st), "H2D");
+      CK(cudaMemsetAsync(c->d_chunk_ctr.p, 0, sizeof(unsigned long long), st), "memset");
+      const float rp_lo_f = f_down(c->thr_rp[0]), rp_hi_f = f_up(c->thr_rp[p.n_bins]);
+      CK(launch_sky_warp(c->d_jobs.p, c->d_chunk0.p, (int)jd.size(), chunk0.back(),
+                         kSkyRowsPerChunk, c->d_chunk_ctr.p, kSkyHostQueue, esum, rp_lo_f,
+                         rp_hi_f, c->thr_rp[0] <= 0.0 ? 1 : 0, p.n_bins, p.n_p_bin, c->sm_count,
+                         c->sky_blocks_per_sm, st), "sky kernel");
+      c->launches += 1;
+      for (size_t m = 0; m < jd.size(); m++) {
+        const SkyPlan &P = plans[idx[m]];
+        CK(launch_fix_to_sums((int64_t)P.n_fix, jd[m].acc_fix, jd[m].acc_sums, c->d_jobs.p + m,
+                              st), "fixed-point sums");
+        c->launches += 1;
+      }
+    }
+  }
+  CK(cudaEventRecord(c->e1, st), "event");
+  CK(cudaEventSynchronize(c->e1), "sync");
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, c->e0, c->e1), "event time");
+  for (size_t k = 0; k < plans.size(); k++)
+    if ((st_ = sky_finish(c, plans[k], k, engine, ms)) != CPC_OK) return st_;
+  return CPC_OK;
+}
+
+// one sky corels2 call
+cpc_status sky_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, int64_t rs,
+                     int64_t ro, cpc_engine engine, cpc_accum *out, int auto_mode = 0) {
+  std::vector<SkyPlan> plans(1);
+  cpc_status s = sky_plan(c, kind, slot_g1, slot_g2, rs, ro, engine, out, auto_mode, 0, plans[0]);
+  if (s != CPC_OK) return s;
+  return sky_run(c, plans, engine);
 }
 
 }  // namespace
@@ -1715,6 +1847,8 @@ cpc_status cpc_create(cpc_ctx **out, const cpc_params *params) try {
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDevice");
   e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "device attribute");
+  if (const char *ev = std::getenv("CPC_SKY_BLOCKS_PER_SM"))
+    c->sky_blocks_per_sm = std::atoi(ev) >= 3 ? 3 : 2;
   e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "stream");
   e = cudaEventCreate(&c->e0);
@@ -1851,19 +1985,22 @@ cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, c
                      int64_t row_stride, int64_t row_offset, cpc_accum *out) try {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
   if (busy(c)) return CPC_ERR_STATE;
-  if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64)
+  if (engine != CPC_ENGINE_FAST && engine != CPC_ENGINE_FP64 && engine != CPC_ENGINE_CELL_FP64)
     return fail(c, CPC_ERR_INVALID, "unknown engine");
   if (kind == CPC_PAIR_SS)
     return fail(c, CPC_ERR_INVALID, "CPC_PAIR_SS pairs one catalogue: use cpc_count_auto");
   // sky: FP32-prefiltered warp kernel (fast) or plain FP64 kernel, both with
   // the FP64 path and the host edge tier for the pairs that can bin
-  if (c->p.coordinates == 0)
+  if (c->p.coordinates == 0) {
+    if (engine == CPC_ENGINE_CELL_FP64)
+      return fail(c, CPC_ERR_INVALID, "the cell-list FP64 engine counts box pairs only");
     return sky_count(c, kind, slot_g1, slot_g2, row_stride, row_offset, engine, out);
+  }
   std::vector<JobPlan> jobs(1);
   cpc_status s = plan_job(c, kind, slot_g1, slot_g2, row_stride, row_offset, out, jobs[0]);
   if (s != CPC_OK) return s;
   if (engine == CPC_ENGINE_FP64) return run_plain(jobs[0]);
-  if (engine != CPC_ENGINE_FAST) return fail(c, CPC_ERR_INVALID, "unknown engine");
+  jobs[0].jd.all_exact = engine == CPC_ENGINE_CELL_FP64 ? 1 : 0;
   return run_fast(jobs);
 } catch (...) {
   return host_exception(c);
@@ -1942,6 +2079,27 @@ cpc_status cpc_count_auto(cpc_ctx *c, cpc_pair_kind kind, int slot, cpc_engine e
   return host_exception(c);
 }
 
+// Pi windows the autotuner tries: for 4, 3 and 2 blocks per SM the largest
+// window whose histograms fit, and three quarters of it (more, narrower units)
+std::vector<int> tune_windows(const cpc_params &p, int corel) {
+  std::vector<int> ws;
+  const int jk = p.do_jk ? 1 : 0, nrp = p.n_bins, npi = p.n_p_bin;
+  const size_t static_b = fast_static_smem_bytes();
+  for (int b = 4; b >= 2; b--) {
+    const size_t budget = (size_t)(228 * 1024) / b - static_b - 1024;
+    int w = npi;
+    while (w > 1 && fast_smem_bytes(corel, jk, nrp, w) > budget) w--;
+    if (fast_smem_bytes(corel, jk, nrp, w) > budget) continue;
+    for (int cand : {w, (3 * w + 3) / 4}) {
+      if (cand < std::min(npi, 8)) continue;
+      if (std::find(ws.begin(), ws.end(), cand) == ws.end()) ws.push_back(cand);
+    }
+    if (w == npi) break;  // every Pi bin fits: fewer blocks gain nothing
+  }
+  if (ws.empty()) ws.push_back(0);
+  return ws;
+}
+
 cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2,
                         int64_t sample_stride, int *cells_per_rmax, int *pi_window) try {
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
@@ -1964,27 +2122,12 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
   acc.num = num.data();
   acc.sums = sums.data();
   const int ks[3] = {2, 3, 4};
-  // Pi windows: for 4, 3 and 2 blocks per SM the largest window whose
-  // histograms fit, and three quarters of it (more, narrower units)
   std::vector<int> ws;
   {
     JobRule rule;
     if (job_rule(p, kind, c->slots[slot_g1].n, c->slots[slot_g2].n, rule) != 0)
       return fail(c, CPC_ERR_INVALID, "bad pair kind");
-    const int jk = p.do_jk ? 1 : 0, nrp = p.n_bins, npi = p.n_p_bin;
-    const size_t static_b = fast_static_smem_bytes();
-    for (int b = 4; b >= 2; b--) {
-      const size_t budget = (size_t)(228 * 1024) / b - static_b - 1024;
-      int w = npi;
-      while (w > 1 && fast_smem_bytes(rule.corel, jk, nrp, w) > budget) w--;
-      if (fast_smem_bytes(rule.corel, jk, nrp, w) > budget) continue;
-      for (int cand : {w, (3 * w + 3) / 4}) {
-        if (cand < std::min(npi, 8)) continue;
-        if (std::find(ws.begin(), ws.end(), cand) == ws.end()) ws.push_back(cand);
-      }
-      if (w == npi) break;  // every Pi bin fits: fewer blocks gain nothing
-    }
-    if (ws.empty()) ws.push_back(0);
+    ws = tune_windows(p, rule.corel);
   }
   const int64_t stride = std::max<int64_t>(1, sample_stride);
   double best = INFINITY;
@@ -2025,6 +2168,102 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
   return host_exception(c);
 }
 
+// The batch of cpc_count_batch on every row_stride-th outer row of each job.
+cpc_status count_batch_rows(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind *kinds,
+                            const int *slots_g1, const int *slots_g2, cpc_accum *outs,
+                            int64_t row_stride) {
+  std::vector<JobPlan> jobs(n_jobs);
+  for (int k = 0; k < n_jobs; k++) {
+    if (ctxs[k]->device != ctxs[0]->device) return fail(ctxs[k], CPC_ERR_INVALID, "batch spans devices");
+    cpc_status s = plan_job(ctxs[k], kinds[k], slots_g1[k], slots_g2[k], row_stride, 0, &outs[k],
+                            jobs[k]);
+    if (s != CPC_OK) return s;
+  }
+  return run_fast(jobs);
+}
+
+cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind *kinds,
+                              const int *slots_g1, const int *slots_g2, int64_t sample_stride,
+                              int *cells_per_rmax, int *pi_window) try {
+  if (n_jobs <= 0 || !ctxs || !kinds || !slots_g1 || !slots_g2)
+    return fail(nullptr, CPC_ERR_INVALID, "bad batch arguments");
+  for (int k = 0; k < n_jobs; k++) {
+    if (!ctxs[k]) return fail(nullptr, CPC_ERR_INVALID, "null context in batch");
+    if (busy(ctxs[k])) return CPC_ERR_STATE;
+    const cpc_ctx *c = ctxs[k];
+    if (slots_g1[k] < 0 || slots_g1[k] >= kMaxSlots || slots_g2[k] < 0 || slots_g2[k] >= kMaxSlots)
+      return fail(ctxs[k], CPC_ERR_INVALID, "slot out of range");
+    if (!c->slots[slots_g1[k]].valid || !c->slots[slots_g2[k]].valid)
+      return fail(ctxs[k], CPC_ERR_STATE, "autotune before upload");
+    if (c->p.coordinates != 6 || c->p.n_bins != ctxs[0]->p.n_bins ||
+        c->p.n_p_bin != ctxs[0]->p.n_p_bin || c->p.which_corr != ctxs[0]->p.which_corr)
+      return fail(ctxs[k], CPC_ERR_INVALID,
+                  "batch autotuning needs box jobs with one binning and which_corr");
+  }
+  JobRule rule;
+  {
+    const cpc_ctx *c0 = ctxs[0];
+    if (job_rule(c0->p, kinds[0], c0->slots[slots_g1[0]].n, c0->slots[slots_g2[0]].n, rule) != 0)
+      return fail(ctxs[0], CPC_ERR_INVALID, "bad pair kind");
+  }
+  const std::vector<int> ws = tune_windows(ctxs[0]->p, rule.corel);
+  std::vector<std::vector<int64_t>> nums(n_jobs);
+  std::vector<std::vector<double>> sums(n_jobs);
+  std::vector<cpc_accum> accs(n_jobs);
+  for (int k = 0; k < n_jobs; k++) {
+    int nh, nb, npb;
+    cpc_accum_shape(ctxs[k], &nh, &nb, &npb);
+    nums[k].resize((size_t)nh * nb * npb);
+    sums[k].resize(nums[k].size() * kNF);
+    accs[k] = cpc_accum{};
+    accs[k].num = nums[k].data();
+    accs[k].sums = sums[k].data();
+  }
+  const int64_t stride = std::max<int64_t>(1, sample_stride);
+  // every slot a job reads, on cells r_max / kc
+  auto regrid = [&](int kc) -> cpc_status {
+    for (int k = 0; k < n_jobs; k++)
+      for (int sl : {slots_g1[k], slots_g2[k]}) {
+        Slot &s = ctxs[k]->slots[sl];
+        if (s.kcells != kc) {
+          const cpc_status st = rebuild_cells(ctxs[k], s, kc);
+          if (st != CPC_OK) return st;
+        }
+      }
+    return CPC_OK;
+  };
+  double best = INFINITY;
+  int bk = ctxs[0]->slots[slots_g1[0]].kcells, bw = ctxs[0]->tune_wpi;
+  for (int kc : {2, 3, 4}) {
+    cpc_status s = regrid(kc);
+    if (s != CPC_OK) return s;
+    for (int w : ws) {
+      for (int k = 0; k < n_jobs; k++) ctxs[k]->tune_wpi = w;
+      // first run builds the work units, the second is timed
+      if (count_batch_rows(n_jobs, ctxs, kinds, slots_g1, slots_g2, accs.data(), stride) != CPC_OK)
+        continue;
+      if (count_batch_rows(n_jobs, ctxs, kinds, slots_g1, slots_g2, accs.data(), stride) != CPC_OK)
+        continue;
+      if (accs[0].pair_kernel_ms < best) {
+        best = accs[0].pair_kernel_ms;
+        bk = kc;
+        bw = w;
+      }
+    }
+  }
+  for (int k = 0; k < n_jobs; k++) {
+    ctxs[k]->tune_k = bk;
+    ctxs[k]->tune_wpi = bw;
+  }
+  const cpc_status s = regrid(bk);
+  if (s != CPC_OK) return s;
+  if (cells_per_rmax) *cells_per_rmax = bk;
+  if (pi_window) *pi_window = bw;
+  return CPC_OK;
+} catch (...) {
+  return host_exception(n_jobs > 0 && ctxs ? ctxs[0] : nullptr);
+}
+
 cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind *kinds,
                            const int *slots_g1, const int *slots_g2, cpc_accum *outs) try {
   if (n_jobs <= 0 || !ctxs || !kinds || !slots_g1 || !slots_g2 || !outs)
@@ -2034,21 +2273,27 @@ cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind
   for (int k = 0; k < n_jobs; k++)
     if (!ctxs[k]) return fail(nullptr, CPC_ERR_INVALID, "null context in batch");
   for (int k = 0; k < n_jobs; k++)
-    if (ctxs[k]->p.coordinates == 0) {  // sky jobs: one launch each
-      for (int m = 0; m < n_jobs; m++) {
+    if (ctxs[k]->p.coordinates == 0) {
+      bool one_ctx = true;
+      for (int m = 0; m < n_jobs; m++) one_ctx = one_ctx && ctxs[m] == ctxs[0];
+      if (one_ctx) {  // the pair types of one sky run: one launch of the fast kernel
+        cpc_ctx *c = ctxs[0];
+        std::vector<SkyPlan> plans(n_jobs);
+        for (int m = 0; m < n_jobs; m++) {
+          const cpc_status s = sky_plan(c, kinds[m], slots_g1[m], slots_g2[m], 1, 0,
+                                        CPC_ENGINE_FAST, &outs[m], 0, (size_t)m, plans[m]);
+          if (s != CPC_OK) return s;
+        }
+        return sky_run(c, plans, CPC_ENGINE_FAST);
+      }
+      for (int m = 0; m < n_jobs; m++) {  // sky jobs of several contexts: one launch each
         const cpc_status s = cpc_count(ctxs[m], kinds[m], slots_g1[m], slots_g2[m],
                                        CPC_ENGINE_FAST, 1, 0, &outs[m]);
         if (s != CPC_OK) return s;
       }
       return CPC_OK;
     }
-  std::vector<JobPlan> jobs(n_jobs);
-  for (int k = 0; k < n_jobs; k++) {
-    if (ctxs[k]->device != ctxs[0]->device) return fail(ctxs[k], CPC_ERR_INVALID, "batch spans devices");
-    cpc_status s = plan_job(ctxs[k], kinds[k], slots_g1[k], slots_g2[k], 1, 0, &outs[k], jobs[k]);
-    if (s != CPC_OK) return s;
-  }
-  return run_fast(jobs);
+  return count_batch_rows(n_jobs, ctxs, kinds, slots_g1, slots_g2, outs, 1);
 } catch (...) {
   return host_exception(n_jobs > 0 && ctxs ? ctxs[0] : nullptr);
 }

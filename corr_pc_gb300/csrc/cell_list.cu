@@ -234,8 +234,14 @@ __global__ void gather_kernel(int64_t n, const uint64_t *__restrict__ keys,
   if (out.pos) {
     out.pos[k] = make_float4((float)x, (float)y, (float)z, (float)w);
     out.shp[k] = make_float4((float)e1, (float)e2, (float)phi, (float)e3);
+    // the weighted ellipticity w (e1, e2) and the weight as float hi + lo parts
+    // (the compensated shape terms of the pair kernel)
+    const double we1 = __dmul_rn(w, e1), we2 = __dmul_rn(w, e2);
+    const float h1 = (float)we1, h2 = (float)we2;
+    out.ewt[k] = make_float4(h1, h2, (float)(we1 - (double)h1), (float)(we2 - (double)h2));
+    out.aux[k] = make_float4((float)(x - (double)(float)x), (float)(y - (double)(float)y),
+                             (float)phi, (float)(w - (double)(float)w));
     out.zf[k] = (float)z;
-    out.lo[k] = make_float2((float)(x - (double)(float)x), (float)(y - (double)(float)y));
     out.zlo[k] = (float)(z - (double)(float)z);
   }
   if (out.bucket) out.bucket[k] = (uint32_t)(keys[k] >> 32);
@@ -327,17 +333,20 @@ __global__ void prep_catalog_kernel(PrepIn in, uint8_t *__restrict__ keep,
     // orderable key of w for the minimum
     const unsigned long long u = (unsigned long long)__double_as_longlong(w);
     wk = (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+    // |e| (with the third ED component): bounds the rotated ellipticities,
+    // kappa (read into e1) and the ED cosine alike
+    double e2sum = 0.0;
     if (in.e1) {
       const double a = in.e1[i], b = in.e2[i];
       bad |= !isfinite(a) || !isfinite(b);
-      em = nonneg_bits(fmax(fabs(a), fabs(b)));
+      e2sum = a * a + b * b;
     }
     if (in.e3) {
       const double c3 = in.e3[i];
       bad |= !isfinite(c3);
-      const double m3 = fabs(c3);
-      if (nonneg_bits(m3) > em) em = nonneg_bits(m3);
+      e2sum += c3 * c3;
     }
+    if (isfinite(e2sum)) em = nonneg_bits(sqrt(e2sum) * (1.0 + 1e-15));
     const double ph = in.phi ? in.phi[i] : -10.0;
     bad |= !isfinite(ph);
     pm = nonneg_bits(fabs(ph));

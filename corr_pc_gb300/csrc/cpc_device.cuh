@@ -3,7 +3,9 @@
 // Data layout in HBM (per uploaded catalogue, "slot"), all in cell-list order
 // (sorted by column, jackknife region, then z):
 //   pos  float4 (x, y, z, w)          16 B  -- the fast kernel's only hot stream
-//   shp  float4 (e1, e2, phi, 0)      16 B  -- read for binned pairs with shapes
+//   shp  float4 (e1, e2, phi, e3)     16 B  -- ED orientation
+//   ewt  float4 (w e1, w e2 hi; lo)   16 B  -- compensated shape terms
+//   aux  float4 (x lo, y lo, phi, w lo) 16 B -- read for binned pairs with shapes
 //   keep uint8  jk_prob >= 0.5         1 B
 //   xd,yd,zd,wd,e1d,e2d,phid double   56 B  -- FP64 edge recheck only
 //   jk   int32 region label            4 B
@@ -50,8 +52,10 @@ struct DCat {
 struct FCat {
   int64_t n;
   const float4 *pos;
-  const float4 *shp;
-  const float2 *lo;   // x - (float)x, y - (float)y (non-float32 inputs)
+  const float4 *shp;  // e1, e2, phi, e3 (ED orientation)
+  const float4 *ewt;  // w e1, w e2 as float hi parts, then their lo parts
+  const float4 *aux;  // x - (float)x, y - (float)y (non-float32 inputs), phi,
+                      // w - (float)w
   const float *zlo;   // z - (float)z (non-float32 inputs)
   const float *zf;
   const uint8_t *keep;
@@ -73,6 +77,18 @@ struct SkyView {
                              // ra_min, ra_max, dec_min, dec_max (host libm)
 };
 
+// float views of a sky catalogue for the fast kernel (hi = float(v),
+// lo = float(v - hi), so hi + lo carries about 48 bits of v)
+struct SkyFast {
+  const float4 *su;  // unit vector (cos d cos a, cos d sin a, sin d) hi parts, D_A
+  const float4 *sl;  // unit vector lo parts, D_C lo part
+  const float4 *sw;  // RA, Dec hi parts, redshift, D_C hi part
+  const float4 *sx;  // RA, Dec lo parts, Dec in radians, weight
+  const float4 *ss;  // w e1, w e2 hi parts, then their lo parts
+  const float4 *sh;  // cos(Dec / 2) hi, lo, sin(Dec / 2) hi, lo (Dec in radians)
+  const float2 *sp;  // phi, w lo part
+};
+
 struct JobDev {
   FCat f1, f2;  // g1 (outer rows) and g2 after the swap rule
   DCat d1, d2;  // same catalogues, FP64, cell order
@@ -82,6 +98,8 @@ struct JobDev {
   int auto_mode;            // 0 corels2; corels1: 1 unsorted, 2 z-sorted scan
   int has_lo;               // positions are not float32-exact: use hi+lo for theta
   int rmu;                  // coordinates 7: bins of r = |(dx, dy, Pi)| and mu = Pi / r
+  int all_exact;            // fast kernel: every window candidate to the FP64 path
+                            // (the cell-list FP64 comparison engine)
   int ncx, ncy;
   int64_t row_stride, row_offset;
   // ---- fast-path single precision constants ----
@@ -110,6 +128,11 @@ struct JobDev {
   unsigned long long *counters;        // [0] window (fast), [1] window (recheck), [2] rechecked
   unsigned long long *acc_fix;         // sky fast path: fixed-point sums, layout of acc_sums
   SkyView sky1, sky2;                  // sky catalogues g1, g2 (FP64 path of the fast kernel)
+  SkyFast sf1, sf2;                    // their float views (fast sky kernel)
+  const int *row_list;                 // sky row sample: the g1 rows counted, else null
+  int64_t n_rows;                      // rows in row_list
+  int2 *hq;                            // sky host-tier queue of this job
+  unsigned long long *hq_n;            // its length
 };
 
 // corels1 (corr.cpp:103-216).  The scan of row i starts at j = i + 1 (j = 0 for

@@ -15,7 +15,8 @@ struct GatherIn {
 };
 struct GatherOut {
   float4 *pos, *shp;  // null for the z-ordered (FP64) copy; shp = (e1, e2, phi, e3)
-  float2 *lo;
+  float4 *ewt;        // (w e1, w e2) hi parts, then their lo parts
+  float4 *aux;        // x lo, y lo, phi, w lo
   float *zlo;
   float *zf;
   uint32_t *bucket;   // null for the z-ordered copy
@@ -101,20 +102,16 @@ cudaError_t launch_plain_fp64(const JobDev *job, const DCat &a, const DCat &b, c
 // Sky pairs (coordinates 0) in FP64; pairs whose r_p may bin differently with
 // the C library's trigonometry are appended to hq (host edge tier).
 constexpr unsigned long long kSkyHostQueue = 1ull << 22;
-// float views of a sky catalogue for the fast kernel (hi = float(v),
-// lo = float(v - hi), so hi + lo carries about 48 bits of v)
-struct SkyFast {
-  const float4 *su;  // unit vector (cos d cos a, cos d sin a, sin d) hi parts, D_A
-  const float4 *sl;  // unit vector lo parts, D_C lo part
-  const float4 *sw;  // RA, Dec hi parts, redshift, D_C hi part
-  const float4 *sx;  // RA, Dec lo parts, Dec in radians, weight
-  const float4 *ss;  // e1, e2, phi, 0
-};
-cudaError_t launch_sky_warp(const JobDev *job, const SkyView &a, const SkyView &b,
-                            const SkyFast &fa, const SkyFast &fb, unsigned int *row_ctr, int2 *hq,
-                            unsigned long long *hq_n, unsigned long long hq_cap, double esum,
+// (SkyFast, the float views of a sky catalogue, is declared in cpc_device.cuh)
+// The fast sky kernel over n_jobs jobs (pair types) in one launch: job k's rows
+// are dealt in chunks chunk0[k] .. chunk0[k+1]-1 of rows_per_chunk rows;
+// chunk_ctr (zeroed) is the chunk queue.  Every job has the same binning.
+// blocks_per_sm: the register bound the kernel is compiled for (2 or 3).
+cudaError_t launch_sky_warp(const JobDev *jobs, const long long *chunk0, int n_jobs,
+                            long long n_chunks, int rows_per_chunk,
+                            unsigned long long *chunk_ctr, unsigned long long hq_cap, double esum,
                             float rp_lo_f, float rp_hi_f, int zero_bin, int nrp, int npi,
-                            int sm_count, cudaStream_t st);
+                            int sm_count, int blocks_per_sm, cudaStream_t st);
 cudaError_t launch_fix_to_sums(int64_t n, const unsigned long long *fix, double *sums,
                                const JobDev *job, cudaStream_t st);
 cudaError_t launch_sky_fp64(const JobDev *job, const SkyView &a, const SkyView &b, int2 *hq,

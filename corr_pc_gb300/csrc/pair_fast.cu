@@ -31,13 +31,18 @@
 // 32-bit counts and fixed-point sums split over two 32-bit words per field
 // (exact integer addition, order independent), flushed to the FP64 global
 // histogram block when the pairs added since the last flush could overflow a
-// word (below) and at the end of the unit.
+// word (below) and at the end of the unit.  The terms of the fields whose sums
+// cancel (rotated ellipticities and their products, kappa) are computed in
+// compensated single precision (pair_df.cuh) and quantised at 2^-29 of their
+// bound, so every bin sum matches the reference's double-precision sum to
+// about 1e-9 of the field's bound.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <climits>
 
 #include "cpc_device.cuh"
 #include "kernels.h"
+#include "pair_df.cuh"
 
 namespace cpc {
 
@@ -166,19 +171,17 @@ size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi) {
 }
 
 // Fixed-point sums in 32-bit shared words.  A term v of field f becomes the
-// integer u = rint(v * 2^S_f), |u| <= 2^26 (S_f from a bound on |v|); u is split
-// into its low 14 bits (0..16383) and the arithmetic shift u >> 14
-// (-2^12..2^12), each added to its own 32-bit word with a plain reduction (no
-// return value: no scoreboard wait; lanes of one instruction that hit the same
-// word are serialised, which red_pair halves).  A block counts the pairs its
-// warps queued since the last flush and flushes before a chunk that could take
-// the count past 2^18 (a chunk adds at most kTile * kChunk pairs), so a bin takes
-// at most 2^18 terms between flushes: the low word stays below 2^32 and the high
-// word, read as a signed integer, within +-2^30.
-constexpr unsigned kFlushTerms = 1u << 18;
-__device__ __forceinline__ int to_fixed(float v, float scale) {
-  return __float2int_rn(v * scale);
-}
+// integer u = rint(v * 2^S_f), |u| < 2^29 (S_f from a bound on |v|); u is split
+// into its low 15 bits (0..32767) and the arithmetic shift u >> 15
+// (-2^14..2^14 - 1), each added to its own 32-bit word with a plain reduction
+// (no return value: no scoreboard wait; lanes of one instruction that hit the
+// same word are serialised, which red_pair halves).  A block counts the pairs
+// its warps queued since the last flush and flushes before a chunk that could
+// take the count past 2^17 (a chunk adds at most kTile * kChunk = 2^17 pairs),
+// so a bin takes at most 2^17 terms between flushes: the low word stays below
+// 2^32 and the high word, read as a signed integer, within [-2^31, 2^31).
+constexpr unsigned kFlushTerms = 1u << 17;
+static_assert((unsigned)kTile * kChunk <= kFlushTerms, "a chunk fits between flushes");
 // The two reductions of one term, even lanes taking the low word first and odd
 // lanes the high word first: lanes of one instruction that hit the same bin then
 // split over two addresses 16 banks apart (same-address shared reductions are
@@ -190,7 +193,7 @@ __device__ __forceinline__ void red_pair(unsigned *lo, unsigned *hi, unsigned wa
   atomicAdd(odd ? lo : hi, wb);
 }
 __device__ __forceinline__ double fixed_total(unsigned lw, unsigned hw, double inv_scale) {
-  const long long tot = (long long)(int)hw * 16384ll + (long long)lw;
+  const long long tot = (long long)(int)hw * 32768ll + (long long)lw;
   return (double)tot * inv_scale;
 }
 
@@ -296,7 +299,7 @@ __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsi
       tm[f] = 0;
       for (int r = 0; r < nrep; r++) {
         const size_t o = (size_t)f * NBm + (r == 0 ? lb : rep_bin(r, n1, elk, nrp, wpi));
-        tm[f] += (long long)(int)mhi[o] * 16384ll + (long long)mlo[o];
+        tm[f] += (long long)(int)mhi[o] * 32768ll + (long long)mlo[o];
         mlo[o] = 0u;
         mhi[o] = 0u;
       }
@@ -312,7 +315,7 @@ __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsi
 #pragma unroll
     for (int g = 0; g < FJ; g++) {
       const size_t o = (size_t)g * NB + lb;
-      const long long tn = (long long)(int)nhi[o] * 16384ll + (long long)nlo[o];
+      const long long tn = (long long)(int)nhi[o] * 32768ll + (long long)nlo[o];
       nlo[o] = 0u;
       nhi[o] = 0u;
       const long long tx = tm[FMAP::jm(g)] - tn;
@@ -351,13 +354,14 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   __shared__ int s_jidx[kBatch];
   __shared__ int s_orig[kBatch];  // input index of each staged candidate (corels1)
   __shared__ unsigned char s_keep[kBatch];
-  __shared__ float2 s_lo[kBatch];
+  __shared__ float4 s_aux[kBatch];  // x lo, y lo, phi, w lo of each staged candidate
   __shared__ unsigned long long s_red[kThreads / 32];
   __shared__ unsigned s_nbin;  // pairs queued by the block's warps since the last flush
   __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
   // the tile's g1 rows, for the heavy step (any lane may process any row)
-  __shared__ float4 s_rpos[kTile], s_rshp[kTile];
-  __shared__ float2 s_rlo[kTile];
+  // s_rshp / s_shp hold the weighted ellipticities (ewt) for the corels with
+  // shape terms and the orientation (shp) for ED
+  __shared__ float4 s_rpos[kTile], s_rshp[kTile], s_raux[kTile];
   __shared__ float s_rzlo[kTile], s_zlo[kBatch];  // z lo parts (ED separations)
   __shared__ unsigned char s_rkeep[kTile];
   // corels1 rule of each row for each z image sz (index sz + 1), as a threshold
@@ -410,6 +414,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     constexpr bool kTheta = C == COREL_SD || C == COREL_SS || C == COREL_SSA || C == COREL_SK;
     const bool has_lo = (kTheta || C == COREL_ED) && J.has_lo;
     const int rmu = J.rmu;
+    const bool all_exact = J.all_exact != 0;  // the cell-list FP64 comparison engine
     // jackknife attribution: jk_check_PB (the box's rule; this kernel runs box
     // jobs only)
     const int gws = J.gws, lin_bin = J.lin_bin;
@@ -431,8 +436,10 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
           const int64_t o = J.d1.orig[i1] - J.row_offset;
           ok = (o % J.row_stride) == 0;
         }
-        if (C != COREL_DD) s_rshp[tr] = J.f1.shp[i1];
-        if (has_lo) s_rlo[tr] = J.f1.lo[i1];
+        if (C != COREL_DD) {
+          s_rshp[tr] = C == COREL_ED ? J.f1.shp[i1] : J.f1.ewt[i1];
+          s_raux[tr] = J.f1.aux[i1];
+        }
         if (C == COREL_ED && has_lo) s_rzlo[tr] = J.f1.zlo[i1];
         if (JK) s_rkeep[tr] = J.f1.keep[i1];
       }
@@ -619,8 +626,10 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             q2.y -= g2sy;
             q2.z -= g2sz;
             s_pos[t] = q2;
-            if (C != COREL_DD) s_shp[t] = J.f2.shp[j2];
-            if (has_lo) s_lo[t] = J.f2.lo[j2];
+            if (C != COREL_DD) {
+              s_shp[t] = C == COREL_ED ? J.f2.shp[j2] : J.f2.ewt[j2];
+              s_aux[t] = J.f2.aux[j2];
+            }
             if (C == COREL_ED && has_lo) s_zlo[t] = J.f2.zlo[j2];
             s_jidx[t] = j2;
             if (J.auto_mode) s_orig[t] = (int)J.d2.orig[j2];
@@ -661,7 +670,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               bool binned = false, edge = false;
               if ((othr < 0 || s_orig[c] > othr) && dz >= pi_out_lo &&
                   dz <= pi_out_hi && m <= xy_out) {
-                if (!(dz >= pi_in_lo && dz <= pi_in_hi && m <= xy_in)) {
+                if (all_exact || !(dz >= pi_in_lo && dz <= pi_in_hi && m <= xy_in)) {
                   // near the window edge: queued with a flag, the heavy step hands
                   // it to the exact FP64 evaluation of the whole pair
                   edge = true;
@@ -747,16 +756,22 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               // raw (un-shifted) separation for the orientation angle
               // (angle_orient_axis_PB); coincident positions give atan(0/0) in
               // the reference: those pairs take the exact path
-              float dxr = 0.f, dyr = 0.f;
+              // The separation is a double-float: the exact difference of the
+              // float hi parts, plus the lo parts for inputs that are not
+              // float32 values (renormalised); it is zero only when the
+              // positions coincide.
+              df32 dxr{0.f, 0.f}, dyr{0.f, 0.f};
               if (kTheta) {
-                dxr = (p2.x + g2sx) - r1.x;
-                dyr = (p2.y + g2sy) - r1.y;
+                const float x2r = p2.x + g2sx, y2r = p2.y + g2sy;  // x2, y2 restored exactly
                 if (has_lo) {
-                  const float2 lo1 = s_rlo[er], lo2 = s_lo[ec];
-                  dxr += lo2.x - lo1.x;
-                  dyr += lo2.y - lo1.y;
+                  const float4 a1 = s_raux[er], a2 = s_aux[ec];
+                  dxr = df_diff_hl(x2r, a2.x, r1.x, a1.x);
+                  dyr = df_diff_hl(y2r, a2.y, r1.y, a1.y);
+                } else {
+                  dxr = two_diff(x2r, r1.x);
+                  dyr = two_diff(y2r, r1.y);
                 }
-                if (dxr == 0.0f && dyr == 0.0f) amb = true;
+                if (dxr.h == 0.0f && dyr.h == 0.0f) amb = true;
               }
               // ED: the shifted separation g1 - (g2 + L*PB) (ED_calc_PB) from
               // hi + lo positions; a zero separation gives 0/0 in the reference
@@ -766,9 +781,9 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                 sye = hdy;
                 sze = -hdz;
                 if (has_lo) {
-                  const float2 lo1 = s_rlo[er], lo2 = s_lo[ec];
-                  sxe += lo1.x - lo2.x;
-                  sye += lo1.y - lo2.y;
+                  const float4 a1 = s_raux[er], a2 = s_aux[ec];
+                  sxe += a1.x - a2.x;
+                  sye += a1.y - a2.y;
                   sze += s_rzlo[er] - s_zlo[ec];
                 }
                 see = fmaf(sxe, sxe, fmaf(sye, sye, sze * sze));
@@ -785,78 +800,30 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                         qcount, qcap);
               } else {
               const int lb = n1 * wpi + elk;
+              // per-field terms: v (float) for every field, vd (double-float)
+              // for the fields whose sums cancel (df_field)
               float v[kNF];
+              df32 vd[kNF];
               const float w = r1.w * p2.w;
               v[0] = w;
-              if (C == COREL_DK) {  // the shape holder's kappa (e[0])
-                v[1] = gws == 1 ? w * s_rshp[er].x : gws == 2 ? w * s_shp[ec].x : 0.0f;
-              } else if (C == COREL_ED) {
+              if (C == COREL_ED) {
                 const float4 es = gws == 2 ? s_shp[ec] : s_rshp[er];
                 const float dot = fmaf(es.x, sxe, fmaf(es.y, sye, es.w * sze));
                 v[11] = __fdividef(dot * dot, see);
                 v[12] = v[11] * v[11];
               } else if (C != COREL_DD) {
-                // wg+ reads only the shape holder's (e1, e2) and the row's phi
-                // (8 + 4 bytes of shared memory); the other corels both rows'
-                const float4 e1v = C == COREL_SD ? make_float4(0.f, 0.f, 0.f, 0.f) : s_rshp[er];
-                const float4 s2 = C == COREL_SD ? make_float4(0.f, 0.f, 0.f, 0.f) : s_shp[ec];
-                const float a = dxr * dxr, b = dyr * dyr;
-                const float inv = __fdividef(1.0f, a + b);
-                const float c2 = (a - b) * inv, s2v = 2.0f * dxr * dyr * inv;
-                const float theta = atanf(__fdividef(dyr, dxr));
-                if (C == COREL_SK) {
-                  // rotate the shape holder's e, weight by the other's kappa
-                  if (gws == 1 || gws == 2) {
-                    const float4 es = gws == 2 ? s2 : e1v;
-                    const float kap = gws == 2 ? e1v.x : s2.x;
-                    const float en0 = c2 * es.x - s2v * es.y, en1 = s2v * es.x + c2 * es.y;
-                    const float ep = w * kap;
-                    v[1] = ep;
-                    v[5] = ep * en0;
-                    v[9] = ep * en1;
-                  } else {
-                    v[1] = v[5] = v[9] = 0.0f;
-                  }
-                } else if (C == COREL_SD) {
-                  const float2 *eh = gws == 2 ? reinterpret_cast<const float2 *>(&s_shp[ec])
-                                              : reinterpret_cast<const float2 *>(&s_rshp[er]);
-                  const float2 e = *eh;
-                  const float es0 = e.x, es1 = e.y;
-                  const float ep = c2 * es0 - s2v * es1, ex = s2v * es0 + c2 * es1;
-                  v[1] = w * ep;
-                  v[2] = v[1] * v[1];
-                  v[3] = w * ex;
-                  v[4] = v[3] * v[3];
-                  v[11] = ephi_f(s_rshp[er].z, theta);
-                  v[12] = v[11] * v[11];
-                } else {
-                  const float ei0 = c2 * e1v.x - s2v * e1v.y, ei1 = s2v * e1v.x + c2 * e1v.y;
-                  const float ej0 = c2 * s2.x - s2v * s2.y, ej1 = s2v * s2.x + c2 * s2.y;
-                  if (C == COREL_SS) {
-                    const bool g2s = gws == 2;
-                    v[1] = w * (g2s ? ej0 : ei0);
-                    v[2] = v[1] * v[1];
-                    v[11] = ephi_f(g2s ? s2.z : e1v.z, theta);
-                    v[12] = v[11] * v[11];
-                  } else {
-                    v[1] = w * (ei0 + ej0) * 0.5f;
-                    const float pa = w * ei0 * 0.5f, pb = w * ej0 * 0.5f;
-                    v[2] = pa * pa + pb * pb;
-                    v[3] = w * (ei1 + ej1) * 0.5f;
-                    const float qa = w * ei1 * 0.5f, qb = w * ej1 * 0.5f;
-                    v[4] = qa * qa + qb * qb;
-                    const float ta = ephi_f(e1v.z, theta), tb = ephi_f(s2.z, theta);
-                    v[11] = ta + tb;
-                    v[12] = ta * ta + tb * tb;
-                  }
-                  v[5] = w * (ei0 * ej0);
-                  v[6] = v[5] * v[5];
-                  v[7] = w * (ei1 * ej1);
-                  v[8] = v[7] * v[7];
-                  v[9] = w * (ei1 * ej0 + ei0 * ej1) * 0.5f;
-                  const float xa = w * (ei1 * ej0) * 0.5f, xb = w * ei0 * ej1 * 0.5f;
-                  v[10] = xa * xa + xb * xb;
+                // (w e1, w e2) hi and lo parts, the weight's lo part and phi
+                const float4 ea = s_rshp[er], eb = s_shp[ec];
+                const float4 xa = s_raux[er], xb = s_aux[ec];
+                const DfGal g1{{ea.x, ea.z}, {ea.y, ea.w}, {r1.w, xa.w}, xa.z};
+                const DfGal g2{{eb.x, eb.z}, {eb.y, eb.w}, {p2.w, xb.w}, xb.z};
+                df32 c2{0.f, 0.f}, s2v{0.f, 0.f};
+                float theta = 0.f;
+                if (kTheta) {
+                  df_cos_sin_2theta(dxr, dyr, c2, s2v);
+                  if (C != COREL_SK) theta = atanf(__fdividef(dyr.h, dxr.h));
                 }
+                df_pair_terms<C>(c2, s2v, theta, g1, g2, gws, J.unit_w != 0, vd, v);
               }
               // fixed-point words of the main fields, in this lane's order (even
               // lanes low word first, odd lanes high word first: red_pair); the
@@ -865,10 +832,12 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               unsigned wa[F::FM], wb[F::FM];
 #pragma unroll
               for (int f = 0; f < F::FM; f++) {
-                const int u = to_fixed(v[F::m(f)], sc.qs[F::m(f)]);
-                const unsigned a = (unsigned)u & 0x3FFFu, b = (unsigned)(u >> 14);
-                wa[f] = odd_lane ? b : a;
-                wb[f] = odd_lane ? a : b;
+                const int q = F::m(f);
+                unsigned lo15, hi;
+                if (df_field(C, q)) df_to_fixed15(vd[q], sc.qs[q], lo15, hi);
+                else f_to_fixed15(v[q], sc.qs[q], lo15, hi);
+                wa[f] = odd_lane ? hi : lo15;
+                wb[f] = odd_lane ? lo15 : hi;
               }
               // the main bin, or one of its copies for a hot r_p bin
               const int rep = (lane >> 1) & (kHotRep - 1);

@@ -24,6 +24,8 @@
 #include "../../include/corrpc.h"
 #include "cpc_device.cuh"
 #include "host_helpers.h"
+#include "pair_values.h"
+#include "param_check.h"
 
 namespace cpc {
 namespace {
@@ -66,54 +68,16 @@ __global__ void check_inputs_kernel(NCat a, NCat b, int n_jk, int *flag) {
       if (a.jk[i] < 0 || a.jk[i] >= n_jk) atomicOr(flag, 2);
 }
 
-// the per-pair values of corels.cpp:48-77, 122-244 in double
+// the per-pair values of corels.cpp:48-77, 122-244 in double: pair_values.h,
+// the function the other FP64 paths use, with the orientation angle of
+// angle_orient_axis_PB (calcs.cpp:54-57)
 __device__ void noalloc_values(const JobDev &J, const NCat &g1, int64_t i, const NCat &g2,
                                int64_t j, double f[kNF]) {
-  for (int q = 0; q < kNF; q++) f[q] = 0.0;
   const double wt = __dmul_rn(nc_w(g1, i), nc_w(g2, j));
-  f[0] = wt;
-  if (J.corel == COREL_DD) return;
-  const double theta = atan((g2.y[j] - g1.y[i]) / (g2.x[j] - g1.x[i]));
-  const double c2 = cos(2.0 * theta), s2 = sin(2.0 * theta);
-  const double kpi = 3.141592653589793;
-  auto ephi = [&](double phi) {
-    double t = fabs(phi - theta);
-    return t > kpi / 2.0 ? kpi - t : t;
-  };
-  if (J.corel == COREL_SD) {
-    const bool s_is_2 = J.gws == 2;
-    const double e0 = s_is_2 ? nc_e1(g2, j) : nc_e1(g1, i), e1 = s_is_2 ? nc_e2(g2, j) : nc_e2(g1, i);
-    f[1] = wt * (c2 * e0 - s2 * e1);
-    f[2] = f[1] * f[1];
-    f[3] = wt * (s2 * e0 + c2 * e1);
-    f[4] = f[3] * f[3];
-    f[11] = ephi(nc_phi(g1, i));
-    f[12] = f[11] * f[11];
-    return;
-  }
-  const double ei0 = c2 * nc_e1(g1, i) - s2 * nc_e2(g1, i), ei1 = s2 * nc_e1(g1, i) + c2 * nc_e2(g1, i);
-  const double ej0 = c2 * nc_e1(g2, j) - s2 * nc_e2(g2, j), ej1 = s2 * nc_e1(g2, j) + c2 * nc_e2(g2, j);
-  if (J.corel == COREL_SS) {
-    f[1] = wt * (J.gws == 2 ? ej0 : ei0);
-    f[2] = f[1] * f[1];
-    f[11] = ephi(J.gws == 2 ? nc_phi(g2, j) : nc_phi(g1, i));
-    f[12] = f[11] * f[11];
-  } else {
-    f[1] = wt * (ei0 + ej0) / 2.0;
-    f[2] = (wt * ei0 / 2.0) * (wt * ei0 / 2.0) + (wt * ej0 / 2.0) * (wt * ej0 / 2.0);
-    f[3] = wt * (ei1 + ej1) / 2.0;
-    f[4] = (wt * ei1 / 2.0) * (wt * ei1 / 2.0) + (wt * ej1 / 2.0) * (wt * ej1 / 2.0);
-    const double a = ephi(nc_phi(g1, i)), b = ephi(nc_phi(g2, j));
-    f[11] = a + b;
-    f[12] = a * a + b * b;
-  }
-  f[5] = wt * (ei0 * ej0);
-  f[6] = f[5] * f[5];
-  f[7] = wt * (ei1 * ej1);
-  f[8] = f[7] * f[7];
-  f[9] = wt * (ei1 * ej0 + ei0 * ej1) / 2.0;
-  const double pa = wt * (ei1 * ej0) / 2.0, pb = wt * ei0 * ej1 / 2.0;
-  f[10] = pa * pa + pb * pb;
+  const double theta =
+      J.corel == COREL_DD ? 0.0 : atan((g2.y[j] - g1.y[i]) / (g2.x[j] - g1.x[i]));
+  pair_values(J.corel, J.gws, wt, theta, PairGal{nc_e1(g1, i), nc_e2(g1, i), nc_phi(g1, i)},
+              PairGal{nc_e1(g2, j), nc_e2(g2, j), nc_phi(g2, j)}, f);
 }
 
 // thread per g1 row, z-window binary search in the z-sorted g2, exact FP64
@@ -196,28 +160,22 @@ void put_err(char *buf, size_t len, const char *msg) {
 
 using namespace cpc;
 
-extern "C" cpc_status cpc_count_fp64_noalloc(const cpc_params *p, cpc_pair_kind kind,
-                                             const cpc_device_catalog *c1,
-                                             const cpc_device_catalog *c2, int64_t *d_num,
-                                             double *d_sums, int64_t *n_window,
-                                             int64_t *n_binned, void *stream, char *err,
-                                             size_t err_len) {
+static cpc_status count_fp64_noalloc(const cpc_params *p, cpc_pair_kind kind,
+                                     const cpc_device_catalog *c1, const cpc_device_catalog *c2,
+                                     int64_t *d_num, double *d_sums, int64_t *n_window,
+                                     int64_t *n_binned, void *stream, char *err, size_t err_len) {
   if (!p || !c1 || !c2 || !d_num || !d_sums) {
     put_err(err, err_len, "null argument");
     return CPC_ERR_INVALID;
   }
-  if (p->coordinates != 6 || p->sig_crit != 0 || p->rand_subsample != 0 || p->which_corr < 0 ||
-      p->which_corr > 2 || (p->do_jk != 0 && p->do_jk != 1) || !(p->periodic_box_size > 0) ||
-      !(p->p_max > p->p_min) || !(p->bin_r_max > p->bin_r_min)) {
-    put_err(err, err_len, "unsupported parameters (coordinates 6, which_corr 0-2, no sig_crit)");
+  if (p->coordinates != 6 || p->which_corr < 0 || p->which_corr > 2) {
+    put_err(err, err_len, "unsupported parameters (coordinates 6 and which_corr 0-2 only)");
     return CPC_ERR_INVALID;
   }
-  if (p->n_bins < 1 || p->n_bins > kMaxRp || p->n_p_bin < 1 || p->n_p_bin > kMaxPi) {
-    put_err(err, err_len, "n_bins must be 1..64 and n_p_bin 1..128 (scratch capacity)");
-    return CPC_ERR_INVALID;
-  }
-  if (p->do_jk && (p->n_jk < 1 || p->n_jk > 100000)) {
-    put_err(err, err_len, "n_jk out of range");
+  // the checks cpc_create applies (bin limits, box, n_bins <= 64 and
+  // n_p_bin <= 128 -- also the scratch capacity)
+  if (const char *m = param_error(*p)) {
+    put_err(err, err_len, m);
     return CPC_ERR_INVALID;
   }
   if (c1->n < 0 || c2->n < 0 || c1->n > 2147483647LL || c2->n > 2147483647LL) {
@@ -265,6 +223,12 @@ extern "C" cpc_status cpc_count_fp64_noalloc(const cpc_params *p, cpc_pair_kind 
   if ((g1->n > 0 && (!g1->x || !g1->y || !g1->z)) || (g2->n > 0 && (!g2->x || !g2->y || !g2->z)) ||
       (p->do_jk && ((g1->n > 0 && !g1->jk) || (g2->n > 0 && !g2->jk)))) {
     put_err(err, err_len, "missing device arrays (positions, or jackknife labels with do_jk)");
+    return CPC_ERR_INVALID;
+  }
+  // the box attribution of a cross-region pair reads both galaxies' jk_prob
+  // draws (jk_check_PB, jk.cpp:64-71): without them it would be lost
+  if (p->do_jk && ((g1->n > 0 && !g1->jk_prob) || (g2->n > 0 && !g2->jk_prob))) {
+    put_err(err, err_len, "jk_prob required with do_jk (the jackknife attribution reads it)");
     return CPC_ERR_INVALID;
   }
   JobDev J;
@@ -344,4 +308,19 @@ extern "C" cpc_status cpc_count_fp64_noalloc(const cpc_params *p, cpc_pair_kind 
   if (n_window) *n_window = (int64_t)cnt[0];
   if (n_binned) *n_binned = (int64_t)cnt[1];
   return CPC_OK;
+}
+
+extern "C" cpc_status cpc_count_fp64_noalloc(const cpc_params *p, cpc_pair_kind kind,
+                                             const cpc_device_catalog *c1,
+                                             const cpc_device_catalog *c2, int64_t *d_num,
+                                             double *d_sums, int64_t *n_window,
+                                             int64_t *n_binned, void *stream, char *err,
+                                             size_t err_len) {
+  try {
+    return count_fp64_noalloc(p, kind, c1, c2, d_num, d_sums, n_window, n_binned, stream, err,
+                              err_len);
+  } catch (...) {  // e.g. std::system_error from the mutex: never across the C ABI
+    put_err(err, err_len, "host exception in cpc_count_fp64_noalloc");
+    return CPC_ERR_HOST;
+  }
 }

@@ -44,6 +44,7 @@
 
 #include "cpc_device.cuh"
 #include "kernels.h"
+#include "pair_df.cuh"
 
 namespace cpc {
 
@@ -179,26 +180,30 @@ __device__ __forceinline__ void sky_accumulate_exact(const JobDev &J, int r1, in
   }
 }
 
-// FP32 values of a pair from the mixed-precision path as fixed-point integers
-// rint(v 2^S_f), |v| 2^S_f <= 2^28 (S_f from bounds on |v|), added as 64-bit
-// integers: the main histogram in shared memory (SMEM) or in the global
-// fixed-point block, the regions in the global fixed-point block.  Field 0
-// (the weight) is skipped when every weight is 1 (wt_num = count).
+// Terms of a pair from the mixed-precision path as fixed-point integers
+// rint(v 2^S_f), |v| 2^S_f < 2^30 (S_f from bounds on |v|): the fields whose
+// sums cancel from double-float terms vd, the others from float terms v; added
+// as 64-bit integers: the main histogram in shared memory (SMEM) or in the
+// global fixed-point block, the regions in the global fixed-point block.
+// Field 0 (the weight) is skipped when every weight is 1 (wt_num = count).
 template <bool SMEM>
 __device__ __forceinline__ void sky_accumulate_fixed(const JobDev &J, int r1, int keep1, int r2,
                                                      int keep2, int64_t cell, const float *v,
-                                                     int nf, const float *s_qs,
+                                                     const df32 *vd, int nf, const float *s_qs,
                                                      unsigned long long *s_num,
                                                      unsigned long long *s_fix) {
   const int f0 = J.unit_w ? 1 : 0;
+  const int corel = J.corel;
   auto fx = [&](int q) {
-    return (unsigned long long)(long long)__float2int_rn(v[q] * s_qs[q]);
+    const int u = df_field(corel, q) ? df_to_int(vd[q], s_qs[q]) : __float2int_rn(v[q] * s_qs[q]);
+    return (unsigned long long)(long long)u;
   };
+  auto nz = [&](int q) { return df_field(corel, q) ? vd[q].h != 0.0f : v[q] != 0.0f; };
   unsigned long long *mfix = SMEM ? s_fix : J.acc_fix;
   atomicAdd(SMEM ? &s_num[cell] : &J.acc_num[cell], 1ull);
 #pragma unroll
   for (int q = 0; q < kNF; q++)  // constant indices: v stays in registers
-    if (q >= f0 && q < nf && v[q] != 0.0f) atomicAdd(&mfix[cell * kNF + q], fx(q));
+    if (q >= f0 && q < nf && nz(q)) atomicAdd(&mfix[cell * kNF + q], fx(q));
   if (!J.do_jk) return;
   const int64_t hstride = (int64_t)J.nrp * J.npi;
   int rs[2];
@@ -211,7 +216,7 @@ __device__ __forceinline__ void sky_accumulate_fixed(const JobDev &J, int r1, in
     if (J.which_corr == 0 || nf == 1) continue;
 #pragma unroll
     for (int q = 1; q < kNF; q += 2)
-      if (v[q] != 0.0f) atomicAdd(&sj[q], fx(q));
+      if (nz(q)) atomicAdd(&sj[q], fx(q));
   }
 }
 
@@ -263,7 +268,8 @@ __device__ __noinline__ void sky_pair_fp64(const JobDev &J, int64_t i, int64_t j
 
 // the row's float quantities for the mixed-precision path
 struct SkyRowF {
-  float4 u, ul, w, x, sh;  // su, sl, sw, sx, ss of the row
+  float4 u, ul, w, x, s, h;  // su, sl, sw, sx, ss, sh of the row
+  float2 p;                  // sp of the row
 };
 
 // estimated bin index confirmed against definite bands: the bin, -1 certainly
@@ -330,63 +336,40 @@ __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r,
   const int64_t cell = (int64_t)k1 * J.npi + k2;
   if (J.corel == COREL_DD) {
     const float f0[1] = {wt};
-    sky_accumulate_fixed<SMEM>(J, r.jk, r.keep, b.d.jk[j], b.d.keep[j], cell, f0, 1, s_qs, s_num,
-                               s_fix);
+    sky_accumulate_fixed<SMEM>(J, r.jk, r.keep, b.d.jk[j], b.d.keep[j], cell, f0, nullptr, 1,
+                               s_qs, s_num, s_fix);
   } else {
-    const float4 sh2 = fb.ss[j];
-    const float dra = (w2.x - rf.w.x) + (x2.x - rf.x.x);
-    const float ddec = (w2.y - rf.w.y) + (x2.y - rf.x.y);
-    const float xx = dra * __cosf(0.5f * (rf.x.z + x2.z)), yy = ddec;
-    const float a = xx * xx, bb = yy * yy;
-    const float inv = __fdividef(1.0f, a + bb);
-    const float cs = (a - bb) * inv, sn = 2.0f * xx * yy * inv;
-    const float theta = atanf(__fdividef(yy, xx));
+    // the separation in RA and Dec (hi + lo degrees) and cos of the mean Dec,
+    // cos(d1/2 + d2/2), as double-floats; X = dRA cos(mean Dec), Y = dDec
+    const float4 se2 = fb.ss[j], sh2 = fb.sh[j];
+    const float2 sp2 = fb.sp[j];
+    const df32 dra = df_diff_hl(w2.x, x2.x, rf.w.x, rf.x.x);
+    const df32 ddec = df_diff_hl(w2.y, x2.y, rf.w.y, rf.x.y);
+    const df32 cm = df_sub(df_mul(df32{rf.h.x, rf.h.y}, df32{sh2.x, sh2.y}),
+                           df_mul(df32{rf.h.z, rf.h.w}, df32{sh2.z, sh2.w}));
+    const df32 X = df_mul(dra, cm);
     float v[kNF];
-    for (int q = 0; q < kNF; q++) v[q] = 0.0f;
-    v[0] = wt;
-    auto ephi = [&](float phi) {
-      float t = fabsf(phi - theta);
-      return t > 1.5707963267948966f ? 3.14159265358979f - t : t;
-    };
-    if (J.corel == COREL_SD) {
-      const float es0 = J.gws == 2 ? sh2.x : rf.sh.x, es1 = J.gws == 2 ? sh2.y : rf.sh.y;
-      const float ep = cs * es0 - sn * es1, ex = sn * es0 + cs * es1;
-      v[1] = wt * ep;
-      v[2] = v[1] * v[1];
-      v[3] = wt * ex;
-      v[4] = v[3] * v[3];
-      v[11] = ephi(rf.sh.z);
-      v[12] = v[11] * v[11];
-    } else {
-      const float ei0 = cs * rf.sh.x - sn * rf.sh.y, ei1 = sn * rf.sh.x + cs * rf.sh.y;
-      const float ej0 = cs * sh2.x - sn * sh2.y, ej1 = sn * sh2.x + cs * sh2.y;
-      if (J.corel == COREL_SS) {
-        const bool g2s = J.gws == 2;
-        v[1] = wt * (g2s ? ej0 : ei0);
-        v[2] = v[1] * v[1];
-        v[11] = ephi(g2s ? sh2.z : rf.sh.z);
-        v[12] = v[11] * v[11];
-      } else {
-        v[1] = wt * (ei0 + ej0) * 0.5f;
-        const float pa = wt * ei0 * 0.5f, pb = wt * ej0 * 0.5f;
-        v[2] = pa * pa + pb * pb;
-        v[3] = wt * (ei1 + ej1) * 0.5f;
-        const float qa = wt * ei1 * 0.5f, qb = wt * ej1 * 0.5f;
-        v[4] = qa * qa + qb * qb;
-        const float ta = ephi(rf.sh.z), tb = ephi(sh2.z);
-        v[11] = ta + tb;
-        v[12] = ta * ta + tb * tb;
-      }
-      v[5] = wt * (ei0 * ej0);
-      v[6] = v[5] * v[5];
-      v[7] = wt * (ei1 * ej1);
-      v[8] = v[7] * v[7];
-      v[9] = wt * (ei1 * ej0 + ei0 * ej1) * 0.5f;
-      const float xa = wt * (ei1 * ej0) * 0.5f, xb = wt * ei0 * ej1 * 0.5f;
-      v[10] = xa * xa + xb * xb;
+    df32 vd[kNF];
+    for (int q = 0; q < kNF; q++) {
+      v[q] = 0.0f;
+      vd[q] = df32{0.0f, 0.0f};
     }
-    sky_accumulate_fixed<SMEM>(J, r.jk, r.keep, b.d.jk[j], b.d.keep[j], cell, v, kNF, s_qs, s_num,
-                               s_fix);
+    v[0] = wt;
+    if (X.h == 0.0f && ddec.h == 0.0f) {  // coincident on the sky: atan(0/0), the FP64 path
+      sky_pair_fp64(J, r.i, j, hq, hq_n, hq_cap, esum);
+      return;
+    }
+    df32 c, sn;
+    df_cos_sin_2theta(X, ddec, c, sn);
+    const float theta = atanf(__fdividef(ddec.h, X.h));
+    const DfGal g1{{rf.s.x, rf.s.z}, {rf.s.y, rf.s.w}, {rf.x.w, rf.p.y}, rf.p.x};
+    const DfGal g2{{se2.x, se2.z}, {se2.y, se2.w}, {x2.w, sp2.y}, sp2.x};
+    const bool uw = J.unit_w != 0;
+    if (J.corel == COREL_SD) df_pair_terms<COREL_SD>(c, sn, theta, g1, g2, J.gws, uw, vd, v);
+    else if (J.corel == COREL_SS) df_pair_terms<COREL_SS>(c, sn, theta, g1, g2, J.gws, uw, vd, v);
+    else df_pair_terms<COREL_SSA>(c, sn, theta, g1, g2, J.gws, uw, vd, v);
+    sky_accumulate_fixed<SMEM>(J, r.jk, r.keep, b.d.jk[j], b.d.keep[j], cell, v, vd, kNF, s_qs,
+                               s_num, s_fix);
   }
 }
 
@@ -412,12 +395,19 @@ __device__ __forceinline__ int fwin(float x, float lo_ru, float hi_rd, float lo_
   return -1;
 }
 
-template <bool SMEM>
-__global__ void __launch_bounds__(kSkyThreads, 2)
-sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast fa, SkyFast fb,
-                unsigned int *row_ctr, int2 *hq, unsigned long long *hq_n,
-                unsigned long long hq_cap, double esum, float rp_lo_f, float rp_hi_f,
-                int zero_bin) {
+// Rows are dealt in chunks of consecutive rows of one job (a pair type of the
+// batch): a block takes a chunk, its warps take the chunk's rows one at a time,
+// and the block meets at a barrier between chunks.  The block-private main
+// histogram belongs to one job; when the next chunk belongs to another job
+// (the chunks are numbered job after job, so a block switches at most
+// n_jobs - 1 times) the block adds it to the previous job's global block and
+// starts the next from zero.  A job's rows are every row of g1 or, for a row
+// sample, the listed rows.
+template <bool SMEM, int MINB>
+__global__ void __launch_bounds__(kSkyThreads, MINB)
+sky_warp_kernel(const JobDev *__restrict__ jobs, const long long *__restrict__ chunk0, int n_jobs,
+                int rows_per_chunk, unsigned long long *chunk_ctr, unsigned long long hq_cap,
+                double esum, float rp_lo_f, float rp_hi_f, int zero_bin) {
   extern __shared__ __align__(16) unsigned char sky_smem[];
   __shared__ int s_q[kSkyWarps][kSkyQ];
   // per warp, kSkyAhead + 1 stages of 32 candidates' sw and su views: the next
@@ -425,31 +415,75 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
   __shared__ float4 s_pw[kSkyWarps][kSkyAhead + 1][32], s_pu[kSkyWarps][kSkyAhead + 1][32];
   __shared__ SkyRowF s_rowf[kSkyWarps];
   __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
-  const JobDev &J = *jobp;
-  const int ncell = J.nrp * J.npi;
-  for (int k = threadIdx.x; k < J.nrp; k += blockDim.x) { s_A[k] = J.A[k]; s_B[k] = J.B[k]; }
-  for (int k = threadIdx.x; k < J.npi; k += blockDim.x) { s_PA[k] = J.PA[k]; s_PB[k] = J.PB[k]; }
   __shared__ float s_qs[kNF];
-  if (threadIdx.x < kNF) s_qs[threadIdx.x] = J.qscale[threadIdx.x];
+  __shared__ long long s_chunk;
+  __shared__ int s_rowctr;
+  __shared__ unsigned long long s_red[kSkyWarps];
+  const int ncell = jobs[0].nrp * jobs[0].npi;  // one binning for every job of a launch
   unsigned long long *s_num = reinterpret_cast<unsigned long long *>(sky_smem);
   unsigned long long *s_fix = s_num + ncell;
-  if (SMEM) {
-    for (int c = threadIdx.x; c < ncell; c += blockDim.x) s_num[c] = 0ull;
-    for (int c = threadIdx.x; c < ncell * kNF; c += blockDim.x) s_fix[c] = 0ull;
-  }
-  __syncthreads();  // bands, scales, zeroed histograms
   const unsigned FULL = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int *q = s_q[warp];
-  const int64_t n1 = a.d.n, n2 = b.d.n;
-  const float pmin_f = (float)J.pmin, pmax_f = (float)J.pmax;
-  unsigned long long nwin = 0;
+  int cur = -1;                 // the job whose histogram the block holds
+  unsigned long long nwin = 0;  // window pairs of this thread's rows of job cur
+  for (;;) {
+    __syncthreads();  // every warp is done with the previous chunk
+    if (threadIdx.x == 0) {
+      s_chunk = (long long)atomicAdd(chunk_ctr, 1ull);
+      s_rowctr = 0;
+    }
+    __syncthreads();
+    const long long ch = s_chunk;
+    int k = 0;
+    while (k < n_jobs && ch >= chunk0[k + 1]) k++;  // block-uniform
+    if (k != cur) {
+      if (cur >= 0) {  // the previous job's block histogram and window count
+        const JobDev &P = jobs[cur];
+        if (SMEM) {
+          for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+            const unsigned long long v = s_num[c];
+            if (!v) continue;
+            atomicAdd(&P.acc_num[c], v);
+            for (int f = 0; f < kNF; f++) {
+              const unsigned long long x = s_fix[c * kNF + f];
+              if (x != 0ull) atomicAdd(&P.acc_fix[c * kNF + f], x);
+            }
+          }
+        }
+        unsigned long long v = nwin;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+        if (lane == 0 && v) atomicAdd(&P.counters[1], v);
+        nwin = 0;
+      }
+      if (k >= n_jobs) break;
+      cur = k;
+      const JobDev &N = jobs[k];
+      for (int c = threadIdx.x; c < N.nrp; c += blockDim.x) { s_A[c] = N.A[c]; s_B[c] = N.B[c]; }
+      for (int c = threadIdx.x; c < N.npi; c += blockDim.x) { s_PA[c] = N.PA[c]; s_PB[c] = N.PB[c]; }
+      if (threadIdx.x < kNF) s_qs[threadIdx.x] = N.qscale[threadIdx.x];
+      if (SMEM) {
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) s_num[c] = 0ull;
+        for (int c = threadIdx.x; c < ncell * kNF; c += blockDim.x) s_fix[c] = 0ull;
+      }
+      __syncthreads();  // bands, scales, zeroed histogram
+    }
+    const JobDev &J = jobs[k];
+    const SkyView &a = J.sky1, &b = J.sky2;
+    const SkyFast &fa = J.sf1, &fb = J.sf2;
+    const int64_t n1 = a.d.n, n2 = b.d.n;
+    const int64_t n_rows = J.row_list ? J.n_rows : n1;
+    const int64_t r0 = (ch - chunk0[k]) * rows_per_chunk;
+    const int64_t r1 = min(r0 + (int64_t)rows_per_chunk, n_rows);
+    const float pmin_f = (float)J.pmin, pmax_f = (float)J.pmax;
+    int2 *hq = J.hq;
+    unsigned long long *hq_n = J.hq_n;
   for (;;) {
     int64_t i = 0;
-    if (lane == 0) i = atomicAdd(row_ctr, 1u);
+    if (lane == 0) i = r0 + atomicAdd(&s_rowctr, 1);
     i = __shfl_sync(FULL, i, 0);
-    if (i >= n1) break;
-    if (J.row_stride > 1 && ((a.d.orig[i] - J.row_offset) % J.row_stride) != 0) continue;
+    if (i >= r1) break;
+    if (J.row_list) i = J.row_list[i];
     if (J.auto_mode == 2 && !(a.d.aflag[i] & kAutoStart0)) continue;  // corels1, sorted
     const int64_t oi = a.d.orig[i];
     // the mixed path reads the row's index, region and keep flag; the FP64 path
@@ -476,7 +510,9 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
       rf.ul = fa.sl[i];
       rf.w = fa.sw[i];
       rf.x = fa.sx[i];
-      rf.sh = fa.ss[i];
+      rf.s = fa.ss[i];
+      rf.h = fa.sh[i];
+      rf.p = fa.sp[i];
     }
     __syncwarp();
     // redshift range [lo, hi): z_min <= z <= z_max
@@ -570,20 +606,8 @@ sky_warp_kernel(const JobDev *__restrict__ jobp, SkyView a, SkyView b, SkyFast f
       sky_pair_mixed<SMEM>(J, r, rf, b, fb, q[lane], s_num, s_fix, s_qs, hq, hq_n, hq_cap, esum, s_A,
                            s_B, s_PA, s_PB);
     __syncwarp();
-  }
-  if (nwin) atomicAdd(&J.counters[1], nwin);
-  if (SMEM) {
-    __syncthreads();
-    for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
-      const unsigned long long v = s_num[c];
-      if (!v) continue;
-      atomicAdd(&J.acc_num[c], v);
-      for (int f = 0; f < kNF; f++) {
-        const unsigned long long x = s_fix[c * kNF + f];
-        if (x != 0ull) atomicAdd(&J.acc_fix[c * kNF + f], x);
-      }
-    }
-  }
+  }  // rows of the chunk
+  }  // chunks
 }
 
 size_t sky_warp_smem_bytes(int nrp, int npi) {
@@ -609,35 +633,52 @@ cudaError_t launch_fix_to_sums(int64_t n, const unsigned long long *fix, double 
   return cudaGetLastError();
 }
 
-cudaError_t launch_sky_warp(const JobDev *job, const SkyView &a, const SkyView &b,
-                            const SkyFast &fa, const SkyFast &fb, unsigned int *row_ctr, int2 *hq,
-                            unsigned long long *hq_n, unsigned long long hq_cap, double esum,
-                            float rp_lo_f, float rp_hi_f, int zero_bin, int nrp, int npi,
-                            int sm_count, cudaStream_t st) {
-  if (a.d.n == 0 || b.d.n == 0) return cudaSuccess;
-  const size_t smem = sky_warp_smem_bytes(nrp, npi);
-  const bool use_smem = smem <= 100 * 1024;
+template <int MINB>
+static cudaError_t launch_sky_warp_t(const JobDev *jobs, const long long *chunk0, int n_jobs,
+                                     long long n_chunks, int rows_per_chunk,
+                                     unsigned long long *chunk_ctr, unsigned long long hq_cap,
+                                     double esum, float rp_lo_f, float rp_hi_f, int zero_bin,
+                                     size_t smem, bool use_smem, int sm_count, cudaStream_t st) {
   int bps = 0;
   cudaError_t e;
   if (use_smem) {
-    e = cudaFuncSetAttribute(sky_warp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
+    e = cudaFuncSetAttribute(sky_warp_kernel<true, MINB>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sky_warp_kernel<true>, kSkyThreads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sky_warp_kernel<true, MINB>,
+                                                      kSkyThreads, smem);
   } else {
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sky_warp_kernel<false>, kSkyThreads, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sky_warp_kernel<false, MINB>,
+                                                      kSkyThreads, 0);
   }
   if (e != cudaSuccess) return e;
   if (bps < 1) bps = 1;
-  const int64_t rows_blocks = (a.d.n + kSkyWarps - 1) / kSkyWarps;
-  const int grid = (int)std::min<int64_t>((int64_t)sm_count * bps, rows_blocks);
+  const int grid = (int)std::min<long long>((long long)sm_count * bps, n_chunks);
   if (use_smem)
-    sky_warp_kernel<true><<<grid, kSkyThreads, smem, st>>>(job, a, b, fa, fb, row_ctr, hq, hq_n,
-                                                           hq_cap, esum, rp_lo_f, rp_hi_f, zero_bin);
+    sky_warp_kernel<true, MINB><<<grid, kSkyThreads, smem, st>>>(
+        jobs, chunk0, n_jobs, rows_per_chunk, chunk_ctr, hq_cap, esum, rp_lo_f, rp_hi_f,
+        zero_bin);
   else
-    sky_warp_kernel<false><<<grid, kSkyThreads, 0, st>>>(job, a, b, fa, fb, row_ctr, hq, hq_n,
-                                                         hq_cap, esum, rp_lo_f, rp_hi_f, zero_bin);
+    sky_warp_kernel<false, MINB><<<grid, kSkyThreads, 0, st>>>(
+        jobs, chunk0, n_jobs, rows_per_chunk, chunk_ctr, hq_cap, esum, rp_lo_f, rp_hi_f,
+        zero_bin);
   return cudaGetLastError();
+}
+
+cudaError_t launch_sky_warp(const JobDev *jobs, const long long *chunk0, int n_jobs,
+                            long long n_chunks, int rows_per_chunk,
+                            unsigned long long *chunk_ctr, unsigned long long hq_cap, double esum,
+                            float rp_lo_f, float rp_hi_f, int zero_bin, int nrp, int npi,
+                            int sm_count, int blocks_per_sm, cudaStream_t st) {
+  if (n_jobs <= 0 || n_chunks <= 0) return cudaSuccess;
+  const size_t smem = sky_warp_smem_bytes(nrp, npi);
+  const bool use_smem = smem <= 100 * 1024;
+  if (blocks_per_sm >= 3)  // 80 registers: more warps, a few spills
+    return launch_sky_warp_t<3>(jobs, chunk0, n_jobs, n_chunks, rows_per_chunk, chunk_ctr,
+                                hq_cap, esum, rp_lo_f, rp_hi_f, zero_bin, smem, use_smem,
+                                sm_count, st);
+  return launch_sky_warp_t<2>(jobs, chunk0, n_jobs, n_chunks, rows_per_chunk, chunk_ctr, hq_cap,
+                              esum, rp_lo_f, rp_hi_f, zero_bin, smem, use_smem, sm_count, st);
 }
 
 cudaError_t launch_sky_fp64(const JobDev *job, const SkyView &a, const SkyView &b, int2 *hq,

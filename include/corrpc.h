@@ -55,8 +55,12 @@ typedef enum {
 
 /* which kernel counts the pairs */
 typedef enum {
-  CPC_ENGINE_FAST = 0, /* FP32 cell-list kernel with FP64 recheck near edges */
-  CPC_ENGINE_FP64 = 1  /* plain all-FP64 kernel: one thread per g1 row      */
+  CPC_ENGINE_FAST = 0,      /* FP32 cell-list kernel with FP64 recheck near edges */
+  CPC_ENGINE_FP64 = 1,      /* plain all-FP64 kernel: one thread per g1 row      */
+  CPC_ENGINE_CELL_FP64 = 2  /* the fast kernel's cell list and work units, every
+                               window candidate evaluated by the FP64 path (box
+                               cross counts, cpc_count only): the precision
+                               comparison at equal algorithm                     */
 } cpc_engine;
 
 /* Parameters: the data_info fields the pair loop reads (data_def.h:46-96),
@@ -191,7 +195,11 @@ cpc_status cpc_accum_shape(const cpc_ctx *ctx, int *n_hist, int *n_bins, int *n_
  * (e.g. many periodic sub-boxes), in ONE persistent launch of the fast
  * kernel that drains a single device work queue.  ctxs[k], kinds[k],
  * slots_g1[k], slots_g2[k] and outs[k] describe job k.  All contexts must
- * live on the current device.  Synchronous. */
+ * live on the current device.  Sky jobs (coordinates 0) that share one
+ * context -- the SRd, RsRd, SD and DRs terms of a sky run, do_corr.cpp:103-131
+ * -- run in one launch of the fast sky kernel, whose blocks take chunks of
+ * each term's outer rows in turn; sky jobs on several contexts run one launch
+ * each.  Synchronous. */
 cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind *kinds,
                            const int *slots_g1, const int *slots_g2, cpc_accum *outs);
 
@@ -209,6 +217,15 @@ cpc_status cpc_set_tuning(cpc_ctx *ctx, int cells_per_rmax, int pi_window, int t
 cpc_status cpc_autotune(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_g2,
                         int64_t sample_stride, int *cells_per_rmax, int *pi_window);
 
+/* Autotuner of a batch (the jobs of cpc_count_batch, box runs with one binning
+ * and which_corr): the same cell widths and Pi windows, each trial one batched
+ * launch over every `sample_stride`-th outer row of every job; the fastest is
+ * kept for every context of the batch and returned.  No counterpart in the
+ * reference (its sub-boxes are separate runs, corr.cpp:219). */
+cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind *kinds,
+                              const int *slots_g1, const int *slots_g2, int64_t sample_stride,
+                              int *cells_per_rmax, int *pi_window);
+
 /* Work sharding over GPUs (replaces the reference's division of the outer
  * rows over OpenMP threads, corr.cpp:299-302 and 329-424): later
  * fast-engine box counts on ctx (cpc_count, cpc_count_async, cpc_count_auto,
@@ -218,8 +235,10 @@ cpc_status cpc_autotune(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_
  * per GPU, each on its own context with the same catalogues) sum to the whole
  * count: counts exactly, sums up to the order of FP64 additions.  Unlike
  * row_stride, whose skipped rows still pass through every unit, each shard does
- * about 1/n_shards of the work.  Sky counts and the FP64 engine shard by rows
- * (row_stride / row_offset), which they skip cheaply.  Default: shard 0 of 1. */
+ * about 1/n_shards of the work.  Fast sky counts take the outer rows at
+ * redshift-ordered positions k with k % n_shards == shard (the shards again
+ * partition the pairs); the FP64 engine shards by rows (row_stride /
+ * row_offset), which it skips cheaply.  Default: shard 0 of 1. */
 cpc_status cpc_set_shard(cpc_ctx *ctx, int shard, int n_shards);
 
 /* Number of GPU kernels this context has launched so far (all entry points;
@@ -299,16 +318,20 @@ cpc_status cpc_host_finalize_auto(const char *inp_path, const int64_t *ss_num,
  *    is larger, shape holder, corel choice); after the swap the scanned
  *    catalogue must be sorted by z (checked; CPC_ERR_INVALID otherwise), as
  *    the reference requires for data_sorted 1.  NULL optional arrays as in
- *    cpc_catalog; jk_prob replaces the host-side keep flags.
+ *    cpc_catalog; jk_prob replaces the host-side keep flags and is required
+ *    with do_jk (CPC_ERR_INVALID otherwise).
  *  - d_num / d_sums: device buffers laid out as cpc_accum's num / sums (raw
  *    region sums); zeroed by the call.  n_window / n_binned: host outputs.
- *  - limits: coordinates 6, n_bins <= 64, n_p_bin <= 128 (the scratch holds
- *    the thresholds), catalogue sizes < 2^31; larger values are rejected with
- *    CPC_ERR_INVALID and a message.
+ *  - limits: coordinates 6, which_corr 0-2, n_bins <= 64, n_p_bin <= 128 (the
+ *    scratch holds the thresholds), catalogue sizes < 2^31, and every check
+ *    cpc_create applies; other values are rejected with CPC_ERR_INVALID and a
+ *    message.
  *  - the first call on a device looks up the scratch array's device address
- *    (with that device current); make that first call before any stream
- *    capture.  The call synchronises `stream` (a cudaStream_t, NULL = legacy
- *    default stream).
+ *    (with that device current) and keeps it for later calls; make that first
+ *    call before any stream capture.  A device reset (cudaDeviceReset) between
+ *    calls is not supported: the kept address would no longer be valid.  The
+ *    call synchronises `stream` (a cudaStream_t, NULL = legacy default
+ *    stream).
  *  - every call on a device shares the one scratch array and leaves its
  *    contents behind; calls are safe one after another, but calls that overlap
  *    on the GPU race on it and must be serialised by the caller.

@@ -36,12 +36,16 @@ def build_port() -> str:
     return PORT_SO
 
 
+# the reference tree (read-only): CPC_REFERENCE_DIR, else its usual place here
+REF_DIR = os.environ.get("CPC_REFERENCE_DIR", "/root/reference")
+
+
 def build_reference() -> str | None:
     """Build the reference harness from the reference sources (no-op where the
     reference tree is absent)."""
-    if not os.path.isdir("/root/reference"):
+    if not os.path.isdir(REF_DIR):
         return None
-    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={REF_DIR}"], check=True)
     return REF_BIN
 
 

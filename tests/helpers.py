@@ -10,8 +10,6 @@ import numpy as np
 from corr_pc_gb300 import synth
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-# fields whose sums do not cancel (weights, squares, theta term): checked per bin
-NONCANCEL = [0, 2, 4, 6, 8, 10, 11, 12]
 
 
 def golden_names():
@@ -134,11 +132,12 @@ class Golden:
 
 
 def check_sums(got, ref, rtol=1e-6, label="", big_frac=1e-2):
-    """Accuracy bar: every bin of every field within rtol relative, with an
-    absolute floor of rtol x the largest |value| of that field for bins whose
-    true value is near zero; non-cancelling fields (weights, squares, theta
-    term) also within rtol per bin wherever the bin holds at least big_frac of
-    the field's largest value (tiny bins are covered by the floor)."""
+    """Accuracy bar, for every field (the cancelling e+/ex and product sums
+    included): bins holding at least big_frac of the field's largest |value|
+    within rtol relative; the other bins, whose true value is near zero, within
+    rtol x that largest value; and the Pi-integrated r_p profile of the full
+    sample (the w(r_p) numerator) within rtol relative wherever it holds at
+    least big_frac of its largest value."""
     got = np.asarray(got)
     ref = np.asarray(ref)
     for f in range(ref.shape[-1]):
@@ -150,10 +149,16 @@ def check_sums(got, ref, rtol=1e-6, label="", big_frac=1e-2):
             continue
         err = np.abs(g - r)
         assert err.max() <= rtol * fmax, f"{label} field {f}: max err {err.max()} vs floor {rtol * fmax}"
-        if f in NONCANCEL:
-            big = np.abs(r) >= big_frac * fmax
-            rel = err[big] / np.abs(r[big])
-            assert rel.max() <= rtol, f"{label} field {f}: per-bin rel err {rel.max()}"
+        big = np.abs(r) >= big_frac * fmax
+        rel = err[big] / np.abs(r[big])
+        assert rel.max() <= rtol, f"{label} field {f}: per-bin rel err {rel.max()}"
+        if r.ndim == 3:  # [histogram, r_p, Pi]: the full sample's r_p profile
+            pr, pg = r[0].sum(axis=-1), g[0].sum(axis=-1)
+            pmax = np.abs(pr).max()
+            if pmax > 0:
+                pb = np.abs(pr) >= big_frac * pmax
+                prel = np.abs(pg - pr)[pb] / np.abs(pr[pb])
+                assert prel.max() <= rtol, f"{label} field {f}: r_p profile rel err {prel.max()}"
 
 
 def parse_table(text):

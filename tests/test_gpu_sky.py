@@ -112,3 +112,28 @@ def test_sky_rejects_bad_input():
     with pytest.raises(ValueError):
         _lib.Context(p)
     ctx.close()
+
+
+@pytest.mark.parametrize("name", ["sky_wgp_jk", "sky_wgg_distinct_wrap"])
+def test_sky_terms_in_one_launch_match_reference(name):
+    """The four terms of a sky run (SRd, RsRd, SD, DRs) counted in one launch of
+    the fast kernel (cpc_count_batch on one context) equal the reference's."""
+    g = SkyGolden(name)
+    p = g.params
+    cats = host.prepare(p, g.read_order(), table=g.table)
+    ctx = _context(p, g.table, cats)
+    l0 = ctx.launches()
+    jobs = [(ctx, SkyGolden.KIND[t][0], SLOTS[SkyGolden.KIND[t][1]], SLOTS[SkyGolden.KIND[t][2]])
+            for t in g.terms]
+    rs = _lib.count_batch(jobs)
+    # one pair kernel plus one fixed-point conversion per term
+    assert ctx.launches() - l0 == 1 + len(g.terms)
+    for t, r in zip(g.terms, rs):
+        rnum, rsums, rin, rtot = g.term(t)
+        assert (r["n_binned"], r["n_window"]) == (rin, rtot), t
+        assert np.array_equal(r["num"], rnum), t
+        if t == "DRs" and g.meta["drs_as_wgg"]:
+            check_sums(r["sums"][..., :1], rsums[..., :1], label=t)
+        else:
+            check_sums(r["sums"], rsums, label=t)
+    ctx.close()
