@@ -478,7 +478,8 @@ def main() -> None:
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD)
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline")
     ap.add_argument("--ref-budget", type=float, default=5.0, help="seconds per reference step")
-    ap.add_argument("--fp64-budget", type=float, default=3.0, help="seconds of FP64 kernel")
+    ap.add_argument("--fp64-budget", type=float, default=3.0,
+                    help="seconds of FP64 kernel (0: skip)")
     ap.add_argument("--cell-fp64-pairs", type=float, default=1e8,
                     help="binned pairs of the cell-list FP64 comparison (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
@@ -544,10 +545,13 @@ def main() -> None:
                          "by (column, region, z), gather of the SoA streams, bucket tables"}
     flush = None if big else torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
-    def step(k=0):
+    def step(k=0, sharded=True):
         if len(ctxs) == 1:
             if n_shards > 1:
-                ctxs[0].set_shard(k % n_shards, n_shards)
+                if sharded:
+                    ctxs[0].set_shard(k % n_shards, n_shards)
+                else:
+                    ctxs[0].set_shard(0, 1)
             r = ctxs[0].count("SD", 0, 1)
             return r["n_binned"], r["kernel_ms"], r["pair_kernel_ms"], r["n_window"]
         rs = _lib.count_batch([(c, "SD", 0, 1) for c in ctxs])
@@ -609,7 +613,7 @@ def main() -> None:
         for c, cat in zip(ctxs, preps):
             c.upload(0, cat["D"])
             c.upload(1, cat["S"])
-        e2e_bin += step()[0]
+        e2e_bin += step(sharded=False)[0]
     e2e_t = (time.perf_counter() - t0) / e2e_steps
     e2e_value = e2e_bin / e2e_steps / e2e_t
     if n_shards > 1:  # one full count: the value's timed steps together count it once
@@ -667,7 +671,7 @@ def main() -> None:
             "source": f"ncu --set full, profiles/fast_pairs_kernel_{wl_name}.md"}
     # plain FP64 GPU kernel on a bounded row sample of the same workload
     fp64 = None
-    if len(ctxs) == 1:
+    if len(ctxs) == 1 and args.fp64_budget > 0:
         est_rate = 1.5e8 if not big else 2e7
         stride = max(1, int(full_pairs / (est_rate * args.fp64_budget)))
         r64 = ctxs[0].count("SD", 0, 1, engine="fp64", row_stride=stride)

@@ -104,6 +104,9 @@ struct Slot {
   std::vector<int32_t> hs_jk;
   std::vector<uint8_t> hs_keep;
   std::vector<int64_t> hs_orig;  // input row of each redshift-ordered row (row samples)
+  // the sky kernel's outer-row order: redshift-ordered positions grouped by
+  // redshift slab (16 of equal size) and jackknife region, redshift order within
+  std::vector<int> hs_rorder;
 };
 
 // device buffers of one job of a sky launch: its histogram block, fixed-point
@@ -429,7 +432,8 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   auto fit = [&](int blocks) {
     const size_t budget = (size_t)(228 * 1024) / blocks - static_b - 1024;
     int w = npi;
-    while (w > (rmu ? 1 : 8) && fast_smem_bytes(jp.rule.corel, jk, nrp, w) > budget) w--;
+    while (w > (rmu ? 1 : 8) && fast_smem_bytes(jp.rule.corel, jk, nrp, w, auto_mode) > budget)
+      w--;
     return w;
   };
   int wpi = npi;
@@ -851,6 +855,7 @@ struct FastGroup {
   int corel, jk, minb, grid;
   size_t first, n_units, smem;
   FastScales sc;
+  int auto_pairs;  // the group holds corels1 jobs (their rules in shared memory)
 };
 
 size_t accum_cells(const cpc_ctx *c) {
@@ -876,7 +881,7 @@ cpc_status fast_body(cpc_ctx *c0, std::vector<JobPlan> &jobs, const std::vector<
     CK(cudaMemsetAsync(c0->d_unit_ctr.p, 0, sizeof(unsigned int), st), "memset");
     CK(launch_fast(g.corel, g.jk, g.minb, c0->d_jobs.p, c0->d_units.p + g.first, (int)g.n_units,
                    c0->d_unit_ctr.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, g.sc, g.smem,
-                   g.grid, st),
+                   g.grid, g.auto_pairs, st),
        "fast kernel");
   }
   CK(cudaEventRecordWithFlags(c0->e2, st, rec_flags), "event");
@@ -916,6 +921,7 @@ std::vector<uint64_t> fast_graph_key(cpc_ctx *c0, const std::vector<JobPlan> &jo
     put(g.first);
     put(g.n_units);
     put(g.smem);
+    put((uint64_t)g.auto_pairs);
     for (int f = 0; f < kNF; f++) {  // the scales are kernel parameters too
       uint32_t b;
       std::memcpy(&b, &g.sc.qs[f], sizeof b);
@@ -1026,13 +1032,16 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
     const int corel = gkeys[g].first, jk = gkeys[g].second;
     size_t smem = 0;  // the largest any job of the group needs
     FastScales sc;    // per field the smallest scale of the group's jobs
+    int auto_pairs = 0;
     for (int f = 0; f < kNF; f++) {
       sc.qs[f] = INFINITY;
       sc.iqs[f] = 0.0;
     }
+    for (size_t k = ranges[g].first; k < ranges[g].second; k++)
+      auto_pairs |= jobs[all[k].job].jd.auto_mode ? 1 : 0;
     for (size_t k = ranges[g].first; k < ranges[g].second; k++) {
       const JobPlan &jp = jobs[all[k].job];
-      smem = std::max(smem, fast_smem_bytes(corel, jk, jp.jd.nrp, jp.wpi));
+      smem = std::max(smem, fast_smem_bytes(corel, jk, jp.jd.nrp, jp.wpi, auto_pairs));
       for (int f = 0; f < kNF; f++)
         if (jp.jd.qscale[f] < sc.qs[f]) {
           sc.qs[f] = jp.jd.qscale[f];
@@ -1045,7 +1054,7 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
     const size_t n_units = ranges[g].second - ranges[g].first;
     if (n_units == 0) continue;
     const int grid = (int)std::min<int64_t>((int64_t)c0->sm_count * bps, (int64_t)n_units);
-    gs.push_back(FastGroup{corel, jk, minb, grid, ranges[g].first, n_units, smem, sc});
+    gs.push_back(FastGroup{corel, jk, minb, grid, ranges[g].first, n_units, smem, sc, auto_pairs});
   }
   return launch_fast_body(c0, jobs, gs);
 }
@@ -1423,6 +1432,20 @@ cpc_status sky_upload(cpc_ctx *c, int slot, const cpc_catalog *cat) {
       aflag[k] = (o + 1 < (uint32_t)n && !(cat->z[o + 1] < win[o])) ? kAutoStart0 : 0;
     }
   });
+  // outer-row order of the fast sky kernel: (redshift slab, region, redshift),
+  // so that a chunk of consecutive rows usually lies in one region
+  {
+    const int kSlabs = 16;
+    const int nreg = p.do_jk ? p.n_jk : 1;
+    std::vector<int64_t> start((size_t)kSlabs * nreg + 1, 0);
+    auto key = [&](int64_t k) {
+      return (int64_t)(k * kSlabs / std::max<int64_t>(n, 1)) * nreg + (p.do_jk ? s.hs_jk[k] : 0);
+    };
+    for (int64_t k = 0; k < n; k++) start[key(k) + 1]++;
+    for (size_t q = 1; q < start.size(); q++) start[q] += start[q - 1];
+    s.hs_rorder.assign(n, 0);
+    for (int64_t k = 0; k < n; k++) s.hs_rorder[start[key(k)]++] = (int)k;
+  }
   auto put = [&](DevBuf<double> &d, const std::vector<double> &h, size_t cnt) -> cudaError_t {
     cudaError_t e = d.alloc(std::max<size_t>(cnt, 1));
     if (e != cudaSuccess || cnt == 0) return e;
@@ -1652,11 +1675,12 @@ cpc_status sky_plan(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   J.row_list = nullptr;
   J.n_rows = g1.n;
   const int W = engine == CPC_ENGINE_FAST ? c->n_shards : 1;
-  if (rs > 1 || W > 1) {
+  if (engine == CPC_ENGINE_FAST) {  // the rows in the kernel's order (hs_rorder)
     std::vector<int> rows;
     rows.reserve((size_t)(g1.n / std::max<int64_t>(1, rs) / W + 1));
-    for (int64_t i = W > 1 ? c->shard : 0; i < g1.n; i += W)
-      if (rs <= 1 || ((g1.hs_orig[i] - ro) % rs) == 0) rows.push_back((int)i);
+    for (const int i : g1.hs_rorder)
+      if ((W <= 1 || i % W == c->shard) && (rs <= 1 || ((g1.hs_orig[i] - ro) % rs) == 0))
+        rows.push_back(i);
     CK(Bf.rows.alloc(std::max<size_t>(rows.size(), 1)), "alloc row sample");
     if (!rows.empty())
       CK(cudaMemcpyAsync(Bf.rows.p, rows.data(), sizeof(int) * rows.size(),
@@ -2088,8 +2112,8 @@ std::vector<int> tune_windows(const cpc_params &p, int corel) {
   for (int b = 4; b >= 2; b--) {
     const size_t budget = (size_t)(228 * 1024) / b - static_b - 1024;
     int w = npi;
-    while (w > 1 && fast_smem_bytes(corel, jk, nrp, w) > budget) w--;
-    if (fast_smem_bytes(corel, jk, nrp, w) > budget) continue;
+    while (w > 1 && fast_smem_bytes(corel, jk, nrp, w, 0) > budget) w--;
+    if (fast_smem_bytes(corel, jk, nrp, w, 0) > budget) continue;
     for (int cand : {w, (3 * w + 3) / 4}) {
       if (cand < std::min(npi, 8)) continue;
       if (std::find(ws.begin(), ws.end(), cand) == ws.end()) ws.push_back(cand);

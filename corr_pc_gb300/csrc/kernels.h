@@ -76,7 +76,9 @@ constexpr int kFastBlocksPerSM = 4;  // occupancy target: registers and shared m
 constexpr int kFastMaxCols = 512;
 constexpr int kFastMaxSeg = 256;
 constexpr int kMaxCellsPerRmax = 9;
-size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi);
+// auto_pairs: the launch holds corels1 (auto-pair) jobs, whose rules take
+// another kBatch + 3 kTile ints of shared memory
+size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs);
 size_t fast_static_smem_bytes();
 int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm);
 // Fixed-point scales of one fast-kernel launch (kernel parameters, read from
@@ -91,7 +93,8 @@ struct FastScales {
 cudaError_t launch_fast(int corel, int jk, int minb, const JobDev *jobs, const UnitDesc *units,
                         int n_units, unsigned int *unit_ctr, QEntry *q,
                         unsigned long long *qcount, unsigned long long qcap,
-                        const FastScales &sc, size_t smem, int grid, cudaStream_t st);
+                        const FastScales &sc, size_t smem, int grid, int auto_pairs,
+                        cudaStream_t st);
 cudaError_t launch_recheck(const JobDev *jobs, const QEntry *q, const unsigned long long *qcount,
                            unsigned long long qcap, int grid, cudaStream_t st);
 

@@ -153,9 +153,20 @@ __host__ __device__ __forceinline__ int rep_bin(int r, int n1, int elk, int nrp,
   return nrp * wpi + ((r - 1) * h + (n1 - (nrp - h))) * wpi + elk;
 }
 
+// Dynamic shared memory of the candidate staging: positions, then (for the
+// corels with values) the weighted ellipticities or orientation and the aux
+// view (x lo, y lo, phi, w lo) of each staged candidate.
+__host__ __device__ constexpr size_t stage_bytes(int corel) {
+  return sizeof(float4) * (corel == COREL_DD ? 2 : 3) * kBatch +
+         (corel == COREL_ED ? sizeof(float) * (kBatch + kTile) : 0);  // ED: z lo parts
+}
+// Dynamic shared memory of the corels1 (auto pair) rules, after the staging:
+// each staged candidate's input index and each row's thresholds per z image.
+constexpr size_t kAutoBytes = sizeof(int) * (kBatch + 3 * kTile);
+
 // Shared-memory bytes a block needs for a job with nrp r_p bins and a wpi-bin
 // Pi window.
-size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi) {
+size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs) {
   const int NB = nrp * wpi, NBm = main_bins(nrp, wpi);
   int FM = 1, FJ = 1;
   if (corel == COREL_SD) { FM = 7; FJ = 4; }
@@ -164,7 +175,7 @@ size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi) {
   if (corel == COREL_DK) { FM = 2; FJ = 2; }
   if (corel == COREL_SK) { FM = 4; FJ = 4; }
   if (corel == COREL_ED) { FM = 3; FJ = 2; }
-  size_t b = sizeof(float4) * 2 * kBatch;                // staging
+  size_t b = stage_bytes(corel) + (auto_pairs ? kAutoBytes : 0);  // staging
   b += 8ull * FM * NBm + 4ull * NBm + 4ull * hi_pad(FM * NBm);
   if (do_jk) b += 2 * (8ull * FJ * NB + 4ull * NB + 4ull * hi_pad(FJ * NB));
   return b;
@@ -335,12 +346,22 @@ __global__ void __launch_bounds__(kThreads, MINB)
 fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ units,
                   int n_units, unsigned int *__restrict__ unit_ctr, QEntry *__restrict__ queue,
                   unsigned long long *__restrict__ qcount, unsigned long long qcap,
-                  const __grid_constant__ FastScales sc, int zero_words) {
+                  const __grid_constant__ FastScales sc, int zero_words, int auto_smem) {
   using F = FieldMap<C>;
   extern __shared__ __align__(16) unsigned char smem[];
   float4 *s_pos = reinterpret_cast<float4 *>(smem);
   float4 *s_shp = s_pos + kBatch;
-  unsigned char *hist_base = smem + sizeof(float4) * 2 * kBatch;
+  float4 *s_aux = s_shp + kBatch;  // x lo, y lo, phi, w lo of each staged candidate
+  // ED: z lo parts of the staged candidates and of the tile's rows
+  float *s_zlo = reinterpret_cast<float *>(smem + sizeof(float4) * 3 * kBatch);
+  float *s_rzlo = s_zlo + kBatch;
+  // corels1 rules (launches with auto-pair jobs only): the input index of each
+  // staged candidate; per row and z image (index sz + 1) a threshold on the
+  // partner's input index: -1 every partner (and every pair outside corels1),
+  // the row's own index: partners after it, INT_MAX: none
+  int *s_orig = auto_smem ? reinterpret_cast<int *>(smem + stage_bytes(C)) : nullptr;
+  int *s_rothr = auto_smem ? s_orig + kBatch : nullptr;
+  unsigned char *hist_base = smem + stage_bytes(C) + (auto_smem ? kAutoBytes : 0);
   // the candidate slots of a unit, used only while the staging buffer is idle
   // (between the unit's slot set-up barriers, before any candidate is staged)
   int *s_slot_b = reinterpret_cast<int *>(s_pos);
@@ -352,9 +373,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   __shared__ int s_seg_a[kMaxSeg], s_seg_len[kMaxSeg], s_seg_key[kMaxSeg];
   __shared__ int s_order[kMaxSeg], s_pre[kMaxSeg + 1];
   __shared__ int s_jidx[kBatch];
-  __shared__ int s_orig[kBatch];  // input index of each staged candidate (corels1)
   __shared__ unsigned char s_keep[kBatch];
-  __shared__ float4 s_aux[kBatch];  // x lo, y lo, phi, w lo of each staged candidate
   __shared__ unsigned long long s_red[kThreads / 32];
   __shared__ unsigned s_nbin;  // pairs queued by the block's warps since the last flush
   __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
@@ -362,12 +381,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   // s_rshp / s_shp hold the weighted ellipticities (ewt) for the corels with
   // shape terms and the orientation (shp) for ED
   __shared__ float4 s_rpos[kTile], s_rshp[kTile], s_raux[kTile];
-  __shared__ float s_rzlo[kTile], s_zlo[kBatch];  // z lo parts (ED separations)
   __shared__ unsigned char s_rkeep[kTile];
-  // corels1 rule of each row for each z image sz (index sz + 1), as a threshold
-  // on the partner's input index: -1 every partner (and every pair outside
-  // corels1), the row's own index: partners after it, INT_MAX: none
-  __shared__ int s_rothr[3][kTile];
   __shared__ unsigned s_wq[kThreads / 32][kQCap];
 
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
@@ -446,9 +460,10 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
       // a row that is not counted gets z = NaN: every window test fails
       if (!ok) p.z = __int_as_float(0x7fc00000);
       s_rpos[tr] = p;
-      for (int z = -1; z <= 1; z++)
-        s_rothr[z + 1][tr] = auto_image_all(J.auto_mode, z, af) ? -1
-                             : auto_image_gt(J.auto_mode, z, af) ? oi : INT_MAX;
+      if (auto_smem)
+        for (int z = -1; z <= 1; z++)
+          s_rothr[(z + 1) * kTile + tr] = auto_image_all(J.auto_mode, z, af) ? -1
+                                          : auto_image_gt(J.auto_mode, z, af) ? oi : INT_MAX;
     }
     const float Lf = J.Lf;
     const float xy_in = J.xy_in, xy_out = J.xy_out;
@@ -632,7 +647,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             }
             if (C == COREL_ED && has_lo) s_zlo[t] = J.f2.zlo[j2];
             s_jidx[t] = j2;
-            if (J.auto_mode) s_orig[t] = (int)J.d2.orig[j2];
+            if (auto_smem && J.auto_mode) s_orig[t] = (int)J.d2.orig[j2];
             if (JK) s_keep[t] = J.f2.keep[j2];
           }
           __syncwarp();
@@ -653,7 +668,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     x1s = sx == 1 ? p1.x - Lf : p1.x;                                         \
     y1s = sy == 1 ? p1.y - Lf : p1.y;                                         \
     z1s = sz == 1 ? p1.z - Lf : p1.z;                                         \
-    othr = s_rothr[sz + 1][tr_];                                              \
+    othr = auto_smem ? s_rothr[(sz + 1) * kTile + tr_] : -1;                  \
   }
           CPC_SET_ROW();
           int step = 0;
@@ -969,6 +984,7 @@ struct LaunchFast {
   const FastScales *sc;
   size_t smem;
   int grid;
+  int auto_pairs;
   cudaStream_t st;
   template <int C, bool JK, int MINB>
   cudaError_t run() const {
@@ -976,9 +992,10 @@ struct LaunchFast {
     cudaError_t err =
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    const int zero_words = (int)((smem - sizeof(float4) * 2 * kBatch) / 4);
+    const int zero_words =
+        (int)((smem - stage_bytes(C) - (auto_pairs ? kAutoBytes : 0)) / 4);
     kern<<<grid, kThreads, smem, st>>>(jobs, units, n_units, unit_ctr, q, qcount, qcap, *sc,
-                                       zero_words);
+                                       zero_words, auto_pairs);
     return cudaGetLastError();
   }
 };
@@ -1000,10 +1017,12 @@ struct Occupancy {
 cudaError_t launch_fast(int corel, int jk, int minb, const JobDev *jobs, const UnitDesc *units,
                         int n_units, unsigned int *unit_ctr, QEntry *q,
                         unsigned long long *qcount, unsigned long long qcap,
-                        const FastScales &sc, size_t smem, int grid, cudaStream_t st) {
+                        const FastScales &sc, size_t smem, int grid, int auto_pairs,
+                        cudaStream_t st) {
   if (corel < COREL_DD || corel > COREL_ED) return cudaErrorInvalidValue;
   return dispatch(corel, jk, minb,
-                  LaunchFast{jobs, units, n_units, unit_ctr, q, qcount, qcap, &sc, smem, grid, st});
+                  LaunchFast{jobs, units, n_units, unit_ctr, q, qcount, qcap, &sc, smem, grid,
+                             auto_pairs, st});
 }
 
 // The register-bound variant for this shared-memory size and its blocks per SM:

@@ -41,6 +41,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <climits>
 
 #include "cpc_device.cuh"
 #include "kernels.h"
@@ -417,7 +418,7 @@ sky_warp_kernel(const JobDev *__restrict__ jobs, const long long *__restrict__ c
   __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
   __shared__ float s_qs[kNF];
   __shared__ long long s_chunk;
-  __shared__ int s_rowctr;
+  __shared__ int s_rowctr, s_xmin, s_xmax;
   __shared__ unsigned long long s_red[kSkyWarps];
   const int ncell = jobs[0].nrp * jobs[0].npi;  // one binning for every job of a launch
   unsigned long long *s_num = reinterpret_cast<unsigned long long *>(sky_smem);
@@ -432,25 +433,16 @@ sky_warp_kernel(const JobDev *__restrict__ jobs, const long long *__restrict__ c
     if (threadIdx.x == 0) {
       s_chunk = (long long)atomicAdd(chunk_ctr, 1ull);
       s_rowctr = 0;
+      s_xmin = INT_MAX;
+      s_xmax = INT_MIN;
     }
     __syncthreads();
     const long long ch = s_chunk;
     int k = 0;
     while (k < n_jobs && ch >= chunk0[k + 1]) k++;  // block-uniform
     if (k != cur) {
-      if (cur >= 0) {  // the previous job's block histogram and window count
+      if (cur >= 0) {  // the previous job's window count (its histogram is flushed)
         const JobDev &P = jobs[cur];
-        if (SMEM) {
-          for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
-            const unsigned long long v = s_num[c];
-            if (!v) continue;
-            atomicAdd(&P.acc_num[c], v);
-            for (int f = 0; f < kNF; f++) {
-              const unsigned long long x = s_fix[c * kNF + f];
-              if (x != 0ull) atomicAdd(&P.acc_fix[c * kNF + f], x);
-            }
-          }
-        }
         unsigned long long v = nwin;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
         if (lane == 0 && v) atomicAdd(&P.counters[1], v);
@@ -478,6 +470,22 @@ sky_warp_kernel(const JobDev *__restrict__ jobs, const long long *__restrict__ c
     const float pmin_f = (float)J.pmin, pmax_f = (float)J.pmax;
     int2 *hq = J.hq;
     unsigned long long *hq_n = J.hq_n;
+    // When every outer row of the chunk lies in one jackknife region xreg and is
+    // kept (jk_prob >= 0.5), that region takes every pair the chunk adds to the
+    // block histogram (jk_check_sky, jk.cpp:53-57): it receives the histogram
+    // when the chunk ends, and the rows' pairs skip their own region update.
+    // (The rows are ordered by redshift slab and region, so most chunks are.)
+    int xreg = -1;
+    if (SMEM && J.do_jk) {
+      for (int64_t t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
+        const int64_t ii = J.row_list ? J.row_list[t] : t;
+        const int reg = a.d.keep[ii] ? a.d.jk[ii] : -1;
+        atomicMin(&s_xmin, reg);
+        atomicMax(&s_xmax, reg);
+      }
+      __syncthreads();
+      xreg = (s_xmin == s_xmax && s_xmin >= 0) ? s_xmin : -1;
+    }
   for (;;) {
     int64_t i = 0;
     if (lane == 0) i = r0 + atomicAdd(&s_rowctr, 1);
@@ -491,7 +499,7 @@ sky_warp_kernel(const JobDev *__restrict__ jobs, const long long *__restrict__ c
     SkyRow r;
     r.i = i;
     r.jk = a.d.jk[i];
-    r.keep = a.d.keep[i];
+    r.keep = xreg >= 0 ? 0 : a.d.keep[i];  // xreg: the region takes the chunk's histogram
     const double z_min = a.win[i], z_max = a.win[n1 + i];
     // RA / Dec windows: float bounds rounded both ways here; the exact double
     // bounds are reloaded in the rare undecided case (fewer live registers)
@@ -607,6 +615,27 @@ sky_warp_kernel(const JobDev *__restrict__ jobs, const long long *__restrict__ c
                            s_B, s_PA, s_PB);
     __syncwarp();
   }  // rows of the chunk
+    if (SMEM) {  // the chunk's block histogram into the job's main block (and region xreg)
+      __syncthreads();
+      const int64_t hx = xreg >= 0 ? (int64_t)(1 + xreg) * ncell : -1;
+      const bool regf = J.which_corr != 0 && J.corel != COREL_DD;
+      const bool wf = !J.unit_w;
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+        const unsigned long long v = s_num[c];
+        if (!v) continue;
+        s_num[c] = 0ull;
+        atomicAdd(&J.acc_num[c], v);
+        if (hx >= 0) atomicAdd(&J.acc_num[hx + c], v);
+        for (int f = 0; f < kNF; f++) {
+          const unsigned long long x = s_fix[c * kNF + f];
+          if (x == 0ull) continue;
+          s_fix[c * kNF + f] = 0ull;
+          atomicAdd(&J.acc_fix[c * kNF + f], x);
+          if (hx >= 0 && ((f == 0 && wf) || ((f & 1) && regf)))
+            atomicAdd(&J.acc_fix[(hx + c) * kNF + f], x);
+        }
+      }
+    }
   }  // chunks
 }
 
