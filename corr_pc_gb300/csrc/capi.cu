@@ -151,6 +151,8 @@ struct cpc_ctx {
   DevBuf<QEntry> d_queue;
   DevBuf<unsigned long long> d_qcount;
   unsigned long long qcap = 0;
+  double q_per_unit = 0;  // most pairs any count queued per work unit (queue sizing)
+  size_t last_units = 0;  // work units of the last fast launch
   DevBuf<unsigned long long> d_num;
   DevBuf<double> d_sums;
   DevBuf<unsigned long long> d_counters;
@@ -1022,6 +1024,20 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
   total_units = all.size();
   cpc_status s;
   if ((s = ensure_scratch(c0, std::max<size_t>(1, total_units), jobs.size())) != CPC_OK) return s;
+  // size the edge queue from the rate earlier counts of this context queued
+  // (per unit): a count whose queue overflows is run again, which a full count
+  // after sharded or sampled ones would otherwise pay
+  {
+    const double need = c0->q_per_unit * (double)total_units * 1.25;
+    if (need > (double)c0->qcap && need < 4e9) {
+      unsigned long long cap = c0->qcap;
+      while ((double)cap < need) cap *= 2;
+      c0->d_queue.reset();
+      CK(c0->d_queue.alloc(cap), "alloc edge queue");
+      c0->qcap = cap;
+    }
+  }
+  c0->last_units = total_units;
   std::vector<JobDev> jds(jobs.size());
   for (size_t k = 0; k < jobs.size(); k++) jds[k] = jobs[k].jd;
   CK(cudaMemcpyAsync(c0->d_jobs.p, jds.data(), sizeof(JobDev) * jds.size(), cudaMemcpyHostToDevice, st), "H2D jobs");
@@ -1070,6 +1086,8 @@ cpc_status finish_fast(std::vector<JobPlan> &jobs, int grow_attempt) {
   CK(cudaEventElapsedTime(&pms, c0->e0, c0->e2), "event time");
   unsigned long long qn = 0;
   CK(cudaMemcpy(&qn, c0->d_qcount.p, sizeof qn, cudaMemcpyDeviceToHost), "D2H");
+  if (c0->last_units > 0 && !jobs[0].jd.all_exact)  // (the FP64 comparison queues every pair)
+    c0->q_per_unit = std::max(c0->q_per_unit, (double)qn / (double)c0->last_units);
   if (qn > c0->qcap) {
     // the edge queue overflowed: grow it to hold every queued pair and count
     // again (the queued set does not depend on the order of execution)
