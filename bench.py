@@ -480,7 +480,7 @@ def main() -> None:
     ap.add_argument("--ref-budget", type=float, default=5.0, help="seconds per reference step")
     ap.add_argument("--fp64-budget", type=float, default=3.0,
                     help="seconds of FP64 kernel (0: skip)")
-    ap.add_argument("--cell-fp64-pairs", type=float, default=1e8,
+    ap.add_argument("--cell-fp64-pairs", type=float, default=1e10,
                     help="binned pairs of the cell-list FP64 comparison (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")
@@ -672,23 +672,26 @@ def main() -> None:
     # plain FP64 GPU kernel on a bounded row sample of the same workload
     fp64 = None
     if len(ctxs) == 1 and args.fp64_budget > 0:
+        # at least 4,000 outer rows: the plain kernel runs one thread per row, and
+        # fewer rows leave the GPU idle (on the 20M box 1,000 rows give 1.2e7
+        # pairs/s, 4,000 2.2e7, 16,000 2.7e7)
         est_rate = 1.5e8 if not big else 2e7
-        stride = max(1, int(full_pairs / (est_rate * args.fp64_budget)))
+        n_rows = wls[0].density.n
+        stride = max(1, min(int(full_pairs / (est_rate * args.fp64_budget)), n_rows // 4000))
         r64 = ctxs[0].count("SD", 0, 1, engine="fp64", row_stride=stride)
         fp64 = {"value": r64["n_binned"] / (r64["kernel_ms"] * 1e-3), "unit": UNIT,
                 "sample": f"every {stride}-th outer row: {r64['n_binned']} binned pairs in "
                           f"{r64['kernel_ms']:.1f} ms"}
         fp64["speedup_of_fast"] = value / fp64["value"]
     # the same cell list and work units with every window candidate evaluated by
-    # the FP64 path (the edge queue and its recheck kernel): the precision
-    # comparison at equal algorithm, on one shard of the work queue sized for
-    # about args.cell_fp64_pairs binned pairs, against the fast engine on the
-    # same shard
+    # the FP64 path (the reference's double arithmetic, global atomics): the
+    # precision comparison at equal algorithm, on one shard of the work queue
+    # sized for about args.cell_fp64_pairs binned pairs, against the fast engine
+    # on the same shard
     cell64 = None
     if len(ctxs) == 1 and args.cell_fp64_pairs > 0:
         K = max(1, int(full_pairs / args.cell_fp64_pairs))
         ctxs[0].set_shard(0, K)
-        ctxs[0].count("SD", 0, 1, engine="cell_fp64")  # sizes the edge queue
         rc = ctxs[0].count("SD", 0, 1, engine="cell_fp64")
         rfs = ctxs[0].count("SD", 0, 1)
         ctxs[0].set_shard(0, 1)

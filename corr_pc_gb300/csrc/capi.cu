@@ -1065,7 +1065,8 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
         }
     }
     int bps = 0;
-    const int minb = fast_variant(corel, jk, smem, &bps);
+    const int minb = fast_variant(corel, jk, smem, &bps,
+                                  jobs[all[ranges[g].first].job].jd.all_exact);
     if (bps <= 0) return fail(c, CPC_ERR_INVALID, "fast kernel does not fit on an SM with these bins");
     const size_t n_units = ranges[g].second - ranges[g].first;
     if (n_units == 0) continue;
@@ -2163,7 +2164,7 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
   cpc_accum acc{};
   acc.num = num.data();
   acc.sums = sums.data();
-  const int ks[3] = {2, 3, 4};
+  const int ks[5] = {2, 3, 4, 5, 6};
   std::vector<int> ws;
   {
     JobRule rule;
@@ -2276,7 +2277,7 @@ cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_k
   };
   double best = INFINITY;
   int bk = ctxs[0]->slots[slots_g1[0]].kcells, bw = ctxs[0]->tune_wpi;
-  for (int kc : {2, 3, 4}) {
+  for (int kc : {2, 3, 4, 5, 6}) {
     cpc_status s = regrid(kc);
     if (s != CPC_OK) return s;
     for (int w : ws) {

@@ -80,7 +80,9 @@ constexpr int kMaxCellsPerRmax = 9;
 // another kBatch + 3 kTile ints of shared memory
 size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs);
 size_t fast_static_smem_bytes();
-int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm);
+// minb 4 or 3: the register bound (blocks per SM) of the fast kernel; 1: the
+// cell-list FP64 comparison engine (all_exact jobs)
+int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm, int all_exact);
 // Fixed-point scales of one fast-kernel launch (kernel parameters, read from
 // the constant bank): field f's terms are rint(v qs[f]), summed back with
 // iqs[f] = 1 / qs[f].  A launch over several jobs takes, per field, the smallest

@@ -342,7 +342,7 @@ constexpr unsigned kEdgeFlag = 0x8000u;  // queue entry: near the window edge
 // MINB: blocks per SM the registers are bounded for (4 when the job's
 // histograms fit a quarter of shared memory, else 3)
 template <int C, bool JK, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB)
+__global__ void __launch_bounds__(kThreads, MINB == 1 ? 2 : MINB)
 fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ units,
                   int n_units, unsigned int *__restrict__ unit_ctr, QEntry *__restrict__ queue,
                   unsigned long long *__restrict__ qcount, unsigned long long qcap,
@@ -428,7 +428,10 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     constexpr bool kTheta = C == COREL_SD || C == COREL_SS || C == COREL_SSA || C == COREL_SK;
     const bool has_lo = (kTheta || C == COREL_ED) && J.has_lo;
     const int rmu = J.rmu;
-    const bool all_exact = J.all_exact != 0;  // the cell-list FP64 comparison engine
+    // MINB == 1: the cell-list FP64 comparison engine (CPC_ENGINE_CELL_FP64): every
+    // candidate inside the outer window bounds is evaluated by the FP64 path,
+    // inline, with global atomics (no FP32 value, no shared histogram)
+    constexpr bool all_exact = MINB == 1;
     // jackknife attribution: jk_check_PB (the box's rule; this kernel runs box
     // jobs only)
     const int gws = J.gws, lin_bin = J.lin_bin;
@@ -806,6 +809,20 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               }
               if (!own) {
                 // another mu slice's pair
+              } else if (all_exact) {
+                // the comparison engine: the reference's double arithmetic for
+                // every candidate (window, bins, values), global FP64 atomics
+                const int64_t gi1 = (int64_t)U.g1_start +
+                                    (int64_t)(((er & 31) * W) + (er >> 5)) * U.g1_stride;
+                const int64_t gj2 = s_jidx[ec];
+                int xn1, xn2;
+                const int r = exact_classify(J, J.d1, gi1, J.d2, gj2, sx, sy, sz, xn1, xn2);
+                if (r >= 1) nwin++;
+                if (r == 2) {
+                  double f[kNF];
+                  exact_values(J, J.d1, gi1, J.d2, gj2, sx, sy, sz, f);
+                  exact_accumulate(J, J.d1, gi1, J.d2, gj2, xn1, xn2, f);
+                }
               } else if (amb || edge) {
                 // near the window edge (not yet counted) or a bin edge (window
                 // counted): exact FP64 evaluation
@@ -960,8 +977,10 @@ template <class Fn>
 static auto dispatch(int corel, int jk, int minb, const Fn &fn) -> decltype(fn.template run<0, false, 3>()) {
 #define CPC_CASE(CC)                                                                  \
   if (corel == CC) {                                                                  \
-    if (jk) return minb == 4 ? fn.template run<CC, true, 4>() : fn.template run<CC, true, 3>(); \
-    return minb == 4 ? fn.template run<CC, false, 4>() : fn.template run<CC, false, 3>();       \
+    if (jk) return minb == 4 ? fn.template run<CC, true, 4>()                        \
+                  : minb == 1 ? fn.template run<CC, true, 1>() : fn.template run<CC, true, 3>(); \
+    return minb == 4 ? fn.template run<CC, false, 4>()                                \
+           : minb == 1 ? fn.template run<CC, false, 1>() : fn.template run<CC, false, 3>();      \
   }
   CPC_CASE(COREL_DD)
   CPC_CASE(COREL_SD)
@@ -1027,8 +1046,12 @@ cudaError_t launch_fast(int corel, int jk, int minb, const JobDev *jobs, const U
 
 // The register-bound variant for this shared-memory size and its blocks per SM:
 // the 4-block variant when 4 blocks fit, else the 3-block one.
-int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm) {
+int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm, int all_exact) {
   if (corel < COREL_DD || corel > COREL_ED) { *blocks_per_sm = 0; return 3; }
+  if (all_exact) {  // the cell-list FP64 comparison engine
+    *blocks_per_sm = dispatch(corel, jk, 1, Occupancy{smem});
+    return 1;
+  }
   const int b4 = dispatch(corel, jk, 4, Occupancy{smem});
   if (b4 >= 4) { *blocks_per_sm = b4; return 4; }
   *blocks_per_sm = dispatch(corel, jk, 3, Occupancy{smem});

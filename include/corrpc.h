@@ -209,7 +209,7 @@ cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind
 cpc_status cpc_set_tuning(cpc_ctx *ctx, int cells_per_rmax, int pi_window, int tile);
 
 /* Autotuner: times the fast kernel on every `sample_stride`-th outer row of
- * this pair type for cell widths r_max / k (k = 2, 3, 4; the cell lists are
+ * this pair type for cell widths r_max / k (k = 2 .. 6; the cell lists are
  * rebuilt on the device) and block-local Pi windows (for 4, 3 and 2 blocks per
  * SM, the largest window that fits and three quarters of it), keeps the
  * fastest for this context (as cpc_set_tuning would) and returns it.  Results
