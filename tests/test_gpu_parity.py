@@ -142,7 +142,7 @@ def test_autotune_keeps_results_identical():
     ctx.upload(0, cats["D"])
     ctx.upload(1, cats["S"])
     k, w = ctx.autotune("SD", 0, 1, sample_stride=2)
-    assert k in (2, 3, 4) and 0 <= w <= p.n_p_bin
+    assert k in (2, 3, 4, 5, 6) and 0 <= w <= p.n_p_bin
     r = ctx.count("SD", 0, 1)
     assert r["n_binned"] == g.n_in and r["n_window"] == g.n_total
     assert np.array_equal(r["num"], g.raw_num)
