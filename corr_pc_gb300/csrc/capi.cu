@@ -1650,8 +1650,8 @@ cpc_status sky_plan(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
     }
   }
   // fixed-point scales of the fast kernel: terms rint(v 2^S_f),
-  // |v| 2^S_f <= 2^30 / (1 + 2^-12) (64-bit integer sums: 2^33 terms per bin
-  // before any overflow, checked after the count)
+  // |v| 2^S_f <= 2^30 / (1 + 2^-12); the global sums keep a low and a high
+  // 64-bit word per bin and field (2^48 terms per bin, checked after the count)
   {
     const double wm = std::max(g1.wmax, 1e-30) * std::max(g2.wmax, 1e-30);
     const double em = std::max({g1.emax, g2.emax, 1e-30});
@@ -1675,9 +1675,10 @@ cpc_status sky_plan(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
     J.unit_w = (engine == CPC_ENGINE_FAST && g1.wmax == 1.0 && g1.wmin == 1.0 &&
                 g2.wmax == 1.0 && g2.wmin == 1.0) ? 1 : 0;
   }
-  CK(Bf.fix.alloc(P.n_fix), "alloc fixed-point sums");
-  CK(cudaMemsetAsync(Bf.fix.p, 0, sizeof(unsigned long long) * P.n_fix, st), "memset");
+  CK(Bf.fix.alloc(2 * P.n_fix), "alloc fixed-point sums");  // low words, then high words
+  CK(cudaMemsetAsync(Bf.fix.p, 0, sizeof(unsigned long long) * 2 * P.n_fix, st), "memset");
   J.acc_fix = Bf.fix.p;
+  J.acc_fixh = Bf.fix.p + P.n_fix;
   J.sky1 = sky_view(g1);
   J.sky2 = sky_view(g2);
   J.sf1 = sky_fast(g1);
@@ -1724,11 +1725,11 @@ cpc_status sky_finish(cpc_ctx *c, SkyPlan &P, size_t k, cpc_engine engine, float
   out->kernel_ms = out->pair_kernel_ms = ms;
   if (P.empty) return CPC_OK;
   if (engine != CPC_ENGINE_FP64) {
-    // the 64-bit fixed-point words hold 2^33 terms of |u| < 2^30 per bin
+    // the low and high fixed-point words hold 2^48 terms of |u| < 2^30 per bin
     for (size_t q = 0; q < P.cells; q++)
-      if ((unsigned long long)out->num[q] >= (1ull << 33))
+      if ((unsigned long long)out->num[q] >= (1ull << 48))
         return fail(c, CPC_ERR_RANGE,
-                    "a sky bin holds 2^33 pairs or more: its fixed-point sums may overflow; "
+                    "a sky bin holds 2^48 pairs or more: its fixed-point sums may overflow; "
                     "count the term in row samples (row_stride)");
   }
   unsigned long long nq = 0;
@@ -1827,8 +1828,8 @@ cpc_status sky_run(cpc_ctx *c, std::vector<SkyPlan> &plans, cpc_engine engine) {
       c->launches += 1;
       for (size_t m = 0; m < jd.size(); m++) {
         const SkyPlan &P = plans[idx[m]];
-        CK(launch_fix_to_sums((int64_t)P.n_fix, jd[m].acc_fix, jd[m].acc_sums, c->d_jobs.p + m,
-                              st), "fixed-point sums");
+        CK(launch_fix_to_sums((int64_t)P.n_fix, jd[m].acc_fix, jd[m].acc_fixh, jd[m].acc_sums,
+                              c->d_jobs.p + m, st), "fixed-point sums");
         c->launches += 1;
       }
     }

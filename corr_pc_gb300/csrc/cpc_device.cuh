@@ -126,7 +126,9 @@ struct JobDev {
   unsigned long long *acc_num;         // [n_hist][nrp][npi]
   double *acc_sums;                    // [n_hist][nrp][npi][kNF]
   unsigned long long *counters;        // [0] window (fast), [1] window (recheck), [2] rechecked
-  unsigned long long *acc_fix;         // sky fast path: fixed-point sums, layout of acc_sums
+  // sky fast path: fixed-point sums in the layout of acc_sums, each as a low
+  // word (sum of the terms' low 15 bits) and a high word (sum of term >> 15)
+  unsigned long long *acc_fix, *acc_fixh;
   SkyView sky1, sky2;                  // sky catalogues g1, g2 (FP64 path of the fast kernel)
   SkyFast sf1, sf2;                    // their float views (fast sky kernel)
   const int *row_list;                 // sky row sample: the g1 rows counted, else null

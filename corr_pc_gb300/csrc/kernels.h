@@ -117,8 +117,9 @@ cudaError_t launch_sky_warp(const JobDev *jobs, const long long *chunk0, int n_j
                             unsigned long long *chunk_ctr, unsigned long long hq_cap, double esum,
                             float rp_lo_f, float rp_hi_f, int zero_bin, int nrp, int npi,
                             int sm_count, int blocks_per_sm, cudaStream_t st);
-cudaError_t launch_fix_to_sums(int64_t n, const unsigned long long *fix, double *sums,
-                               const JobDev *job, cudaStream_t st);
+cudaError_t launch_fix_to_sums(int64_t n, const unsigned long long *lo,
+                               const unsigned long long *hi, double *sums, const JobDev *job,
+                               cudaStream_t st);
 cudaError_t launch_sky_fp64(const JobDev *job, const SkyView &a, const SkyView &b, int2 *hq,
                             unsigned long long *hq_n, unsigned long long hq_cap, double esum,
                             cudaStream_t st);

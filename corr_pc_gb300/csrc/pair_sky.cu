@@ -182,6 +182,20 @@ __device__ __forceinline__ void sky_accumulate_exact(const JobDev &J, int r1, in
 }
 
 // Terms of a pair from the mixed-precision path as fixed-point integers
+// Add x (a term rint(v 2^S_f), or a block's partial sum of terms) to the
+// global fixed-point sum of one bin and field: its low 15 bits (0 .. 2^15 - 1)
+// into word lo, its arithmetic shift x >> 15 into word hi.  Terms have
+// |x| < 2^30 and a block's partial sum holds fewer than 2^33 of them, so a bin
+// takes 2^48 terms before either word can overflow; the value is
+// hi 2^15 + lo (fix_to_sums_kernel).
+__device__ __forceinline__ void fix_add(unsigned long long *lo, unsigned long long *hi,
+                                        long long x) {
+  const unsigned long long l = (unsigned long long)x & 0x7FFFull;
+  const long long h = x >> 15;
+  if (l) atomicAdd(lo, l);
+  if (h) atomicAdd(hi, (unsigned long long)h);
+}
+
 // rint(v 2^S_f), |v| 2^S_f < 2^30 (S_f from bounds on |v|): the fields whose
 // sums cancel from double-float terms vd, the others from float terms v; added
 // as 64-bit integers: the main histogram in shared memory (SMEM) or in the
@@ -196,15 +210,18 @@ __device__ __forceinline__ void sky_accumulate_fixed(const JobDev &J, int r1, in
   const int f0 = J.unit_w ? 1 : 0;
   const int corel = J.corel;
   auto fx = [&](int q) {
-    const int u = df_field(corel, q) ? df_to_int(vd[q], s_qs[q]) : __float2int_rn(v[q] * s_qs[q]);
-    return (unsigned long long)(long long)u;
+    return (long long)(df_field(corel, q) ? df_to_int(vd[q], s_qs[q])
+                                          : __float2int_rn(v[q] * s_qs[q]));
   };
   auto nz = [&](int q) { return df_field(corel, q) ? vd[q].h != 0.0f : v[q] != 0.0f; };
-  unsigned long long *mfix = SMEM ? s_fix : J.acc_fix;
   atomicAdd(SMEM ? &s_num[cell] : &J.acc_num[cell], 1ull);
 #pragma unroll
-  for (int q = 0; q < kNF; q++)  // constant indices: v stays in registers
-    if (q >= f0 && q < nf && nz(q)) atomicAdd(&mfix[cell * kNF + q], fx(q));
+  for (int q = 0; q < kNF; q++) {  // constant indices: v stays in registers
+    if (q < f0 || q >= nf || !nz(q)) continue;
+    const int64_t o = cell * kNF + q;
+    if (SMEM) atomicAdd(&s_fix[o], (unsigned long long)fx(q));
+    else fix_add(&J.acc_fix[o], &J.acc_fixh[o], fx(q));
+  }
   if (!J.do_jk) return;
   const int64_t hstride = (int64_t)J.nrp * J.npi;
   int rs[2];
@@ -212,12 +229,12 @@ __device__ __forceinline__ void sky_accumulate_fixed(const JobDev &J, int r1, in
   for (int t = 0; t < nr; t++) {
     const int64_t hc = (int64_t)(1 + rs[t]) * hstride + cell;
     atomicAdd(&J.acc_num[hc], 1ull);
-    unsigned long long *sj = J.acc_fix + hc * kNF;
-    if (f0 == 0 && v[0] != 0.0f) atomicAdd(&sj[0], fx(0));
+    unsigned long long *sj = J.acc_fix + hc * kNF, *sh = J.acc_fixh + hc * kNF;
+    if (f0 == 0 && v[0] != 0.0f) fix_add(&sj[0], &sh[0], fx(0));
     if (J.which_corr == 0 || nf == 1) continue;
 #pragma unroll
     for (int q = 1; q < kNF; q += 2)
-      if (nz(q)) atomicAdd(&sj[q], fx(q));
+      if (nz(q)) fix_add(&sj[q], &sh[q], fx(q));
   }
 }
 
@@ -627,12 +644,13 @@ sky_warp_kernel(const JobDev *__restrict__ jobs, const long long *__restrict__ c
         atomicAdd(&J.acc_num[c], v);
         if (hx >= 0) atomicAdd(&J.acc_num[hx + c], v);
         for (int f = 0; f < kNF; f++) {
-          const unsigned long long x = s_fix[c * kNF + f];
-          if (x == 0ull) continue;
+          const long long x = (long long)s_fix[c * kNF + f];
+          if (x == 0) continue;
           s_fix[c * kNF + f] = 0ull;
-          atomicAdd(&J.acc_fix[c * kNF + f], x);
+          const int64_t o = c * kNF + f, ox = (hx + c) * kNF + f;
+          fix_add(&J.acc_fix[o], &J.acc_fixh[o], x);
           if (hx >= 0 && ((f == 0 && wf) || ((f & 1) && regf)))
-            atomicAdd(&J.acc_fix[(hx + c) * kNF + f], x);
+            fix_add(&J.acc_fix[ox], &J.acc_fixh[ox], x);
         }
       }
     }
@@ -643,22 +661,27 @@ size_t sky_warp_smem_bytes(int nrp, int npi) {
   return (size_t)nrp * npi * (1 + kNF) * sizeof(unsigned long long);
 }
 
-// fixed-point block -> FP64 sums: sums[i] += fix[i] 2^-S_f, f = i mod kNF
-__global__ void fix_to_sums_kernel(int64_t n, const unsigned long long *__restrict__ fix,
+// fixed-point block -> FP64 sums: sums[i] += (hi[i] 2^15 + lo[i]) 2^-S_f,
+// f = i mod kNF (fix_add)
+__global__ void fix_to_sums_kernel(int64_t n, const unsigned long long *__restrict__ lo,
+                                   const unsigned long long *__restrict__ hi,
                                    double *__restrict__ sums, const JobDev *__restrict__ jobp) {
   const JobDev &J = *jobp;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const long long v = (long long)fix[i];
-    if (v != 0) sums[i] += (double)v * J.inv_qscale[i % kNF];
+    const unsigned long long l = lo[i];
+    const long long h = (long long)hi[i];
+    if (l != 0 || h != 0)
+      sums[i] += fma((double)h, 32768.0, (double)l) * J.inv_qscale[i % kNF];
   }
 }
 
-cudaError_t launch_fix_to_sums(int64_t n, const unsigned long long *fix, double *sums,
-                               const JobDev *job, cudaStream_t st) {
+cudaError_t launch_fix_to_sums(int64_t n, const unsigned long long *lo,
+                               const unsigned long long *hi, double *sums, const JobDev *job,
+                               cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4096);
-  fix_to_sums_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, fix, sums, job);
+  fix_to_sums_kernel<<<(unsigned)blocks, 256, 0, st>>>(n, lo, hi, sums, job);
   return cudaGetLastError();
 }
 
