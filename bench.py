@@ -532,7 +532,8 @@ def main() -> None:
     if len(ctxs) == 1 and not args.no_tune and not args.tune:  # outside the timed region
         n_rows = wls[0].density.n
         k, w = ctxs[0].autotune("SD", 0, 1, sample_stride=max(1, n_rows // 25000))
-        tuning = {"cells_per_rmax": k, "pi_window": w, "by": "cpc_autotune on a row sample"}
+        tuning = {"cells_per_rmax": k, "pi_window": w if w else "automatic (every mu bin that fits)",
+                  "by": "cpc_autotune on a row sample"}
     elif len(ctxs) > 1 and not args.no_tune and not args.tune:
         k, w = _lib.autotune_batch([(c, "SD", 0, 1) for c in ctxs])
         tuning = {"cells_per_rmax": k, "pi_window": w,

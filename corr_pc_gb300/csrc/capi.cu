@@ -2124,9 +2124,12 @@ cpc_status cpc_count_auto(cpc_ctx *c, cpc_pair_kind kind, int slot, cpc_engine e
 }
 
 // Pi windows the autotuner tries: for 4, 3 and 2 blocks per SM the largest
-// window whose histograms fit, and three quarters of it (more, narrower units)
+// window whose histograms fit, and three quarters of it (more, narrower units).
+// With coordinates 7 the mu window is automatic (every mu bin when they fit):
+// only the cell width is tuned.
 std::vector<int> tune_windows(const cpc_params &p, int corel) {
   std::vector<int> ws;
+  if (p.coordinates == 7) return {0};
   const int jk = p.do_jk ? 1 : 0, nrp = p.n_bins, npi = p.n_p_bin;
   const size_t static_b = fast_static_smem_bytes();
   for (int b = 4; b >= 2; b--) {
@@ -2153,7 +2156,7 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
     return fail(c, CPC_ERR_INVALID, "slot out of range");
   if (!c->slots[slot_g1].valid || !c->slots[slot_g2].valid)
     return fail(c, CPC_ERR_STATE, "autotune before upload");
-  if (p.coordinates != 6) {  // the sky kernel has no cell or window knobs
+  if (c->slots[slot_g1].sky) {  // the sky kernel has no cell or window knobs
     if (cells_per_rmax) *cells_per_rmax = 0;
     if (pi_window) *pi_window = 0;
     return CPC_OK;
@@ -2239,8 +2242,9 @@ cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_k
       return fail(ctxs[k], CPC_ERR_INVALID, "slot out of range");
     if (!c->slots[slots_g1[k]].valid || !c->slots[slots_g2[k]].valid)
       return fail(ctxs[k], CPC_ERR_STATE, "autotune before upload");
-    if (c->p.coordinates != 6 || c->p.n_bins != ctxs[0]->p.n_bins ||
-        c->p.n_p_bin != ctxs[0]->p.n_p_bin || c->p.which_corr != ctxs[0]->p.which_corr)
+    if (c->slots[slots_g1[k]].sky || c->p.coordinates != ctxs[0]->p.coordinates ||
+        c->p.n_bins != ctxs[0]->p.n_bins || c->p.n_p_bin != ctxs[0]->p.n_p_bin ||
+        c->p.which_corr != ctxs[0]->p.which_corr)
       return fail(ctxs[k], CPC_ERR_INVALID,
                   "batch autotuning needs box jobs with one binning and which_corr");
   }

@@ -213,7 +213,9 @@ cpc_status cpc_set_tuning(cpc_ctx *ctx, int cells_per_rmax, int pi_window, int t
  * rebuilt on the device) and block-local Pi windows (for 4, 3 and 2 blocks per
  * SM, the largest window that fits and three quarters of it), keeps the
  * fastest for this context (as cpc_set_tuning would) and returns it.  Results
- * never depend on the choice.  Box runs only (sky runs return zeros). */
+ * never depend on the choice.  With coordinates 7 (r-mu) only the cell width is
+ * tuned and pi_window returns 0 (the mu window stays automatic).  Box runs only
+ * (sky runs return zeros). */
 cpc_status cpc_autotune(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_g2,
                         int64_t sample_stride, int *cells_per_rmax, int *pi_window);
 

@@ -154,6 +154,24 @@ def test_autotune_keeps_results_identical():
     ctx.close()
 
 
+def test_autotune_rmu_tunes_cells_only():
+    """r-mu binning (coordinates 7): the autotuner picks a cell width and
+    leaves the mu window automatic (0); the counts stay the reference's."""
+    g = Golden("box_ed_rmu")
+    p = g.params
+    cats = host.prepare(p, [("S", g.S), ("D", g.D)])
+    ctx = _lib.Context(p)
+    ctx.upload(0, cats["D"])
+    ctx.upload(1, cats["S"])
+    k, w = ctx.autotune("SD", 0, 1, sample_stride=2)
+    assert k in (2, 3, 4, 5, 6) and w == 0
+    r = ctx.count("SD", 0, 1)
+    assert r["n_binned"] == g.n_in and r["n_window"] == g.n_total
+    assert np.array_equal(r["num"], g.raw_num)
+    check_sums(r["sums"], g.raw_sums)
+    ctx.close()
+
+
 @pytest.mark.parametrize("engine", ["fast", "fp64"])
 def test_async_count_on_a_caller_stream(engine):
     """cpc_count_async after work queued on a caller stream equals cpc_count;
