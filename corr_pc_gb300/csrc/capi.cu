@@ -401,6 +401,12 @@ struct JobPlan {
   bool empty;
 };
 
+// every weight of both catalogues is 1: the weight sum is the count (the fast
+// kernel keeps no words for it)
+int unit_weights(const Slot &a, const Slot &b) {
+  return (a.wmax == 1.0 && a.wmin == 1.0 && b.wmax == 1.0 && b.wmin == 1.0) ? 1 : 0;
+}
+
 cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, int64_t rs,
                     int64_t ro, cpc_accum *out, JobPlan &jp, int auto_mode = 0) {
   if (slot_g1 < 0 || slot_g1 >= kMaxSlots || slot_g2 < 0 || slot_g2 >= kMaxSlots)
@@ -434,7 +440,8 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   auto fit = [&](int blocks) {
     const size_t budget = (size_t)(228 * 1024) / blocks - static_b - 1024;
     int w = npi;
-    while (w > (rmu ? 1 : 8) && fast_smem_bytes(jp.rule.corel, jk, nrp, w, auto_mode) > budget)
+    while (w > (rmu ? 1 : 8) &&
+           fast_smem_bytes(jp.rule.corel, jk, nrp, w, auto_mode, unit_weights(g1, g2)) > budget)
       w--;
     return w;
   };
@@ -572,7 +579,7 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
     }
   }
   J.qbias = 1 << 29;
-  J.unit_w = (g1.wmax == 1.0 && g1.wmin == 1.0 && g2.wmax == 1.0 && g2.wmin == 1.0) ? 1 : 0;
+  J.unit_w = unit_weights(g1, g2);
   return CPC_OK;
 }
 
@@ -609,6 +616,11 @@ const std::vector<UnitDesc> &build_units(JobPlan &jp) {
     if (wpi < npi) Emax = std::min(Emax, (wpi - 6) * ps / 2.0);
     Emax = std::max(Emax, std::min(2.0 * ps, 0.25 * (p.p_max - p.p_min)));
   }
+  // sparse buckets: a chunk of extent Emax may hold fewer rows than a warp has
+  // lanes (the other lanes then test rows that do not exist); such a chunk grows
+  // up to Ehi, the widest extent whose units still fit the window
+  // ((wpi - 4) ps - extent >= ps), until it holds 32 rows
+  const double Ehi = (!rmu && wpi < npi) ? std::max(Emax, (wpi - 5) * ps) : Emax;
   const int ncx = g1.ncx, ncy = g1.ncy;
   const double inv_cwx = 1.0 / g1.cw_x, inv_cwy = 1.0 / g1.cw_y;
   std::vector<UnitDesc> &units = uc.units;
@@ -627,7 +639,8 @@ const std::vector<UnitDesc> &build_units(JobPlan &jp) {
         const float z0 = g1.h_pos[i].z;
         int j = i;
         float bx0 = INFINITY, bx1 = -INFINITY, by0 = INFINITY, by1 = -INFINITY;
-        while (j < e && (double)g1.h_pos[j].z - z0 <= Emax) {
+        while (j < e && ((double)g1.h_pos[j].z - z0 <= Emax ||
+                         (j - i < 32 && (double)g1.h_pos[j].z - z0 <= Ehi))) {
           bx0 = std::min(bx0, g1.h_pos[j].x);
           bx1 = std::max(bx1, g1.h_pos[j].x);
           by0 = std::min(by0, g1.h_pos[j].y);
@@ -1057,7 +1070,8 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
       auto_pairs |= jobs[all[k].job].jd.auto_mode ? 1 : 0;
     for (size_t k = ranges[g].first; k < ranges[g].second; k++) {
       const JobPlan &jp = jobs[all[k].job];
-      smem = std::max(smem, fast_smem_bytes(corel, jk, jp.jd.nrp, jp.wpi, auto_pairs));
+      smem = std::max(smem,
+                      fast_smem_bytes(corel, jk, jp.jd.nrp, jp.wpi, auto_pairs, jp.jd.unit_w));
       for (int f = 0; f < kNF; f++)
         if (jp.jd.qscale[f] < sc.qs[f]) {
           sc.qs[f] = jp.jd.qscale[f];
@@ -2127,7 +2141,7 @@ cpc_status cpc_count_auto(cpc_ctx *c, cpc_pair_kind kind, int slot, cpc_engine e
 // window whose histograms fit, and three quarters of it (more, narrower units).
 // With coordinates 7 the mu window is automatic (every mu bin when they fit):
 // only the cell width is tuned.
-std::vector<int> tune_windows(const cpc_params &p, int corel) {
+std::vector<int> tune_windows(const cpc_params &p, int corel, int unit_w) {
   std::vector<int> ws;
   if (p.coordinates == 7) return {0};
   const int jk = p.do_jk ? 1 : 0, nrp = p.n_bins, npi = p.n_p_bin;
@@ -2135,8 +2149,8 @@ std::vector<int> tune_windows(const cpc_params &p, int corel) {
   for (int b = 4; b >= 2; b--) {
     const size_t budget = (size_t)(228 * 1024) / b - static_b - 1024;
     int w = npi;
-    while (w > 1 && fast_smem_bytes(corel, jk, nrp, w, 0) > budget) w--;
-    if (fast_smem_bytes(corel, jk, nrp, w, 0) > budget) continue;
+    while (w > 1 && fast_smem_bytes(corel, jk, nrp, w, 0, unit_w) > budget) w--;
+    if (fast_smem_bytes(corel, jk, nrp, w, 0, unit_w) > budget) continue;
     for (int cand : {w, (3 * w + 3) / 4}) {
       if (cand < std::min(npi, 8)) continue;
       if (std::find(ws.begin(), ws.end(), cand) == ws.end()) ws.push_back(cand);
@@ -2174,7 +2188,7 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
     JobRule rule;
     if (job_rule(p, kind, c->slots[slot_g1].n, c->slots[slot_g2].n, rule) != 0)
       return fail(c, CPC_ERR_INVALID, "bad pair kind");
-    ws = tune_windows(p, rule.corel);
+    ws = tune_windows(p, rule.corel, unit_weights(c->slots[slot_g1], c->slots[slot_g2]));
   }
   const int64_t stride = std::max<int64_t>(1, sample_stride);
   double best = INFINITY;
@@ -2254,7 +2268,10 @@ cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_k
     if (job_rule(c0->p, kinds[0], c0->slots[slots_g1[0]].n, c0->slots[slots_g2[0]].n, rule) != 0)
       return fail(ctxs[0], CPC_ERR_INVALID, "bad pair kind");
   }
-  const std::vector<int> ws = tune_windows(ctxs[0]->p, rule.corel);
+  int unit_w = 1;
+  for (int k = 0; k < n_jobs; k++)
+    unit_w &= unit_weights(ctxs[k]->slots[slots_g1[k]], ctxs[k]->slots[slots_g2[k]]);
+  const std::vector<int> ws = tune_windows(ctxs[0]->p, rule.corel, unit_w);
   std::vector<std::vector<int64_t>> nums(n_jobs);
   std::vector<std::vector<double>> sums(n_jobs);
   std::vector<cpc_accum> accs(n_jobs);

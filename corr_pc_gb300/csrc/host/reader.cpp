@@ -50,6 +50,10 @@ bool parse_span(const char *b, const char *e, std::vector<T> &out) {
     while (p < e && is_ws(*p)) p++;
     if (p >= e) return false;
     const char *q = *p == '+' ? p + 1 : p;
+    // istream >> double reads no "inf" or "nan" (from_chars would): a letter
+    // where the digits start ends the numbers
+    const char *d = (q < e && *q == '-') ? q + 1 : q;
+    if (d < e && ((*d >= 'a' && *d <= 'z') || (*d >= 'A' && *d <= 'Z'))) return true;
     T v;
     const auto r = std::from_chars(q, e, v);
     if (r.ec != std::errc()) return true;

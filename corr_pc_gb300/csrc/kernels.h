@@ -78,7 +78,7 @@ constexpr int kFastMaxSeg = 256;
 constexpr int kMaxCellsPerRmax = 9;
 // auto_pairs: the launch holds corels1 (auto-pair) jobs, whose rules take
 // another kBatch + 3 kTile ints of shared memory
-size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs);
+size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs, int unit_w);
 size_t fast_static_smem_bytes();
 // minb 4 or 3: the register bound (blocks per SM) of the fast kernel; 1: the
 // cell-list FP64 comparison engine (all_exact jobs)

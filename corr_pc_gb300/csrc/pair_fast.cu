@@ -165,8 +165,9 @@ __host__ __device__ constexpr size_t stage_bytes(int corel) {
 constexpr size_t kAutoBytes = sizeof(int) * (kBatch + 3 * kTile);
 
 // Shared-memory bytes a block needs for a job with nrp r_p bins and a wpi-bin
-// Pi window.
-size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs) {
+// Pi window.  With unit weights (unit_w) field 0 (the weight sum, equal to the
+// count) is not accumulated and has no words.
+size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs, int unit_w) {
   const int NB = nrp * wpi, NBm = main_bins(nrp, wpi);
   int FM = 1, FJ = 1;
   if (corel == COREL_SD) { FM = 7; FJ = 4; }
@@ -175,6 +176,9 @@ size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs) {
   if (corel == COREL_DK) { FM = 2; FJ = 2; }
   if (corel == COREL_SK) { FM = 4; FJ = 4; }
   if (corel == COREL_ED) { FM = 3; FJ = 2; }
+  const int f0 = unit_w ? 1 : 0;
+  FM -= f0;
+  FJ -= f0;
   size_t b = stage_bytes(corel) + (auto_pairs ? kAutoBytes : 0);  // staging
   b += 8ull * FM * NBm + 4ull * NBm + 4ull * hi_pad(FM * NBm);
   if (do_jk) b += 2 * (8ull * FJ * NB + 4ull * NB + 4ull * hi_pad(FJ * NB));
@@ -270,12 +274,11 @@ __device__ __forceinline__ void flush_region(unsigned *cnt, unsigned *lo, unsign
     cnt[lb] = 0u;
 #pragma unroll
     for (int g = 0; g < FMAP::FJ; g++) {
+      if (g < f0) continue;  // field 0 of unit weights: no words
       const size_t o = (size_t)g * NB + lb;
       const int fld = FMAP::j(g);
-      if (g >= f0) {
-        const double v = fixed_total(lo[o], hi[o], s_iqs[fld]);
-        if (v != 0.0) atomicAdd(&J.acc_sums[cell * kNF + fld], v);
-      }
+      const double v = fixed_total(lo[o], hi[o], s_iqs[fld]);
+      if (v != 0.0) atomicAdd(&J.acc_sums[cell * kNF + fld], v);
       lo[o] = 0u;
       hi[o] = 0u;
     }
@@ -308,6 +311,7 @@ __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsi
 #pragma unroll
     for (int f = 0; f < FM; f++) {
       tm[f] = 0;
+      if (f < f0) continue;  // field 0 of unit weights: no words
       for (int r = 0; r < nrep; r++) {
         const size_t o = (size_t)f * NBm + (r == 0 ? lb : rep_bin(r, n1, elk, nrp, wpi));
         tm[f] += (long long)(int)mhi[o] * 32768ll + (long long)mlo[o];
@@ -315,8 +319,7 @@ __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsi
         mhi[o] = 0u;
       }
       const int fld = FMAP::m(f);
-      if (f >= f0 && tm[f] != 0)
-        atomicAdd(&J.acc_sums[cell * kNF + fld], (double)tm[f] * s_iqs[fld]);
+      if (tm[f] != 0) atomicAdd(&J.acc_sums[cell * kNF + fld], (double)tm[f] * s_iqs[fld]);
     }
     if (!jk) continue;
     const int64_t xc = (int64_t)hx * hsz + cell;
@@ -325,13 +328,14 @@ __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsi
     if (n - nx) atomicAdd(&J.acc_num[xc], (unsigned long long)(n - nx));
 #pragma unroll
     for (int g = 0; g < FJ; g++) {
+      if (g < f0) continue;
       const size_t o = (size_t)g * NB + lb;
       const long long tn = (long long)(int)nhi[o] * 32768ll + (long long)nlo[o];
       nlo[o] = 0u;
       nhi[o] = 0u;
       const long long tx = tm[FMAP::jm(g)] - tn;
       const int fld = FMAP::j(g);
-      if (g >= f0 && tx != 0) atomicAdd(&J.acc_sums[xc * kNF + fld], (double)tx * s_iqs[fld]);
+      if (tx != 0) atomicAdd(&J.acc_sums[xc * kNF + fld], (double)tx * s_iqs[fld]);
     }
   }
 }
@@ -403,19 +407,26 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     const int nrp = J.nrp, wpi = J.wpi, npi = J.npi, NB = nrp * wpi;
     const int NBm = main_bins(nrp, wpi), hot0 = nrp - hot_rows(nrp);
     // per histogram: count[NB], low words [F][NB], high words [F][NB] (main:
-    // NBm bins, the hot bins' copies included)
+    // NBm bins, the hot bins' copies included).  Unit weights: wt_num = count,
+    // field 0 is not accumulated and gets no words; the word arrays are indexed
+    // by field f >= f0 from a base f0 rows before their first stored row (which
+    // then coincides with the count array, never read through it).
+    const int f0 = J.unit_w ? 1 : 0;
+    const int FMs = F::FM - f0, FJs = F::FJ - f0;  // stored fields
     unsigned *s_mnum = reinterpret_cast<unsigned *>(hist_base);
     // the high words sit hi_pad words after a 32-word-aligned offset from the low
     // words, so the low and high word of one bin are 16 banks apart (red_pair)
-    unsigned *s_mlo = s_mnum + NBm;
-    unsigned *s_mhi = s_mlo + (size_t)F::FM * NBm + hi_pad(F::FM * NBm);
-    unsigned *s_nxnum = s_mhi + (size_t)F::FM * NBm;
-    unsigned *s_nxlo = s_nxnum + NB;
-    unsigned *s_nxhi = s_nxlo + (size_t)F::FJ * NB + hi_pad(F::FJ * NB);
-    unsigned *s_ynum = s_nxhi + (size_t)F::FJ * NB;
-    unsigned *s_ylo = s_ynum + NB;
-    unsigned *s_yhi = s_ylo + (size_t)F::FJ * NB + hi_pad(F::FJ * NB);
-    const int f0 = J.unit_w ? 1 : 0;  // unit weights: wt_num = count, not accumulated
+    unsigned *s_mlo0 = s_mnum + NBm;
+    unsigned *s_mhi0 = s_mlo0 + (size_t)FMs * NBm + hi_pad(FMs * NBm);
+    unsigned *s_nxnum = s_mhi0 + (size_t)FMs * NBm;
+    unsigned *s_nxlo0 = s_nxnum + NB;
+    unsigned *s_nxhi0 = s_nxlo0 + (size_t)FJs * NB + hi_pad(FJs * NB);
+    unsigned *s_ynum = s_nxhi0 + (size_t)FJs * NB;
+    unsigned *s_ylo0 = s_ynum + NB;
+    unsigned *s_yhi0 = s_ylo0 + (size_t)FJs * NB + hi_pad(FJs * NB);
+    unsigned *s_mlo = s_mlo0 - (size_t)f0 * NBm, *s_mhi = s_mhi0 - (size_t)f0 * NBm;
+    unsigned *s_nxlo = s_nxlo0 - (size_t)f0 * NB, *s_nxhi = s_nxhi0 - (size_t)f0 * NB;
+    unsigned *s_ylo = s_ylo0 - (size_t)f0 * NB, *s_yhi = s_yhi0 - (size_t)f0 * NB;
 
     // ---- the tile's g1 rows, in shared memory.  Row slot tr = s * 32 + l holds
     // tile row q = l * W + s (s < W): a warp holds slots s * 32 .. s * 32 + 31 in

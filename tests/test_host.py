@@ -242,10 +242,12 @@ def test_auto_finalisation_matches_reference_files(name, tmp_path):
 
 
 def test_integration_binding_links_into_the_reference():
-    """The corels2/corels1 binding (integration/corr_gpu.cpp) compiles against
-    the reference's own headers and links, with the reference's objects (its
-    pair loops renamed away) and main.cpp, into a corr_pc executable that calls
-    this library (built here; the GPU test test_gpu_cli runs it)."""
+    """The corels2/corels1 binding (corr_pc_gb300/csrc/binding/corr_gpu.cpp)
+    compiles against the reference's own headers and links, with the
+    reference's objects (its pair loops renamed away) and main.cpp, into a
+    corr_pc executable that calls this library.  It is built where the
+    reference's sources are and not run (they do not exist on the GPU
+    machines); test_gpu_cli runs the same seam through the C++ driver."""
     import shutil
     import subprocess
     ref_dir = os.environ.get("CPC_REFERENCE_DIR", "/root/reference")
@@ -409,6 +411,15 @@ def test_chunked_reader_under_sanitizers(asan_driver, tmp_path):
     assert r.returncode == 1
     assert f"gal data reading ended unexpectedly at row {bad_row} " in r.stdout, r.stdout
     assert "runtime error" not in r.stderr
+    # "inf" and "nan" tokens, which from_chars would accept and istream >> double
+    # does not: reading stops at the first of them
+    lines[bad_row] = lines[bad_row][1:]
+    for tok, row in (("inf", 98765), ("-nan", 45678)):
+        lines[row] = tok
+        open(zf, "w").write("\n".join(lines))
+        r = _run_sanitized([asan_driver, "--dump", inp, out])
+        assert r.returncode == 1
+        assert f"gal data reading ended unexpectedly at row {row} " in r.stdout, (tok, r.stdout)
 
 
 def test_host_threads_under_thread_sanitizer(tmp_path):
