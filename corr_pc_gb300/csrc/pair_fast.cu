@@ -133,7 +133,9 @@ __host__ __device__ constexpr int hi_pad(int words) { return (16 - (words & 31) 
 // words), and the flush adds the copies together in exact integer arithmetic.
 // Measured on GB300: 4 copies of the top 4 bins gain 2% on the 200k wg+ box and
 // lose 3-4% on the kappa and ED workloads (the copies take shared memory from
-// the Pi window), so the default is one copy.
+// the Pi window); on the 2M w++ box 2 copies of the top one or two rows or 4
+// of the top row gain nothing (777, 773 and 786 ms against 773 ms), so the
+// default is one copy.
 #ifndef CPC_HOT_REP
 #define CPC_HOT_REP 1
 #endif
@@ -818,22 +820,25 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                 see = fmaf(sxe, sxe, fmaf(sye, sye, sze * sze));
                 if (!(see > 0.0f)) amb = true;
               }
-              if (!own) {
-                // another mu slice's pair
-              } else if (all_exact) {
+              if (all_exact) {
                 // the comparison engine: the reference's double arithmetic for
-                // every candidate (window, bins, values), global FP64 atomics
+                // every candidate (window, bins, values), global FP64 atomics.
+                // With coordinates 7 every mu slice visits the pair: the window
+                // count is kept from slice 0 only, the pair's values go in by the
+                // slice that holds its exact mu bin
                 const int64_t gi1 = (int64_t)U.g1_start +
                                     (int64_t)(((er & 31) * W) + (er >> 5)) * U.g1_stride;
                 const int64_t gj2 = s_jidx[ec];
                 int xn1, xn2;
                 const int r = exact_classify(J, J.d1, gi1, J.d2, gj2, sx, sy, sz, xn1, xn2);
                 if (r >= 1) nwin++;
-                if (r == 2) {
+                if (r == 2 && (!rmu || (xn2 >= n2_base && xn2 < n2_base + wpi))) {
                   double f[kNF];
                   exact_values(J, J.d1, gi1, J.d2, gj2, sx, sy, sz, f);
                   exact_accumulate(J, J.d1, gi1, J.d2, gj2, xn1, xn2, f);
                 }
+              } else if (!own) {
+                // another mu slice's pair
               } else if (amb || edge) {
                 // near the window edge (not yet counted) or a bin edge (window
                 // counted): exact FP64 evaluation

@@ -20,7 +20,7 @@ def _ctx_for(p, S, D, tuning=None):
     return ctx
 
 
-@pytest.mark.parametrize("engine", ["fast", "fp64"])
+@pytest.mark.parametrize("engine", ["fast", "fp64", "cell_fp64"])
 @pytest.mark.parametrize("name", golden_names())
 def test_matches_reference_golden(name, engine):
     g = Golden(name)

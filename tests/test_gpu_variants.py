@@ -66,7 +66,7 @@ def test_rmu_mu_slices():
     p = synth._box_params(which_corr=2, L=100.0, rmin=0.1, rmax=20.0, nrp=40, npi=100, pmax=1.0,
                           njk=8, n=c.n)
     p.coordinates = 7
-    _run(p, c, c, engines=("fast",))
+    _run(p, c, c, engines=("fast", "cell_fp64"))
 
 
 def test_ed_rppi_large_row_sample():
