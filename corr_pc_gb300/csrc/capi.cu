@@ -2202,11 +2202,15 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
       return s;
     for (int w : ws) {
       c->tune_wpi = w;
-      // first run builds the work units, the second is timed
+      // first run builds the work units, the next two are timed (the faster counts)
       if (cpc_count(c, kind, slot_g1, slot_g2, CPC_ENGINE_FAST, stride, 0, &acc) != CPC_OK) continue;
-      if (cpc_count(c, kind, slot_g1, slot_g2, CPC_ENGINE_FAST, stride, 0, &acc) != CPC_OK) continue;
-      if (acc.pair_kernel_ms < best) {
-        best = acc.pair_kernel_ms;
+      double t = INFINITY;
+      for (int rep = 0; rep < 2; rep++) {
+        if (cpc_count(c, kind, slot_g1, slot_g2, CPC_ENGINE_FAST, stride, 0, &acc) != CPC_OK) break;
+        t = std::min(t, (double)acc.pair_kernel_ms);
+      }
+      if (t < best) {
+        best = t;
         bk = k;
         bw = w;
       }
@@ -2304,13 +2308,18 @@ cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_k
     if (s != CPC_OK) return s;
     for (int w : ws) {
       for (int k = 0; k < n_jobs; k++) ctxs[k]->tune_wpi = w;
-      // first run builds the work units, the second is timed
+      // first run builds the work units, the next two are timed (the faster counts)
       if (count_batch_rows(n_jobs, ctxs, kinds, slots_g1, slots_g2, accs.data(), stride) != CPC_OK)
         continue;
-      if (count_batch_rows(n_jobs, ctxs, kinds, slots_g1, slots_g2, accs.data(), stride) != CPC_OK)
-        continue;
-      if (accs[0].pair_kernel_ms < best) {
-        best = accs[0].pair_kernel_ms;
+      double t = INFINITY;
+      for (int rep = 0; rep < 2; rep++) {
+        if (count_batch_rows(n_jobs, ctxs, kinds, slots_g1, slots_g2, accs.data(), stride) !=
+            CPC_OK)
+          break;
+        t = std::min(t, (double)accs[0].pair_kernel_ms);
+      }
+      if (t < best) {
+        best = t;
         bk = kc;
         bw = w;
       }

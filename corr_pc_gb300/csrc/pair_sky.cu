@@ -319,6 +319,17 @@ __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r,
                                                const float *s_A, const float *s_B,
                                                const float *s_PA, const float *s_PB) {
   const float4 w2 = fb.sw[j], l2 = fb.sl[j], u2 = fb.su[j];
+  // every load of the pair issued before the first test: one memory round trip
+  // instead of three (most queued pairs bin)
+  const float4 x2 = fb.sx[j];
+  const int jk2 = b.d.jk[j], keep2 = b.d.keep[j];
+  float4 se2 = make_float4(0.f, 0.f, 0.f, 0.f), sh2 = se2;
+  float2 sp2 = make_float2(0.f, 0.f);
+  if (J.corel != COREL_DD) {
+    se2 = fb.ss[j];
+    sh2 = fb.sh[j];
+    sp2 = fb.sp[j];
+  }
   // Pi: (dc2_hi - dc1_hi) + (dc2_lo - dc1_lo); the bands carry the error bound
   const float pf = (w2.w - rf.w.w) + (l2.w - rf.ul.w);
   const int k2 = band_bin(pf, 0.0f, (int)floorf(fmaf(pf, J.inv_ps_f, J.tp0)), J.npi, s_PA, s_PB,
@@ -349,18 +360,15 @@ __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r,
     return;
   }
   // values: theta = atan(dDec / (dRA cos(mean Dec))) (sky_calcs.cpp:13-22)
-  const float4 x2 = fb.sx[j];
   const float wt = rf.x.w * x2.w;
   const int64_t cell = (int64_t)k1 * J.npi + k2;
   if (J.corel == COREL_DD) {
     const float f0[1] = {wt};
-    sky_accumulate_fixed<SMEM>(J, r.jk, r.keep, b.d.jk[j], b.d.keep[j], cell, f0, nullptr, 1,
-                               s_qs, s_num, s_fix);
+    sky_accumulate_fixed<SMEM>(J, r.jk, r.keep, jk2, keep2, cell, f0, nullptr, 1, s_qs, s_num,
+                               s_fix);
   } else {
     // the separation in RA and Dec (hi + lo degrees) and cos of the mean Dec,
     // cos(d1/2 + d2/2), as double-floats; X = dRA cos(mean Dec), Y = dDec
-    const float4 se2 = fb.ss[j], sh2 = fb.sh[j];
-    const float2 sp2 = fb.sp[j];
     const df32 dra = df_diff_hl(w2.x, x2.x, rf.w.x, rf.x.x);
     const df32 ddec = df_diff_hl(w2.y, x2.y, rf.w.y, rf.x.y);
     const df32 cm = df_sub(df_mul(df32{rf.h.x, rf.h.y}, df32{sh2.x, sh2.y}),
@@ -386,8 +394,8 @@ __device__ __forceinline__ void sky_pair_mixed(const JobDev &J, const SkyRow &r,
     if (J.corel == COREL_SD) df_pair_terms<COREL_SD>(c, sn, theta, g1, g2, J.gws, uw, vd, v);
     else if (J.corel == COREL_SS) df_pair_terms<COREL_SS>(c, sn, theta, g1, g2, J.gws, uw, vd, v);
     else df_pair_terms<COREL_SSA>(c, sn, theta, g1, g2, J.gws, uw, vd, v);
-    sky_accumulate_fixed<SMEM>(J, r.jk, r.keep, b.d.jk[j], b.d.keep[j], cell, v, vd, kNF, s_qs,
-                               s_num, s_fix);
+    sky_accumulate_fixed<SMEM>(J, r.jk, r.keep, jk2, keep2, cell, v, vd, kNF, s_qs, s_num,
+                               s_fix);
   }
 }
 
