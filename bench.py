@@ -533,11 +533,11 @@ def main() -> None:
         n_rows = wls[0].density.n
         k, w = ctxs[0].autotune("SD", 0, 1, sample_stride=max(1, n_rows // 25000))
         tuning = {"cells_per_rmax": k, "pi_window": w if w else "automatic (every mu bin that fits)",
-                  "by": "cpc_autotune on a row sample"}
+                  "by": "cpc_autotune on a shard of the work units"}
     elif len(ctxs) > 1 and not args.no_tune and not args.tune:
         k, w = _lib.autotune_batch([(c, "SD", 0, 1) for c in ctxs])
         tuning = {"cells_per_rmax": k, "pi_window": w,
-                  "by": "cpc_autotune_batch on row samples of every box"}
+                  "by": "cpc_autotune_batch on a shard of every box's work units"}
     # the uploads (copy, device checks, radix sort into the cell list, gather of
     # the SoA streams, host bucket tables), wall clock, outside the timed steps
     cell_list = {"upload_wall_ms_per_catalog": 1e3 * upload_s / (2 * len(ctxs)),
@@ -582,6 +582,7 @@ def main() -> None:
             tot_pair_ms += pms
     torch.cuda.synchronize()
     launches = sum(c.launches() for c in ctxs) - l0
+    twin_used = ctxs[0].last_twin()
     if n_shards > 1:
         ctxs[0].set_shard(0, 1)
     g_cap, g_rep = ctxs[0].graph_stats()
@@ -688,13 +689,16 @@ def main() -> None:
     # the FP64 path (the reference's double arithmetic, global atomics): the
     # precision comparison at equal algorithm, on one shard of the work queue
     # sized for about args.cell_fp64_pairs binned pairs, against the fast engine
-    # on the same shard
+    # on the same shard counting every order (a twin count's shard holds other
+    # pairs: both orders of the pairs whose row it holds)
     cell64 = None
     if len(ctxs) == 1 and args.cell_fp64_pairs > 0:
         K = max(1, int(full_pairs / args.cell_fp64_pairs))
         ctxs[0].set_shard(0, K)
         rc = ctxs[0].count("SD", 0, 1, engine="cell_fp64")
+        ctxs[0].set_twin(False)
         rfs = ctxs[0].count("SD", 0, 1)
+        ctxs[0].set_twin(True)
         ctxs[0].set_shard(0, 1)
         v64 = rc["n_binned"] / (rc["kernel_ms"] * 1e-3)
         vf = rfs["n_binned"] / (rfs["kernel_ms"] * 1e-3)
@@ -702,6 +706,7 @@ def main() -> None:
                   "sample": f"shard 0 of {K} of the work queue: {rc['n_binned']} binned pairs in "
                             f"{rc['kernel_ms']:.1f} ms",
                   "fast_on_same_shard": vf, "speedup_of_fast": vf / v64,
+                  "speedup_of_value": value / v64,
                   "counts_equal_fast": bool(np.array_equal(rc["num"], rfs["num"])),
                   "accuracy_fast_vs_cell_fp64": metrics.accuracy_report(
                       rfs["num"], rfs["sums"], rc["num"], rc["sums"])["ok"]}
@@ -724,7 +729,10 @@ def main() -> None:
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64", "data": "synthetic (seeded generator, in memory)",
-            "config": dict(_describe(wls), tuning=tuning),
+            "config": dict(_describe(wls), tuning=tuning,
+                           pair_orders=("twin count: S and D hold the same galaxies, each "
+                                        "unordered pair tested once and both orders added"
+                                        if twin_used else "every order counted separately")),
             "step_definition": _step_definition(wl_name, "gb300"),
             "value_scope": "device time of the count (zeroing, pair kernel, FP64 edge recheck) "
                            "with both catalogues' cell lists resident; the cell-list build is "

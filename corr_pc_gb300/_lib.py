@@ -100,6 +100,8 @@ def load() -> ctypes.CDLL:
     lib.cpc_set_graph_replay.argtypes = [V, I]
     lib.cpc_set_shard.argtypes = [V, I, I]
     lib.cpc_graph_stats.argtypes = [V, P(I64), P(I64)]
+    lib.cpc_set_twin.argtypes = [V, I]
+    lib.cpc_last_twin.argtypes = [V, P(I)]
     lib.cpc_host_finalize_cross.argtypes = [ctypes.c_char_p] + [V] * 9
     lib.cpc_host_finalize_auto.argtypes = [ctypes.c_char_p] + [V] * 7
     lib.cpc_host_finalize_auto.restype = I
@@ -112,7 +114,7 @@ def load() -> ctypes.CDLL:
                "cpc_count_batch", "cpc_set_tuning", "cpc_host_rand_uniform",
                "cpc_host_elip_angle", "cpc_host_rp_thresholds", "cpc_host_pi_thresholds",
                "cpc_launch_count", "cpc_host_finalize_cross", "cpc_set_graph_replay",
-               "cpc_graph_stats", "cpc_set_shard"):
+               "cpc_graph_stats", "cpc_set_shard", "cpc_set_twin", "cpc_last_twin"):
         getattr(lib, fn).restype = I
     _lib = lib
     return lib
@@ -190,8 +192,8 @@ class Context:
         check(self.lib.cpc_set_tuning(self.h, cells_per_rmax, pi_window, tile), self.h)
 
     def autotune(self, kind: str, slot_g1: int, slot_g2: int, sample_stride: int = 8):
-        """Pick the fastest cell width and Pi window for this pair type on a row
-        sample; returns (cells_per_rmax, pi_window)."""
+        """Pick the fastest cell width and Pi window for this pair type on every
+        sample_stride-th work unit; returns (cells_per_rmax, pi_window)."""
         k, w = ctypes.c_int(), ctypes.c_int()
         check(self.lib.cpc_autotune(self.h, PAIR[kind], slot_g1, slot_g2, sample_stride,
                                     ctypes.byref(k), ctypes.byref(w)), self.h)
@@ -237,6 +239,17 @@ class Context:
         """Replay fast counts from a captured CUDA graph (default) or launch
         their kernels directly."""
         check(self.lib.cpc_set_graph_replay(self.h, 1 if enable else 0), self.h)
+
+    def set_twin(self, enable: bool) -> None:
+        """Twin counts on (default) or off: a cross term of two slots holding
+        the same galaxies tests each unordered pair once and adds both orders."""
+        check(self.lib.cpc_set_twin(self.h, 1 if enable else 0), self.h)
+
+    def last_twin(self) -> bool:
+        """Whether this context's last fast count ran as a twin count."""
+        v = ctypes.c_int()
+        check(self.lib.cpc_last_twin(self.h, ctypes.byref(v)), self.h)
+        return bool(v.value)
 
     def graph_stats(self) -> tuple:
         """(captures, replays) of this context's fast-count graph."""
@@ -293,10 +306,10 @@ class Context:
 
 def autotune_batch(jobs, sample_stride: int = 0) -> tuple:
     """jobs: list of (Context, kind, slot_g1, slot_g2) as for count_batch.
-    Times batched launches on a row sample of every job for the cell widths
-    and Pi windows the single-job autotuner tries, keeps the fastest on every
-    context and returns (cells_per_rmax, pi_window).  sample_stride 0: about
-    a 25,000-row sample of the largest job's g1 catalogue."""
+    Times batched launches on every sample_stride-th work unit of every job
+    for the cell widths and Pi windows the single-job autotuner tries, keeps
+    the fastest on every context and returns (cells_per_rmax, pi_window).
+    sample_stride 0: the largest job's g1 rows // 25,000."""
     lib = load()
     n = len(jobs)
     if sample_stride <= 0:

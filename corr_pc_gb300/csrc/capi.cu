@@ -120,7 +120,7 @@ struct SkyJobBufs {
 
 struct UnitCache {
   uint64_t v1 = 0, v2 = 0;
-  int s1 = -1, s2 = -1, wpi = 0, tile = 0;
+  int s1 = -1, s2 = -1, wpi = 0, tile = 0, twin = 0;
   std::vector<UnitDesc> units;  // job field filled at launch
 };
 
@@ -182,6 +182,14 @@ struct cpc_ctx {
   int64_t launches = 0;  // kernels launched by this context (all entry points)
   // work-unit shard of the fast box engine (cpc_set_shard)
   int shard = 0, n_shards = 1;
+  // whether two box slots hold the same galaxies in the same order (twin jobs),
+  // for the slot pair and versions last compared; CPC_TWIN=0 turns twin jobs off
+  int twin_s1 = -1, twin_s2 = -1;
+  uint64_t twin_v1 = 0, twin_v2 = 0;
+  bool twin_same = false;
+  int twin_on = 1;
+  int last_twin = 0;  // the last fast count ran a twin job
+  DevBuf<unsigned> d_differ;
   // register bound of the fast sky kernel: 2 or 3 blocks of 256 threads per SM
   // (CPC_SKY_BLOCKS_PER_SM in the environment; the autotuner of a sky context
   // would set it)
@@ -407,8 +415,94 @@ int unit_weights(const Slot &a, const Slot &b) {
   return (a.wmax == 1.0 && a.wmin == 1.0 && b.wmax == 1.0 && b.wmin == 1.0) ? 1 : 0;
 }
 
+// A context's unit shard replaced for the autotuner's trials, restored when the
+// trials end (or on any early return).
+struct ShardOverride {
+  cpc_ctx *c;
+  int shard, n_shards;
+  bool active = true;
+  ShardOverride(cpc_ctx *ctx, int sh, int nsh) : c(ctx), shard(ctx->shard), n_shards(ctx->n_shards) {
+    c->shard = sh;
+    c->n_shards = nsh;
+  }
+  void restore() {
+    if (!active) return;
+    c->shard = shard;
+    c->n_shards = n_shards;
+    active = false;
+  }
+  ~ShardOverride() { restore(); }
+};
+
+// Whether box slots sa and sb hold the same galaxies in the same (cell) order:
+// positions, weights, shapes, orientations, regions and input rows identical
+// (the keep flags, drawn from rand() per read, may differ).  A cross term of a
+// catalogue with itself, uploaded as two samples, is such a pair.  Compared on
+// the device, cached per slot versions.
+bool slots_twin(cpc_ctx *c, int sa, int sb) {
+  if (sa == sb) return true;
+  Slot &A = c->slots[sa], &B = c->slots[sb];
+  if (!A.valid || !B.valid || A.sky || B.sky || A.n != B.n || A.has_e != B.has_e ||
+      A.kcells != B.kcells || A.ncx != B.ncx || A.ncy != B.ncy || A.n_reg != B.n_reg)
+    return false;
+  if (c->twin_s1 == sa && c->twin_s2 == sb && c->twin_v1 == A.version && c->twin_v2 == B.version)
+    return c->twin_same;
+  const int64_t n = A.n;
+  bool same = false;
+  if (c->d_differ.alloc(1) == cudaSuccess &&
+      cudaMemsetAsync(c->d_differ.p, 0, sizeof(unsigned), c->st) == cudaSuccess) {
+    const std::pair<const void *, const void *> arr8[] = {
+        {A.x.p, B.x.p}, {A.y.p, B.y.p}, {A.z.p, B.z.p}, {A.w.p, B.w.p}, {A.e1.p, B.e1.p},
+        {A.e2.p, B.e2.p}, {A.phi.p, B.phi.p}, {A.e3.p, B.e3.p}, {A.orig.p, B.orig.p}};
+    bool ok = true;
+    for (const auto &ab : arr8)
+      ok = ok && launch_bytes_differ(ab.first, ab.second, 8 * n, c->d_differ.p, c->st) ==
+                     cudaSuccess;
+    ok = ok && launch_bytes_differ(A.jk.p, B.jk.p, 4 * n, c->d_differ.p, c->st) == cudaSuccess;
+    unsigned d = 1;
+    if (ok && cudaMemcpyAsync(&d, c->d_differ.p, sizeof d, cudaMemcpyDeviceToHost, c->st) ==
+                  cudaSuccess &&
+        cudaStreamSynchronize(c->st) == cudaSuccess)
+      same = d == 0;
+    c->launches += ok ? 10 : 0;
+  }
+  c->twin_s1 = sa;
+  c->twin_s2 = sb;
+  c->twin_v1 = A.version;
+  c->twin_v2 = B.version;
+  c->twin_same = same;
+  return same;
+}
+
+// Whether a box cross term counts as a twin job: the fast engine on every
+// outer row (no row sample), coordinates 6, a corel whose other order differs
+// only in the fields FieldMap::a lists (density_density, shape_shape), a Pi
+// binning symmetric about 0 and twin slots.  Symmetric: the exact thresholds
+// satisfy |thr[k] + thr[npi - k]| <= 2^-24 |thr| + 1e-13 L (the reference's
+// floor((Pi - p_min) / p_size) leaves them a few ulps from exact symmetry),
+// a quarter of the guard of the fast path's Pi bands at most, so the other
+// order of every pair the fast path bins has Pi bin npi - 1 - bin.
+bool twin_job(cpc_ctx *c, const JobRule &rule, int s1, int s2, int64_t rs, int64_t ro,
+              int auto_mode) {
+  const cpc_params &p = c->p;
+  if (!c->twin_on || auto_mode || rs > 1 || ro != 0 || p.coordinates != 6) return false;
+  if (rule.corel != COREL_DD && rule.corel != COREL_SS && rule.corel != COREL_SSA) return false;
+  const int npi = p.n_p_bin;
+  if (npi < 1 || npi > kMaxPi) return false;
+  const double tol_abs = 1e-13 * p.periodic_box_size;
+  for (int k = 0; k <= npi; k++) {
+    const double a = c->thr_pi[k], b = c->thr_pi[npi - k];
+    if (!(std::fabs(a + b) <= std::ldexp(1.0, -24) * std::max(std::fabs(a), std::fabs(b)) + tol_abs))
+      return false;
+  }
+  return slots_twin(c, s1, s2);
+}
+
+// allow_twin: false for the cell-list FP64 comparison engine, which counts every
+// order and keeps the plain job's window
 cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, int64_t rs,
-                    int64_t ro, cpc_accum *out, JobPlan &jp, int auto_mode = 0) {
+                    int64_t ro, cpc_accum *out, JobPlan &jp, int auto_mode = 0,
+                    bool allow_twin = true) {
   if (slot_g1 < 0 || slot_g1 >= kMaxSlots || slot_g2 < 0 || slot_g2 >= kMaxSlots)
     return fail(c, CPC_ERR_INVALID, "slot out of range");
   Slot &A = c->slots[slot_g1], &B = c->slots[slot_g2];
@@ -434,14 +528,20 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   // coordinates 7 the mu bins have no locality in z: a block holds every mu bin
   // when they fit (else the units are repeated over slices of wpi mu bins)
   const bool rmu = p.coordinates == 7;
+  // twin job: each unordered pair once, both orders added (its block holds the
+  // other order's histograms too, so the window is narrower; it covers only
+  // the pair order with g2 ahead, whose units span half the Pi range)
+  const int twin =
+      (allow_twin && !jp.empty && twin_job(c, jp.rule, jp.s1, jp.s2, rs, ro, auto_mode)) ? 1 : 0;
+  const int wmin = rmu ? 1 : twin ? 5 : 8;
   // Automatic window: the largest that fits 4 blocks per SM when it holds at
   // least 12 Pi bins (or all of them), else the largest for 3 blocks.
-  const size_t static_b = fast_static_smem_bytes();
+  const size_t static_b = fast_static_smem_bytes(twin);
   auto fit = [&](int blocks) {
     const size_t budget = (size_t)(228 * 1024) / blocks - static_b - 1024;
     int w = npi;
-    while (w > (rmu ? 1 : 8) &&
-           fast_smem_bytes(jp.rule.corel, jk, nrp, w, auto_mode, unit_weights(g1, g2)) > budget)
+    while (w > wmin && fast_smem_bytes(jp.rule.corel, jk, nrp, w, auto_mode,
+                                       unit_weights(g1, g2), twin) > budget)
       w--;
     return w;
   };
@@ -452,7 +552,7 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
     wpi = fit(kFastBlocksPerSM);
     if (wpi < npi && wpi < 12) wpi = std::max(wpi, fit(kFastBlocksPerSM - 1));
   }
-  if (!rmu && wpi < npi && wpi < 8) wpi = std::min(npi, 8);
+  if (!rmu && wpi < npi && wpi < wmin) wpi = std::min(npi, wmin);
   jp.wpi = wpi;
   jp.tile = kTileThreads;
 
@@ -462,6 +562,7 @@ cpc_status plan_job(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, in
   fill_views(g2, J.f2, J.d2);
   J.corel = jp.rule.corel;
   J.gws = jp.rule.gws;
+  J.twin = twin;
   J.which_corr = p.which_corr;
   J.estimator = p.estimator;
   J.do_jk = jk;
@@ -588,7 +689,8 @@ const std::vector<UnitDesc> &build_units(JobPlan &jp) {
   cpc_ctx *c = jp.c;
   for (auto &uc : c->unit_cache)
     if (uc.s1 == jp.s1 && uc.s2 == jp.s2 && uc.v1 == c->slots[jp.s1].version &&
-        uc.v2 == c->slots[jp.s2].version && uc.wpi == jp.wpi && uc.tile == jp.tile)
+        uc.v2 == c->slots[jp.s2].version && uc.wpi == jp.wpi && uc.tile == jp.tile &&
+        uc.twin == jp.jd.twin)
       return uc.units;
   if (c->unit_cache.size() >= 8) c->unit_cache.erase(c->unit_cache.begin());
   c->unit_cache.emplace_back();
@@ -599,6 +701,7 @@ const std::vector<UnitDesc> &build_units(JobPlan &jp) {
   uc.v2 = c->slots[jp.s2].version;
   uc.wpi = jp.wpi;
   uc.tile = jp.tile;
+  uc.twin = jp.jd.twin;
   const cpc_params &p = c->p;
   const Slot &g1 = c->slots[jp.s1];
   const double L = p.periodic_box_size;
@@ -660,7 +763,9 @@ const std::vector<UnitDesc> &build_units(JobPlan &jp) {
           cx0 = std::max(cx0, 0); cx1 = std::min(cx1, ncx - 1);
           cy0 = std::max(cy0, 0); cy1 = std::min(cy1, ncy - 1);
         }
-        const double Zlo = zt0 + zw0 - guard, Zhi = zt1 + zw1 + guard;
+        // twin jobs: only candidates ahead of the rows (Pi >= 0; the other order
+        // is added with each pair)
+        const double Zlo = zt0 + (jp.jd.twin ? 0.0 : zw0) - guard, Zhi = zt1 + zw1 + guard;
         for (int k = 0; k < nt; k++) {
           UnitDesc u;
           std::memset(&u, 0, sizeof u);
@@ -871,6 +976,7 @@ struct FastGroup {
   size_t first, n_units, smem;
   FastScales sc;
   int auto_pairs;  // the group holds corels1 jobs (their rules in shared memory)
+  int twin;        // the group's jobs are twin jobs (their own kernel)
 };
 
 size_t accum_cells(const cpc_ctx *c) {
@@ -894,7 +1000,8 @@ cpc_status fast_body(cpc_ctx *c0, std::vector<JobPlan> &jobs, const std::vector<
   CK(cudaEventRecordWithFlags(c0->e0, st, rec_flags), "event");
   for (const FastGroup &g : gs) {
     CK(cudaMemsetAsync(c0->d_unit_ctr.p, 0, sizeof(unsigned int), st), "memset");
-    CK(launch_fast(g.corel, g.jk, g.minb, c0->d_jobs.p, c0->d_units.p + g.first, (int)g.n_units,
+    CK(launch_fast(g.corel, g.jk, g.minb, g.twin, c0->d_jobs.p, c0->d_units.p + g.first,
+                   (int)g.n_units,
                    c0->d_unit_ctr.p, c0->d_queue.p, c0->d_qcount.p, c0->qcap, g.sc, g.smem,
                    g.grid, g.auto_pairs, st),
        "fast kernel");
@@ -937,6 +1044,7 @@ std::vector<uint64_t> fast_graph_key(cpc_ctx *c0, const std::vector<JobPlan> &jo
     put(g.n_units);
     put(g.smem);
     put((uint64_t)g.auto_pairs);
+    put((uint64_t)g.twin);
     for (int f = 0; f < kNF; f++) {  // the scales are kernel parameters too
       uint32_t b;
       std::memcpy(&b, &g.sc.qs[f], sizeof b);
@@ -1008,12 +1116,14 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
     jobs[k].jd.counters = jobs[k].c->d_counters.p;
   }
   // group by kernel template
-  std::map<std::pair<int, int>, std::vector<int>> groups;
+  // group by kernel instantiation: corel, jackknife, twin
+  std::map<std::tuple<int, int, int>, std::vector<int>> groups;
   for (size_t k = 0; k < jobs.size(); k++)
-    if (!jobs[k].empty) groups[{jobs[k].jd.corel, jobs[k].jd.do_jk}].push_back((int)k);
+    if (!jobs[k].empty)
+      groups[std::make_tuple(jobs[k].jd.corel, jobs[k].jd.do_jk, jobs[k].jd.twin)].push_back((int)k);
   size_t total_units = 0;
   std::vector<std::pair<size_t, size_t>> ranges;
-  std::vector<std::pair<int, int>> gkeys;
+  std::vector<std::tuple<int, int, int>> gkeys;
   for (auto &g : groups) {
     const size_t b = all.size();
     for (int k : g.second) {
@@ -1051,6 +1161,8 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
     }
   }
   c0->last_units = total_units;
+  c0->last_twin = 0;
+  for (const JobPlan &jp : jobs) c0->last_twin |= jp.jd.twin;
   std::vector<JobDev> jds(jobs.size());
   for (size_t k = 0; k < jobs.size(); k++) jds[k] = jobs[k].jd;
   CK(cudaMemcpyAsync(c0->d_jobs.p, jds.data(), sizeof(JobDev) * jds.size(), cudaMemcpyHostToDevice, st), "H2D jobs");
@@ -1058,7 +1170,7 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
     CK(cudaMemcpyAsync(c0->d_units.p, all.data(), sizeof(UnitDesc) * total_units, cudaMemcpyHostToDevice, st), "H2D units");
   std::vector<FastGroup> gs;
   for (size_t g = 0; g < ranges.size(); g++) {
-    const int corel = gkeys[g].first, jk = gkeys[g].second;
+    const int corel = std::get<0>(gkeys[g]), jk = std::get<1>(gkeys[g]), twin = std::get<2>(gkeys[g]);
     size_t smem = 0;  // the largest any job of the group needs
     FastScales sc;    // per field the smallest scale of the group's jobs
     int auto_pairs = 0;
@@ -1070,8 +1182,8 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
       auto_pairs |= jobs[all[k].job].jd.auto_mode ? 1 : 0;
     for (size_t k = ranges[g].first; k < ranges[g].second; k++) {
       const JobPlan &jp = jobs[all[k].job];
-      smem = std::max(smem,
-                      fast_smem_bytes(corel, jk, jp.jd.nrp, jp.wpi, auto_pairs, jp.jd.unit_w));
+      smem = std::max(smem, fast_smem_bytes(corel, jk, jp.jd.nrp, jp.wpi, auto_pairs,
+                                            jp.jd.unit_w, jp.jd.twin));
       for (int f = 0; f < kNF; f++)
         if (jp.jd.qscale[f] < sc.qs[f]) {
           sc.qs[f] = jp.jd.qscale[f];
@@ -1080,12 +1192,13 @@ cpc_status enqueue_fast(std::vector<JobPlan> &jobs) {
     }
     int bps = 0;
     const int minb = fast_variant(corel, jk, smem, &bps,
-                                  jobs[all[ranges[g].first].job].jd.all_exact);
+                                  jobs[all[ranges[g].first].job].jd.all_exact, twin);
     if (bps <= 0) return fail(c, CPC_ERR_INVALID, "fast kernel does not fit on an SM with these bins");
     const size_t n_units = ranges[g].second - ranges[g].first;
     if (n_units == 0) continue;
     const int grid = (int)std::min<int64_t>((int64_t)c0->sm_count * bps, (int64_t)n_units);
-    gs.push_back(FastGroup{corel, jk, minb, grid, ranges[g].first, n_units, smem, sc, auto_pairs});
+    gs.push_back(
+        FastGroup{corel, jk, minb, grid, ranges[g].first, n_units, smem, sc, auto_pairs, twin});
   }
   return launch_fast_body(c0, jobs, gs);
 }
@@ -1907,6 +2020,7 @@ cpc_status cpc_create(cpc_ctx **out, const cpc_params *params) try {
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "device attribute");
   if (const char *ev = std::getenv("CPC_SKY_BLOCKS_PER_SM"))
     c->sky_blocks_per_sm = std::atoi(ev) >= 3 ? 3 : 2;
+  if (const char *ev = std::getenv("CPC_TWIN")) c->twin_on = std::atoi(ev) != 0 ? 1 : 0;
   e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "stream");
   e = cudaEventCreate(&c->e0);
@@ -2055,7 +2169,8 @@ cpc_status cpc_count(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2, c
     return sky_count(c, kind, slot_g1, slot_g2, row_stride, row_offset, engine, out);
   }
   std::vector<JobPlan> jobs(1);
-  cpc_status s = plan_job(c, kind, slot_g1, slot_g2, row_stride, row_offset, out, jobs[0]);
+  cpc_status s = plan_job(c, kind, slot_g1, slot_g2, row_stride, row_offset, out, jobs[0], 0,
+                          engine == CPC_ENGINE_FAST);
   if (s != CPC_OK) return s;
   if (engine == CPC_ENGINE_FP64) return run_plain(jobs[0]);
   jobs[0].jd.all_exact = engine == CPC_ENGINE_CELL_FP64 ? 1 : 0;
@@ -2141,18 +2256,19 @@ cpc_status cpc_count_auto(cpc_ctx *c, cpc_pair_kind kind, int slot, cpc_engine e
 // window whose histograms fit, and three quarters of it (more, narrower units).
 // With coordinates 7 the mu window is automatic (every mu bin when they fit):
 // only the cell width is tuned.
-std::vector<int> tune_windows(const cpc_params &p, int corel, int unit_w) {
+std::vector<int> tune_windows(const cpc_params &p, int corel, int unit_w, int twin) {
   std::vector<int> ws;
   if (p.coordinates == 7) return {0};
+  const int wmin = twin ? 5 : 8;
   const int jk = p.do_jk ? 1 : 0, nrp = p.n_bins, npi = p.n_p_bin;
-  const size_t static_b = fast_static_smem_bytes();
+  const size_t static_b = fast_static_smem_bytes(twin);
   for (int b = 4; b >= 2; b--) {
     const size_t budget = (size_t)(228 * 1024) / b - static_b - 1024;
     int w = npi;
-    while (w > 1 && fast_smem_bytes(corel, jk, nrp, w, 0, unit_w) > budget) w--;
-    if (fast_smem_bytes(corel, jk, nrp, w, 0, unit_w) > budget) continue;
+    while (w > 1 && fast_smem_bytes(corel, jk, nrp, w, 0, unit_w, twin) > budget) w--;
+    if (fast_smem_bytes(corel, jk, nrp, w, 0, unit_w, twin) > budget) continue;
     for (int cand : {w, (3 * w + 3) / 4}) {
-      if (cand < std::min(npi, 8)) continue;
+      if (cand < std::min(npi, wmin)) continue;
       if (std::find(ws.begin(), ws.end(), cand) == ws.end()) ws.push_back(cand);
     }
     if (w == npi) break;  // every Pi bin fits: fewer blocks gain nothing
@@ -2188,9 +2304,14 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
     JobRule rule;
     if (job_rule(p, kind, c->slots[slot_g1].n, c->slots[slot_g2].n, rule) != 0)
       return fail(c, CPC_ERR_INVALID, "bad pair kind");
-    ws = tune_windows(p, rule.corel, unit_weights(c->slots[slot_g1], c->slots[slot_g2]));
+    const int s1 = rule.swapped ? slot_g2 : slot_g1, s2 = rule.swapped ? slot_g1 : slot_g2;
+    ws = tune_windows(p, rule.corel, unit_weights(c->slots[slot_g1], c->slots[slot_g2]),
+                      twin_job(c, rule, s1, s2, 1, 0, 0) ? 1 : 0);
   }
+  // the trials count every sample_stride-th work unit (a unit shard: whole
+  // tiles, so each trial's per-unit costs are those of the full count)
   const int64_t stride = std::max<int64_t>(1, sample_stride);
+  ShardOverride so(c, 0, (int)std::min<int64_t>(stride, 1 << 30));
   double best = INFINITY;
   int bk = c->slots[slot_g1].kcells, bw = c->tune_wpi;
   for (int k : ks) {
@@ -2203,10 +2324,10 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
     for (int w : ws) {
       c->tune_wpi = w;
       // first run builds the work units, the next two are timed (the faster counts)
-      if (cpc_count(c, kind, slot_g1, slot_g2, CPC_ENGINE_FAST, stride, 0, &acc) != CPC_OK) continue;
+      if (cpc_count(c, kind, slot_g1, slot_g2, CPC_ENGINE_FAST, 1, 0, &acc) != CPC_OK) continue;
       double t = INFINITY;
       for (int rep = 0; rep < 2; rep++) {
-        if (cpc_count(c, kind, slot_g1, slot_g2, CPC_ENGINE_FAST, stride, 0, &acc) != CPC_OK) break;
+        if (cpc_count(c, kind, slot_g1, slot_g2, CPC_ENGINE_FAST, 1, 0, &acc) != CPC_OK) break;
         t = std::min(t, (double)acc.pair_kernel_ms);
       }
       if (t < best) {
@@ -2216,6 +2337,7 @@ cpc_status cpc_autotune(cpc_ctx *c, cpc_pair_kind kind, int slot_g1, int slot_g2
       }
     }
   }
+  so.restore();
   // keep the best: every box slot on the chosen grid (counts pair slots of one grid)
   c->tune_k = bk;
   c->tune_wpi = bw;
@@ -2272,10 +2394,17 @@ cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_k
     if (job_rule(c0->p, kinds[0], c0->slots[slots_g1[0]].n, c0->slots[slots_g2[0]].n, rule) != 0)
       return fail(ctxs[0], CPC_ERR_INVALID, "bad pair kind");
   }
-  int unit_w = 1;
-  for (int k = 0; k < n_jobs; k++)
-    unit_w &= unit_weights(ctxs[k]->slots[slots_g1[k]], ctxs[k]->slots[slots_g2[k]]);
-  const std::vector<int> ws = tune_windows(ctxs[0]->p, rule.corel, unit_w);
+  int unit_w = 1, twin = 1;
+  for (int k = 0; k < n_jobs; k++) {
+    cpc_ctx *c = ctxs[k];
+    unit_w &= unit_weights(c->slots[slots_g1[k]], c->slots[slots_g2[k]]);
+    JobRule rk;
+    if (job_rule(c->p, kinds[k], c->slots[slots_g1[k]].n, c->slots[slots_g2[k]].n, rk) != 0)
+      return fail(c, CPC_ERR_INVALID, "bad pair kind");
+    const int s1 = rk.swapped ? slots_g2[k] : slots_g1[k], s2 = rk.swapped ? slots_g1[k] : slots_g2[k];
+    twin &= twin_job(c, rk, s1, s2, 1, 0, 0) ? 1 : 0;
+  }
+  const std::vector<int> ws = tune_windows(ctxs[0]->p, rule.corel, unit_w, twin);
   std::vector<std::vector<int64_t>> nums(n_jobs);
   std::vector<std::vector<double>> sums(n_jobs);
   std::vector<cpc_accum> accs(n_jobs);
@@ -2288,7 +2417,17 @@ cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_k
     accs[k].num = nums[k].data();
     accs[k].sums = sums[k].data();
   }
+  // the trials count every sample_stride-th work unit of each context (unit
+  // shards: whole tiles, so each trial's per-unit costs are those of the full
+  // count)
   const int64_t stride = std::max<int64_t>(1, sample_stride);
+  std::vector<std::unique_ptr<ShardOverride>> sos;
+  for (int k = 0; k < n_jobs; k++) {
+    bool seen = false;
+    for (const auto &so : sos) seen = seen || so->c == ctxs[k];
+    if (!seen)
+      sos.emplace_back(new ShardOverride(ctxs[k], 0, (int)std::min<int64_t>(stride, 1 << 30)));
+  }
   // every slot a job reads, on cells r_max / kc
   auto regrid = [&](int kc) -> cpc_status {
     for (int k = 0; k < n_jobs; k++)
@@ -2309,12 +2448,11 @@ cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_k
     for (int w : ws) {
       for (int k = 0; k < n_jobs; k++) ctxs[k]->tune_wpi = w;
       // first run builds the work units, the next two are timed (the faster counts)
-      if (count_batch_rows(n_jobs, ctxs, kinds, slots_g1, slots_g2, accs.data(), stride) != CPC_OK)
+      if (count_batch_rows(n_jobs, ctxs, kinds, slots_g1, slots_g2, accs.data(), 1) != CPC_OK)
         continue;
       double t = INFINITY;
       for (int rep = 0; rep < 2; rep++) {
-        if (count_batch_rows(n_jobs, ctxs, kinds, slots_g1, slots_g2, accs.data(), stride) !=
-            CPC_OK)
+        if (count_batch_rows(n_jobs, ctxs, kinds, slots_g1, slots_g2, accs.data(), 1) != CPC_OK)
           break;
         t = std::min(t, (double)accs[0].pair_kernel_ms);
       }
@@ -2325,6 +2463,7 @@ cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_k
       }
     }
   }
+  sos.clear();  // the contexts' own shards again
   for (int k = 0; k < n_jobs; k++) {
     ctxs[k]->tune_k = bk;
     ctxs[k]->tune_wpi = bw;
@@ -2424,6 +2563,21 @@ cpc_status cpc_graph_stats(const cpc_ctx *c, int64_t *captures, int64_t *replays
   if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
   if (captures) *captures = c->graph_captures;
   if (replays) *replays = c->graph_replays;
+  return CPC_OK;
+}
+
+cpc_status cpc_set_twin(cpc_ctx *c, int enable) try {
+  if (!c) return fail(nullptr, CPC_ERR_INVALID, "null context");
+  if (busy(c)) return CPC_ERR_STATE;
+  c->twin_on = enable ? 1 : 0;
+  return CPC_OK;
+} catch (...) {
+  return host_exception(c);
+}
+
+cpc_status cpc_last_twin(const cpc_ctx *c, int *twin) {
+  if (!c || !twin) return fail(nullptr, CPC_ERR_INVALID, "null argument");
+  *twin = c->last_twin;
   return CPC_OK;
 }
 

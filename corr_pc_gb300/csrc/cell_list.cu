@@ -402,4 +402,29 @@ cudaError_t launch_gather_u8(int64_t n, const uint32_t *perm, const uint8_t *in,
   return cudaGetLastError();
 }
 
+// *differ becomes nonzero when the bytes [0, n) of a and b differ anywhere
+// (4-byte words, then the tail bytes)
+__global__ void bytes_differ_kernel(const uint8_t *__restrict__ a, const uint8_t *__restrict__ b,
+                                    int64_t n, unsigned *__restrict__ differ) {
+  const int64_t nw = n / 4;
+  const uint32_t *wa = reinterpret_cast<const uint32_t *>(a);
+  const uint32_t *wb = reinterpret_cast<const uint32_t *>(b);
+  unsigned d = 0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nw;
+       k += (int64_t)gridDim.x * blockDim.x)
+    d |= wa[k] ^ wb[k];
+  if (blockIdx.x == 0 && threadIdx.x < (unsigned)(n - 4 * nw))
+    d |= a[4 * nw + threadIdx.x] ^ b[4 * nw + threadIdx.x];
+  if (__any_sync(0xffffffffu, d != 0) && (threadIdx.x & 31) == 0) atomicOr(differ, 1u);
+}
+
+cudaError_t launch_bytes_differ(const void *a, const void *b, int64_t n, unsigned *differ,
+                                cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n / 4 + 255) / 256 + 1, 2048);
+  bytes_differ_kernel<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const uint8_t *>(a),
+                                                       static_cast<const uint8_t *>(b), n, differ);
+  return cudaGetLastError();
+}
+
 }  // namespace cpc

@@ -100,6 +100,10 @@ struct JobDev {
   int rmu;                  // coordinates 7: bins of r = |(dx, dy, Pi)| and mu = Pi / r
   int all_exact;            // fast kernel: every window candidate to the FP64 path
                             // (the cell-list FP64 comparison engine)
+  int twin;                 // fast kernel: g1 and g2 hold the same galaxies in the
+                            // same order (a cross term of a catalogue with itself):
+                            // each unordered pair is tested once and adds both
+                            // orders (g1 = i, g2 = j) and (g1 = j, g2 = i)
   int ncx, ncy;
   int64_t row_stride, row_offset;
   // ---- fast-path single precision constants ----

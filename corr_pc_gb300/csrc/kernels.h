@@ -42,6 +42,9 @@ cudaError_t launch_gather(int64_t n, const uint64_t *keys, const uint32_t *perm,
 
 cudaError_t launch_gather_u8(int64_t n, const uint32_t *perm, const uint8_t *in, uint8_t *out,
                              cudaStream_t st);
+// *differ |= 1 when the n bytes at a and b differ (device memory, 4-byte aligned)
+cudaError_t launch_bytes_differ(const void *a, const void *b, int64_t n, unsigned *differ,
+                                cudaStream_t st);
 
 // Checks and derived per-row data of a box catalogue (input order), on the
 // device: the first failing row of each check, the statistics the error bounds
@@ -78,11 +81,13 @@ constexpr int kFastMaxSeg = 256;
 constexpr int kMaxCellsPerRmax = 9;
 // auto_pairs: the launch holds corels1 (auto-pair) jobs, whose rules take
 // another kBatch + 3 kTile ints of shared memory
-size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs, int unit_w);
-size_t fast_static_smem_bytes();
+size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs, int unit_w,
+                       int twin);
+size_t fast_static_smem_bytes(int twin);
 // minb 4 or 3: the register bound (blocks per SM) of the fast kernel; 1: the
-// cell-list FP64 comparison engine (all_exact jobs)
-int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm, int all_exact);
+// cell-list FP64 comparison engine (all_exact jobs).  twin: the twin kernels
+// (density_density and shape_shape jobs whose slots hold the same galaxies)
+int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm, int all_exact, int twin);
 // Fixed-point scales of one fast-kernel launch (kernel parameters, read from
 // the constant bank): field f's terms are rint(v qs[f]), summed back with
 // iqs[f] = 1 / qs[f].  A launch over several jobs takes, per field, the smallest
@@ -92,8 +97,8 @@ struct FastScales {
   float qs[kNF];
   double iqs[kNF];
 };
-cudaError_t launch_fast(int corel, int jk, int minb, const JobDev *jobs, const UnitDesc *units,
-                        int n_units, unsigned int *unit_ctr, QEntry *q,
+cudaError_t launch_fast(int corel, int jk, int minb, int twin, const JobDev *jobs,
+                        const UnitDesc *units, int n_units, unsigned int *unit_ctr, QEntry *q,
                         unsigned long long *qcount, unsigned long long qcap,
                         const FastScales &sc, size_t smem, int grid, int auto_pairs,
                         cudaStream_t st);

@@ -48,9 +48,14 @@ DF_HD float ephi32(float phi, float theta) {  // ephi_calc (calcs.cpp:97-105)
 // fields df_field(C, q); f[q]: float terms of the others (f[0] is set by the
 // caller).  c, s: cos 2theta and sin 2theta of the raw separation; theta the
 // orientation angle (float, for the phi term only); unit_w: every weight is 1.
+// dm, fm (shape_shape estimator 0, when not null): the fields 1, 2, 11 and 12
+// of the same pair in the other order (g2, g1), the only ones that differ when
+// both galaxies carry the same data in either role (the orientation angle and
+// the rotations are those of the pair; the products are symmetric).
 template <int C>
 DF_HD void df_pair_terms(df32 c, df32 s, float theta, const DfGal &g1, const DfGal &g2, int gws,
-                         bool unit_w, df32 *d, float *f) {
+                         bool unit_w, df32 *d, float *f, df32 *dm = nullptr,
+                         float *fm = nullptr) {
   if (C == kDfDK) {  // density_convergence (corels.cpp:79-90): wt kappa of the shape holder
     const df32 z{0.0f, 0.0f};
     if (gws == 1) d[1] = unit_w ? g1.e1 : df_mul(g2.w, g1.e1);
@@ -88,18 +93,36 @@ DF_HD void df_pair_terms(df32 c, df32 s, float theta, const DfGal &g1, const DfG
   df_rotate(c, s, g1.e1, g1.e2, ei0, ei1);  // w_1 * rotated e_1
   df_rotate(c, s, g2.e1, g2.e2, ej0, ej1);  // w_2 * rotated e_2
   if (C == kDfSS) {  // estimator 0: e+ and the phi term of the shape holder; ex stays 0
+    // the shape holder's terms for the holder in role 2 (g2) and in role 1 (g1);
+    // the other order (g2, g1) swaps them
+    const df32 e_of2 = unit_w ? ej0 : df_mul(g1.w, ej0), e_of1 = unit_w ? ei0 : df_mul(g2.w, ei0);
+    const float t_of2 = ephi32(g2.phi, theta), t_of1 = ephi32(g1.phi, theta);
     if (gws == 2) {
-      d[1] = unit_w ? ej0 : df_mul(g1.w, ej0);
-      f[11] = ephi32(g2.phi, theta);
+      d[1] = e_of2;
+      f[11] = t_of2;
     } else if (gws == 1) {
-      d[1] = unit_w ? ei0 : df_mul(g2.w, ei0);
-      f[11] = ephi32(g1.phi, theta);
+      d[1] = e_of1;
+      f[11] = t_of1;
     } else {
       d[1] = df32{0.0f, 0.0f};
       f[11] = 0.0f;
     }
     f[2] = d[1].h * d[1].h;
     f[12] = f[11] * f[11];
+    if (dm) {
+      if (gws == 2) {
+        dm[1] = e_of1;
+        fm[11] = t_of1;
+      } else if (gws == 1) {
+        dm[1] = e_of2;
+        fm[11] = t_of2;
+      } else {
+        dm[1] = df32{0.0f, 0.0f};
+        fm[11] = 0.0f;
+      }
+      fm[2] = dm[1].h * dm[1].h;
+      fm[12] = fm[11] * fm[11];
+    }
   } else {  // the other estimators: the pair's mean e+ and ex, both phi terms
     const df32 pa = unit_w ? ei0 : df_mul(g2.w, ei0), pb = unit_w ? ej0 : df_mul(g1.w, ej0);
     const df32 qa = unit_w ? ei1 : df_mul(g2.w, ei1), qb = unit_w ? ej1 : df_mul(g1.w, ej1);

@@ -56,15 +56,22 @@ constexpr int kMaxCols = kFastMaxCols;
 constexpr int kChunk = 4 * kThreads;
 
 // Per corel: the main fields m(k), k < FM, the jackknife fields j(g), g < FJ, and
-// jm(g), the main slot holding jackknife field g (m(jm(g)) == j(g)).
+// jm(g), the main slot holding jackknife field g (m(jm(g)) == j(g)).  FA, a(i):
+// the main slots whose terms differ between the two orders of a pair whose
+// galaxies carry the same data in either role (twin jobs); the others are the
+// same in both orders.  Twin jobs run the corels with FA = 0 and shape_shape.
+struct NoAsym {
+  static constexpr int FA = 0;
+  __host__ __device__ static constexpr int a(int) { return -1; }
+};
 template <int C> struct FieldMap;
-template <> struct FieldMap<COREL_DD> {
+template <> struct FieldMap<COREL_DD> : NoAsym {
   static constexpr int FM = 1, FJ = 1;
   __host__ __device__ static constexpr int m(int) { return 0; }
   __host__ __device__ static constexpr int j(int) { return 0; }
   __host__ __device__ static constexpr int jm(int) { return 0; }
 };
-template <> struct FieldMap<COREL_SD> {
+template <> struct FieldMap<COREL_SD> : NoAsym {
   static constexpr int FM = 7, FJ = 4;
   __host__ __device__ static constexpr int m(int k) {
     return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 2 : k == 3 ? 3 : k == 4 ? 4 : k == 5 ? 11 : 12;
@@ -77,29 +84,33 @@ template <> struct FieldMap<COREL_SS> {
   __host__ __device__ static constexpr int m(int k) { return k < 2 ? k : k == 2 ? 2 : k + 2; }
   __host__ __device__ static constexpr int j(int k) { return k == 0 ? 0 : 2 * k - 1 + (k >= 2 ? 2 : 0); }
   __host__ __device__ static constexpr int jm(int g) { return g == 0 ? 0 : 2 * g - 1; }
+  // estimator 0: e+ of the shape holder (data[1]) and its square, the phi term
+  // (data[6]) and its square: fields 1, 2, 11, 12
+  static constexpr int FA = 4;
+  __host__ __device__ static constexpr int a(int i) { return i == 0 ? 1 : i == 1 ? 2 : i == 2 ? 9 : 10; }
 };
-template <> struct FieldMap<COREL_SSA> {
+template <> struct FieldMap<COREL_SSA> : NoAsym {
   static constexpr int FM = 13, FJ = 7;
   __host__ __device__ static constexpr int m(int k) { return k; }
   __host__ __device__ static constexpr int j(int k) { return k == 0 ? 0 : 2 * k - 1; }
   __host__ __device__ static constexpr int jm(int g) { return g == 0 ? 0 : 2 * g - 1; }
 };
 // density_convergence: wt, data[1].val
-template <> struct FieldMap<COREL_DK> {
+template <> struct FieldMap<COREL_DK> : NoAsym {
   static constexpr int FM = 2, FJ = 2;
   __host__ __device__ static constexpr int m(int k) { return k; }
   __host__ __device__ static constexpr int j(int k) { return k; }
   __host__ __device__ static constexpr int jm(int g) { return g; }
 };
 // shape_convergence: wt, data[1].val, data[3].val, data[5].val
-template <> struct FieldMap<COREL_SK> {
+template <> struct FieldMap<COREL_SK> : NoAsym {
   static constexpr int FM = 4, FJ = 4;
   __host__ __device__ static constexpr int m(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 5 : 9; }
   __host__ __device__ static constexpr int j(int k) { return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 5 : 9; }
   __host__ __device__ static constexpr int jm(int g) { return g; }
 };
 // ED: wt, data[6].val, data[6].err (regions: wt, data[6].val)
-template <> struct FieldMap<COREL_ED> {
+template <> struct FieldMap<COREL_ED> : NoAsym {
   static constexpr int FM = 3, FJ = 2;
   __host__ __device__ static constexpr int m(int k) { return k == 0 ? 0 : k == 1 ? 11 : 12; }
   __host__ __device__ static constexpr int j(int k) { return k == 0 ? 0 : 11; }
@@ -114,6 +125,18 @@ constexpr bool jm_consistent() {
     return FM::m(FM::jm(G)) == FM::j(G) && jm_consistent<FM, G + 1>();
   }
 }
+// position of main slot k among the order-dependent slots a(i), or -1
+template <class FM>
+__host__ __device__ constexpr int asym_pos(int k) {
+  for (int i = 0; i < FM::FA; i++)
+    if (FM::a(i) == k) return i;
+  return -1;
+}
+static_assert(FieldMap<COREL_SS>::m(FieldMap<COREL_SS>::a(0)) == 1 &&
+                  FieldMap<COREL_SS>::m(FieldMap<COREL_SS>::a(1)) == 2 &&
+                  FieldMap<COREL_SS>::m(FieldMap<COREL_SS>::a(2)) == 11 &&
+                  FieldMap<COREL_SS>::m(FieldMap<COREL_SS>::a(3)) == 12,
+              "order-dependent shape_shape fields");
 static_assert(jm_consistent<FieldMap<COREL_DD>>() && jm_consistent<FieldMap<COREL_SD>>() &&
                   jm_consistent<FieldMap<COREL_SS>>() && jm_consistent<FieldMap<COREL_SSA>>() &&
                   jm_consistent<FieldMap<COREL_DK>>() && jm_consistent<FieldMap<COREL_SK>>() &&
@@ -168,8 +191,10 @@ constexpr size_t kAutoBytes = sizeof(int) * (kBatch + 3 * kTile);
 
 // Shared-memory bytes a block needs for a job with nrp r_p bins and a wpi-bin
 // Pi window.  With unit weights (unit_w) field 0 (the weight sum, equal to the
-// count) is not accumulated and has no words.
-size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs, int unit_w) {
+// count) is not accumulated and has no words.  A twin job adds the other
+// order's order-dependent main fields and its two region histograms.
+size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs, int unit_w,
+                       int twin) {
   const int NB = nrp * wpi, NBm = main_bins(nrp, wpi);
   int FM = 1, FJ = 1;
   if (corel == COREL_SD) { FM = 7; FJ = 4; }
@@ -178,12 +203,17 @@ size_t fast_smem_bytes(int corel, int do_jk, int nrp, int wpi, int auto_pairs, i
   if (corel == COREL_DK) { FM = 2; FJ = 2; }
   if (corel == COREL_SK) { FM = 4; FJ = 4; }
   if (corel == COREL_ED) { FM = 3; FJ = 2; }
+  const int FA = corel == COREL_SS ? FieldMap<COREL_SS>::FA : 0;
   const int f0 = unit_w ? 1 : 0;
   FM -= f0;
   FJ -= f0;
   size_t b = stage_bytes(corel) + (auto_pairs ? kAutoBytes : 0);  // staging
   b += 8ull * FM * NBm + 4ull * NBm + 4ull * hi_pad(FM * NBm);
   if (do_jk) b += 2 * (8ull * FJ * NB + 4ull * NB + 4ull * hi_pad(FJ * NB));
+  if (twin) {
+    b += 8ull * FA * NB + 4ull * hi_pad(FA * NB);
+    if (do_jk) b += 2 * (8ull * FJ * NB + 4ull * NB + 4ull * hi_pad(FJ * NB));
+  }
   return b;
 }
 
@@ -262,16 +292,19 @@ __device__ __forceinline__ float ephi_f(float phi, float theta) {
 }
 
 // Flush the partner-region histogram (jackknife fields) into the global FP64
-// block at histogram index h, and zero it.
+// block at histogram index h, and zero it.  mirror: the histogram holds the
+// other order of twin pairs, whose Pi bin is npi - 1 - (the window's bin).
 template <class FMAP>
 __device__ __forceinline__ void flush_region(unsigned *cnt, unsigned *lo, unsigned *hi, int NB,
                                              int wpi, int npi, int nrp, int n2_base, int h, int f0,
-                                             const double *s_iqs, const JobDev &J) {
+                                             const double *s_iqs, const JobDev &J,
+                                             bool mirror = false) {
   const int64_t hb = (int64_t)h * nrp * npi;
   for (int lb = threadIdx.x; lb < NB; lb += kThreads) {
     const unsigned n = cnt[lb];
     if (!n) continue;
-    const int64_t cell = hb + (int64_t)(lb / wpi) * npi + n2_base + lb % wpi;
+    const int n2 = n2_base + lb % wpi;
+    const int64_t cell = hb + (int64_t)(lb / wpi) * npi + (mirror ? npi - 1 - n2 : n2);
     atomicAdd(&J.acc_num[cell], (unsigned long long)n);
     cnt[lb] = 0u;
 #pragma unroll
@@ -287,18 +320,33 @@ __device__ __forceinline__ void flush_region(unsigned *cnt, unsigned *lo, unsign
   }
 }
 
+// The histograms of the other order of twin pairs (a twin job's block): its
+// order-dependent main fields (FA words per bin, low and high) and its two
+// region histograms (the tile's region: the pairs it does not take; the
+// partner's region), all indexed by the window bin of the pair's own order.
+struct TwinHist {
+  bool on;
+  unsigned *alo, *ahi;              // order-dependent main fields [FA][NB]
+  unsigned *ncnt, *nlo, *nhi;       // tile's region, pairs it does not take
+  unsigned *ycnt, *ylo, *yhi;       // partner's region
+};
+
 // Flush the main histogram (into h = 0) and the tile's region (into hx): the
 // region takes main minus NX, in exact integer arithmetic; zero both.
 // Main bins are strided by NBm (main_bins: the hot bins' copies after the NB
-// plain bins); the copies of a hot bin are summed into it.
+// plain bins); the copies of a hot bin are summed into it.  Twin blocks also
+// add the other order of each bin's pairs to the mirrored Pi bin
+// npi - 1 - n2: the same count and order-independent sums, its own
+// order-dependent sums, and its own tile-region exclusions.
 template <int FM, int FJ, class FMAP>
 __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsigned *mhi,
                                              unsigned *ncnt, unsigned *nlo, unsigned *nhi, int NB,
                                              int NBm, int wpi, int npi, int nrp, int n2_base,
                                              int hx, bool jk, int f0, const double *s_iqs,
-                                             const JobDev &J) {
+                                             const JobDev &J, const TwinHist &tw) {
   const int64_t hsz = (int64_t)nrp * npi;
   const int hot0 = nrp - hot_rows(nrp);
+  constexpr int FA = FMAP::FA > 0 ? FMAP::FA : 1;
   for (int lb = threadIdx.x; lb < NB; lb += kThreads) {
     const int n1 = lb / wpi, elk = lb - n1 * wpi;
     const int nrep = (kHotRep > 1 && n1 >= hot0) ? kHotRep : 1;
@@ -323,6 +371,26 @@ __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsi
       const int fld = FMAP::m(f);
       if (tm[f] != 0) atomicAdd(&J.acc_sums[cell * kNF + fld], (double)tm[f] * s_iqs[fld]);
     }
+    long long ta[FA];
+    const int64_t cm = (int64_t)n1 * npi + (npi - 1 - (n2_base + elk));
+    if (tw.on) {
+      atomicAdd(&J.acc_num[cm], (unsigned long long)n);
+#pragma unroll
+      for (int i = 0; i < FMAP::FA; i++) {
+        const size_t o = (size_t)i * NB + lb;
+        ta[i] = (long long)(int)tw.ahi[o] * 32768ll + (long long)tw.alo[o];
+        tw.alo[o] = 0u;
+        tw.ahi[o] = 0u;
+      }
+#pragma unroll
+      for (int f = 0; f < FM; f++) {
+        if (f < f0) continue;
+        const int ap = asym_pos<FMAP>(f);
+        const long long v = ap >= 0 ? ta[ap] : tm[f];
+        const int fld = FMAP::m(f);
+        if (v != 0) atomicAdd(&J.acc_sums[cm * kNF + fld], (double)v * s_iqs[fld]);
+      }
+    }
     if (!jk) continue;
     const int64_t xc = (int64_t)hx * hsz + cell;
     const unsigned nx = ncnt[lb];
@@ -339,6 +407,23 @@ __device__ __forceinline__ void flush_main_x(unsigned *mcnt, unsigned *mlo, unsi
       const int fld = FMAP::j(g);
       if (tx != 0) atomicAdd(&J.acc_sums[xc * kNF + fld], (double)tx * s_iqs[fld]);
     }
+    if (!tw.on) continue;
+    const int64_t xm = (int64_t)hx * hsz + cm;
+    const unsigned nxm = tw.ncnt[lb];
+    tw.ncnt[lb] = 0u;
+    if (n - nxm) atomicAdd(&J.acc_num[xm], (unsigned long long)(n - nxm));
+#pragma unroll
+    for (int g = 0; g < FJ; g++) {
+      if (g < f0) continue;
+      const size_t o = (size_t)g * NB + lb;
+      const long long tn = (long long)(int)tw.nhi[o] * 32768ll + (long long)tw.nlo[o];
+      tw.nlo[o] = 0u;
+      tw.nhi[o] = 0u;
+      const int ap = asym_pos<FMAP>(FMAP::jm(g));
+      const long long tx = (ap >= 0 ? ta[ap] : tm[FMAP::jm(g)]) - tn;
+      const int fld = FMAP::j(g);
+      if (tx != 0) atomicAdd(&J.acc_sums[xm * kNF + fld], (double)tx * s_iqs[fld]);
+    }
   }
 }
 
@@ -346,8 +431,10 @@ constexpr int kQCap = 64;  // per-warp ring of binned pairs awaiting the heavy s
 constexpr unsigned kEdgeFlag = 0x8000u;  // queue entry: near the window edge
 
 // MINB: blocks per SM the registers are bounded for (4 when the job's
-// histograms fit a quarter of shared memory, else 3)
-template <int C, bool JK, int MINB>
+// histograms fit a quarter of shared memory, else 3).  TW: twin jobs (every job
+// of the launch), compiled apart so that the other jobs' kernel carries none of
+// the twin code.
+template <int C, bool JK, int MINB, bool TW>
 __global__ void __launch_bounds__(kThreads, MINB == 1 ? 2 : MINB)
 fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ units,
                   int n_units, unsigned int *__restrict__ unit_ctr, QEntry *__restrict__ queue,
@@ -380,6 +467,9 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   __shared__ int s_order[kMaxSeg], s_pre[kMaxSeg + 1];
   __shared__ int s_jidx[kBatch];
   __shared__ unsigned char s_keep[kBatch];
+  // twin jobs: the other role's keep flag of each staged candidate (g1's) and of
+  // each tile row (g2's)
+  __shared__ unsigned char s_keep2[TW ? kBatch : 1];
   __shared__ unsigned long long s_red[kThreads / 32];
   __shared__ unsigned s_nbin;  // pairs queued by the block's warps since the last flush
   __shared__ float s_A[kMaxRp], s_B[kMaxRp], s_PA[kMaxPi], s_PB[kMaxPi];
@@ -387,7 +477,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
   // s_rshp / s_shp hold the weighted ellipticities (ewt) for the corels with
   // shape terms and the orientation (shp) for ED
   __shared__ float4 s_rpos[kTile], s_rshp[kTile], s_raux[kTile];
-  __shared__ unsigned char s_rkeep[kTile];
+  __shared__ unsigned char s_rkeep[kTile], s_rkeep2[TW ? kTile : 1];
   __shared__ unsigned s_wq[kThreads / 32][kQCap];
 
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
@@ -429,6 +519,26 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     unsigned *s_mlo = s_mlo0 - (size_t)f0 * NBm, *s_mhi = s_mhi0 - (size_t)f0 * NBm;
     unsigned *s_nxlo = s_nxlo0 - (size_t)f0 * NB, *s_nxhi = s_nxhi0 - (size_t)f0 * NB;
     unsigned *s_ylo = s_ylo0 - (size_t)f0 * NB, *s_yhi = s_yhi0 - (size_t)f0 * NB;
+    // twin jobs: the other order's histograms after the region histograms
+    constexpr bool twin = TW;
+    constexpr int FA = F::FA;
+    TwinHist tw;
+    {
+      unsigned *base = JK ? s_yhi0 + (size_t)FJs * NB : s_nxnum;
+      tw.on = twin;
+      tw.alo = base;
+      tw.ahi = tw.alo + (size_t)FA * NB + hi_pad(FA * NB);
+      tw.ncnt = tw.ahi + (size_t)FA * NB;
+      unsigned *nlo0 = tw.ncnt + NB;
+      unsigned *nhi0 = nlo0 + (size_t)FJs * NB + hi_pad(FJs * NB);
+      tw.ycnt = nhi0 + (size_t)FJs * NB;
+      unsigned *ylo0 = tw.ycnt + NB;
+      unsigned *yhi0 = ylo0 + (size_t)FJs * NB + hi_pad(FJs * NB);
+      tw.nlo = nlo0 - (size_t)f0 * NB;
+      tw.nhi = nhi0 - (size_t)f0 * NB;
+      tw.ylo = ylo0 - (size_t)f0 * NB;
+      tw.yhi = yhi0 - (size_t)f0 * NB;
+    }
 
     // ---- the tile's g1 rows, in shared memory.  Row slot tr = s * 32 + l holds
     // tile row q = l * W + s (s < W): a warp holds slots s * 32 .. s * 32 + 31 in
@@ -472,6 +582,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         }
         if (C == COREL_ED && has_lo) s_rzlo[tr] = J.f1.zlo[i1];
         if (JK) s_rkeep[tr] = J.f1.keep[i1];
+        if (JK && TW) s_rkeep2[tr] = J.f2.keep[i1];
       }
       // a row that is not counted gets z = NaN: every window test fails
       if (!ok) p.z = __int_as_float(0x7fc00000);
@@ -595,6 +706,15 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
         int sx, sy, sz;
         shift_decode(code, sx, sy, sz);
         const bool same_region = region2 == U.region;
+        // twin jobs test each unordered pair once, in the order whose g2 is
+        // ahead of g1: z image +1, or image 0 with a larger z (ties: the image
+        // shift in y, then x, then the index).  Image -1 candidates are the
+        // other order of image +1 pairs of their own tiles.
+        if (twin && sz < 0) {
+          k = g;
+          continue;
+        }
+        const int tie_dir = sy != 0 ? sy : sx;  // z ties within image 0
         // staging order: position (i * ks) mod N over the group's N candidates,
         // ks coprime with N and ~0.618 N, so a batch is a spread-out sample of
         // the group's columns and z range (decorrelated bins, fewer collisions)
@@ -609,6 +729,9 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             __syncthreads();
             flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
                                        1 + cur_y, f0, sc.iqs, J);
+            if (twin)
+              flush_region<F>(tw.ycnt, tw.ylo, tw.yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y, f0,
+                              sc.iqs, J, true);
             __syncthreads();
           }
           cur_y = region2;
@@ -625,10 +748,14 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             __syncthreads();
             flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_nxnum, s_nxlo, s_nxhi, NB, NBm,
                                           wpi, npi, nrp, n2_base, 1 + U.region, JK, f0, sc.iqs,
-                                          J);
-            if (JK && cur_y >= 0)
+                                          J, tw);
+            if (JK && cur_y >= 0) {
               flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base,
                                          1 + cur_y, f0, sc.iqs, J);
+              if (twin)
+                flush_region<F>(tw.ycnt, tw.ylo, tw.yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y,
+                                f0, sc.iqs, J, true);
+            }
             if (t == 0) s_nbin = 0u;
             __syncthreads();
           }
@@ -665,6 +792,7 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
             s_jidx[t] = j2;
             if (auto_smem && J.auto_mode) s_orig[t] = (int)J.d2.orig[j2];
             if (JK) s_keep[t] = J.f2.keep[j2];
+            if (JK && twin) s_keep2[t] = J.f1.keep[j2];
           }
           __syncwarp();
 
@@ -699,14 +827,29 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
               const float dy = y1s - p2.y;
               const float m = fmaxf(fabsf(dx), fabsf(dy));
               bool binned = false, edge = false;
-              if ((othr < 0 || s_orig[c] > othr) && dz >= pi_out_lo &&
+              // twin jobs, image 0: the order with g2 ahead of g1 (the sign of a
+              // float difference is exact); a pair of a row with itself counts once
+              bool canon = true, tself = false;
+              if (twin && sz == 0 && !(dz > 0.0f)) {
+                canon = false;
+                if (dz == 0.0f) {
+                  if (tie_dir > 0) {
+                    canon = true;
+                  } else if (tie_dir == 0) {
+                    const int gi = U.g1_start + (lane * W + pass) * U.g1_stride;
+                    canon = s_jidx[c] >= gi;
+                    tself = s_jidx[c] == gi;
+                  }
+                }
+              }
+              if (canon && (othr < 0 || s_orig[c] > othr) && dz >= pi_out_lo &&
                   dz <= pi_out_hi && m <= xy_out) {
                 if (all_exact || !(dz >= pi_in_lo && dz <= pi_in_hi && m <= xy_in)) {
                   // near the window edge: queued with a flag, the heavy step hands
                   // it to the exact FP64 evaluation of the whole pair
                   edge = true;
                 } else {
-                  nwin++;
+                  nwin += (twin && !tself) ? 2u : 1u;
                   // r_p^2, or r^2 = r_p^2 + dz^2 for coordinates 7
                   float r2 = fmaf(dx, dx, dy * dy);
                   if (rmu) r2 = fmaf(dz, dz, r2);
@@ -820,6 +963,14 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                 see = fmaf(sxe, sxe, fmaf(sye, sye, sze * sze));
                 if (!(see > 0.0f)) amb = true;
               }
+              // twin jobs: a row paired with itself has no other order; it takes
+              // the exact path (its count is not mirrored)
+              bool tself = false;
+              if (twin && sx == 0 && sy == 0 && sz == 0 && hdz == 0.0f) {
+                const int gi = U.g1_start + (((er & 31) * W) + (er >> 5)) * U.g1_stride;
+                tself = s_jidx[ec] == gi;
+                if (tself) amb = true;
+              }
               if (all_exact) {
                 // the comparison engine: the reference's double arithmetic for
                 // every candidate (window, bins, values), global FP64 atomics.
@@ -846,12 +997,23 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                                     (int64_t)(((er & 31) * W) + (er >> 5)) * U.g1_stride;
                 enqueue(U.job, gi1, s_jidx[ec], edge ? code : (code | kWindowCounted), queue,
                         qcount, qcap);
+                // twin jobs: the other order, (g1 = the candidate, g2 = the row)
+                // at the opposite image
+                if (twin && !tself) {
+                  const int mcode = shift_code(-sx, -sy, -sz);
+                  enqueue(U.job, s_jidx[ec], gi1, edge ? mcode : (mcode | kWindowCounted), queue,
+                          qcount, qcap);
+                }
               } else {
               const int lb = n1 * wpi + elk;
               // per-field terms: v (float) for every field, vd (double-float)
               // for the fields whose sums cancel (df_field)
               float v[kNF];
               df32 vd[kNF];
+              // twin jobs: the other order's order-dependent terms (shape_shape)
+              constexpr bool kMir = F::FA > 0;
+              float vm[kMir ? kNF : 1];
+              df32 vdm[kMir ? kNF : 1];
               const float w = r1.w * p2.w;
               v[0] = w;
               if (C == COREL_ED) {
@@ -871,7 +1033,11 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                   df_cos_sin_2theta(dxr, dyr, c2, s2v);
                   if (C != COREL_SK) theta = atanf(__fdividef(dyr.h, dxr.h));
                 }
-                df_pair_terms<C>(c2, s2v, theta, g1, g2, gws, J.unit_w != 0, vd, v);
+                if constexpr (kMir)
+                  df_pair_terms<C>(c2, s2v, theta, g1, g2, gws, J.unit_w != 0, vd, v,
+                                   twin ? vdm : nullptr, twin ? vm : nullptr);
+                else
+                  df_pair_terms<C>(c2, s2v, theta, g1, g2, gws, J.unit_w != 0, vd, v);
               }
               // fixed-point words of the main fields, in this lane's order (even
               // lanes low word first, odd lanes high word first: red_pair); the
@@ -920,6 +1086,53 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
                                wa[F::jm(g)], wb[F::jm(g)], odd_lane);
                 }
               }
+              if (twin) {
+                // the other order (g1 = the candidate, g2 = the row): the same bin
+                // count and order-independent terms (added at the flush), its
+                // order-dependent terms here, and its own region attribution:
+                // the tile's region takes it when the row is kept in the g2 role,
+                // the partner's region when the candidate is kept in the g1 role
+                unsigned xa[kMir ? F::FA : 1], xb[kMir ? F::FA : 1];
+                if constexpr (kMir) {
+#pragma unroll
+                  for (int i = 0; i < F::FA; i++) {
+                    const int q = F::m(F::a(i));
+                    unsigned lo15, hi;
+                    if (df_field(C, q)) df_to_fixed15(vdm[q], sc.qs[q], lo15, hi);
+                    else f_to_fixed15(vm[q], sc.qs[q], lo15, hi);
+                    xa[i] = odd_lane ? hi : lo15;
+                    xb[i] = odd_lane ? lo15 : hi;
+                    red_pair(&tw.alo[(size_t)i * NB + lb], &tw.ahi[(size_t)i * NB + lb], xa[i],
+                             xb[i], odd_lane);
+                  }
+                }
+                if (JK) {
+                  const bool nxm = !same_region && !s_rkeep2[er];
+                  const bool ym = !same_region && s_keep2[ec];
+                  if (nxm) {
+                    atomicAdd(&tw.ncnt[lb], 1u);
+#pragma unroll
+                    for (int g = 0; g < F::FJ; g++) {
+                      if (g < f0) continue;
+                      const int ap = asym_pos<F>(F::jm(g));
+                      red_pair(&tw.nlo[(size_t)g * NB + lb], &tw.nhi[(size_t)g * NB + lb],
+                               ap >= 0 ? xa[ap] : wa[F::jm(g)], ap >= 0 ? xb[ap] : wb[F::jm(g)],
+                               odd_lane);
+                    }
+                  }
+                  if (ym) {
+                    atomicAdd(&tw.ycnt[lb], 1u);
+#pragma unroll
+                    for (int g = 0; g < F::FJ; g++) {
+                      if (g < f0) continue;
+                      const int ap = asym_pos<F>(F::jm(g));
+                      red_pair(&tw.ylo[(size_t)g * NB + lb], &tw.yhi[(size_t)g * NB + lb],
+                               ap >= 0 ? xa[ap] : wa[F::jm(g)], ap >= 0 ? xb[ap] : wb[F::jm(g)],
+                               odd_lane);
+                    }
+                  }
+                }
+              }
               }
             }
             qhead += take;
@@ -943,10 +1156,14 @@ fast_pairs_kernel(const JobDev *__restrict__ jobs, const UnitDesc *__restrict__ 
     // ---- flush main, X and the last Y ----
     __syncthreads();
     flush_main_x<F::FM, F::FJ, F>(s_mnum, s_mlo, s_mhi, s_nxnum, s_nxlo, s_nxhi, NB, NBm, wpi, npi,
-                                  nrp, n2_base, 1 + U.region, JK, f0, sc.iqs, J);
-    if (JK && cur_y >= 0)
+                                  nrp, n2_base, 1 + U.region, JK, f0, sc.iqs, J, tw);
+    if (JK && cur_y >= 0) {
       flush_region<F>(s_ynum, s_ylo, s_yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y, f0,
                                  sc.iqs, J);
+      if (twin)
+        flush_region<F>(tw.ycnt, tw.ylo, tw.yhi, NB, wpi, npi, nrp, n2_base, 1 + cur_y, f0,
+                        sc.iqs, J, true);
+    }
     if (t == 0) s_nbin = 0u;
     // window-pair counter (once per pair: mu slices other than the first skip it)
     {
@@ -990,13 +1207,30 @@ __global__ void recheck_kernel(const JobDev *__restrict__ jobs, const QEntry *__
 // ---- host-side launchers (called from capi.cu) ----
 // Calls fn.run<C, JK, MINB>() for the runtime corel, jackknife flag and bound.
 template <class Fn>
-static auto dispatch(int corel, int jk, int minb, const Fn &fn) -> decltype(fn.template run<0, false, 3>()) {
+static auto dispatch(int corel, int jk, int minb, int twin, const Fn &fn)
+    -> decltype(fn.template run<0, false, 3, false>()) {
+  // twin jobs: density_density and shape_shape, 4 or 3 blocks per SM
+#define CPC_TCASE(CC)                                                                 \
+  if (corel == CC) {                                                                  \
+    if (jk) return minb == 4 ? fn.template run<CC, true, 4, true>()                  \
+                             : fn.template run<CC, true, 3, true>();                  \
+    return minb == 4 ? fn.template run<CC, false, 4, true>()                          \
+                     : fn.template run<CC, false, 3, true>();                         \
+  }
+  if (twin && minb != 1) {
+    CPC_TCASE(COREL_DD)
+    CPC_TCASE(COREL_SS)
+    CPC_TCASE(COREL_SSA)
+  }
+#undef CPC_TCASE
 #define CPC_CASE(CC)                                                                  \
   if (corel == CC) {                                                                  \
-    if (jk) return minb == 4 ? fn.template run<CC, true, 4>()                        \
-                  : minb == 1 ? fn.template run<CC, true, 1>() : fn.template run<CC, true, 3>(); \
-    return minb == 4 ? fn.template run<CC, false, 4>()                                \
-           : minb == 1 ? fn.template run<CC, false, 1>() : fn.template run<CC, false, 3>();      \
+    if (jk) return minb == 4 ? fn.template run<CC, true, 4, false>()                 \
+                  : minb == 1 ? fn.template run<CC, true, 1, false>()                 \
+                              : fn.template run<CC, true, 3, false>();                \
+    return minb == 4 ? fn.template run<CC, false, 4, false>()                         \
+           : minb == 1 ? fn.template run<CC, false, 1, false>()                       \
+                       : fn.template run<CC, false, 3, false>();                      \
   }
   CPC_CASE(COREL_DD)
   CPC_CASE(COREL_SD)
@@ -1006,7 +1240,7 @@ static auto dispatch(int corel, int jk, int minb, const Fn &fn) -> decltype(fn.t
   CPC_CASE(COREL_SK)
   CPC_CASE(COREL_ED)
 #undef CPC_CASE
-  return fn.template run<COREL_DD, false, 3>();  // unreachable for valid corels
+  return fn.template run<COREL_DD, false, 3, false>();  // unreachable for valid corels
 }
 
 struct LaunchFast {
@@ -1021,9 +1255,9 @@ struct LaunchFast {
   int grid;
   int auto_pairs;
   cudaStream_t st;
-  template <int C, bool JK, int MINB>
+  template <int C, bool JK, int MINB, bool TW>
   cudaError_t run() const {
-    auto kern = fast_pairs_kernel<C, JK, MINB>;
+    auto kern = fast_pairs_kernel<C, JK, MINB, TW>;
     cudaError_t err =
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
@@ -1037,9 +1271,9 @@ struct LaunchFast {
 
 struct Occupancy {
   size_t smem;
-  template <int C, bool JK, int MINB>
+  template <int C, bool JK, int MINB, bool TW>
   int run() const {
-    auto kern = fast_pairs_kernel<C, JK, MINB>;
+    auto kern = fast_pairs_kernel<C, JK, MINB, TW>;
     int nb = 0;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess ||
@@ -1049,28 +1283,28 @@ struct Occupancy {
   }
 };
 
-cudaError_t launch_fast(int corel, int jk, int minb, const JobDev *jobs, const UnitDesc *units,
-                        int n_units, unsigned int *unit_ctr, QEntry *q,
+cudaError_t launch_fast(int corel, int jk, int minb, int twin, const JobDev *jobs,
+                        const UnitDesc *units, int n_units, unsigned int *unit_ctr, QEntry *q,
                         unsigned long long *qcount, unsigned long long qcap,
                         const FastScales &sc, size_t smem, int grid, int auto_pairs,
                         cudaStream_t st) {
   if (corel < COREL_DD || corel > COREL_ED) return cudaErrorInvalidValue;
-  return dispatch(corel, jk, minb,
+  return dispatch(corel, jk, minb, twin,
                   LaunchFast{jobs, units, n_units, unit_ctr, q, qcount, qcap, &sc, smem, grid,
                              auto_pairs, st});
 }
 
 // The register-bound variant for this shared-memory size and its blocks per SM:
 // the 4-block variant when 4 blocks fit, else the 3-block one.
-int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm, int all_exact) {
+int fast_variant(int corel, int jk, size_t smem, int *blocks_per_sm, int all_exact, int twin) {
   if (corel < COREL_DD || corel > COREL_ED) { *blocks_per_sm = 0; return 3; }
   if (all_exact) {  // the cell-list FP64 comparison engine
-    *blocks_per_sm = dispatch(corel, jk, 1, Occupancy{smem});
+    *blocks_per_sm = dispatch(corel, jk, 1, 0, Occupancy{smem});
     return 1;
   }
-  const int b4 = dispatch(corel, jk, 4, Occupancy{smem});
+  const int b4 = dispatch(corel, jk, 4, twin, Occupancy{smem});
   if (b4 >= 4) { *blocks_per_sm = b4; return 4; }
-  *blocks_per_sm = dispatch(corel, jk, 3, Occupancy{smem});
+  *blocks_per_sm = dispatch(corel, jk, 3, twin, Occupancy{smem});
   return 3;
 }
 
@@ -1083,9 +1317,11 @@ cudaError_t launch_recheck(const JobDev *jobs, const QEntry *q, const unsigned l
 }  // namespace cpc
 
 namespace cpc {
-size_t fast_static_smem_bytes() {
+size_t fast_static_smem_bytes(int twin) {
   cudaFuncAttributes a;
-  if (cudaFuncGetAttributes(&a, fast_pairs_kernel<COREL_SS, true, 4>) != cudaSuccess) return 24 * 1024;
+  const cudaError_t e = twin ? cudaFuncGetAttributes(&a, fast_pairs_kernel<COREL_SS, true, 4, true>)
+                             : cudaFuncGetAttributes(&a, fast_pairs_kernel<COREL_SS, true, 4, false>);
+  if (e != cudaSuccess) return 24 * 1024;
   return a.sharedSizeBytes;
 }
 }  // namespace cpc

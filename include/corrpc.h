@@ -208,8 +208,10 @@ cpc_status cpc_count_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind
  * per block (0 or 128). */
 cpc_status cpc_set_tuning(cpc_ctx *ctx, int cells_per_rmax, int pi_window, int tile);
 
-/* Autotuner: times the fast kernel on every `sample_stride`-th outer row of
- * this pair type for cell widths r_max / k (k = 2 .. 6; the cell lists are
+/* Autotuner: times the fast kernel on every `sample_stride`-th work unit (a
+ * unit shard: whole tiles of outer rows, so per-unit costs are those of the
+ * full count; twin counts run as twins) of this pair type, the faster of two
+ * timed runs per candidate, for cell widths r_max / k (k = 2 .. 6; the cell lists are
  * rebuilt on the device) and block-local Pi windows (for 4, 3 and 2 blocks per
  * SM, the largest window that fits and three quarters of it), keeps the
  * fastest for this context (as cpc_set_tuning would) and returns it.  Results
@@ -221,7 +223,7 @@ cpc_status cpc_autotune(cpc_ctx *ctx, cpc_pair_kind kind, int slot_g1, int slot_
 
 /* Autotuner of a batch (the jobs of cpc_count_batch, box runs with one binning
  * and which_corr): the same cell widths and Pi windows, each trial one batched
- * launch over every `sample_stride`-th outer row of every job; the fastest is
+ * launch over every `sample_stride`-th work unit of every job; the fastest is
  * kept for every context of the batch and returned.  No counterpart in the
  * reference (its sub-boxes are separate runs, corr.cpp:219). */
 cpc_status cpc_autotune_batch(int n_jobs, cpc_ctx *const *ctxs, const cpc_pair_kind *kinds,
@@ -262,6 +264,19 @@ cpc_status cpc_set_graph_replay(cpc_ctx *ctx, int enable);
 
 /* Graph captures and replays of this context's fast counts so far. */
 cpc_status cpc_graph_stats(const cpc_ctx *ctx, int64_t *captures, int64_t *replays);
+
+/* Twin counts (no counterpart in the reference; results do not depend on it):
+ * a fast box count over every outer row of two slots that hold the same
+ * galaxies in the same order -- positions, weights, shapes, regions and input
+ * rows equal, as when the S and D samples of a cross term read the same files
+ * -- with a density_density or shape_shape accumulator and a Pi binning
+ * symmetric about 0, tests each unordered pair once and adds both orders
+ * (g1 = i, g2 = j) and (g1 = j, g2 = i), each with its own keep flags and
+ * order-dependent terms.  cpc_set_twin(ctx, 0) counts every order separately
+ * (default 1; CPC_TWIN=0 in the environment at cpc_create does the same);
+ * cpc_last_twin reports whether the context's last fast count ran so. */
+cpc_status cpc_set_twin(cpc_ctx *ctx, int enable);
+cpc_status cpc_last_twin(const cpc_ctx *ctx, int *twin);
 
 /* ---- host helpers of the reference's read path (no GPU needed) ---- */
 

@@ -40,6 +40,28 @@ def test_box_20M_wpp_row_sample_matches_oracle():
     ctx.close()
 
 
+def test_box_2M_wpp_twin_count_equals_every_order_count():
+    """The 2M-point clustered w++ box (the 20M box's geometry at a tenth of the
+    points) in full: the twin count (each unordered pair tested once, both
+    orders added) equals the count of every order -- counts identical, every
+    field within the bar -- and so do its window pairs."""
+    wl = synth.box_ns_large_wpp(n_parents=20000)
+    p = wl.params
+    cats = host.prepare(p, [("S", wl.shape), ("D", wl.density)])
+    ctx = _lib.Context(p)
+    ctx.upload(0, cats["D"])
+    ctx.upload(1, cats["S"])
+    rt = ctx.count("SD", 0, 1)
+    assert ctx.last_twin()
+    ctx.set_twin(False)
+    ro = ctx.count("SD", 0, 1)
+    assert not ctx.last_twin()
+    assert (rt["n_binned"], rt["n_window"]) == (ro["n_binned"], ro["n_window"])
+    assert np.array_equal(rt["num"], ro["num"])
+    check_sums(rt["sums"], ro["sums"], label="twin vs every order")
+    ctx.close()
+
+
 def test_sky_500k_5M_row_sample_matches_oracle():
     wl = synth.sky_wgp(500_000, 5_000_000)
     p = wl.params

@@ -42,6 +42,9 @@ def test_replayed_counts_match_reference(name):
 def test_changed_launch_shape_captures_again():
     g = Golden("box_wpp_uniform")
     ctx = _ctx_for(g.params, g.S, g.D)
+    # S and D read the same file: counted in every order here (a twin count
+    # takes other units than a row sample; it is checked at the end)
+    ctx.set_twin(False)
     _check(ctx.count("SD", 0, 1), g, "first")
     ctx.set_tuning(0, 9, 0)  # another Pi window: other units, grid, shared memory
     _check(ctx.count("SD", 0, 1), g, "window 9")
@@ -53,6 +56,11 @@ def test_changed_launch_shape_captures_again():
     assert 0 < r["n_binned"] < g.n_in
     _check(ctx.count("SD", 0, 1), g, "full again")
     assert ctx.graph_stats() == (2, 5)
+    # the twin count (each unordered pair once, both orders added) runs other
+    # units and shared memory: a capture of its own, the reference's results
+    ctx.set_twin(True)
+    _check(ctx.count("SD", 0, 1), g, "twin")
+    assert ctx.last_twin() and ctx.graph_stats() == (3, 6)
 
 
 def test_async_count_replays_on_a_caller_stream():

@@ -55,6 +55,48 @@ def test_large_box_matches_oracle():
     check_sums(r["sums"], sums)
 
 
+@pytest.mark.parametrize("name", ["box_lattice_edges", "box_wgg_uniform", "box_wpp_uniform",
+                                  "box_linear_bins_nojk"])
+def test_twin_counts_match_reference_golden(name):
+    """Cross terms whose S and D samples read the same file (wgg, w++; an
+    integer lattice with pairs exactly on bin edges; linear bins with self
+    pairs): the twin count -- each unordered pair tested once, both orders
+    added -- equals the reference, and so does the count of every order."""
+    g = Golden(name)
+    ctx = _ctx_for(g.params, g.S, g.D)
+    for twin in (True, False):
+        ctx.set_twin(twin)
+        r = ctx.count("SD", 0, 1)
+        assert ctx.last_twin() == twin, name
+        assert (r["n_binned"], r["n_window"]) == (g.n_in, g.n_total), (name, twin)
+        assert np.array_equal(r["num"], g.raw_num), (name, twin)
+        check_sums(r["sums"], g.raw_sums, label=f"{name} twin={twin}")
+    ctx.close()
+
+
+def test_twin_clustered_wpp_matches_oracle():
+    """A clustered periodic w++ box with 27 cubes, S = D read twice (the
+    jackknife keep flags differ between the reads): the twin count equals the
+    oracle's corels2 over every row, and a row sample (no twin) still does."""
+    c = synth.neyman_scott(300, 80.0, 3.0, 300.0, 71, nside_jk=3)
+    p = synth._box_params(which_corr=2, L=300.0, rmin=0.1, rmax=50.0, nrp=20, npi=40,
+                          pmax=80.0, njk=27, n=c.n)
+    ocats = oracle.read_like_reference(p, [("S", c), ("D", c)])
+    num, sums, n_total, n_in = oracle.port_corels2(p, "SD", ocats["D"], ocats["S"])
+    ctx = _ctx_for(p, c, c)
+    r = ctx.count("SD", 0, 1)
+    assert ctx.last_twin()
+    assert (r["n_binned"], r["n_window"]) == (n_in, n_total)
+    assert np.array_equal(r["num"], num)
+    check_sums(r["sums"], sums, label="twin")
+    rs = ctx.count("SD", 0, 1, row_stride=7, row_offset=2)
+    assert not ctx.last_twin()
+    ref = oracle.port_corels2(p, "SD", ocats["D"], ocats["S"], row_stride=7, row_offset=2)
+    assert np.array_equal(rs["num"], ref[0])
+    check_sums(rs["sums"], ref[1], label="row sample")
+    ctx.close()
+
+
 def test_clustered_shapes_row_subsample_matches_oracle():
     """The 200,000-galaxy clustered wg+ box on every 97th outer row."""
     wl = synth.box_ns_wgp()
